@@ -1,0 +1,259 @@
+"""ctypes binding of libamaru_gpu.so (include/amaru_gpu.h).
+
+The shared library is built in-tree (amaru.jl_gb300/build.py).  Loading fails
+loudly when it is missing: there is no CPU fallback for any operation.
+"""
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libamaru_gpu.so")
+
+AMR_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENEGJAC", -4: "ERETMAP", -5: "ENAN", -6: "ESINGULAR", -7: "ENOCONV",
+          -8: "ETIMEOUT", -9: "ENOMEM", -10: "EUNSUPPORTED", -11: "ESTAGE"}
+
+LIN2, LIN3, TRI3, TRI6, QUAD4, QUAD8, QUAD9, TET4, TET10, HEX8, HEX20 = range(1, 12)
+D3, PLANESTRAIN, PLANESTRESS, AXISYMMETRIC = 0, 1, 2, 3
+LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
+LOAD_FACET, LOAD_BODY = 0, 1
+SOLVER_MIXED, SOLVER_FP64 = 0, 1
+
+
+class AmrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%s)" % (msg, ERRORS.get(code, code)))
+        self.code = code
+        self.msg = msg
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int32), ("stressmodel", C.c_int32), ("thickness", C.c_double), ("nnodes", C.c_int64),
+                ("coords", C.c_void_p), ("nelems", C.c_int64), ("shape", C.c_void_p), ("nips", C.c_void_p),
+                ("conn_ptr", C.c_void_p), ("conn", C.c_void_p), ("mat_type", C.c_void_p), ("mat_params", C.c_void_p)]
+
+
+class Load(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("dir", C.c_int32), ("edge_key", C.c_int32), ("facet_shape", C.c_int32),
+                ("nitems", C.c_int64), ("items", C.c_void_p), ("coef", C.c_double * 5)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("method", C.c_int32), ("rtol", C.c_double), ("max_iters", C.c_int32), ("refine_every", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("rel_residual", C.c_double),
+                ("seconds", C.c_double)]
+
+
+class StageParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("rtol", C.c_double), ("rspan", C.c_double), ("dT0", C.c_double),
+                ("dTmin", C.c_double), ("dTmax", C.c_double), ("scheme", C.c_int32), ("maxits", C.c_int32),
+                ("autoinc", C.c_int32), ("nincs", C.c_int32), ("nouts", C.c_int32), ("linear", SolveOpts)]
+
+
+class StageStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("increments", C.c_int32), ("iterations", C.c_int32),
+                ("krylov_iterations", C.c_int32), ("residue", C.c_double), ("T", C.c_double)]
+
+
+# Every exported entry point of include/amaru_gpu.h with its ctypes signature.
+P = C.c_void_p
+SIGNATURES = {
+    "amr_model_create": (C.c_int, [C.POINTER(ModelDesc), C.POINTER(C.c_void_p)]),
+    "amr_model_destroy": (C.c_int, [P]),
+    "amr_last_error": (C.c_int, [P, C.c_char_p, C.c_size_t]),
+    "amr_create_error": (C.c_char_p, []),
+    "amr_set_dofs": (C.c_int, [P, P, C.c_int64, C.c_int64]),
+    "amr_set_youngs": (C.c_int, [P, P]),
+    "amr_assemble_K": (C.c_int, [P]),
+    "amr_get_K_nnz": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "amr_get_K_csc": (C.c_int, [P, P, P, P]),
+    "amr_update_state": (C.c_int, [P, P, P]),
+    "amr_state_commit": (C.c_int, [P]),
+    "amr_state_restore": (C.c_int, [P]),
+    "amr_get_state": (C.c_int, [P, P]),
+    "amr_get_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_int64)]),
+    "amr_assemble_loads": (C.c_int, [P, C.POINTER(Load), C.c_int32, C.c_double, P]),
+    "amr_solve": (C.c_int, [P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
+    "amr_stage_run": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
+    "amr_default_solve_opts": (None, [C.POINTER(SolveOpts)]),
+    "amr_default_stage_params": (None, [C.POINTER(StageParams)]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError("libamaru_gpu.so is not built (run amaru.jl_gb300/build.py); "
+                                   "the GPU path has no CPU fallback")
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def check(h, rc):
+    if rc != AMR_OK:
+        buf = C.create_string_buffer(1024)
+        if h:
+            lib().amr_last_error(h, buf, 1024)
+            msg = buf.value.decode("utf-8", "replace")
+        else:
+            msg = (lib().amr_create_error() or b"").decode("utf-8", "replace")
+        raise AmrError(rc, msg)
+    return rc
+
+
+def default_solve_opts(**kw):
+    o = SolveOpts()
+    lib().amr_default_solve_opts(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def default_stage_params(**kw):
+    p = StageParams()
+    lib().amr_default_stage_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "linear":
+            p.linear = v
+        else:
+            setattr(p, k, v)
+    return p
+
+
+class DeviceModel:
+    """Owning wrapper of an amr_model handle."""
+
+    def __init__(self, ndim, stressmodel, thickness, coords, shape, nips, conn_ptr, conn, mat_type, mat_params):
+        self._keep = [np.ascontiguousarray(coords, dtype=np.float64), np.ascontiguousarray(shape, dtype=np.int32),
+                      np.ascontiguousarray(nips, dtype=np.int32), np.ascontiguousarray(conn_ptr, dtype=np.int64),
+                      np.ascontiguousarray(conn, dtype=np.int64), np.ascontiguousarray(mat_type, dtype=np.int32),
+                      np.ascontiguousarray(mat_params, dtype=np.float64)]
+        c, s, n, cp, cn, mt, mp = self._keep
+        d = ModelDesc()
+        d.ndim, d.stressmodel, d.thickness = ndim, stressmodel, thickness
+        d.nnodes, d.coords = c.shape[0], ptr(c)
+        d.nelems, d.shape, d.nips = s.shape[0], ptr(s), ptr(n)
+        d.conn_ptr, d.conn, d.mat_type, d.mat_params = ptr(cp), ptr(cn), ptr(mt), ptr(mp)
+        h = C.c_void_p()
+        check(None, lib().amr_model_create(C.byref(d), C.byref(h)))
+        self.h = h
+        self._keep = None
+        self.ndim = ndim
+        self.ndofs = 0
+        self.nu = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().amr_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sizes(self):
+        a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(self.h, lib().amr_get_sizes(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return dict(nnodes=a.value, nelems=b.value, nip_total=c.value, nblocks=d.value)
+
+    def set_dofs(self, eq_id, ndofs, nu):
+        eq = np.ascontiguousarray(eq_id, dtype=np.int64)
+        check(self.h, lib().amr_set_dofs(self.h, ptr(eq), ndofs, nu))
+        self.ndofs, self.nu = ndofs, nu
+
+    def set_youngs(self, E):
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        check(self.h, lib().amr_set_youngs(self.h, ptr(E)))
+
+    def assemble_K(self):
+        check(self.h, lib().amr_assemble_K(self.h))
+
+    def K_csc(self):
+        """K as a scipy CSC matrix in eq_id order with the reference's stored-entry pattern."""
+        import scipy.sparse as sp
+        nnz = C.c_int64()
+        check(self.h, lib().amr_get_K_nnz(self.h, C.byref(nnz)))
+        cp = np.zeros(self.ndofs + 1, dtype=np.int64)
+        rv = np.zeros(max(nnz.value, 1), dtype=np.int64)
+        nz = np.zeros(max(nnz.value, 1))
+        check(self.h, lib().amr_get_K_csc(self.h, ptr(cp), ptr(rv), ptr(nz)))
+        return sp.csc_matrix((nz[:nnz.value], rv[:nnz.value], cp), shape=(self.ndofs, self.ndofs))
+
+    def update_state(self, dU):
+        dU = np.ascontiguousarray(dU, dtype=np.float64)
+        dF = np.zeros(self.ndofs)
+        check(self.h, lib().amr_update_state(self.h, ptr(dU), ptr(dF)))
+        return dF
+
+    def commit(self):
+        check(self.h, lib().amr_state_commit(self.h))
+
+    def restore(self):
+        check(self.h, lib().amr_state_restore(self.h))
+
+    def state(self):
+        n = self.sizes()["nip_total"]
+        s = np.zeros((n, 16))
+        check(self.h, lib().amr_get_state(self.h, ptr(s)))
+        return s
+
+    def assemble_loads(self, loads, F, t=0.0):
+        arr = (Load * max(len(loads), 1))()
+        keep = []
+        for i, (kind, dr, edge, fshape, items, coef) in enumerate(loads):
+            it = np.ascontiguousarray(items, dtype=np.int64)
+            keep.append(it)
+            arr[i].kind, arr[i].dir, arr[i].edge_key, arr[i].facet_shape = kind, dr, edge, fshape
+            arr[i].nitems = it.shape[0] if it.ndim > 0 else 0
+            arr[i].items = ptr(it)
+            for k in range(5):
+                arr[i].coef[k] = coef[k]
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        check(self.h, lib().amr_assemble_loads(self.h, arr, len(loads), t, ptr(F)))
+        return F
+
+    def solve(self, U, F, opts=None):
+        U = np.ascontiguousarray(U, dtype=np.float64).copy()
+        F = np.ascontiguousarray(F, dtype=np.float64).copy()
+        st = SolveStats()
+        o = opts if opts is not None else default_solve_opts()
+        check(self.h, lib().amr_solve(self.h, ptr(U), ptr(F), C.byref(o), C.byref(st)))
+        return U, F, st
+
+    def stage_run(self, Uex, Fex, params):
+        Uex = np.ascontiguousarray(Uex, dtype=np.float64)
+        Fex = np.ascontiguousarray(Fex, dtype=np.float64)
+        U = np.zeros(self.ndofs)
+        F = np.zeros(self.ndofs)
+        st = StageStats()
+        rc = lib().amr_stage_run(self.h, ptr(Uex), ptr(Fex), C.byref(params), ptr(U), ptr(F), C.byref(st))
+        return rc, U, F, st
+
+    def last_error(self):
+        buf = C.create_string_buffer(1024)
+        lib().amr_last_error(self.h, buf, 1024)
+        return buf.value.decode("utf-8", "replace")

@@ -1,0 +1,307 @@
+"""Amaru's element/material/stage API on top of the GB300 library.
+
+Mirrors FEModel (src/fe-model.jl:66-255), MechContext / MechAnalysis / solve!
+(src/mech/mech-solver.jl:6-181), addstage! (src/analysis.jl:27-32), the
+boundary-condition types (src/bc.jl) and the solver-level plugin functions
+mount_K / update_state! / solve_system! that the GPU library replaces.
+All numerical work runs in libamaru_gpu.so; this module numbers DOFs,
+evaluates essential values and nodal loads, and moves arrays across the ABI.
+"""
+import numpy as np
+
+from . import _lib as L
+from .expr import affine_coefficients, evaluate
+from .mesh import NPOINTS, Mesh
+
+STRESSMODELS = {"d3": L.D3, "planestrain": L.PLANESTRAIN, "planestress": L.PLANESTRESS,
+                "axisymmetric": L.AXISYMMETRIC}
+
+
+# ---- materials (src/mech/mat/*.jl) and the element type
+class MechSolid:
+    """Isoparametric bulk element (src/mech/elem/mech-solid.jl)."""
+
+
+class _Mat:
+    kind = None
+
+    def __init__(self, **p):
+        self.p = p
+
+    def params(self):
+        raise NotImplementedError
+
+
+class LinearElastic(_Mat):
+    """LinearElastic(E, nu): src/mech/mat/linear-elastic.jl:5-20"""
+    kind = L.LINEAR_ELASTIC
+
+    def params(self):
+        return [self.p["E"], self.p.get("nu", 0.0), 0, 0, 0, 0, 0, 0]
+
+
+class VonMises(_Mat):
+    """VonMises(E, nu, fy, H): src/mech/mat/von-mises.jl:3-27"""
+    kind = L.VON_MISES
+
+    def params(self):
+        return [self.p["E"], self.p.get("nu", 0.0), self.p["fy"], self.p.get("H", 0.0), 0, 0, 0, 0]
+
+
+class DruckerPrager(_Mat):
+    """DruckerPrager(E, nu, alpha, kappa, H): src/mech/mat/drucker-prager.jl:5-33"""
+    kind = L.DRUCKER_PRAGER
+
+    def params(self):
+        return [self.p["E"], self.p.get("nu", 0.0), self.p.get("alpha", 0.0), self.p["kappa"], self.p.get("H", 0.0),
+                0, 0, 0]
+
+
+# ---- boundary conditions (src/bc.jl)
+class _BC:
+    def __init__(self, **conds):
+        if not conds:
+            raise ValueError("a boundary condition needs at least one condition")
+        self.conds = conds
+
+
+class NodeBC(_BC):
+    pass
+
+
+class SurfaceBC(_BC):
+    pass
+
+
+class EdgeBC(_BC):
+    pass
+
+
+class BodyC(_BC):
+    pass
+
+
+FaceBC = SurfaceBC
+ElemBC = BodyC
+_NAT = {"fx": 0, "fy": 1, "fz": 2}
+_DIR = {"x": 0, "y": 1, "z": 2, "n": 3}
+
+
+def number_dofs(active_nodes, presc, nnodes):
+    """DOF numbering of configure_dofs! (src/bc.jl:198-233): active nodes by id, (ux, uy[, uz]) per node,
+    unknown DOFs first and prescribed ones last, both in that order.  Returns (eq_id, ndofs, nu, node, comp)."""
+    ndim = presc.shape[1]
+    act = np.asarray(active_nodes, dtype=np.int64)
+    flags = presc[act].reshape(-1)
+    dn = np.repeat(act, ndim)
+    dk = np.tile(np.arange(ndim), len(act))
+    order = np.concatenate([np.nonzero(~flags)[0], np.nonzero(flags)[0]])
+    eq_id = -np.ones((nnodes, 3), dtype=np.int64)
+    eq_id[dn[order], dk[order]] = np.arange(len(order))
+    return eq_id, len(order), int((~flags).sum()), dn[order], dk[order]
+
+
+class MechContext:
+    """MechContext(ndim, stressmodel): src/mech/mech-solver.jl:6-33"""
+
+    def __init__(self, ndim=0, stressmodel="d3"):
+        self.ndim, self.stressmodel = ndim, stressmodel
+
+
+class FEModel:
+    """FEModel(mesh, matbinds, ctx; thickness): model on the device.
+
+    matbinds: list of (filter, MechSolid, MaterialType, params-dict) or (filter, material instance);
+    filter is a tag, an expression over the element's nodes, or "all"."""
+
+    def __init__(self, mesh, matbinds, ctx=None, thickness=1.0, nips=0, E=None):
+        ctx = ctx or MechContext()
+        self.mesh = mesh
+        self.ndim = mesh.ndim
+        sm = ctx.stressmodel
+        if self.ndim == 2 and sm == "d3":
+            sm = "planestrain"
+        self.stressmodel = STRESSMODELS[sm]
+        self.thickness = float(thickness)
+        ne = len(mesh.shape)
+        self.mat_type = np.full(ne, -1, dtype=np.int32)
+        self.mat_params = np.zeros((ne, 8))
+        enodes = mesh.elem_nodes()
+        for bind in matbinds:
+            if len(bind) == 4:
+                filt, _elem, mtype, params = bind
+                mat = mtype(**params)
+            else:
+                filt, mat = bind
+            if isinstance(filt, str) and (filt == "all" or not any(ch in filt for ch in "=<>")):
+                sel = np.arange(ne) if filt == "all" else np.nonzero(mesh.tags == filt)[0]
+            else:
+                sel = mesh.select_cells(enodes, filt)
+            self.mat_type[sel] = mat.kind
+            self.mat_params[sel] = mat.params()
+        if (self.mat_type < 0).any():
+            raise ValueError("FEModel: some elements have no material")
+        if E is not None:
+            self.mat_params[:, 0] = E
+        self.nips = np.full(ne, nips, dtype=np.int32)
+        self.dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, mesh.coords, mesh.shape, self.nips,
+                                 mesh.conn_ptr, mesh.conn, self.mat_type, self.mat_params)
+        self.nnodes = len(mesh.coords)
+        self.U = np.zeros((self.nnodes, self.ndim))  # dof.vals of the displacement keys
+        self.F = np.zeros((self.nnodes, self.ndim))  # dof.vals of the natural keys
+        self.eq_id = -np.ones((self.nnodes, 3), dtype=np.int64)
+        self.ndofs = self.nu = 0
+        self.active_nodes = np.unique(mesh.conn)
+        self._dof_names = ["ux", "uy", "uz"][: self.ndim]
+
+    def changequadrature(self, n):
+        """changequadrature!(elems, n) (src/element.jl:185-188): rebuilds the device model."""
+        self.nips[:] = n
+        self.dev.close()
+        self.dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, self.mesh.coords, self.mesh.shape,
+                                 self.nips, self.mesh.conn_ptr, self.mesh.conn, self.mat_type, self.mat_params)
+
+    # ---- configure_dofs! (src/bc.jl:198-233)
+    def _select(self, bc, filt):
+        mesh = self.mesh
+        if isinstance(bc, NodeBC):
+            if isinstance(filt, (int, np.integer)):
+                return np.array([filt]), np.array([[filt]])
+            if isinstance(filt, (list, tuple, np.ndarray)):
+                a = np.asarray(filt, dtype=np.int64)
+                return a, a[:, None]
+            ids = mesh.select_nodes(filt)
+            return ids, ids[:, None]
+        if isinstance(bc, SurfaceBC) or isinstance(bc, EdgeBC):
+            if isinstance(bc, EdgeBC) or self.ndim == 2:
+                table, shapes = mesh.edge_nodes, mesh.edge_shape
+            else:
+                table, shapes = mesh.face_nodes, mesh.face_shape
+            sel = mesh.select_cells(table, filt)
+            return sel, (table[sel], shapes[sel])
+        enodes = mesh.elem_nodes()
+        if isinstance(filt, str) and not any(ch in filt for ch in "=<>") and filt != "all":
+            sel = np.nonzero(mesh.tags == filt)[0]
+        else:
+            sel = mesh.select_cells(enodes, filt)
+        return sel, enodes[sel]
+
+    def configure_dofs(self, bcs):
+        presc = np.zeros((self.nnodes, self.ndim), dtype=bool)
+        setup = []
+        for filt, bc in bcs:
+            sel, objs = self._select(bc, filt)
+            nodes = objs if isinstance(bc, NodeBC) else (objs[0] if isinstance(objs, tuple) else objs)
+            nodes = np.unique(nodes[nodes >= 0]) if len(nodes) else np.zeros(0, dtype=np.int64)
+            for key in bc.conds:
+                if key in self._dof_names:
+                    presc[nodes, self._dof_names.index(key)] = True
+            setup.append((bc, sel, objs, nodes))
+        self.eq_id, self.ndofs, self.nu, self.dof_node, self.dof_comp = number_dofs(self.active_nodes, presc,
+                                                                                   self.nnodes)
+        self.dev.set_dofs(self.eq_id, self.ndofs, self.nu)
+        return setup
+
+    # ---- get_bc_vals (src/bc.jl:237-249)
+    def get_bc_vals(self, setup, t=0.0):
+        U = np.zeros(self.ndofs)
+        F = np.zeros(self.ndofs)
+        loads = []
+        c = self.mesh.coords
+        for bc, sel, objs, nodes in setup:
+            for key, val in bc.conds.items():
+                if key in self._dof_names:
+                    k = self._dof_names.index(key)
+                    v = np.broadcast_to(evaluate(val, x=c[nodes, 0], y=c[nodes, 1], z=c[nodes, 2], t=t), nodes.shape)
+                    U[self.eq_id[nodes, k]] = v
+                elif isinstance(bc, NodeBC):
+                    if key not in _NAT or _NAT[key] >= self.ndim:
+                        raise ValueError("NodeBC key %s not applicable" % key)
+                    k = _NAT[key]
+                    v = np.broadcast_to(evaluate(val, x=c[nodes, 0], y=c[nodes, 1], z=c[nodes, 2], t=t), nodes.shape)
+                    np.add.at(F, self.eq_id[nodes, k], v)
+                elif isinstance(bc, (SurfaceBC, EdgeBC)):
+                    table, shapes = objs
+                    if len(table) == 0:
+                        continue
+                    if key[0] not in "tq" or key[1:] not in _DIR:
+                        raise ValueError("boundary condition %s is not applicable as distributed bc" % key)
+                    cf = affine_coefficients(val, self.ndim)
+                    for fs in np.unique(shapes):
+                        rows = table[shapes == fs][:, :NPOINTS[int(fs)]]
+                        loads.append((L.LOAD_FACET, _DIR[key[1:]], 1 if key[0] == "q" else 0, int(fs), rows, cf))
+                else:
+                    if key not in ("wx", "wy", "wz"):
+                        raise ValueError("body condition %s is not applicable" % key)
+                    cf = affine_coefficients(val, self.ndim)
+                    loads.append((L.LOAD_BODY, _DIR[key[1]], 0, 0, np.asarray(sel, dtype=np.int64), cf))
+        if loads:
+            F = self.dev.assemble_loads(loads, F, t)
+        return U, F
+
+    # ---- the solver-level plugin functions the library replaces
+    def mount_K(self):
+        """mount_K(elems, ndofs) (src/mech/mech-solver.jl:78-110): device assembly, reference CSC layout."""
+        self.dev.assemble_K()
+        return self.dev.K_csc()
+
+    def update_state(self, dU):
+        """update_state!(elems, dU, t) (src/mech/mech-solver.jl:124-144): returns dFin."""
+        return self.dev.update_state(dU)
+
+    def solve_system(self, U, F, **opts):
+        """solve_system!(K, U, F, nu) (src/solver.jl:5-79) on the last assembled K."""
+        o = L.default_solve_opts(**opts)
+        U2, F2, st = self.dev.solve(U, F, o)
+        U[:self.nu] = U2[:self.nu]
+        F[self.nu:] = F2[self.nu:]
+        return st
+
+    def state(self):
+        return self.dev.state()
+
+
+class Stage:
+    def __init__(self, bcs, nincs=1, nouts=0):
+        self.bcs, self.nincs, self.nouts, self.status = list(bcs), nincs, nouts, "pending"
+
+
+class MechAnalysis:
+    """MechAnalysis(model): staged Newton solver on the device."""
+
+    def __init__(self, model):
+        self.model = model
+        self.stages = []
+        self.stats = []
+
+    def addstage(self, bcs, nincs=1, nouts=0):
+        """addstage!(ana, bcs; nincs, nouts): src/analysis.jl:27-32"""
+        self.stages.append(Stage(bcs, nincs, nouts))
+
+    def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
+              autoinc=False, quiet=True, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000):
+        """solve!(ana; args...) (src/mech/mech-solver.jl:155-181): returns (success, message)."""
+        if not (1 <= maxits <= 10):
+            raise ValueError("maxits must be in 1..10")
+        model = self.model
+        lin = L.default_solve_opts(method=L.SOLVER_FP64 if solver == "fp64" else L.SOLVER_MIXED, rtol=linear_rtol,
+                                   refine_every=refine_every, max_iters=max_iters)
+        for st in self.stages:
+            if st.status == "done":
+                continue
+            setup = model.configure_dofs(st.bcs)
+            Uex, Fex = model.get_bc_vals(setup)
+            p = L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,
+                                       scheme={"FE": 0, "ME": 1, "BE": 2, "Ralston": 3}[scheme], maxits=maxits,
+                                       autoinc=int(autoinc), nincs=st.nincs, nouts=st.nouts, linear=lin)
+            rc, U, F, stats = model.dev.stage_run(Uex, Fex, p)
+            self.stats.append(stats)
+            if rc not in (0, -11):
+                raise L.AmrError(rc, model.dev.last_error())
+            model.U[model.dof_node, model.dof_comp] += U
+            model.F[model.dof_node, model.dof_comp] += F
+            if rc != 0:
+                st.status = "error"
+                return False, model.dev.last_error()
+            st.status = "done"
+        return True, ""

@@ -1,0 +1,158 @@
+// Internal declarations of the GB300 mechanical-path library (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "amaru_gpu.h"
+
+#define AMR_MAXN 20     // largest element (HEX20)
+#define AMR_MAXIP 27    // largest quadrature (HEX 3x3x3)
+#define AMR_NST 14      // IP state fields: sigma[6] eps[6] epa dlambda
+#define AMR_ST_EPA 12
+#define AMR_ST_DL 13
+
+// Host shape library (shapes.cpp): the library's own statement of Amaru's
+// shape functions and Gauss tables, used to build per-shape device tables.
+namespace amr {
+int shape_npoints(int shape);
+int shape_ndim(int shape);
+int shape_facet_shape(int shape);
+void shape_func(int shape, const double *R, double *N);
+void shape_deriv(int shape, const double *R, double *D);  // D[i*ndim+k]
+int quadrature(int shape, int nips, double *R, double *w);  // returns count or -1
+}  // namespace amr
+
+struct AmrGroup {             // elements sharing (shape, quadrature)
+    int shape = 0, nen = 0, nip = 0;
+    int64_t first = 0, count = 0;  // range in the sorted element order
+    double *tab = nullptr;    // device: [nip][nen*ndim] dN/dR, then [nip] w, then [nip][nen] N
+    int epb = 1;              // elements per CTA for the stiffness kernel (autotuned)
+};
+
+struct AmrSolveWork;          // solver workspace (solver.cu)
+
+struct amr_model {
+    int ndim = 3, B = 3, BB = 9, stressmodel = 0;
+    double thickness = 1.0;
+    int64_t nnodes = 0, nelems = 0, nip_total = 0;
+    std::vector<AmrGroup> groups;
+    // host-side copies (sorted element order)
+    std::vector<int64_t> perm;      // sorted -> caller element id
+    std::vector<int64_t> inv_perm;  // caller element id -> sorted
+    std::vector<int64_t> h_conn_ptr, h_ip_ptr, h_kel_ptr;
+    std::vector<int32_t> h_conn, h_shape, h_nips;
+    std::vector<double> h_coords;
+    // device model
+    double *coords = nullptr;       // nnodes x 3
+    int32_t *conn = nullptr;        // sorted elements, flat
+    int64_t *conn_ptr = nullptr;    // nelems+1
+    int32_t *mat_type = nullptr;    // sorted
+    double *mat_par = nullptr;      // sorted, nelems x 8
+    int64_t *ip_ptr = nullptr;      // nelems+1
+    int64_t *kel_ptr = nullptr;     // nelems+1 (in blocks: sum nen^2)
+    int64_t kel_blocks = 0;
+    // node -> (element, local node) incidence, ordered by caller element id
+    int64_t *inc_ptr = nullptr;     // nnodes+1
+    int64_t *inc = nullptr;         // (sorted elem << 8) | local
+    int64_t ninc = 0;
+    // node-block sparsity pattern
+    int64_t nblocks = 0;
+    int64_t *brow_ptr = nullptr;    // nnodes+1
+    int32_t *bcol = nullptr;        // nblocks
+    int64_t *contrib_ptr = nullptr; // nblocks+1
+    int64_t *contrib = nullptr;     // element block slots, element order
+    int64_t ncontrib = 0;
+    std::vector<int64_t> h_brow_ptr;
+    std::vector<int32_t> h_bcol;
+    // values
+    double *Kel = nullptr;          // kel_blocks x BB element blocks (staging)
+    double *K64 = nullptr;          // SoA [BB][nblocks]
+    float *K32 = nullptr;           // SoA [BB][nblocks], Dirichlet-masked
+    uint16_t *keep = nullptr;       // nblocks: bit (c*B+d) set if some |Ke| >= eps
+    float *Minv32 = nullptr;        // nnodes x BB block-Jacobi inverse (masked)
+    double *Minv64 = nullptr;       // nnodes x BB (FP64 block-Jacobi, comparator path)
+    bool K_valid = false;
+    // dofs
+    int64_t ndofs = 0, nu = 0;
+    std::vector<int64_t> h_eq_id;   // nnodes x 3
+    int64_t *eq_id = nullptr;       // device nnodes x 3
+    uint8_t *free_mask = nullptr;   // nnodes x B : 1 free, 0 prescribed or absent
+    int64_t *dof_node = nullptr;    // ndofs: node*B + comp for each eq_id
+    bool dofs_set = false;
+    // IP states, SoA [AMR_NST][nip_total]
+    double *st = nullptr, *stbk = nullptr;
+    // element force staging and vectors
+    double *Fel = nullptr;          // sum nen*B per element
+    int64_t *fel_ptr = nullptr;     // nelems+1 (in doubles)
+    // device status: [0] code, [1] first failing element (sorted)
+    int32_t *d_status = nullptr;
+    int32_t *h_status = nullptr;    // pinned
+    // scratch
+    double *vtmp[8] = {nullptr};    // node-major FP64 vectors (nnodes*B)
+    AmrSolveWork *sw = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    bool any_plastic = false;
+};
+
+// helpers
+#define AMR_CUDA(call)                                                                 \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            throw AmrError(AMR_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        }                                                                              \
+    } while (0)
+
+struct AmrError {
+    int code;
+    std::string msg;
+    AmrError(int c, std::string m) : code(c), msg(std::move(m)) {}
+};
+
+template <class T>
+inline void amr_alloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw AmrError(AMR_ENOMEM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes: " +
+                                       cudaGetErrorString(e));
+    }
+}
+template <class T>
+inline void amr_free(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// pattern.cu
+void amr_build_pattern(amr_model *m);
+void amr_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);  // exclusive, out has n+1
+// element.cu
+void amr_stiffness(amr_model *m);                       // Kel + gather into K64/K32/Minv
+void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm);  // node-major device vectors
+void amr_apply_dofs(amr_model *m);                      // masks after amr_set_dofs
+void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double *F_nm);  // F_nm += (device)
+int amr_check_status(amr_model *m);                     // reads d_status, resets, returns code
+// solver.cu
+struct AmrSolveResult {
+    int status;
+    int iterations, refinements;
+    double rel_residual, seconds;
+};
+// Solves K11 x1 = b1 - K12 x2 on node-major device vectors: x (in: prescribed values at
+// prescribed slots; out: free slots), b (free slots), reac (out: K x at prescribed slots).
+AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o);
+void amr_solver_free(amr_model *m);
+// vector helpers (solver.cu)
+double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask_or_null);
+void amr_eq_to_nm(amr_model *m, const double *d_eq, double *d_nm);  // scatter eq_id-ordered -> node-major (0 elsewhere)
+void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq);
+// stage.cpp-equivalent (capi.cu)
+int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
+                     double *U_nm, double *F_nm, amr_stage_stats *stats);

@@ -1,0 +1,706 @@
+// C ABI of the library (include/amaru_gpu.h): model lifecycle, DOFs, assembly,
+// parity export, state update, linear solve, loads and the staged Newton
+// driver (mech_stage_solver!, src/mech/mech-solver.jl:186-492) whose vectors
+// all stay on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+
+#include "amr_internal.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// elementwise ops on node-major vectors
+enum VecOp {
+    V_SET_AXPBY = 0,   // o = a x + b y
+    V_MASK_FREE = 1,   // o = x at free slots, 0 at prescribed
+    V_MASK_PRESC = 2,  // o = x at prescribed slots, 0 at free
+};
+
+__global__ void k_vec(int64_t n, int op, double a, const double *x, double b, const double *y, double *o,
+                      const uint8_t *fm) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    switch (op) {
+    case V_SET_AXPBY: o[i] = a * x[i] + (y ? b * y[i] : 0.0); break;
+    case V_MASK_FREE: o[i] = fm[i] ? x[i] : 0.0; break;
+    case V_MASK_PRESC: o[i] = fm[i] ? 0.0 : x[i]; break;
+    }
+}
+
+__global__ void k_free_mask(int64_t nnodes, int B, const int64_t *eq_id, int64_t nu, uint8_t *fm) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t e = eq_id[(t / B) * 3 + t % B];
+    fm[t] = (e >= 0 && e < nu) ? 1 : 0;
+}
+
+void vec(amr_model *m, int op, double a, const double *x, double b, const double *y, double *o) {
+    int64_t n = m->nnodes * m->B;
+    k_vec<<<nblk(n, 256), 256, 0, m->stream>>>(n, op, a, x, b, y, o, m->free_mask);
+}
+
+void upload(void *d, const void *h, size_t bytes, cudaStream_t s) {
+    AMR_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s));
+}
+
+void check_dofs(amr_model *m) {
+    if (!m->dofs_set) throw AmrError(AMR_EINVAL, "amr_set_dofs must be called first");
+}
+
+int fail(amr_model *m, const AmrError &e) {
+    if (m) m->err = e.msg;
+    return e.code;
+}
+
+template <class F>
+int guarded(amr_model *m, F f) {
+    if (!m) return AMR_EINVAL;
+    try {
+        m->err.clear();
+        return f();
+    } catch (const AmrError &e) {
+        return fail(m, e);
+    } catch (const std::exception &e) {
+        return fail(m, AmrError(AMR_EINVAL, e.what()));
+    }
+}
+
+// eq_id-ordered host array -> node-major device vector (0 where no DOF)
+void eq_host_to_nm(amr_model *m, const double *h, double *d_nm) {
+    double *d_eq;
+    amr_alloc(&d_eq, m->ndofs);
+    upload(d_eq, h, m->ndofs * sizeof(double), m->stream);
+    amr_eq_to_nm(m, d_eq, d_nm);
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    amr_free(d_eq);
+}
+
+void nm_to_eq_host(amr_model *m, const double *d_nm, double *h) {
+    double *d_eq;
+    amr_alloc(&d_eq, m->ndofs);
+    amr_nm_to_eq(m, d_nm, d_eq);
+    AMR_CUDA(cudaMemcpyAsync(h, d_eq, m->ndofs * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    amr_free(d_eq);
+}
+
+void assemble(amr_model *m) {
+    check_dofs(m);
+    amr_stiffness(m);
+    int rc = amr_check_status(m);
+    if (rc == AMR_ENEGJAC) throw AmrError(rc, "Negative Jacobian determinant in cell " + std::to_string(m->perm[m->h_status[1]] + 1));
+    if (rc == AMR_ENAN) throw AmrError(rc, "NaN values in coefficients matrix");
+    if (rc) throw AmrError(rc, "assembly failed");
+    m->K_valid = true;
+}
+
+double round_sig3(double x) {
+    if (x == 0.0 || !std::isfinite(x)) return x;
+    double e = std::floor(std::log10(std::fabs(x)));
+    double sc = std::pow(10.0, 2.0 - e);
+    return std::round(x * sc) / sc;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char *amr_create_error(void) { return g_create_error.c_str(); }
+
+void amr_default_solve_opts(amr_solve_opts *o) {
+    o->method = AMR_SOLVER_MIXED;
+    o->rtol = 1e-8;
+    o->max_iters = 20000;
+    o->refine_every = 32;
+}
+
+void amr_default_stage_params(amr_stage_params *p) {
+    p->tol = 0.01; p->rtol = 0.01; p->rspan = 0.01; p->dT0 = 0.01; p->dTmin = 1e-7; p->dTmax = 0.1;
+    p->scheme = AMR_SCHEME_FE; p->maxits = 5; p->autoinc = 0; p->nincs = 1; p->nouts = 0;
+    amr_default_solve_opts(&p->linear);
+}
+
+int amr_model_create(const amr_model_desc *d, amr_model **out) {
+    g_create_error.clear();
+    if (!d || !out) { g_create_error = "null argument"; return AMR_EINVAL; }
+    *out = nullptr;
+    amr_model *m = new amr_model();
+    try {
+        if (d->ndim != 2 && d->ndim != 3) throw AmrError(AMR_EINVAL, "ndim must be 2 or 3");
+        if (d->stressmodel == AMR_AXISYMMETRIC) throw AmrError(AMR_EUNSUPPORTED, "axisymmetric analyses are not on the GPU path");
+        if (d->stressmodel < 0 || d->stressmodel > 3) throw AmrError(AMR_EINVAL, "bad stress model");
+        if (d->ndim == 3 && d->stressmodel != AMR_D3) throw AmrError(AMR_EINVAL, "3-D analyses use the d3 stress model");
+        if (d->nnodes <= 0 || d->nelems <= 0) throw AmrError(AMR_EINVAL, "empty model");
+        if (d->nnodes >= INT32_MAX) throw AmrError(AMR_EUNSUPPORTED, "more than 2^31 nodes");
+        m->ndim = d->ndim; m->B = d->ndim; m->BB = d->ndim * d->ndim;
+        m->stressmodel = d->stressmodel; m->thickness = d->thickness;
+        m->nnodes = d->nnodes; m->nelems = d->nelems;
+        AMR_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+        AMR_CUDA(cudaEventCreate(&m->ev0));
+        AMR_CUDA(cudaEventCreate(&m->ev1));
+        // validate elements and group them by (shape, quadrature), stable
+        std::vector<int> nq(d->nelems);
+        for (int64_t e = 0; e < d->nelems; e++) {
+            int sh = d->shape[e];
+            int np = amr::shape_npoints(sh);
+            if (np <= 0 || amr::shape_ndim(sh) != d->ndim) throw AmrError(AMR_EUNSUPPORTED, "element " + std::to_string(e) + ": shape not a bulk cell of this dimension");
+            if (d->conn_ptr[e + 1] - d->conn_ptr[e] != np) throw AmrError(AMR_EINVAL, "element " + std::to_string(e) + ": wrong node count");
+            for (int64_t p = d->conn_ptr[e]; p < d->conn_ptr[e + 1]; p++)
+                if (d->conn[p] < 0 || d->conn[p] >= d->nnodes) throw AmrError(AMR_EINVAL, "element " + std::to_string(e) + ": node index out of range");
+            double R[64 * 3], w[64];
+            nq[e] = amr::quadrature(sh, d->nips[e], R, w);
+            if (nq[e] <= 0) throw AmrError(AMR_EINVAL, "element " + std::to_string(e) + ": unsupported number of integration points");
+            int mt = d->mat_type[e];
+            if (mt < 0 || mt > 2) throw AmrError(AMR_EUNSUPPORTED, "unsupported material");
+            if (mt != AMR_LINEAR_ELASTIC) m->any_plastic = true;
+            const double *p = d->mat_params + 8 * e;
+            if (!(p[0] > 0.0) || !(p[1] >= 0.0 && p[1] < 0.5)) throw AmrError(AMR_EINVAL, "element " + std::to_string(e) + ": E > 0 and 0 <= nu < 0.5 required");
+        }
+        m->perm.resize(d->nelems);
+        std::iota(m->perm.begin(), m->perm.end(), 0);
+        std::stable_sort(m->perm.begin(), m->perm.end(), [&](int64_t a, int64_t b) {
+            if (d->shape[a] != d->shape[b]) return d->shape[a] < d->shape[b];
+            return nq[a] < nq[b];
+        });
+        m->inv_perm.resize(d->nelems);
+        for (int64_t s = 0; s < d->nelems; s++) m->inv_perm[m->perm[s]] = s;
+        m->h_conn_ptr.resize(d->nelems + 1);
+        m->h_ip_ptr.resize(d->nelems + 1);
+        m->h_kel_ptr.resize(d->nelems + 1);
+        std::vector<int64_t> fel(d->nelems + 1);
+        m->h_shape.resize(d->nelems);
+        m->h_nips.resize(d->nelems);
+        std::vector<int32_t> mt(d->nelems);
+        std::vector<double> mp(8 * d->nelems);
+        m->h_conn_ptr[0] = m->h_ip_ptr[0] = m->h_kel_ptr[0] = fel[0] = 0;
+        m->h_conn.clear();
+        for (int64_t s = 0; s < d->nelems; s++) {
+            int64_t e = m->perm[s];
+            int np = amr::shape_npoints(d->shape[e]);
+            for (int64_t p = d->conn_ptr[e]; p < d->conn_ptr[e + 1]; p++) m->h_conn.push_back((int32_t)d->conn[p]);
+            m->h_conn_ptr[s + 1] = m->h_conn_ptr[s] + np;
+            m->h_ip_ptr[s + 1] = m->h_ip_ptr[s] + nq[e];
+            m->h_kel_ptr[s + 1] = m->h_kel_ptr[s] + (int64_t)np * np;
+            fel[s + 1] = fel[s] + (int64_t)np * d->ndim;
+            m->h_shape[s] = d->shape[e];
+            m->h_nips[s] = nq[e];
+            mt[s] = d->mat_type[e];
+            std::memcpy(&mp[8 * s], d->mat_params + 8 * e, 8 * sizeof(double));
+            if (s == 0 || m->groups.back().shape != d->shape[e] || m->groups.back().nip != nq[e]) {
+                AmrGroup g;
+                g.shape = d->shape[e]; g.nen = np; g.nip = nq[e]; g.first = s; g.count = 0;
+                g.epb = (np >= 20) ? 1 : (np >= 10 ? 4 : 6);
+                m->groups.push_back(g);
+            }
+            m->groups.back().count++;
+        }
+        m->nip_total = m->h_ip_ptr.back();
+        m->kel_blocks = m->h_kel_ptr.back();
+        cudaStream_t s = m->stream;
+        m->h_coords.assign(d->coords, d->coords + 3 * d->nnodes);
+        amr_alloc(&m->coords, 3 * d->nnodes);
+        upload(m->coords, d->coords, 3 * d->nnodes * sizeof(double), s);
+        amr_alloc(&m->conn, m->h_conn.size());
+        upload(m->conn, m->h_conn.data(), m->h_conn.size() * sizeof(int32_t), s);
+        amr_alloc(&m->conn_ptr, d->nelems + 1);
+        upload(m->conn_ptr, m->h_conn_ptr.data(), (d->nelems + 1) * sizeof(int64_t), s);
+        amr_alloc(&m->ip_ptr, d->nelems + 1);
+        upload(m->ip_ptr, m->h_ip_ptr.data(), (d->nelems + 1) * sizeof(int64_t), s);
+        amr_alloc(&m->kel_ptr, d->nelems + 1);
+        upload(m->kel_ptr, m->h_kel_ptr.data(), (d->nelems + 1) * sizeof(int64_t), s);
+        amr_alloc(&m->fel_ptr, d->nelems + 1);
+        upload(m->fel_ptr, fel.data(), (d->nelems + 1) * sizeof(int64_t), s);
+        amr_alloc(&m->mat_type, d->nelems);
+        upload(m->mat_type, mt.data(), d->nelems * sizeof(int32_t), s);
+        amr_alloc(&m->mat_par, 8 * d->nelems);
+        upload(m->mat_par, mp.data(), 8 * d->nelems * sizeof(double), s);
+        // per-group tables: dN/dR at the IPs, weights, N
+        for (AmrGroup &g : m->groups) {
+            double R[64 * 3], w[64];
+            amr::quadrature(g.shape, d->nips[m->perm[g.first]], R, w);
+            std::vector<double> tab((size_t)g.nip * g.nen * m->ndim + g.nip + (size_t)g.nip * g.nen);
+            for (int q = 0; q < g.nip; q++) {
+                amr::shape_deriv(g.shape, R + 3 * q, tab.data() + (size_t)q * g.nen * m->ndim);
+                tab[(size_t)g.nip * g.nen * m->ndim + q] = w[q];
+                amr::shape_func(g.shape, R + 3 * q, tab.data() + (size_t)g.nip * g.nen * m->ndim + g.nip + (size_t)q * g.nen);
+            }
+            amr_alloc(&g.tab, tab.size());
+            upload(g.tab, tab.data(), tab.size() * sizeof(double), s);
+            AMR_CUDA(cudaStreamSynchronize(s));
+        }
+        // pattern and contribution map
+        amr_build_pattern(m);
+        // values and states
+        amr_alloc(&m->Kel, (size_t)m->kel_blocks * m->BB);
+        amr_alloc(&m->K64, (size_t)m->nblocks * m->BB);
+        amr_alloc(&m->K32, (size_t)m->nblocks * m->BB);
+        amr_alloc(&m->keep, m->nblocks);
+        amr_alloc(&m->Minv32, (size_t)m->nnodes * m->BB);
+        amr_alloc(&m->Minv64, (size_t)m->nnodes * m->BB);
+        amr_alloc(&m->st, (size_t)AMR_NST * m->nip_total);
+        amr_alloc(&m->stbk, (size_t)AMR_NST * m->nip_total);
+        AMR_CUDA(cudaMemsetAsync(m->st, 0, (size_t)AMR_NST * m->nip_total * sizeof(double), s));
+        AMR_CUDA(cudaMemsetAsync(m->stbk, 0, (size_t)AMR_NST * m->nip_total * sizeof(double), s));
+        amr_alloc(&m->Fel, fel.back());
+        amr_alloc(&m->d_status, 2);
+        int32_t init[2] = {0, INT32_MAX};
+        upload(m->d_status, init, sizeof init, s);
+        AMR_CUDA(cudaMallocHost(&m->h_status, 2 * sizeof(int32_t)));
+        for (int i = 0; i < 8; i++) amr_alloc(&m->vtmp[i], m->nnodes * m->B);
+        amr_alloc(&m->eq_id, 3 * m->nnodes);
+        amr_alloc(&m->free_mask, m->nnodes * m->B);
+        AMR_CUDA(cudaStreamSynchronize(s));
+    } catch (const AmrError &e) {
+        g_create_error = e.msg;
+        amr_model_destroy(m);
+        return e.code;
+    } catch (const std::exception &e) {
+        g_create_error = e.what();
+        amr_model_destroy(m);
+        return AMR_EINVAL;
+    }
+    *out = m;
+    return AMR_OK;
+}
+
+int amr_model_destroy(amr_model *m) {
+    if (!m) return AMR_OK;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    amr_solver_free(m);
+    for (AmrGroup &g : m->groups) amr_free(g.tab);
+    amr_free(m->coords); amr_free(m->conn); amr_free(m->conn_ptr); amr_free(m->mat_type); amr_free(m->mat_par);
+    amr_free(m->ip_ptr); amr_free(m->kel_ptr); amr_free(m->inc_ptr); amr_free(m->inc); amr_free(m->brow_ptr);
+    amr_free(m->bcol); amr_free(m->contrib_ptr); amr_free(m->contrib); amr_free(m->Kel); amr_free(m->K64);
+    amr_free(m->K32); amr_free(m->keep); amr_free(m->Minv32); amr_free(m->Minv64); amr_free(m->eq_id);
+    amr_free(m->free_mask); amr_free(m->dof_node); amr_free(m->st); amr_free(m->stbk); amr_free(m->Fel);
+    amr_free(m->fel_ptr); amr_free(m->d_status);
+    for (int i = 0; i < 8; i++) amr_free(m->vtmp[i]);
+    if (m->h_status) cudaFreeHost(m->h_status);
+    if (m->ev0) cudaEventDestroy(m->ev0);
+    if (m->ev1) cudaEventDestroy(m->ev1);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return AMR_OK;
+}
+
+int amr_last_error(const amr_model *m, char *buf, size_t n) {
+    if (!m || !buf || n == 0) return AMR_EINVAL;
+    std::snprintf(buf, n, "%s", m->err.c_str());
+    return AMR_OK;
+}
+
+int amr_get_sizes(const amr_model *m, int64_t *nnodes, int64_t *nelems, int64_t *nip_total, int64_t *nblocks) {
+    if (!m) return AMR_EINVAL;
+    if (nnodes) *nnodes = m->nnodes;
+    if (nelems) *nelems = m->nelems;
+    if (nip_total) *nip_total = m->nip_total;
+    if (nblocks) *nblocks = m->nblocks;
+    return AMR_OK;
+}
+
+int amr_set_dofs(amr_model *m, const int64_t *eq_id, int64_t ndofs, int64_t nu) {
+    return guarded(m, [&] {
+        if (!eq_id || ndofs < 0 || nu < 0 || nu > ndofs) throw AmrError(AMR_EINVAL, "bad dof numbering");
+        std::vector<uint8_t> seen(ndofs, 0);
+        for (int64_t n = 0; n < m->nnodes; n++)
+            for (int c = 0; c < 3; c++) {
+                int64_t e = eq_id[3 * n + c];
+                if (c >= m->ndim) {
+                    if (e >= 0) throw AmrError(AMR_EINVAL, "eq_id set for a component beyond ndim");
+                    continue;
+                }
+                if (e < -1 || e >= ndofs) throw AmrError(AMR_EINVAL, "eq_id out of range");
+                if (e >= 0) {
+                    if (seen[e]) throw AmrError(AMR_EINVAL, "eq_id used twice");
+                    seen[e] = 1;
+                }
+            }
+        for (int64_t i = 0; i < ndofs; i++)
+            if (!seen[i]) throw AmrError(AMR_EINVAL, "eq_id numbering has gaps");
+        // every element node must carry all its DOFs
+        for (int32_t v : m->h_conn)
+            for (int c = 0; c < m->ndim; c++)
+                if (eq_id[3 * (int64_t)v + c] < 0) throw AmrError(AMR_EINVAL, "an element node has no DOF");
+        m->h_eq_id.assign(eq_id, eq_id + 3 * m->nnodes);
+        m->ndofs = ndofs;
+        m->nu = nu;
+        upload(m->eq_id, eq_id, 3 * m->nnodes * sizeof(int64_t), m->stream);
+        int64_t nt = m->nnodes * m->B;
+        k_free_mask<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->eq_id, nu, m->free_mask);
+        AMR_CUDA(cudaGetLastError());
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        m->dofs_set = true;
+        m->K_valid = false;
+        if (m->sw) amr_solver_free(m);  // the comparator CSR depends on the numbering
+        return AMR_OK;
+    });
+}
+
+int amr_set_youngs(amr_model *m, const double *E) {
+    return guarded(m, [&] {
+        std::vector<double> mp(8 * m->nelems);
+        AMR_CUDA(cudaMemcpy(mp.data(), m->mat_par, mp.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int64_t s = 0; s < m->nelems; s++) {
+            double v = E[m->perm[s]];
+            if (!(v > 0.0)) throw AmrError(AMR_EINVAL, "E must be > 0");
+            mp[8 * s] = v;
+        }
+        AMR_CUDA(cudaMemcpy(m->mat_par, mp.data(), mp.size() * sizeof(double), cudaMemcpyHostToDevice));
+        m->K_valid = false;
+        return AMR_OK;
+    });
+}
+
+int amr_assemble_K(amr_model *m) {
+    return guarded(m, [&] {
+        assemble(m);
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        return AMR_OK;
+    });
+}
+
+// Host export of K in the reference layout (CSC over eq_id order, eps drop rule)
+static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t *rowval, double *nzval) {
+    if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+    int B = m->B, BB = m->BB;
+    std::vector<uint16_t> keep(m->nblocks);
+    AMR_CUDA(cudaMemcpy(keep.data(), m->keep, m->nblocks * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    std::vector<double> K;
+    if (nzval) {
+        K.resize((size_t)m->nblocks * BB);
+        AMR_CUDA(cudaMemcpy(K.data(), m->K64, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    const std::vector<int64_t> &eq = m->h_eq_id;
+    // count per column (= per row of the symmetric pattern walk)
+    std::vector<int64_t> cnt(m->ndofs + 1, 0);
+    for (int64_t n = 0; n < m->nnodes; n++)
+        for (int64_t k = m->h_brow_ptr[n]; k < m->h_brow_ptr[n + 1]; k++) {
+            int64_t j = m->h_bcol[k];
+            for (int c = 0; c < B; c++) {
+                int64_t r = eq[3 * n + c];
+                if (r < 0) continue;
+                for (int d = 0; d < B; d++) {
+                    int64_t col = eq[3 * j + d];
+                    if (col < 0 || !(keep[k] >> (c * B + d) & 1)) continue;
+                    cnt[col + 1]++;
+                }
+            }
+        }
+    for (int64_t i = 0; i < m->ndofs; i++) cnt[i + 1] += cnt[i];
+    *nnz_out = cnt[m->ndofs];
+    if (!colptr) return;
+    std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+    for (int64_t n = 0; n < m->nnodes; n++)
+        for (int64_t k = m->h_brow_ptr[n]; k < m->h_brow_ptr[n + 1]; k++) {
+            int64_t j = m->h_bcol[k];
+            for (int c = 0; c < B; c++) {
+                int64_t r = eq[3 * n + c];
+                if (r < 0) continue;
+                for (int d = 0; d < B; d++) {
+                    int64_t col = eq[3 * j + d];
+                    if (col < 0 || !(keep[k] >> (c * B + d) & 1)) continue;
+                    int64_t p = pos[col]++;
+                    rowval[p] = r;
+                    if (nzval) nzval[p] = K[(size_t)(c * B + d) * m->nblocks + k];
+                }
+            }
+        }
+    for (int64_t i = 0; i <= m->ndofs; i++) colptr[i] = cnt[i];
+    // sort rows within each column
+    std::vector<std::pair<int64_t, double>> tmp;
+    for (int64_t col = 0; col < m->ndofs; col++) {
+        int64_t a = cnt[col], b = cnt[col + 1];
+        tmp.resize(b - a);
+        for (int64_t p = a; p < b; p++) tmp[p - a] = {rowval[p], nzval ? nzval[p] : 0.0};
+        std::sort(tmp.begin(), tmp.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+        for (int64_t p = a; p < b; p++) {
+            rowval[p] = tmp[p - a].first;
+            if (nzval) nzval[p] = tmp[p - a].second;
+        }
+    }
+}
+
+int amr_get_K_nnz(amr_model *m, int64_t *nnz) {
+    return guarded(m, [&] {
+        export_csc(m, nnz, nullptr, nullptr, nullptr);
+        return AMR_OK;
+    });
+}
+
+int amr_get_K_csc(amr_model *m, int64_t *colptr, int64_t *rowval, double *nzval) {
+    return guarded(m, [&] {
+        int64_t nnz = 0;
+        export_csc(m, &nnz, colptr, rowval, nzval);
+        return AMR_OK;
+    });
+}
+
+int amr_update_state(amr_model *m, const double *dU, double *dFin) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        double *u = m->vtmp[0], *f = m->vtmp[1];
+        eq_host_to_nm(m, dU, u);
+        amr_update_elements(m, u, f);
+        int rc = amr_check_status(m);
+        if (rc == AMR_ERETMAP) throw AmrError(rc, "VonMises: return mapping failed in cell " + std::to_string(m->perm[m->h_status[1]] + 1));
+        if (rc == AMR_ENAN) throw AmrError(rc, "solve_system!: NaN values in internal forces vector");
+        if (rc) throw AmrError(rc, "update_state failed");
+        nm_to_eq_host(m, f, dFin);
+        return AMR_OK;
+    });
+}
+
+int amr_state_commit(amr_model *m) {
+    return guarded(m, [&] {
+        AMR_CUDA(cudaMemcpyAsync(m->stbk, m->st, (size_t)AMR_NST * m->nip_total * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, m->stream));
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        return AMR_OK;
+    });
+}
+
+int amr_state_restore(amr_model *m) {
+    return guarded(m, [&] {
+        AMR_CUDA(cudaMemcpyAsync(m->st, m->stbk, (size_t)AMR_NST * m->nip_total * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, m->stream));
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        if (m->any_plastic) m->K_valid = false;
+        return AMR_OK;
+    });
+}
+
+int amr_get_state(amr_model *m, double *state) {
+    return guarded(m, [&] {
+        std::vector<double> st((size_t)AMR_NST * m->nip_total);
+        AMR_CUDA(cudaMemcpy(st.data(), m->st, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        int64_t o = 0;
+        for (int64_t e = 0; e < m->nelems; e++) {
+            int64_t s = m->inv_perm[e];
+            for (int64_t g = m->h_ip_ptr[s]; g < m->h_ip_ptr[s + 1]; g++, o++) {
+                for (int f = 0; f < 16; f++) state[16 * o + f] = f < AMR_NST ? st[(size_t)f * m->nip_total + g] : 0.0;
+            }
+        }
+        return AMR_OK;
+    });
+}
+
+int amr_assemble_loads(amr_model *m, const amr_load *loads, int32_t nloads, double t, double *F) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        double *f = m->vtmp[0];
+        eq_host_to_nm(m, F, f);
+        amr_loads(m, loads, nloads, t, f);
+        nm_to_eq_host(m, f, F);
+        return AMR_OK;
+    });
+}
+
+int amr_solve(amr_model *m, double *U, double *F, const amr_solve_opts *opts, amr_solve_stats *stats) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+        amr_solve_opts o;
+        amr_default_solve_opts(&o);
+        if (opts) o = *opts;
+        double *x = m->vtmp[0], *b = m->vtmp[1], *reac = m->vtmp[2];
+        eq_host_to_nm(m, U, x);
+        vec(m, V_MASK_PRESC, 1.0, x, 0.0, nullptr, x);  // free slots start at 0
+        eq_host_to_nm(m, F, b);
+        AMR_CUDA(cudaMemsetAsync(reac, 0, m->nnodes * m->B * sizeof(double), m->stream));
+        AmrSolveResult r = amr_solve_device(m, x, b, reac, o);
+        if (stats) {
+            stats->iterations = r.iterations;
+            stats->refinements = r.refinements;
+            stats->rel_residual = r.rel_residual;
+            stats->seconds = r.seconds;
+        }
+        if (r.status) throw AmrError(r.status, "solve_system!: Krylov solver did not converge (relative residual " + std::to_string(r.rel_residual) + ")");
+        double umax = amr_norm_inf(m, x, m->free_mask);
+        if (std::isnan(umax) || std::isinf(umax)) throw AmrError(AMR_ENAN, "solve_system!: NaN values in the solution");
+        if (umax > 1e8) throw AmrError(AMR_ESINGULAR, "solve_system!: Possible syngular matrix");
+        std::vector<double> xs(m->ndofs), rs(m->ndofs);
+        nm_to_eq_host(m, x, xs.data());
+        nm_to_eq_host(m, reac, rs.data());
+        for (int64_t i = 0; i < m->nu; i++) U[i] = xs[i];
+        for (int64_t i = m->nu; i < m->ndofs; i++) F[i] = rs[i];
+        return AMR_OK;
+    });
+}
+
+int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params *p, double *U, double *F,
+                  amr_stage_stats *stats) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        amr_stage_params prm;
+        amr_default_stage_params(&prm);
+        if (p) prm = *p;
+        int64_t n = m->nnodes * m->B;
+        double *uex, *fex, *u, *f;
+        amr_alloc(&uex, n); amr_alloc(&fex, n); amr_alloc(&u, n); amr_alloc(&f, n);
+        int rc;
+        try {
+            eq_host_to_nm(m, Uex, uex);
+            eq_host_to_nm(m, Fex, fex);
+            rc = amr_stage_device(m, uex, fex, prm, u, f, stats);
+            if (rc == AMR_OK || rc == AMR_ESTAGE) {
+                nm_to_eq_host(m, u, U);
+                nm_to_eq_host(m, f, F);
+            }
+        } catch (...) {
+            amr_free(uex); amr_free(fex); amr_free(u); amr_free(f);
+            throw;
+        }
+        amr_free(uex); amr_free(fex); amr_free(u); amr_free(f);
+        return rc;
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// mech_stage_solver! (src/mech/mech-solver.jl:186-492), device vectors
+// ---------------------------------------------------------------------------
+int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params &p, double *U,
+                     double *F, amr_stage_stats *stats) {
+    int64_t n = m->nnodes * m->B;
+    cudaStream_t s = m->stream;
+    if (p.scheme != AMR_SCHEME_FE) throw AmrError(AMR_EUNSUPPORTED, "only the FE predictor scheme is on the GPU path");
+    if (p.maxits < 1 || p.nincs < 1) throw AmrError(AMR_EINVAL, "bad stage parameters");
+    std::vector<double *> v(10, nullptr);
+    for (auto &x : v) amr_alloc(&x, n);
+    double *R = v[0], *dUa = v[1], *dUi = v[2], *Rc = v[3], *dFin = v[4], *dFex = v[5], *dUitr = v[6], *Rtr = v[7],
+           *reac = v[8], *dUt = v[9];
+    auto release = [&]() {
+        for (auto &x : v) amr_free(x);
+    };
+    int status = AMR_OK;
+    amr_stage_stats st{};
+    try {
+        for (double *x : {U, F, R, dUa, dUi, Rc, dFin}) AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+        double tol = p.tol, rtol = p.rtol, dTmin = p.dTmin;
+        bool autoinc = p.autoinc != 0;
+        bool saveouts = p.nouts > 0;
+        int nincs = p.nincs;
+        if (saveouts && !autoinc) {  // src/solver.jl:128-140
+            if (p.nouts > nincs) nincs = p.nouts;
+            if (nincs % p.nouts != 0) nincs = nincs - (nincs % p.nouts) + p.nouts;
+        }
+        double dTcheck = saveouts ? 1.0 / p.nouts : 1.0, Tcheck = dTcheck;
+        double T = 0.0, dT = 1.0 / nincs, dTbk = 0.0;
+        if (autoinc) dT = std::min({dT, p.dTmax, dTcheck, p.dT0});
+        const double p1 = 1.0, q11 = 1.0;
+        // committed states = current states at stage start
+        AMR_CUDA(cudaMemcpyAsync(m->stbk, m->st, (size_t)AMR_NST * m->nip_total * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
+        const double eps = 2.220446049250313e-16;
+        while (T < 1.0 - dTmin) {
+            // dUex, dFex (+ carried residue)
+            double dTcr = std::min(p.rspan, 1 - T);
+            double acr = std::min(dT / dTcr, 1.0);
+            vec(m, V_SET_AXPBY, dT, Fex, (T < 1 - p.rspan) ? acr : 0.0, Rc, dFex);
+            AMR_CUDA(cudaMemcpyAsync(R, dFex, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            AMR_CUDA(cudaMemsetAsync(dUa, 0, n * sizeof(double), s));
+            vec(m, V_SET_AXPBY, dT, Uex, 0.0, nullptr, dUi);
+            double res = 0.0, res1 = 0.0, err = 0.0;
+            bool converged = false, syserror = false, still_linear = true;
+            std::string sysmsg;
+            int nits = 0;
+            for (int it = 1; it <= p.maxits; it++) {
+                nits++;
+                if (it > 1) AMR_CUDA(cudaMemsetAsync(dUi, 0, n * sizeof(double), s));
+                double lastres = res;
+                if (m->any_plastic || !m->K_valid) assemble(m);
+                // predictor solve: x = p1 dUi at prescribed slots, b = q11 R
+                vec(m, V_MASK_PRESC, p1, dUi, 0.0, nullptr, dUitr);
+                vec(m, V_SET_AXPBY, q11, R, 0.0, nullptr, Rtr);
+                AmrSolveResult sr = amr_solve_device(m, dUitr, Rtr, reac, p.linear);
+                st.krylov_iterations += sr.iterations;
+                if (sr.status) { syserror = true; sysmsg = "solve_system!: Krylov solver did not converge"; break; }
+                double umax = amr_norm_inf(m, dUitr, m->free_mask);
+                if (!(umax <= 1e8)) { syserror = true; sysmsg = "solve_system!: Possible syngular matrix"; break; }
+                // restore states (update reads the committed copy) and update
+                vec(m, V_SET_AXPBY, 1.0, dUa, 1.0, dUitr, dUt);
+                amr_update_elements(m, dUt, dFin);
+                int rc = amr_check_status(m);
+                if (rc) { syserror = true; sysmsg = rc == AMR_ERETMAP ? "return mapping failed" : "NaN values in internal forces vector"; break; }
+                AMR_CUDA(cudaMemcpyAsync(dUi, dUitr, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+                vec(m, V_SET_AXPBY, 1.0, dUa, 1.0, dUi, dUa);
+                vec(m, V_SET_AXPBY, 1.0, dFex, -1.0, dFin, R);
+                vec(m, V_MASK_FREE, 1.0, R, 0.0, nullptr, R);
+                res = amr_norm_inf(m, R, nullptr);
+                double nui = amr_norm_inf(m, dUi, nullptr), nua = amr_norm_inf(m, dUa, nullptr);
+                err = nui / nua;
+                st.iterations++;
+                if (it == 1) res1 = res;
+                if (it > 1) still_linear = false;
+                if (res < tol) { converged = true; break; }
+                if (err < rtol) { converged = true; break; }
+                if (std::isnan(res)) break;
+                if (it > 1 && res > lastres) break;
+            }
+            (void)still_linear;
+            if (syserror) converged = false;
+            st.residue = res;
+            if (converged) {
+                vec(m, V_SET_AXPBY, 1.0, U, 1.0, dUa, U);
+                vec(m, V_SET_AXPBY, 1.0, F, 1.0, dFin, F);
+                vec(m, V_SET_AXPBY, 1.0 - acr, Rc, 1.0, R, Rc);
+                AMR_CUDA(cudaMemcpyAsync(m->stbk, m->st, (size_t)AMR_NST * m->nip_total * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, s));
+                T += dT;
+                st.increments++;
+                bool checkpoint = T > Tcheck - dTmin;
+                if (checkpoint) Tcheck += dTcheck;
+                if (autoinc) {
+                    if (dTbk > 0.0) {
+                        dT = std::min(dTbk, Tcheck - T);
+                        dTbk = 0.0;
+                    } else {
+                        double q = 1 + std::tanh(std::log10(tol / (res1 + eps)));
+                        q = std::max(q, 1.1);
+                        double dTtr = std::min({q * dT, p.dTmax, 1 - T});
+                        if (T + dTtr > Tcheck - dTmin) {
+                            dTbk = dT;
+                            dT = Tcheck - T;
+                        } else {
+                            dT = dTtr;
+                            dTbk = 0.0;
+                        }
+                    }
+                }
+            } else {
+                AMR_CUDA(cudaMemcpyAsync(m->st, m->stbk, (size_t)AMR_NST * m->nip_total * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, s));
+                if (m->any_plastic) m->K_valid = false;
+                if (autoinc) {
+                    double q = 1 + std::tanh(std::log10(tol / (res1 + eps)));
+                    q = std::min(std::max(q, 0.2), 0.9);
+                    if (syserror) q = 0.7;
+                    dT = round_sig3(q * dT);
+                    if (dT < dTmin) { status = AMR_ESTAGE; m->err = "Solver did not converge."; break; }
+                } else {
+                    status = AMR_ESTAGE;
+                    m->err = syserror ? sysmsg : "Solver did not converge. Try `autoinc=true`. ";
+                    break;
+                }
+            }
+        }
+        st.T = T;
+        st.status = status;
+        AMR_CUDA(cudaStreamSynchronize(s));
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+    if (stats) *stats = st;
+    return status;
+}

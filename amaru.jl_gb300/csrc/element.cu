@@ -1,0 +1,874 @@
+// Element kernels of the mechanical hot path (FP64), sm_103a.
+//
+//  * stiffness_kernel   -- elem_stiffness (src/mech/elem/mech-solid.jl:124-166)
+//  * gather_kernel      -- the duplicate summation of mount_K / sparse()
+//                          (src/mech/mech-solver.jl:78-110), deterministic, no atomics
+//  * internal_kernel    -- update_elem! + update_state!(mat, ...) (mech-solid.jl:243-279,
+//                          src/mech/mat/{linear-elastic,von-mises,drucker-prager}.jl)
+//  * node_gather_kernel -- the dFin[map] .+= dF accumulation (mech-solver.jl:124-144)
+//  * load kernels       -- mech_boundary_forces / mech_solid_body_forces
+//                          (src/mech/elem/distributed.jl:76-217)
+//
+// Every material of the path has a tangent of the form D = De(lambda, mu) - gamma m m^T
+// (isotropic elastic part plus a symmetric rank-one plastic correction), so the
+// element stiffness is assembled per node pair (a, b) as
+//     K_ab = lambda T_ab + mu T_ab^T + mu tr(T_ab) I - P_ab,
+//     T_ab = sum_ip w_ip g_a g_b^T,   P_ab = sum_ip w_ip gamma_ip (S g_a)(S g_b)^T,
+// with g = dN/dX at the IP, w_ip = detJ * weight * thickness and S the symmetric
+// tensor of m.  This is B^T D B written without the zeros of B.
+#include <cfloat>
+#include <cmath>
+
+#include "amr_internal.h"
+
+#define SQ2 1.4142135623730951
+#define ISQ2 0.70710678118654752
+
+namespace {
+
+struct GroupArgs {
+    const double *tab;  // [nip][nen*dim] dNdR, [nip] w, [nip][nen] N
+    int nip;
+    int64_t first, count;
+};
+
+struct ModelArgs {
+    const double *coords;
+    const int32_t *conn;
+    const int64_t *conn_ptr;
+    const int32_t *mat_type;
+    const double *mat_par;
+    const int64_t *ip_ptr;
+    const int64_t *kel_ptr;
+    const int64_t *fel_ptr;
+    int64_t nip_total;
+    int stressmodel;
+    double thickness;
+};
+
+__device__ __forceinline__ void set_status(int32_t *st, int code, int64_t elem) {
+    atomicCAS(&st[0], 0, code);
+    atomicMin(&st[1], (int32_t)(elem < INT32_MAX ? elem : INT32_MAX));
+}
+
+// Lame constants of De (plane stress uses lambda* = E nu / (1 - nu^2))
+__device__ __forceinline__ void lame(double E, double nu, bool ps, double &lam, double &mu) {
+    mu = E / (2.0 * (1.0 + nu));
+    lam = ps ? E * nu / (1.0 - nu * nu) : E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+}
+
+// y = De x (Mandel, 6 components); plane stress has a zero zz row/column
+__device__ __forceinline__ void De_mul(double lam, double mu, bool ps, const double *x, double *y) {
+    if (ps) {
+        double t = lam * (x[0] + x[1]);
+        y[0] = t + 2.0 * mu * x[0]; y[1] = t + 2.0 * mu * x[1]; y[2] = 0.0;
+    } else {
+        double t = lam * (x[0] + x[1] + x[2]);
+        y[0] = t + 2.0 * mu * x[0]; y[1] = t + 2.0 * mu * x[1]; y[2] = t + 2.0 * mu * x[2];
+    }
+    y[3] = 2.0 * mu * x[3]; y[4] = 2.0 * mu * x[4]; y[5] = 2.0 * mu * x[5];
+}
+
+// J2 and dev in Mandel notation (src/tools/tensors.jl:4-27)
+__device__ __forceinline__ double J2(const double *s) {
+    double t23 = s[3] * ISQ2, t13 = s[4] * ISQ2, t12 = s[5] * ISQ2;
+    double a = s[0] - s[1], b = s[1] - s[2], c = s[2] - s[0];
+    return (a * a + b * b + c * c) / 6.0 + t23 * t23 + t13 * t13 + t12 * t12;
+}
+__device__ __forceinline__ void dev(const double *t, double *s) {
+    double p = (t[0] + t[1] + t[2]) / 3.0;
+    s[0] = t[0] - p; s[1] = t[1] - p; s[2] = t[2] - p; s[3] = t[3]; s[4] = t[4]; s[5] = t[5];
+}
+__device__ __forceinline__ double norm6(const double *v) {
+    return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+}
+
+// Rank-one plastic part of the tangent: D = De - gamma m m^T.  Returns gamma (0 if elastic).
+__device__ double plastic_tangent(int mtype, const double *par, bool ps, const double *sig, double epa, double dl,
+                                  double lam, double mu, double *m) {
+    if (mtype == AMR_LINEAR_ELASTIC || dl == 0.0) return 0.0;
+    if (mtype == AMR_VON_MISES) {
+        double fy = par[2], H = par[3];
+        double a[6];
+        if (!ps) {  // von-mises.jl:112-126: a = sqrt(1.5) s/|s|, den = a.De.a + sqrt(1.5) H
+            double s[6];
+            dev(sig, s);
+            double ns = norm6(s);
+            for (int i = 0; i < 6; i++) a[i] = sqrt(1.5) * s[i] / ns;
+            De_mul(lam, mu, false, a, m);
+            double den = 0.0;
+            for (int i = 0; i < 6; i++) den += a[i] * m[i];
+            return 1.0 / (den + sqrt(1.5) * H);
+        }
+        // plane stress (von-mises.jl:187-198)
+        a[0] = 2.0 / 3.0 * sig[0] - 1.0 / 3.0 * sig[1];
+        a[1] = 2.0 / 3.0 * sig[1] - 1.0 / 3.0 * sig[0];
+        a[2] = -1.0 / 3.0 * sig[0] - 1.0 / 3.0 * sig[1];
+        a[3] = sig[3]; a[4] = sig[4]; a[5] = sig[5];
+        double dfdep = -2.0 / 3.0 * H * (fy + H * epa);
+        De_mul(lam, mu, true, a, m);
+        double den = 0.0;
+        for (int i = 0; i < 6; i++) den += a[i] * m[i];
+        return 1.0 / (den - norm6(a) * dfdep);
+    }
+    // Drucker-Prager (drucker-prager.jl:86-109): D = De - (De Nu)(De V)^T / (V.De.Nu + H), Nu = V/|V|
+    double alpha = par[2], H = par[4];
+    double V[6];
+    double nv;
+    if (J2(sig) != 0.0) {
+        double s[6];
+        dev(sig, s);
+        double ns = norm6(s);
+        for (int i = 0; i < 6; i++) V[i] = (i < 3 ? alpha : 0.0) + (s[i] / ns) * ISQ2;
+        nv = norm6(V);
+    } else {
+        for (int i = 0; i < 6; i++) V[i] = (i < 3) ? 1.0 / sqrt(3.0) : 0.0;
+        nv = 1.0;
+    }
+    De_mul(lam, mu, ps, V, m);
+    double VDV = 0.0;
+    for (int i = 0; i < 6; i++) VDV += V[i] * m[i];
+    return 1.0 / (VDV + nv * H);  // = 1 / (|V| (V.De.Nu + H))
+}
+
+// Plane-stress von Mises stress for a given dlambda (von-mises.jl:306-333)
+__device__ void vm_ps_sigma(double E, double nu, double epa0, const double *str, double dl, double *sig, double *epa) {
+    double G = E / (2 * (1 + nu));
+    double den = E * E * dl * dl - 2 * E * nu * dl + 4 * E * dl - 3 * nu * nu + 3;
+    double m11 = (2 * E * dl - E * nu * dl - 3 * nu * nu + 3) / den;
+    double m12 = (E * dl - 2 * E * nu * dl) / den;
+    double m66 = 1 / (2 * G * dl + 1);
+    sig[0] = m11 * str[0] + m12 * str[1];
+    sig[1] = m12 * str[0] + m11 * str[1];
+    sig[2] = 0.0;
+    sig[3] = m66 * str[3]; sig[4] = m66 * str[4]; sig[5] = m66 * str[5];
+    double d[6] = {2.0 / 3.0 * sig[0] - 1.0 / 3.0 * sig[1], 2.0 / 3.0 * sig[1] - 1.0 / 3.0 * sig[0],
+                   -1.0 / 3.0 * sig[0] - 1.0 / 3.0 * sig[1], sig[3], sig[4], sig[5]};
+    *epa = epa0 + dl * norm6(d);
+}
+__device__ __forceinline__ double vm_ps_yield(double fy, double H, const double *sig, double epa) {
+    double k = fy + H * epa;
+    return J2(sig) - k * k / 3.0;
+}
+
+// Constitutive update of one IP: st0 (committed, 14 fields) -> st1 (trial), returns dsig.
+// 0 on success, AMR_ERETMAP on failure.
+__device__ int material_update(int mtype, const double *par, bool ps, const double *st0, double *st1, const double *de,
+                               double *dsig) {
+    double E = par[0], nu = par[1], lam, mu;
+    lame(E, nu, ps, lam, mu);
+    double sig0[6], str[6], t[6];
+    for (int i = 0; i < 6; i++) sig0[i] = st0[i];
+    De_mul(lam, mu, ps, de, t);
+    for (int i = 0; i < 6; i++) str[i] = sig0[i] + t[i];
+    double epa = st0[AMR_ST_EPA], dl = st0[AMR_ST_DL];
+    double sig[6];
+    if (mtype == AMR_LINEAR_ELASTIC) {
+        for (int i = 0; i < 6; i++) sig[i] = str[i];
+    } else if (mtype == AMR_VON_MISES && !ps) {  // von-mises.jl:128-157
+        double fy = par[2], H = par[3];
+        double j2 = J2(str);
+        double ftr = sqrt(3.0 * j2) - fy - H * epa;
+        if (ftr < 1e-8) {
+            dl = 0.0;
+            for (int i = 0; i < 6; i++) sig[i] = str[i];
+        } else {
+            double G = E / (2 * (1 + nu));
+            dl = ftr / (3 * G + sqrt(1.5) * H);
+            if (!(sqrt(j2) - dl * sqrt(3.0) * G >= 0.0)) return AMR_ERETMAP;
+            double s[6];
+            dev(str, s);
+            double f = 1 - sqrt(3.0) * G * dl / sqrt(j2);
+            for (int i = 0; i < 6; i++) s[i] *= f;
+            double ns = norm6(s);
+            for (int i = 0; i < 6; i++) sig[i] = str[i] - sqrt(6.0) * G * dl * s[i] / ns;
+            epa += dl;
+        }
+    } else if (mtype == AMR_VON_MISES) {  // plane stress, bisection (von-mises.jl:200-303)
+        double fy = par[2], H = par[3];
+        double ftr = vm_ps_yield(fy, H, str, epa);
+        if (ftr < 1e-8) {
+            dl = 0.0;
+            for (int i = 0; i < 6; i++) sig[i] = str[i];
+        } else {
+            double dfds[6] = {2.0 / 3.0 * str[0] - 1.0 / 3.0 * str[1], 2.0 / 3.0 * str[1] - 1.0 / 3.0 * str[0],
+                              -1.0 / 3.0 * str[0] - 1.0 / 3.0 * str[1], str[3], str[4], str[5]};
+            double Dd[6], dd[6];
+            De_mul(lam, mu, true, dfds, Dd);
+            for (int i = 0; i < 6; i++) dd[i] = str[i] - sig0[i];
+            double dl0 = norm6(dd) / norm6(Dd);
+            double a = 0.0, b = dl0, sg[6], ep, fa, fb, f = 0.0;
+            vm_ps_sigma(E, nu, epa, str, a, sg, &ep);
+            fa = vm_ps_yield(fy, H, sg, ep);
+            vm_ps_sigma(E, nu, epa, str, b, sg, &ep);
+            fb = vm_ps_yield(fy, H, sg, ep);
+            if (fa * fb > 0) {
+                bool found = false;
+                double g = 1.0;
+                for (int i = 1; i <= 50; i++) {
+                    g *= 1.6;
+                    b += dl0 * g;
+                    vm_ps_sigma(E, nu, epa, str, b, sg, &ep);
+                    fb = vm_ps_yield(fy, H, sg, ep);
+                    if (fa * fb < 0.0) { found = true; break; }
+                }
+                if (!found) return AMR_ERETMAP;
+            }
+            double s0[6] = {0, 0, 0, 0, 0, 0};
+            double tol = pow(10.0, -(10.0 - log10(fy)));
+            bool done = false;
+            for (int i = 1; i <= 50; i++) {
+                dl = 0.5 * (a + b);
+                vm_ps_sigma(E, nu, epa, str, dl, sg, &ep);
+                f = vm_ps_yield(fy, H, sg, ep);
+                if (fa * f < 0) b = dl;
+                else { a = dl; fa = f; }
+                double mx = 0.0;
+                for (int k = 0; k < 6; k++) mx = fmax(mx, fabs(sg[k] - s0[k]));
+                if (mx <= tol) { done = true; break; }
+                for (int k = 0; k < 6; k++) s0[k] = sg[k];
+            }
+            if (!done) return AMR_ERETMAP;
+            for (int i = 0; i < 6; i++) sig[i] = sg[i];
+            epa = ep;
+        }
+    } else {  // Drucker-Prager (drucker-prager.jl:112-149)
+        double alpha = par[2], kappa = par[3], H = par[4];
+        double j1 = str[0] + str[1] + str[2];
+        double j2 = J2(str);
+        double ftr = alpha * j1 + sqrt(j2) - kappa - H * epa;
+        if (ftr < 1.e-8) {
+            dl = 0.0;
+            for (int i = 0; i < 6; i++) sig[i] = str[i];
+        } else {
+            double K = E / (3.0 * (1.0 - 2.0 * nu)), G = E / (2.0 * (1.0 + nu));
+            double n = 1.0 / sqrt(3.0 * alpha * alpha + 0.5);
+            if (sqrt(j2) - dl * n * G > 0.0) {  // uses the committed dgamma, as the reference does
+                dl = ftr / (9 * alpha * alpha * n * K + n * G + H);
+                double jj1 = j1 - 9 * dl * alpha * n * K;
+                double mm = 1.0 - dl * n * G / sqrt(j2);
+                double d[6];
+                dev(str, d);
+                for (int i = 0; i < 6; i++) sig[i] = mm * d[i] + (i < 3 ? jj1 / 3.0 : 0.0);
+            } else {
+                dl = (alpha * j1 - kappa - H * epa) / (3 * sqrt(3.0) * alpha * K + H);
+                double jj1 = j1 - 3 * sqrt(3.0) * dl * K;
+                for (int i = 0; i < 6; i++) sig[i] = (i < 3 ? jj1 / 3.0 : 0.0);
+            }
+            epa += dl;
+        }
+    }
+    for (int i = 0; i < 6; i++) {
+        st1[i] = sig[i];
+        st1[6 + i] = st0[6 + i] + de[i];
+        dsig[i] = sig[i] - sig0[i];
+    }
+    st1[AMR_ST_EPA] = epa;
+    st1[AMR_ST_DL] = dl;
+    return 0;
+}
+
+// Geometry at one IP: g = dN/dX (nen x DIM) and detJ from coordinates C (nen x DIM)
+template <int DIM>
+__device__ __forceinline__ double ip_geometry(int nen, const double *dNdR, const double *C, double *g) {
+    double J[DIM * DIM];
+#pragma unroll
+    for (int q = 0; q < DIM * DIM; q++) J[q] = 0.0;
+    for (int i = 0; i < nen; i++)
+#pragma unroll
+        for (int a = 0; a < DIM; a++)
+#pragma unroll
+            for (int b = 0; b < DIM; b++) J[a * DIM + b] += C[i * DIM + a] * dNdR[i * DIM + b];
+    double det, iJ[DIM * DIM];
+    if (DIM == 2) {
+        det = J[0] * J[3] - J[1] * J[2];
+        double r = 1.0 / det;
+        iJ[0] = J[3] * r; iJ[1] = -J[1] * r; iJ[2] = -J[2] * r; iJ[3] = J[0] * r;
+    } else {
+        double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[5] * J[6] - J[3] * J[8], c2 = J[3] * J[7] - J[4] * J[6];
+        det = J[0] * c0 + J[1] * c1 + J[2] * c2;
+        double r = 1.0 / det;
+        iJ[0] = c0 * r; iJ[1] = (J[2] * J[7] - J[1] * J[8]) * r; iJ[2] = (J[1] * J[5] - J[2] * J[4]) * r;
+        iJ[3] = c1 * r; iJ[4] = (J[0] * J[8] - J[2] * J[6]) * r; iJ[5] = (J[2] * J[3] - J[0] * J[5]) * r;
+        iJ[6] = c2 * r; iJ[7] = (J[1] * J[6] - J[0] * J[7]) * r; iJ[8] = (J[0] * J[4] - J[1] * J[3]) * r;
+    }
+    for (int i = 0; i < nen; i++)
+#pragma unroll
+        for (int b = 0; b < DIM; b++) {
+            double s = 0.0;
+#pragma unroll
+            for (int a = 0; a < DIM; a++) s += dNdR[i * DIM + a] * iJ[a * DIM + b];
+            g[i * DIM + b] = s;
+        }
+    return det;
+}
+
+// S(m) g : the symmetric tensor of Mandel vector m applied to g (= B_a^T m)
+template <int DIM>
+__device__ __forceinline__ void sym_apply(const double *m, const double *g, double *v) {
+    if (DIM == 3) {
+        v[0] = m[0] * g[0] + m[5] * ISQ2 * g[1] + m[4] * ISQ2 * g[2];
+        v[1] = m[5] * ISQ2 * g[0] + m[1] * g[1] + m[3] * ISQ2 * g[2];
+        v[2] = m[4] * ISQ2 * g[0] + m[3] * ISQ2 * g[1] + m[2] * g[2];
+    } else {
+        v[0] = m[0] * g[0] + m[5] * ISQ2 * g[1];
+        v[1] = m[5] * ISQ2 * g[0] + m[1] * g[1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stiffness: EPB elements per CTA.  Phase 1: thread per (element, IP) builds
+// g, w and the plastic vectors in shared memory.  Phase 2: thread per
+// (element, node pair a<=b) accumulates T_ab / P_ab over the IPs and writes
+// the two element blocks (a,b), (b,a) to the staging array.
+// ---------------------------------------------------------------------------
+template <int DIM, int NEN>
+__global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G, int epb, double *Kel,
+                                                        const double *st, int32_t *status) {
+    constexpr int NP = NEN * (NEN + 1) / 2;
+    constexpr int BB = DIM * DIM;
+    extern __shared__ double sm[];
+    const int nip = G.nip;
+    double *sC = sm;                              // epb x NEN*DIM
+    double *sG = sC + epb * NEN * DIM;            // epb x nip x NEN*DIM
+    double *sV = sG + epb * nip * NEN * DIM;      // epb x nip x NEN*DIM (plastic vectors)
+    double *sW = sV + epb * nip * NEN * DIM;      // epb x nip
+    double *sGam = sW + epb * nip;                // epb x nip
+    __shared__ int sPl[8];                        // per element: any plastic IP
+
+    const int64_t e0 = G.first + (int64_t)blockIdx.x * epb;
+    const int ne = (int)min((int64_t)epb, G.first + G.count - e0);
+    const double *dNdR = G.tab;
+    const double *wq = G.tab + nip * NEN * DIM;
+    const bool ps = (M.stressmodel == AMR_PLANESTRESS);
+
+    for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
+        int el = t / (NEN * DIM), q = t % (NEN * DIM);
+        int32_t node = M.conn[M.conn_ptr[e0 + el] + q / DIM];
+        sC[t] = M.coords[3 * (int64_t)node + q % DIM];
+    }
+    if (threadIdx.x < epb) sPl[threadIdx.x] = 0;
+    __syncthreads();
+
+    for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
+        int el = t / nip, ip = t % nip;
+        int64_t e = e0 + el;
+        double *g = sG + (el * nip + ip) * NEN * DIM;
+        double det = ip_geometry<DIM>(NEN, dNdR + ip * NEN * DIM, sC + el * NEN * DIM, g);
+        if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
+        double th = M.thickness;
+        double w = det * wq[ip] * th;
+        sW[el * nip + ip] = w;
+        const double *par = M.mat_par + 8 * e;
+        int64_t gi = M.ip_ptr[e] + ip;
+        double sig[6];
+        for (int i = 0; i < 6; i++) sig[i] = st[i * M.nip_total + gi];
+        double lam, mu, m[6];
+        lame(par[0], par[1], ps, lam, mu);
+        double gam = plastic_tangent(M.mat_type[e], par, ps, sig, st[AMR_ST_EPA * M.nip_total + gi],
+                                     st[AMR_ST_DL * M.nip_total + gi], lam, mu, m);
+        sGam[el * nip + ip] = gam * w;
+        if (gam != 0.0) {
+            sPl[el] = 1;
+            double *v = sV + (el * nip + ip) * NEN * DIM;
+            for (int a = 0; a < NEN; a++) sym_apply<DIM>(m, g + a * DIM, v + a * DIM);
+        }
+    }
+    __syncthreads();
+
+    for (int t = threadIdx.x; t < ne * NP; t += blockDim.x) {
+        int el = t / NP, p = t % NP;
+        int a = 0, rem = p;
+        while (rem >= NEN - a) { rem -= NEN - a; a++; }
+        int b = a + rem;
+        int64_t e = e0 + el;
+        double T[BB], P[BB];
+#pragma unroll
+        for (int q = 0; q < BB; q++) { T[q] = 0.0; P[q] = 0.0; }
+        const double *gbase = sG + el * nip * NEN * DIM;
+        for (int ip = 0; ip < nip; ip++) {
+            const double *ga = gbase + ip * NEN * DIM + a * DIM;
+            const double *gb = gbase + ip * NEN * DIM + b * DIM;
+            double w = sW[el * nip + ip];
+            double wa[DIM];
+#pragma unroll
+            for (int i = 0; i < DIM; i++) wa[i] = w * ga[i];
+#pragma unroll
+            for (int i = 0; i < DIM; i++)
+#pragma unroll
+                for (int j = 0; j < DIM; j++) T[i * DIM + j] = fma(wa[i], gb[j], T[i * DIM + j]);
+        }
+        if (sPl[el]) {
+            const double *vbase = sV + el * nip * NEN * DIM;
+            for (int ip = 0; ip < nip; ip++) {
+                double gm = sGam[el * nip + ip];
+                if (gm == 0.0) continue;
+                const double *va = vbase + ip * NEN * DIM + a * DIM;
+                const double *vb = vbase + ip * NEN * DIM + b * DIM;
+#pragma unroll
+                for (int i = 0; i < DIM; i++) {
+                    double x = gm * va[i];
+#pragma unroll
+                    for (int j = 0; j < DIM; j++) P[i * DIM + j] = fma(x, vb[j], P[i * DIM + j]);
+                }
+            }
+        }
+        const double *par = M.mat_par + 8 * e;
+        double lam, mu;
+        lame(par[0], par[1], ps, lam, mu);
+        double tr = 0.0;
+#pragma unroll
+        for (int i = 0; i < DIM; i++) tr += T[i * DIM + i];
+        double K[BB];
+#pragma unroll
+        for (int i = 0; i < DIM; i++)
+#pragma unroll
+            for (int j = 0; j < DIM; j++)
+                K[i * DIM + j] = lam * T[i * DIM + j] + mu * T[j * DIM + i] + (i == j ? mu * tr : 0.0) - P[i * DIM + j];
+        int64_t base = M.kel_ptr[e];
+        double *o1 = Kel + (base + (int64_t)a * NEN + b) * BB;
+#pragma unroll
+        for (int q = 0; q < BB; q++) o1[q] = K[q];
+        if (a != b) {
+            double *o2 = Kel + (base + (int64_t)b * NEN + a) * BB;
+#pragma unroll
+            for (int i = 0; i < DIM; i++)
+#pragma unroll
+                for (int j = 0; j < DIM; j++) o2[j * DIM + i] = K[i * DIM + j];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gather: warp per node row, lane per nonzero block.  Contributions are summed
+// in element order skipping |Ke_ij| < eps() (the mount_K drop rule); the keep
+// bits record which scalar entries the reference's sparse() would store.
+// Also writes the Dirichlet-masked FP32 copy and the block-Jacobi inverses.
+// ---------------------------------------------------------------------------
+template <int B>
+__device__ void invert_block(const double *A, double *X) {
+    if (B == 2) {
+        double d = A[0] * A[3] - A[1] * A[2];
+        X[0] = A[3] / d; X[1] = -A[1] / d; X[2] = -A[2] / d; X[3] = A[0] / d;
+    } else {
+        double c0 = A[4] * A[8] - A[5] * A[7], c1 = A[5] * A[6] - A[3] * A[8], c2 = A[3] * A[7] - A[4] * A[6];
+        double d = A[0] * c0 + A[1] * c1 + A[2] * c2;
+        X[0] = c0 / d; X[1] = (A[2] * A[7] - A[1] * A[8]) / d; X[2] = (A[1] * A[5] - A[2] * A[4]) / d;
+        X[3] = c1 / d; X[4] = (A[0] * A[8] - A[2] * A[6]) / d; X[5] = (A[2] * A[3] - A[0] * A[5]) / d;
+        X[6] = c2 / d; X[7] = (A[1] * A[6] - A[0] * A[7]) / d; X[8] = (A[0] * A[4] - A[1] * A[3]) / d;
+    }
+}
+
+template <int B>
+__global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *brow_ptr, const int32_t *bcol,
+                              const int64_t *contrib_ptr, const int64_t *contrib, const double *Kel,
+                              const uint8_t *free_mask, double *K64, float *K32, uint16_t *keep, float *Minv32,
+                              double *Minv64, int32_t *status) {
+    constexpr int BB = B * B;
+    int lane = threadIdx.x & 31;
+    int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= nnodes) return;
+    uint8_t fr[B];
+#pragma unroll
+    for (int c = 0; c < B; c++) fr[c] = free_mask ? free_mask[n * B + c] : 1;
+    for (int64_t k = brow_ptr[n] + lane; k < brow_ptr[n + 1]; k += 32) {
+        double v[BB];
+#pragma unroll
+        for (int q = 0; q < BB; q++) v[q] = 0.0;
+        unsigned kb = 0;
+        for (int64_t c = contrib_ptr[k]; c < contrib_ptr[k + 1]; c++) {
+            const double *src = Kel + contrib[c] * BB;
+#pragma unroll
+            for (int q = 0; q < BB; q++) {
+                double x = src[q];
+                if (fabs(x) >= DBL_EPSILON) { v[q] += x; kb |= 1u << q; }
+            }
+        }
+        int32_t j = bcol[k];
+        bool nan = false;
+#pragma unroll
+        for (int q = 0; q < BB; q++) {
+            K64[(int64_t)q * nblocks + k] = v[q];
+            nan |= isnan(v[q]);
+        }
+        if (nan) set_status(status, AMR_ENAN, -1);
+        if (keep) keep[k] = (uint16_t)kb;
+        if (K32 || Minv32) {
+            uint8_t fc[B];
+#pragma unroll
+            for (int d = 0; d < B; d++) fc[d] = free_mask ? free_mask[(int64_t)j * B + d] : 1;
+            double mk[BB];
+#pragma unroll
+            for (int c = 0; c < B; c++)
+#pragma unroll
+                for (int d = 0; d < B; d++) {
+                    double x = (fr[c] && fc[d]) ? v[c * B + d] : 0.0;
+                    if (j == n && c == d && !fr[c]) x = 1.0;
+                    mk[c * B + d] = x;
+                }
+            if (K32)
+#pragma unroll
+                for (int q = 0; q < BB; q++) K32[(int64_t)q * nblocks + k] = (float)mk[q];
+            if (j == n) {
+                double X[BB];
+                invert_block<B>(mk, X);
+#pragma unroll
+                for (int q = 0; q < BB; q++) {
+                    if (Minv32) Minv32[n * BB + q] = (float)X[q];
+                    if (Minv64) Minv64[n * BB + q] = X[q];
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Internal forces with the constitutive update: thread per (element, IP).
+// ---------------------------------------------------------------------------
+template <int DIM, int NEN>
+__global__ void __launch_bounds__(256) internal_kernel(ModelArgs M, GroupArgs G, int epb, const double *dU,
+                                                       const double *stbk, double *st, double *Fel, int32_t *status) {
+    extern __shared__ double sm[];
+    const int nip = G.nip;
+    double *sC = sm;                          // epb x NEN*DIM
+    double *sU = sC + epb * NEN * DIM;        // epb x NEN*DIM
+    double *sF = sU + epb * NEN * DIM;        // epb x nip x NEN*DIM
+    const int64_t e0 = G.first + (int64_t)blockIdx.x * epb;
+    const int ne = (int)min((int64_t)epb, G.first + G.count - e0);
+    const double *dNdR = G.tab;
+    const double *wq = G.tab + nip * NEN * DIM;
+    const bool ps = (M.stressmodel == AMR_PLANESTRESS);
+    for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
+        int el = t / (NEN * DIM), q = t % (NEN * DIM);
+        int64_t node = M.conn[M.conn_ptr[e0 + el] + q / DIM];
+        sC[t] = M.coords[3 * node + q % DIM];
+        sU[t] = dU[node * DIM + q % DIM];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
+        int el = t / nip, ip = t % nip;
+        int64_t e = e0 + el;
+        double g[NEN * DIM];
+        double det = ip_geometry<DIM>(NEN, dNdR + ip * NEN * DIM, sC + el * NEN * DIM, g);
+        const double *u = sU + el * NEN * DIM;
+        double de[6] = {0, 0, 0, 0, 0, 0};
+        for (int a = 0; a < NEN; a++) {
+            const double *ga = g + a * DIM;
+            const double *ua = u + a * DIM;
+            if (DIM == 3) {
+                de[0] += ga[0] * ua[0];
+                de[1] += ga[1] * ua[1];
+                de[2] += ga[2] * ua[2];
+                de[3] += (ga[2] * ua[1] + ga[1] * ua[2]) * ISQ2;
+                de[4] += (ga[2] * ua[0] + ga[0] * ua[2]) * ISQ2;
+                de[5] += (ga[1] * ua[0] + ga[0] * ua[1]) * ISQ2;
+            } else {
+                de[0] += ga[0] * ua[0];
+                de[1] += ga[1] * ua[1];
+                de[5] += (ga[1] * ua[0] + ga[0] * ua[1]) * ISQ2;
+            }
+        }
+        int64_t gi = M.ip_ptr[e] + ip;
+        double s0[AMR_NST], s1[AMR_NST], ds[6];
+        for (int f = 0; f < AMR_NST; f++) s0[f] = stbk[f * M.nip_total + gi];
+        int rc = material_update(M.mat_type[e], M.mat_par + 8 * e, ps, s0, s1, de, ds);
+        if (rc) {
+            set_status(status, rc, e);
+            for (int f = 0; f < AMR_NST; f++) s1[f] = s0[f];
+            for (int i = 0; i < 6; i++) ds[i] = 0.0;
+        }
+        for (int f = 0; f < AMR_NST; f++) st[f * M.nip_total + gi] = s1[f];
+        double coef = det * wq[ip] * M.thickness;
+        double *fo = sF + (el * nip + ip) * NEN * DIM;
+        for (int a = 0; a < NEN; a++) {
+            double v[DIM];
+            sym_apply<DIM>(ds, g + a * DIM, v);
+#pragma unroll
+            for (int c = 0; c < DIM; c++) fo[a * DIM + c] = coef * v[c];
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
+        int el = t / (NEN * DIM), q = t % (NEN * DIM);
+        double s = 0.0;
+        for (int ip = 0; ip < nip; ip++) s += sF[(el * nip + ip) * NEN * DIM + q];
+        Fel[M.fel_ptr[e0 + el] + q] = s;
+    }
+}
+
+// dFin[node] = sum over incident (element, local) in element order
+__global__ void node_gather_kernel(int64_t nnodes, int B, const int64_t *inc_ptr, const int64_t *inc,
+                                   const int64_t *conn_ptr, const int64_t *fel_ptr, const double *Fel, double *out,
+                                   int accumulate, int32_t *status) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t n = t / B;
+    int c = (int)(t % B);
+    double s = 0.0;
+    for (int64_t q = inc_ptr[n]; q < inc_ptr[n + 1]; q++) {
+        int64_t e = inc[q] >> 8;
+        int a = (int)(inc[q] & 0xff);
+        s += Fel[fel_ptr[e] + a * B + c];
+    }
+    if (isnan(s)) set_status(status, AMR_ENAN, -1);
+    out[t] = accumulate ? out[t] + s : s;
+}
+
+// ---------------------------------------------------------------------------
+// Distributed loads on facets / bodies: thread per item, staging per
+// (item, local node, component); gathered per node in item order.
+// tab: [nq][np*fd] dN/dR, [nq] w, [nq][np] N.
+// ---------------------------------------------------------------------------
+__global__ void load_kernel(int kind, int dir, int edge_key, int np, int fd, int nq, const double *tab,
+                            const int64_t *items, int64_t nitems, const int32_t *conn, const int64_t *conn_ptr,
+                            const int64_t *inv_perm, const double *coords, int ndim, int stressmodel,
+                            double thickness, const double *cf, double t, double *Fst) {
+    int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nitems) return;
+    double C[AMR_MAXN * 3];
+    for (int a = 0; a < np; a++) {
+        int64_t node;
+        if (kind == AMR_LOAD_FACET) node = items[it * np + a];
+        else node = conn[conn_ptr[inv_perm[items[it]]] + a];
+        for (int k = 0; k < ndim; k++) C[a * ndim + k] = coords[3 * node + k];
+    }
+    double F[AMR_MAXN * 3];
+    for (int q = 0; q < np * ndim; q++) F[q] = 0.0;
+    const double *Dt = tab, *W = tab + nq * np * fd, *Nt = W + nq;
+    for (int q = 0; q < nq; q++) {
+        const double *D = Dt + q * np * fd;
+        const double *N = Nt + q * np;
+        double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, X[3] = {0, 0, 0};
+        for (int a = 0; a < np; a++) {
+            for (int k = 0; k < ndim; k++) {
+                X[k] += C[a * ndim + k] * N[a];
+                for (int l = 0; l < fd; l++) J[k * fd + l] += C[a * ndim + k] * D[a * fd + l];
+            }
+        }
+        double val = cf[0] + cf[1] * X[0] + cf[2] * X[1] + (ndim == 3 ? cf[3] * X[2] : 0.0) + cf[4] * t;
+        double Q[3] = {0, 0, 0};
+        double jn;  // norm2(J) (src/tools/linalg.jl:50-72)
+        if (fd == ndim) {
+            jn = (ndim == 2) ? J[0] * J[3] - J[1] * J[2]
+                             : J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                                   J[2] * (J[3] * J[7] - J[4] * J[6]);
+        } else if (fd == 1) {
+            double s = 0.0;
+            for (int k = 0; k < ndim; k++) s += J[k] * J[k];
+            jn = sqrt(s);
+        } else {  // 3 x 2
+            double j1 = J[0] * J[3] - J[1] * J[2], j2 = J[0] * J[5] - J[1] * J[4], j3 = J[2] * J[5] - J[3] * J[4];
+            jn = sqrt(j1 * j1 + j2 * j2 + j3 * j3);
+        }
+        if (dir < 3) {
+            Q[dir] = val;
+        } else {
+            double nv[3];
+            if (ndim == 2) { nv[0] = J[1]; nv[1] = -J[0]; nv[2] = 0.0; }
+            else {
+                nv[0] = J[2] * J[5] - J[4] * J[3];
+                nv[1] = J[4] * J[1] - J[0] * J[5];
+                nv[2] = J[0] * J[3] - J[2] * J[1];
+            }
+            double ln = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+            for (int k = 0; k < ndim; k++) Q[k] = val * nv[k] / ln;
+        }
+        double th = (kind == AMR_LOAD_FACET && edge_key) ? 1.0 : thickness;
+        double coef = jn * W[q] * th;
+        for (int a = 0; a < np; a++)
+            for (int k = 0; k < ndim; k++) F[a * ndim + k] += coef * N[a] * Q[k];
+    }
+    for (int q = 0; q < np * ndim; q++) Fst[it * np * ndim + q] = F[q];
+}
+
+__global__ void load_gather_kernel(int64_t nnodes, int B, const int64_t *ptr, const int64_t *lst, int np,
+                                   const double *Fst, double *F) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t n = t / B;
+    int c = (int)(t % B);
+    if (ptr[n] == ptr[n + 1]) return;
+    double s = 0.0;
+    for (int64_t q = ptr[n]; q < ptr[n + 1]; q++) s += Fst[(lst[q] / np * np + lst[q] % np) * B + c];
+    F[t] += s;
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+ModelArgs margs(amr_model *m) {
+    ModelArgs a;
+    a.coords = m->coords; a.conn = m->conn; a.conn_ptr = m->conn_ptr; a.mat_type = m->mat_type;
+    a.mat_par = m->mat_par; a.ip_ptr = m->ip_ptr; a.kel_ptr = m->kel_ptr; a.fel_ptr = m->fel_ptr;
+    a.nip_total = m->nip_total; a.stressmodel = m->stressmodel; a.thickness = m->thickness;
+    return a;
+}
+
+template <int DIM, int NEN>
+void launch_stiff(amr_model *m, const AmrGroup &g) {
+    GroupArgs ga{g.tab, g.nip, g.first, g.count};
+    int epb = g.epb;
+    size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + 2 * g.nip * NEN * DIM + 2 * g.nip);
+    constexpr int NP = NEN * (NEN + 1) / 2;
+    int threads = epb * NP;
+    threads = ((threads + 31) / 32) * 32;
+    if (threads > 256) threads = 256;
+    if (smem > 48 * 1024) AMR_CUDA(cudaFuncSetAttribute(stiffness_kernel<DIM, NEN>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    unsigned grid = nblk(g.count, epb);
+    stiffness_kernel<DIM, NEN><<<grid, threads, smem, m->stream>>>(margs(m), ga, epb, m->Kel, m->st, m->d_status);
+    AMR_CUDA(cudaGetLastError());
+}
+
+template <int DIM, int NEN>
+void launch_internal(amr_model *m, const AmrGroup &g, const double *dU) {
+    GroupArgs ga{g.tab, g.nip, g.first, g.count};
+    int epb = (g.nip * 1 >= 16) ? 4 : 16;
+    size_t smem = sizeof(double) * (size_t)epb * (2 * NEN * DIM + g.nip * NEN * DIM);
+    int threads = std::max(epb * g.nip, epb * NEN * DIM);
+    threads = ((threads + 31) / 32) * 32;
+    if (threads > 256) threads = 256;
+    if (smem > 48 * 1024) AMR_CUDA(cudaFuncSetAttribute(internal_kernel<DIM, NEN>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    unsigned grid = nblk(g.count, epb);
+    internal_kernel<DIM, NEN><<<grid, threads, smem, m->stream>>>(margs(m), ga, epb, dU, m->stbk, m->st, m->Fel,
+                                                                  m->d_status);
+    AMR_CUDA(cudaGetLastError());
+}
+
+template <typename F3, typename F2>
+void dispatch(amr_model *m, const AmrGroup &g, F3 f3, F2 f2) {
+    switch (g.shape) {
+    case AMR_HEX8: f3(std::integral_constant<int, 8>()); break;
+    case AMR_HEX20: f3(std::integral_constant<int, 20>()); break;
+    case AMR_TET4: f3(std::integral_constant<int, 4>()); break;
+    case AMR_TET10: f3(std::integral_constant<int, 10>()); break;
+    case AMR_TRI3: f2(std::integral_constant<int, 3>()); break;
+    case AMR_TRI6: f2(std::integral_constant<int, 6>()); break;
+    case AMR_QUAD4: f2(std::integral_constant<int, 4>()); break;
+    case AMR_QUAD8: f2(std::integral_constant<int, 8>()); break;
+    case AMR_QUAD9: f2(std::integral_constant<int, 9>()); break;
+    default: throw AmrError(AMR_EUNSUPPORTED, "shape not supported on the GPU path");
+    }
+}
+
+}  // namespace
+
+int amr_check_status(amr_model *m) {
+    AMR_CUDA(cudaMemcpyAsync(m->h_status, m->d_status, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    int code = m->h_status[0];
+    if (code) {
+        int32_t reset[2] = {0, INT32_MAX};
+        AMR_CUDA(cudaMemcpy(m->d_status, reset, sizeof reset, cudaMemcpyHostToDevice));
+    }
+    return code;
+}
+
+void amr_stiffness(amr_model *m) {
+    for (const AmrGroup &g : m->groups) {
+        dispatch(
+            m, g, [&](auto n) { launch_stiff<3, decltype(n)::value>(m, g); },
+            [&](auto n) { launch_stiff<2, decltype(n)::value>(m, g); });
+    }
+    unsigned grid = nblk(m->nnodes * 32, 256);
+    if (m->B == 3)
+        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
+                                                      m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
+                                                      m->Minv32, m->Minv64, m->d_status);
+    else
+        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
+                                                      m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
+                                                      m->Minv32, m->Minv64, m->d_status);
+    AMR_CUDA(cudaGetLastError());
+}
+
+void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm) {
+    for (const AmrGroup &g : m->groups) {
+        dispatch(
+            m, g, [&](auto n) { launch_internal<3, decltype(n)::value>(m, g, dU_nm); },
+            [&](auto n) { launch_internal<2, decltype(n)::value>(m, g, dU_nm); });
+    }
+    int64_t nt = m->nnodes * m->B;
+    node_gather_kernel<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->inc_ptr, m->inc, m->conn_ptr,
+                                                             m->fel_ptr, m->Fel, dFin_nm, 0, m->d_status);
+    AMR_CUDA(cudaGetLastError());
+}
+
+void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double *F_nm) {
+    for (int l = 0; l < nloads; l++) {
+        const amr_load &L = loads[l];
+        if (L.nitems <= 0) continue;
+        int np, fd, shape;
+        std::vector<int64_t> nodes;  // per (item, local) node ids for the incidence
+        if (L.kind == AMR_LOAD_FACET) {
+            shape = L.facet_shape;
+            np = amr::shape_npoints(shape);
+            fd = amr::shape_ndim(shape);
+            if (np <= 0) throw AmrError(AMR_EINVAL, "bad facet shape");
+            nodes.assign(L.items, L.items + L.nitems * np);
+        } else {
+            int64_t e0 = L.items[0];
+            if (e0 < 0 || e0 >= m->nelems) throw AmrError(AMR_EINVAL, "bad element id in body load");
+            shape = m->h_shape[m->inv_perm[e0]];
+            np = amr::shape_npoints(shape);
+            fd = amr::shape_ndim(shape);
+            nodes.resize(L.nitems * np);
+            for (int64_t i = 0; i < L.nitems; i++) {
+                int64_t e = L.items[i];
+                if (e < 0 || e >= m->nelems) throw AmrError(AMR_EINVAL, "bad element id in body load");
+                int64_t s = m->inv_perm[e];
+                if (m->h_shape[s] != shape) throw AmrError(AMR_EUNSUPPORTED, "body load over mixed shapes");
+                for (int a = 0; a < np; a++) nodes[i * np + a] = m->h_conn[m->h_conn_ptr[s] + a];
+            }
+        }
+        if (L.dir < 0 || L.dir > 3 || (L.dir == 2 && m->ndim == 2)) throw AmrError(AMR_EINVAL, "bad load direction");
+        for (int64_t v : nodes)
+            if (v < 0 || v >= m->nnodes) throw AmrError(AMR_EINVAL, "bad node id in load");
+        // quadrature table of the facet / element default rule
+        double R[64 * 3], w[64];
+        int nq = amr::quadrature(shape, 0, R, w);
+        std::vector<double> tab((size_t)nq * np * fd + nq + (size_t)nq * np);
+        for (int q = 0; q < nq; q++) {
+            amr::shape_deriv(shape, R + 3 * q, tab.data() + (size_t)q * np * fd);
+            tab[(size_t)nq * np * fd + q] = w[q];
+            amr::shape_func(shape, R + 3 * q, tab.data() + (size_t)nq * np * fd + nq + (size_t)q * np);
+        }
+        // host incidence node -> (item*np + local), in item order (counting sort)
+        std::vector<int64_t> ptr(m->nnodes + 1, 0), lst(nodes.size());
+        for (int64_t v : nodes) ptr[v + 1]++;
+        for (int64_t i = 0; i < m->nnodes; i++) ptr[i + 1] += ptr[i];
+        {
+            std::vector<int64_t> pos(ptr.begin(), ptr.end() - 1);
+            for (int64_t q = 0; q < (int64_t)nodes.size(); q++) lst[pos[nodes[q]]++] = q;
+        }
+        double *dtab, *dcf, *Fst;
+        int64_t *ditems, *dptr, *dlst;
+        amr_alloc(&dtab, tab.size());
+        amr_alloc(&dcf, 5);
+        amr_alloc(&Fst, (size_t)L.nitems * np * m->B);
+        amr_alloc(&ditems, (size_t)L.nitems * (L.kind == AMR_LOAD_FACET ? np : 1));
+        amr_alloc(&dptr, ptr.size());
+        amr_alloc(&dlst, lst.size());
+        cudaStream_t s = m->stream;
+        AMR_CUDA(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        AMR_CUDA(cudaMemcpyAsync(dcf, L.coef, 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+        AMR_CUDA(cudaMemcpyAsync(ditems, L.items, (size_t)L.nitems * (L.kind == AMR_LOAD_FACET ? np : 1) * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice, s));
+        AMR_CUDA(cudaMemcpyAsync(dptr, ptr.data(), ptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        AMR_CUDA(cudaMemcpyAsync(dlst, lst.data(), lst.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        int64_t *dinv = nullptr;
+        if (L.kind == AMR_LOAD_BODY) {
+            amr_alloc(&dinv, m->nelems);
+            AMR_CUDA(cudaMemcpyAsync(dinv, m->inv_perm.data(), m->nelems * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        }
+        load_kernel<<<nblk(L.nitems, 128), 128, 0, s>>>(L.kind, L.dir, L.edge_key, np, fd, nq, dtab, ditems, L.nitems,
+                                                        m->conn, m->conn_ptr, dinv, m->coords, m->ndim,
+                                                        m->stressmodel, m->thickness, dcf, t, Fst);
+        int64_t nt = m->nnodes * m->B;
+        load_gather_kernel<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, m->B, dptr, dlst, np, Fst, F_nm);
+        AMR_CUDA(cudaGetLastError());
+        AMR_CUDA(cudaStreamSynchronize(s));
+        amr_free(dtab); amr_free(dcf); amr_free(Fst); amr_free(ditems); amr_free(dptr); amr_free(dlst);
+        amr_free(dinv);
+    }
+}

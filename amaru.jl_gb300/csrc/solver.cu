@@ -1,0 +1,737 @@
+// Linear solve of the Newton corrector, K11 U1 = F1 - K12 U2 (solve_system!,
+// src/solver.jl:5-79), on the device.
+//
+// AMR_SOLVER_MIXED: preconditioned CG whose SpMV, block-Jacobi preconditioner
+//   and vector updates run in FP32 over the node-block (BSR) matrix K32 with
+//   Dirichlet rows/columns masked; every `refine_every` iterations the FP64
+//   true residual r = b - K64 u is recomputed from the FP64 matrix, the FP32
+//   correction is folded into the FP64 solution and the recursive residual is
+//   replaced (iterative refinement by reliable updates; the search direction
+//   is kept).  Convergence is decided on the FP64 true residual only.
+// AMR_SOLVER_FP64: the plain all-FP64 comparator: scalar CSR of K11 in eq_id
+//   order, Jacobi-preconditioned CG, all vectors FP64.
+//
+// Scalars (alpha, beta, norms) live in a device control block; each kernel's
+// last CTA reduces the per-CTA partials in a fixed order, so results are
+// bitwise reproducible run to run.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+#include "amr_internal.h"
+
+namespace {
+
+struct Ctl {
+    double rz, pq, alpha, beta, rr, rr_true, bnorm2;
+    int32_t stop, converged, breakdown, pad;
+    unsigned int ticket[4];
+};
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-wide sum of up to 2 values, fixed order; result valid in thread 0
+template <int NV>
+__device__ void block_sum(double (&v)[NV], double (*sh)[kThreads / 32]) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        double x = warp_sum(v[i]);
+        if (lane == 0) sh[i][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            double x = (lane < (int)(blockDim.x >> 5)) ? sh[i][lane] : 0.0;
+            v[i] = warp_sum(x);
+        }
+    }
+    __syncthreads();
+}
+
+// Writes this CTA's partials; returns true in the last CTA to finish, which then
+// holds the fixed-order totals in tot[] (all threads).
+template <int NV>
+__device__ bool grid_sum(double (&v)[NV], double *partials, unsigned int *ticket, double (&tot)[NV]) {
+    __shared__ double sh[NV][kThreads / 32];
+    __shared__ bool last;
+    block_sum<NV>(v, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) partials[i * gridDim.x + blockIdx.x] = v[i];
+        __threadfence();
+        unsigned int t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        acc[i] = 0.0;
+        for (unsigned j = threadIdx.x; j < gridDim.x; j += blockDim.x)
+            acc[i] += ((volatile double *)partials)[i * gridDim.x + j];
+    }
+    block_sum<NV>(acc, sh);
+    __shared__ double res[NV];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) res[i] = acc[i];
+        *ticket = 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; i++) tot[i] = res[i];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed path kernels (BSR, B x B blocks, SoA values [BB][nblocks])
+// ---------------------------------------------------------------------------
+// p_new = z + beta p_old (own rows), q = K32 p_new, pq = p_new . q
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_spmv32(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
+                                                     const int32_t *__restrict__ cj, const float *__restrict__ A,
+                                                     const float *__restrict__ z, const float *__restrict__ pold,
+                                                     float *__restrict__ pnew, float *__restrict__ q, Ctl *ctl,
+                                                     double *partials) {
+    if (ctl->stop) return;
+    const float beta = (float)ctl->beta;
+    int lane = threadIdx.x & 31;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (int64_t n = warp; n < nn; n += nw) {
+        float acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0f;
+        for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
+            int64_t j = cj[k];
+            float pj[B];
+#pragma unroll
+            for (int d = 0; d < B; d++) pj[d] = fmaf(beta, pold[j * B + d], z[j * B + d]);
+#pragma unroll
+            for (int c = 0; c < B; c++)
+#pragma unroll
+                for (int d = 0; d < B; d++) acc[c] = fmaf(A[(int64_t)(c * B + d) * nb + k], pj[d], acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = warp_sumf(acc[c]);
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                float pn = fmaf(beta, pold[n * B + c], z[n * B + c]);
+                pnew[n * B + c] = pn;
+                q[n * B + c] = acc[c];
+                dot += (double)pn * (double)acc[c];
+            }
+        }
+    }
+    double v[1] = {dot}, tot[1];
+    if (grid_sum<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
+        ctl->pq = tot[0];
+        if (!(tot[0] > 0.0)) { ctl->breakdown = 1; ctl->stop = 1; }
+        else ctl->alpha = ctl->rz / tot[0];
+    }
+}
+
+// x += alpha p ; r -= alpha q ; z = Minv r ; rz, rr partials ; beta
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *__restrict__ Minv,
+                                                       const float *__restrict__ p, const float *__restrict__ q,
+                                                       float *__restrict__ x, float *__restrict__ r,
+                                                       float *__restrict__ z, Ctl *ctl, double *partials,
+                                                       double stop_rr) {
+    if (ctl->stop) return;
+    const float alpha = (float)ctl->alpha;
+    double rz = 0.0, rr = 0.0;
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        float rv[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            x[n * B + c] = fmaf(alpha, p[n * B + c], x[n * B + c]);
+            rv[c] = fmaf(-alpha, q[n * B + c], r[n * B + c]);
+            r[n * B + c] = rv[c];
+        }
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            float s = 0.0f;
+#pragma unroll
+            for (int d = 0; d < B; d++) s = fmaf(Minv[n * B * B + c * B + d], rv[d], s);
+            z[n * B + c] = s;
+            rz += (double)rv[c] * (double)s;
+            rr += (double)rv[c] * (double)rv[c];
+        }
+    }
+    double v[2] = {rz, rr}, tot[2];
+    if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
+        ctl->beta = tot[0] / ctl->rz;
+        ctl->rz = tot[0];
+        ctl->rr = tot[1];
+        if (!(tot[1] > stop_rr)) ctl->stop = 1;  // recursive residual small (or NaN): refresh now
+    }
+}
+
+// FP64 true residual: u64 += x32 (free slots), x32 = 0; r64 = mask(b - K64 u64);
+// reac = (K64 u64) at prescribed slots; r32 = r64; z = Minv r32 ; rz, |r64|^2
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_refine(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
+                                                     const int32_t *__restrict__ cj, const double *__restrict__ A,
+                                                     const uint8_t *__restrict__ fmask, const double *__restrict__ b,
+                                                     const double *__restrict__ u64, double *__restrict__ reac,
+                                                     float *__restrict__ r32, float *__restrict__ z,
+                                                     const float *__restrict__ Minv, Ctl *ctl, double *partials,
+                                                     int first, double tol2) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double rz = 0.0, rr = 0.0;
+    for (int64_t n = warp; n < nn; n += nw) {
+        double acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0;
+        for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
+            int64_t j = cj[k];
+#pragma unroll
+            for (int c = 0; c < B; c++)
+#pragma unroll
+                for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u64[j * B + d], acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = warp_sum(acc[c]);
+        if (lane == 0) {
+            float rv[B];
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                double res = 0.0;
+                if (fmask[n * B + c]) res = b[n * B + c] - acc[c];
+                else if (reac) reac[n * B + c] = acc[c];
+                rv[c] = (float)res;
+                r32[n * B + c] = rv[c];
+                rr += res * res;
+            }
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                float s = 0.0f;
+#pragma unroll
+                for (int d = 0; d < B; d++) s = fmaf(Minv[n * B * B + c * B + d], rv[d], s);
+                z[n * B + c] = s;
+                rz += (double)rv[c] * (double)s;
+            }
+        }
+    }
+    double v[2] = {rz, rr}, tot[2];
+    if (grid_sum<2>(v, partials, &ctl->ticket[2], tot) && threadIdx.x == 0) {
+        ctl->rz = tot[0];
+        ctl->rr_true = tot[1];
+        ctl->rr = tot[1];
+        if (first) ctl->bnorm2 = tot[1];
+        double ref = first ? tot[1] : ctl->bnorm2;
+        ctl->converged = (tot[1] <= tol2 * ref) ? 1 : 0;
+        ctl->stop = ctl->converged;
+        if (isnan(tot[1])) { ctl->breakdown = 1; ctl->stop = 1; }
+    }
+}
+
+// u64 += x32 at free slots; x32 = 0
+template <int B>
+__global__ void k_fold(int64_t n, const uint8_t *fmask, float *x32, double *u64) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * B) return;
+    if (fmask[i]) u64[i] += (double)x32[i];
+    x32[i] = 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP64 comparator: CSR over free eq ids, Jacobi PCG
+// ---------------------------------------------------------------------------
+__global__ void k_csr_count(int64_t nnodes, int B, const int64_t *rp, const int32_t *cj, const int64_t *eq_id,
+                            int64_t nu, int64_t *rowcnt) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t n = t / B;
+    int c = (int)(t % B);
+    int64_t row = eq_id[n * 3 + c];
+    if (row < 0 || row >= nu) return;
+    int64_t cnt = 0;
+    for (int64_t k = rp[n]; k < rp[n + 1]; k++) {
+        int64_t m = cj[k];
+        for (int d = 0; d < B; d++) {
+            int64_t col = eq_id[m * 3 + d];
+            cnt += (col >= 0 && col < nu);
+        }
+    }
+    rowcnt[row] = cnt;
+}
+
+__global__ void k_csr_fill(int64_t nnodes, int B, const int64_t *rp, const int32_t *cj, const int64_t *eq_id,
+                           int64_t nu, int64_t nb, const int64_t *crp, int32_t *ccol, int64_t *csrc) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t n = t / B;
+    int c = (int)(t % B);
+    int64_t row = eq_id[n * 3 + c];
+    if (row < 0 || row >= nu) return;
+    int64_t o = crp[row];
+    for (int64_t k = rp[n]; k < rp[n + 1]; k++) {
+        int64_t m = cj[k];
+        for (int d = 0; d < B; d++) {
+            int64_t col = eq_id[m * 3 + d];
+            if (col >= 0 && col < nu) {
+                ccol[o] = (int32_t)col;
+                csrc[o] = (int64_t)(c * B + d) * nb + k;
+                o++;
+            }
+        }
+    }
+}
+
+__global__ void k_csr_values(int64_t nnz, const int64_t *src, const double *K64, double *val) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nnz) val[i] = K64[src[i]];
+}
+
+__global__ void k_csr_diag(int64_t nu, const int64_t *crp, const int32_t *ccol, const double *val, double *dinv) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nu) return;
+    double d = 0.0;
+    for (int64_t k = crp[i]; k < crp[i + 1]; k++)
+        if (ccol[k] == i) d += val[k];
+    dinv[i] = 1.0 / d;
+}
+
+// p = z + beta p (own rows) computed on the fly, q = A p, pq
+__global__ void __launch_bounds__(kThreads) k_csr_spmv(int64_t nr, const int64_t *__restrict__ rp,
+                                                       const int32_t *__restrict__ cj, const double *__restrict__ A,
+                                                       const double *__restrict__ z, const double *__restrict__ pold,
+                                                       double *__restrict__ pnew, double *__restrict__ q, Ctl *ctl,
+                                                       double *partials) {
+    if (ctl->stop) return;
+    const double beta = ctl->beta;
+    int lane = threadIdx.x & 31;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (int64_t i = warp; i < nr; i += nw) {
+        double acc = 0.0;
+        for (int64_t k = rp[i] + lane; k < rp[i + 1]; k += 32) {
+            int64_t j = cj[k];
+            acc = fma(A[k], fma(beta, pold[j], z[j]), acc);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            double pn = fma(beta, pold[i], z[i]);
+            pnew[i] = pn;
+            q[i] = acc;
+            dot += pn * acc;
+        }
+    }
+    double v[1] = {dot}, tot[1];
+    if (grid_sum<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
+        ctl->pq = tot[0];
+        if (!(tot[0] > 0.0)) { ctl->breakdown = 1; ctl->stop = 1; }
+        else ctl->alpha = ctl->rz / tot[0];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_csr_update(int64_t nr, const double *__restrict__ dinv,
+                                                         const double *__restrict__ p, const double *__restrict__ q,
+                                                         double *__restrict__ x, double *__restrict__ r,
+                                                         double *__restrict__ z, Ctl *ctl, double *partials,
+                                                         double tol2) {
+    if (ctl->stop) return;
+    const double alpha = ctl->alpha;
+    double rz = 0.0, rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = fma(alpha, p[i], x[i]);
+        double rv = fma(-alpha, q[i], r[i]);
+        r[i] = rv;
+        double zv = dinv[i] * rv;
+        z[i] = zv;
+        rz += rv * zv;
+        rr += rv * rv;
+    }
+    double v[2] = {rz, rr}, tot[2];
+    if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
+        ctl->beta = tot[0] / ctl->rz;
+        ctl->rz = tot[0];
+        ctl->rr = tot[1];
+        if (tot[1] <= tol2 * ctl->bnorm2) { ctl->converged = 1; ctl->stop = 1; }
+        if (isnan(tot[1])) { ctl->breakdown = 1; ctl->stop = 1; }
+    }
+}
+
+// r = b - K12 u2 on the free eq rows, from the BSR FP64 matrix (u = prescribed part only)
+__global__ void k_scatter_eq(int64_t nnodes, int B, const int64_t *eq_id, int64_t nu, double *nm, double *eq,
+                             int to_eq) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t n = t / B;
+    int c = (int)(t % B);
+    int64_t e = eq_id[n * 3 + c];
+    if (e < 0 || e >= nu) return;
+    if (to_eq) eq[e] = nm[t];
+    else nm[t] = eq[e];
+}
+
+__global__ void k_csr_init(int64_t nr, const double *b, const double *dinv, double *r, double *z, double *x,
+                           Ctl *ctl, double *partials) {
+    double rz = 0.0, rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += (int64_t)gridDim.x * blockDim.x) {
+        double rv = b[i];
+        r[i] = rv;
+        double zv = dinv[i] * rv;
+        z[i] = zv;
+        x[i] = 0.0;
+        rz += rv * zv;
+        rr += rv * rv;
+    }
+    double v[2] = {rz, rr}, tot[2];
+    if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
+        ctl->rz = tot[0];
+        ctl->rr = tot[1];
+        ctl->bnorm2 = tot[1];
+        ctl->beta = 0.0;
+        ctl->stop = (tot[1] == 0.0);
+        ctl->converged = ctl->stop;
+        ctl->breakdown = 0;
+    }
+}
+
+// y = K64 u (BSR FP64): used to form b - K12 u2 and the reactions
+template <int B>
+__global__ void k_bsr64(int64_t nn, int64_t nb, const int64_t *rp, const int32_t *cj, const double *A, const double *u,
+                        double *y) {
+    int lane = threadIdx.x & 31;
+    int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= nn) return;
+    double acc[B];
+#pragma unroll
+    for (int c = 0; c < B; c++) acc[c] = 0.0;
+    for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
+        int64_t j = cj[k];
+#pragma unroll
+        for (int c = 0; c < B; c++)
+#pragma unroll
+            for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u[j * B + d], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < B; c++) acc[c] = warp_sum(acc[c]);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < B; c++) y[n * B + c] = acc[c];
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+void amr_axpy_d(int64_t n, double a, const double *x, double *y, cudaStream_t s);
+double amr_masked_residual(amr_model *m, const double *b, const double *Kx, double *reac);
+
+struct AmrSolveWork {
+    int64_t n = 0;               // nnodes * B
+    float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32[2] = {nullptr, nullptr}, *q32 = nullptr;
+    double *partials = nullptr;
+    Ctl *ctl = nullptr;
+    Ctl *h_ctl = nullptr;        // pinned
+    int grid = 0;
+    // plain FP64 CSR path
+    int64_t csr_nnz = -1;
+    int64_t *crp = nullptr, *csrc = nullptr;
+    int32_t *ccol = nullptr;
+    double *cval = nullptr, *dinv = nullptr, *cx = nullptr, *cr = nullptr, *cz = nullptr, *cp[2] = {nullptr, nullptr},
+           *cq = nullptr, *cb = nullptr, *tmp = nullptr;
+    int64_t csr_for_nu = -1;
+};
+
+static AmrSolveWork *work(amr_model *m) {
+    if (!m->sw) m->sw = new AmrSolveWork();
+    AmrSolveWork *w = m->sw;
+    int64_t n = m->nnodes * m->B;
+    if (w->n != n) {
+        w->n = n;
+        amr_free(w->x32); amr_free(w->r32); amr_free(w->z32); amr_free(w->p32[0]); amr_free(w->p32[1]);
+        amr_free(w->q32);
+        amr_alloc(&w->x32, n); amr_alloc(&w->r32, n); amr_alloc(&w->z32, n); amr_alloc(&w->p32[0], n);
+        amr_alloc(&w->p32[1], n); amr_alloc(&w->q32, n);
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        w->grid = sms * 8;
+        amr_free(w->partials);
+        amr_alloc(&w->partials, 4 * (size_t)w->grid);
+        if (!w->ctl) {
+            amr_alloc(&w->ctl, 1);
+            AMR_CUDA(cudaMemset(w->ctl, 0, sizeof(Ctl)));
+            AMR_CUDA(cudaMallocHost(&w->h_ctl, sizeof(Ctl)));
+        }
+    }
+    return w;
+}
+
+void amr_solver_free(amr_model *m) {
+    AmrSolveWork *w = m->sw;
+    if (!w) return;
+    amr_free(w->x32); amr_free(w->r32); amr_free(w->z32); amr_free(w->p32[0]); amr_free(w->p32[1]); amr_free(w->q32);
+    amr_free(w->partials); amr_free(w->ctl);
+    if (w->h_ctl) cudaFreeHost(w->h_ctl);
+    amr_free(w->crp); amr_free(w->csrc); amr_free(w->ccol); amr_free(w->cval); amr_free(w->dinv); amr_free(w->cx);
+    amr_free(w->cr); amr_free(w->cz); amr_free(w->cp[0]); amr_free(w->cp[1]); amr_free(w->cq); amr_free(w->cb);
+    amr_free(w->tmp);
+    delete w;
+    m->sw = nullptr;
+}
+
+template <int B>
+static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
+    AmrSolveWork *w = work(m);
+    cudaStream_t s = m->stream;
+    int64_t nn = m->nnodes;
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    double tol2 = o.rtol * o.rtol;
+    AMR_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), s));
+    AMR_CUDA(cudaMemsetAsync(w->x32, 0, w->n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, w->n * sizeof(float), s));
+    // free slots of x start at zero (the reduced system's initial guess)
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    unsigned g = (unsigned)w->grid;
+    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac, w->r32,
+                                       w->z32, m->Minv32, w->ctl, w->partials, 1, tol2);
+    AMR_CUDA(cudaGetLastError());
+    int cur = 0;
+    int every = o.refine_every > 0 ? o.refine_every : 32;
+    double stop_rr_rel = 0.25 * 0.25 * tol2;  // refresh early once the FP32 residual looks converged
+    for (;;) {
+        AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        Ctl c = *w->h_ctl;
+        if (c.bnorm2 == 0.0 || c.converged) break;
+        if (c.breakdown) { res.status = AMR_ENOCONV; break; }
+        if (res.iterations >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        double stop_rr = stop_rr_rel * c.bnorm2;
+        int nit = std::min(every, o.max_iters - res.iterations);
+        for (int it = 0; it < nit; it++) {
+            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->p32[cur],
+                                               w->p32[cur ^ 1], w->q32, w->ctl, w->partials);
+            k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[cur ^ 1], w->q32, w->x32, w->r32, w->z32,
+                                                 w->ctl, w->partials, stop_rr);
+            cur ^= 1;
+        }
+        AMR_CUDA(cudaGetLastError());
+        res.iterations += nit;
+        // fold the FP32 correction into the FP64 solution and refresh the true residual
+        k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
+        AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
+        k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac,
+                                           w->r32, w->z32, m->Minv32, w->ctl, w->partials, 0, tol2);
+        res.refinements++;
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    res.seconds = ms * 1e-3;
+    Ctl c = *w->h_ctl;
+    res.rel_residual = c.bnorm2 > 0 ? std::sqrt(c.rr_true / c.bnorm2) : 0.0;
+    // the iteration count is the number of launched iterations that did work; an early
+    // stop inside a chunk makes the remainder no-ops
+    return res;
+}
+
+template <int B>
+static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
+    AmrSolveWork *w = work(m);
+    cudaStream_t s = m->stream;
+    int64_t nu = m->nu;
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    if (w->csr_for_nu != nu || w->csr_nnz < 0) {  // build the scalar CSR of K11 once per DOF numbering
+        amr_free(w->crp); amr_free(w->csrc); amr_free(w->ccol); amr_free(w->cval); amr_free(w->dinv);
+        amr_free(w->cx); amr_free(w->cr); amr_free(w->cz); amr_free(w->cp[0]); amr_free(w->cp[1]); amr_free(w->cq);
+        amr_free(w->cb); amr_free(w->tmp);
+        int64_t *cnt;
+        amr_alloc(&cnt, nu);
+        AMR_CUDA(cudaMemsetAsync(cnt, 0, nu * sizeof(int64_t), s));
+        int64_t nt = m->nnodes * B;
+        k_csr_count<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, cnt);
+        amr_alloc(&w->crp, nu + 1);
+        amr_scan_i64(cnt, w->crp, nu, s);
+        AMR_CUDA(cudaMemcpy(&w->csr_nnz, w->crp + nu, sizeof(int64_t), cudaMemcpyDeviceToHost));
+        amr_alloc(&w->ccol, w->csr_nnz);
+        amr_alloc(&w->csrc, w->csr_nnz);
+        amr_alloc(&w->cval, w->csr_nnz);
+        k_csr_fill<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, m->nblocks, w->crp,
+                                                 w->ccol, w->csrc);
+        amr_free(cnt);
+        amr_alloc(&w->dinv, nu); amr_alloc(&w->cx, nu); amr_alloc(&w->cr, nu); amr_alloc(&w->cz, nu);
+        amr_alloc(&w->cp[0], nu); amr_alloc(&w->cp[1], nu); amr_alloc(&w->cq, nu); amr_alloc(&w->cb, nu);
+        amr_alloc(&w->tmp, m->nnodes * B);
+        w->csr_for_nu = nu;
+        AMR_CUDA(cudaGetLastError());
+    }
+    // values of the last assembly (part of assembly for this path, not of the solve time)
+    k_csr_values<<<nblk(w->csr_nnz, 256), 256, 0, s>>>(w->csr_nnz, w->csrc, m->K64, w->cval);
+    k_csr_diag<<<nblk(nu, 256), 256, 0, s>>>(nu, w->crp, w->ccol, w->cval, w->dinv);
+    // b_red = b - K12 u2: tmp = K64 x (x holds prescribed values, zero at free slots on entry)
+    int64_t nt = m->nnodes * B;
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, x,
+                                                         w->tmp);
+    // cb = b - K12 u2 on the free eq rows (b and K64 x scattered to eq order)
+    k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, (double *)b, w->cb, 1);
+    k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, w->tmp, w->cq, 1);
+    AMR_CUDA(cudaGetLastError());
+    double tol2 = o.rtol * o.rtol;
+    AMR_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), s));
+    AMR_CUDA(cudaMemsetAsync(w->cp[0], 0, nu * sizeof(double), s));
+    unsigned g = (unsigned)w->grid;
+    amr_axpy_d(nu, -1.0, w->cq, w->cb, s);
+    k_csr_init<<<g, kThreads, 0, s>>>(nu, w->cb, w->dinv, w->cr, w->cz, w->cx, w->ctl, w->partials);
+    int cur = 0;
+    int every = o.refine_every > 0 ? o.refine_every : 32;
+    for (;;) {
+        AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        Ctl c = *w->h_ctl;
+        if (c.converged) break;
+        if (c.breakdown) { res.status = AMR_ENOCONV; break; }
+        if (res.iterations >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        int nit = std::min(every, o.max_iters - res.iterations);
+        for (int it = 0; it < nit; it++) {
+            k_csr_spmv<<<g, kThreads, 0, s>>>(nu, w->crp, w->ccol, w->cval, w->cz, w->cp[cur], w->cp[cur ^ 1], w->cq,
+                                              w->ctl, w->partials);
+            k_csr_update<<<g, kThreads, 0, s>>>(nu, w->dinv, w->cp[cur ^ 1], w->cq, w->cx, w->cr, w->cz, w->ctl,
+                                                w->partials, tol2);
+            cur ^= 1;
+        }
+        AMR_CUDA(cudaGetLastError());
+        res.iterations += nit;
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    res.seconds = ms * 1e-3;
+    // x (node-major) free slots <- cx ; reactions and the true residual from the BSR FP64 matrix
+    k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, x, w->cx, 0);
+    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, x,
+                                                         w->tmp);
+    double rr = amr_masked_residual(m, b, w->tmp, reac);
+    Ctl c = *w->h_ctl;
+    res.rel_residual = c.bnorm2 > 0 ? std::sqrt(rr / c.bnorm2) : 0.0;
+    return res;
+}
+
+// ---- small vector helpers ----
+namespace {
+__global__ void k_axpy(int64_t n, double a, const double *x, double *y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+__global__ void k_masked_res(int64_t n, const uint8_t *fm, const double *b, const double *Kx, double *reac,
+                             double *partials, unsigned int *ticket, double *out) {
+    double rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (fm[i]) {
+            double r = b[i] - Kx[i];
+            rr += r * r;
+        } else if (reac) {
+            reac[i] = Kx[i];
+        }
+    }
+    double v[1] = {rr}, tot[1];
+    if (grid_sum<1>(v, partials, ticket, tot) && threadIdx.x == 0) *out = tot[0];
+}
+__global__ void k_absmax(int64_t n, const double *v, const uint8_t *fm, double *partials, unsigned int *ticket,
+                         double *out) {
+    double mx = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (fm && !fm[i]) continue;
+        double a = fabs(v[i]);
+        if (isnan(a)) a = INFINITY;  // NaN propagates as +inf; caller checks isnan separately
+        mx = fmax(mx, a);
+    }
+    // max-reduction: reuse the sum tree on a max via shared memory
+    __shared__ double sh[kThreads];
+    __shared__ bool last;
+    sh[threadIdx.x] = mx;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = sh[0];
+        __threadfence();
+        last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double a = 0.0;
+    for (unsigned j = threadIdx.x; j < gridDim.x; j += blockDim.x) a = fmax(a, ((volatile double *)partials)[j]);
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { *out = sh[0]; *ticket = 0; }
+}
+}  // namespace
+
+void amr_axpy_d(int64_t n, double a, const double *x, double *y, cudaStream_t s) {
+    if (n <= 0) return;
+    k_axpy<<<nblk(n, 256), 256, 0, s>>>(n, a, x, y);
+}
+
+double amr_masked_residual(amr_model *m, const double *b, const double *Kx, double *reac) {
+    AmrSolveWork *w = work(m);
+    double *out = (double *)(w->partials + 3 * (size_t)w->grid);
+    k_masked_res<<<w->grid, kThreads, 0, m->stream>>>(w->n, m->free_mask, b, Kx, reac, w->partials, &w->ctl->ticket[3],
+                                                      out);
+    double h = 0.0;
+    AMR_CUDA(cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    return h;
+}
+
+double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask) {
+    AmrSolveWork *w = work(m);
+    double *out = (double *)(w->partials + 3 * (size_t)w->grid);
+    k_absmax<<<w->grid, kThreads, 0, m->stream>>>(w->n, v, mask, w->partials, &w->ctl->ticket[3], out);
+    double h = 0.0;
+    AMR_CUDA(cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    return h;
+}
+
+void amr_eq_to_nm(amr_model *m, const double *d_eq, double *d_nm) {
+    int64_t nt = m->nnodes * m->B;
+    AMR_CUDA(cudaMemsetAsync(d_nm, 0, nt * sizeof(double), m->stream));
+    k_scatter_eq<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->eq_id, m->ndofs, d_nm, (double *)d_eq, 0);
+}
+
+void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq) {
+    int64_t nt = m->nnodes * m->B;
+    k_scatter_eq<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->eq_id, m->ndofs, (double *)d_nm, d_eq, 1);
+}
+
+AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
+    if (o.method == AMR_SOLVER_FP64)
+        return m->B == 3 ? solve_fp64_csr<3>(m, x, b, reac, o) : solve_fp64_csr<2>(m, x, b, reac, o);
+    return m->B == 3 ? solve_mixed<3>(m, x, b, reac, o) : solve_mixed<2>(m, x, b, reac, o);
+}

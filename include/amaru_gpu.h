@@ -1,0 +1,200 @@
+/*
+ * amaru_gpu.h -- C ABI of the GB300 (sm_103a) library for Amaru's mechanical
+ * hot path: solid-element stiffness and internal-force integration with the
+ * constitutive update, global sparse assembly of K and the RHS, and the
+ * linear solve K*dU = dR inside the staged Newton loop.
+ *
+ * Conventions
+ *  - Plain C types only; every call returns an int status (AMR_OK == 0,
+ *    negative on failure) and never throws across the ABI.  The message of the
+ *    last failure on a handle is available from amr_last_error().
+ *  - Indices are 0-based int64 (the Julia binding subtracts 1).  Nodal arrays
+ *    are node-major with 3 slots per node (x, y, z) even in 2-D.
+ *  - The caller owns every host buffer; the library copies inputs in and
+ *    results out and keeps no host pointer after a call returns.  Each handle
+ *    owns its device memory and one CUDA stream; amr_model_destroy frees both.
+ *  - A handle is used by one host thread at a time; different handles may be
+ *    used concurrently from different threads.
+ *
+ * Each entry point names the reference function (Amaru.jl source path:line)
+ * whose behaviour it replaces.
+ */
+#ifndef AMARU_GPU_H
+#define AMARU_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: mirror ReturnStatus (src/tools/returnstatus.jl:1-13) ---- */
+#define AMR_OK 0
+#define AMR_EINVAL -1       /* bad argument or call order */
+#define AMR_ECUDA -2        /* CUDA runtime error */
+#define AMR_ENEGJAC -3      /* detJ <= 0 (src/mech/elem/mech-solid.jl:150) */
+#define AMR_ERETMAP -4      /* return-mapping failure (src/mech/mat/von-mises.jl:146) */
+#define AMR_ENAN -5         /* NaN in K or internal forces (src/mech/mech-solver.jl:142, src/solver.jl:60) */
+#define AMR_ESINGULAR -6    /* |U1|max > 1e8 (src/solver.jl:68-71) */
+#define AMR_ENOCONV -7      /* Krylov solver did not reach its tolerance / broke down */
+#define AMR_ETIMEOUT -8     /* a bounded device wait gave up */
+#define AMR_ENOMEM -9       /* device allocation failed or admission refused */
+#define AMR_EUNSUPPORTED -10 /* element/material/stress model not on the GPU path */
+#define AMR_ESTAGE -11      /* staged Newton loop did not converge (src/mech/mech-solver.jl:478-483) */
+
+/* ---- cell shapes (src/shape/*.jl) ---- */
+enum {
+    AMR_LIN2 = 1, AMR_LIN3 = 2, AMR_TRI3 = 3, AMR_TRI6 = 4, AMR_QUAD4 = 5, AMR_QUAD8 = 6,
+    AMR_QUAD9 = 7, AMR_TET4 = 8, AMR_TET10 = 9, AMR_HEX8 = 10, AMR_HEX20 = 11
+};
+
+/* ---- stress models (src/mech/mech-solver.jl:9) ---- */
+enum { AMR_D3 = 0, AMR_PLANESTRAIN = 1, AMR_PLANESTRESS = 2, AMR_AXISYMMETRIC = 3 };
+
+/* ---- materials: parameters are 8 doubles per element ----
+ * LinearElastic  (src/mech/mat/linear-elastic.jl:12-20):  E, nu
+ * VonMises       (src/mech/mat/von-mises.jl:14-27):       E, nu, fy, H
+ * DruckerPrager  (src/mech/mat/drucker-prager.jl:15-33):  E, nu, alpha, kappa, H */
+enum { AMR_LINEAR_ELASTIC = 0, AMR_VON_MISES = 1, AMR_DRUCKER_PRAGER = 2 };
+
+typedef struct amr_model amr_model;
+
+/* Model description: nodes, MechSolid elements and their materials.
+ * Mirrors FEModel(mesh, "tag" => MechSolid => Mat => params, MechContext)
+ * (src/fe-model.jl:66-255). */
+typedef struct {
+    int32_t ndim;            /* 2 or 3 (MechContext.ndim) */
+    int32_t stressmodel;     /* AMR_D3, AMR_PLANESTRAIN, AMR_PLANESTRESS */
+    double thickness;        /* FEModel thickness (2-D) */
+    int64_t nnodes;
+    const double *coords;    /* nnodes x 3 */
+    int64_t nelems;
+    const int32_t *shape;    /* nelems: AMR_* shape code */
+    const int32_t *nips;     /* nelems: quadrature key, 0 = shape default (src/element.jl:119-166) */
+    const int64_t *conn_ptr; /* nelems + 1 */
+    const int64_t *conn;     /* node indices in Amaru's local node order */
+    const int32_t *mat_type; /* nelems: AMR_LINEAR_ELASTIC ... */
+    const double *mat_params;/* nelems x 8 */
+} amr_model_desc;
+
+/* Distributed natural load on facets or element bodies, with its value an
+ * affine function of the evaluation point: v = c[0] + c[1] x + c[2] y + c[3] z + c[4] t.
+ * Replaces mech_boundary_forces (src/mech/elem/distributed.jl:76-152) and
+ * mech_solid_body_forces (:157-217) as called by compute_bc_vals!
+ * (src/bc.jl:116-136,175-194). */
+enum { AMR_LOAD_FACET = 0, AMR_LOAD_BODY = 1 };
+typedef struct {
+    int32_t kind;            /* AMR_LOAD_FACET or AMR_LOAD_BODY */
+    int32_t dir;             /* 0,1,2 = x,y,z component; 3 = facet normal (tn/qn) */
+    int32_t edge_key;        /* 1 for q* keys on edges (thickness 1), 0 for t* / w* keys */
+    int32_t facet_shape;     /* facet cell shape (FACET kind) */
+    int64_t nitems;          /* number of facets or elements */
+    const int64_t *items;    /* FACET: nitems x npoints(facet_shape) node ids; BODY: element ids */
+    double coef[5];
+} amr_load;
+
+/* Linear-solver options for the Newton corrector solve. */
+enum { AMR_SOLVER_MIXED = 0, AMR_SOLVER_FP64 = 1 };
+typedef struct {
+    int32_t method;          /* AMR_SOLVER_MIXED: FP32 block-Jacobi PCG in FP64 iterative refinement
+                                AMR_SOLVER_FP64:  plain all-FP64 CSR Jacobi PCG */
+    double rtol;             /* relative residual ||b - K u|| / ||b|| to reach (default 1e-8) */
+    int32_t max_iters;       /* cap on inner Krylov iterations (default 20000) */
+    int32_t refine_every;    /* FP64 true-residual refresh interval in inner iterations (default 32) */
+} amr_solve_opts;
+
+typedef struct {
+    int32_t iterations;      /* Krylov iterations */
+    int32_t refinements;     /* FP64 residual refreshes */
+    double rel_residual;     /* final ||b - K u|| / ||b|| in FP64 */
+    double seconds;          /* device time of the solve */
+} amr_solve_stats;
+
+/* Newton solver parameters: mech_solver_params (src/mech/mech-solver.jl:155-168). */
+enum { AMR_SCHEME_FE = 0, AMR_SCHEME_ME = 1, AMR_SCHEME_BE = 2, AMR_SCHEME_RALSTON = 3 };
+typedef struct {
+    double tol, rtol, rspan, dT0, dTmin, dTmax;
+    int32_t scheme, maxits, autoinc, nincs, nouts;
+    amr_solve_opts linear;
+} amr_stage_params;
+
+typedef struct {
+    int32_t status;          /* AMR_OK or the failure code */
+    int32_t increments;      /* converged increments */
+    int32_t iterations;      /* Newton iterations, all increments */
+    int32_t krylov_iterations;
+    double residue;          /* last Newton residue ||R||inf */
+    double T;                /* pseudo-time reached */
+} amr_stage_stats;
+
+/* ---- lifecycle ---- */
+
+/* FEModel construction (src/fe-model.jl:66-255): uploads nodes and elements,
+ * sorts elements by (shape, quadrature) for the element kernels and builds
+ * the node-block sparsity pattern, the element-entry -> nonzero contribution
+ * map and the IP state arrays on the device. */
+int amr_model_create(const amr_model_desc *desc, amr_model **out);
+int amr_model_destroy(amr_model *m);
+/* Copies the last error message of the handle (NUL-terminated). */
+int amr_last_error(const amr_model *m, char *buf, size_t n);
+/* Message of a failure in amr_model_create (no handle yet). */
+const char *amr_create_error(void);
+
+/* DOF numbering from configure_dofs! (src/bc.jl:198-233): eq_id is nnodes x 3
+ * (only the first ndim used), -1 for nodes without DOFs; unknown DOFs are
+ * numbered 0..nu-1, prescribed ones nu..ndofs-1. */
+int amr_set_dofs(amr_model *m, const int64_t *eq_id, int64_t ndofs, int64_t nu);
+
+/* Overrides Young's modulus per element (e.g. a random field). */
+int amr_set_youngs(amr_model *m, const double *E);
+
+/* ---- element / assembly operations (the drop-in for mount_K) ---- */
+
+/* mount_K (src/mech/mech-solver.jl:78-110): element stiffness
+ * (src/mech/elem/mech-solid.jl:124-166) with the tangent of each IP's current
+ * state, deterministic assembly into the device pattern. */
+int amr_assemble_K(amr_model *m);
+/* Number of stored entries of K in the reference's SparseMatrixCSC after its
+ * |Ke_ij| >= eps() drop rule (src/mech/mech-solver.jl:90). */
+int amr_get_K_nnz(amr_model *m, int64_t *nnz);
+/* K in the reference's layout: CSC over eq_id order (colptr ndofs+1, rowval/nzval nnz). */
+int amr_get_K_csc(amr_model *m, int64_t *colptr, int64_t *rowval, double *nzval);
+
+/* update_state!(elems, dU, t) (src/mech/mech-solver.jl:124-144 and
+ * update_elem!, src/mech/elem/mech-solid.jl:243-279): trial IP states from the
+ * committed ones and dU (ndofs, eq_id order); returns dFin (ndofs). */
+int amr_update_state(amr_model *m, const double *dU, double *dFin);
+/* StateBk <- State and State <- StateBk (src/mech/mech-solver.jl:333,391,461). */
+int amr_state_commit(amr_model *m);
+int amr_state_restore(amr_model *m);
+/* IP states out (nip_total x 16: sigma[6], eps[6], epa, dlambda, 0, 0) in the
+ * caller's element order and IP order; nip_total via amr_get_sizes. */
+int amr_get_state(amr_model *m, double *state);
+int amr_get_sizes(const amr_model *m, int64_t *nnodes, int64_t *nelems, int64_t *nip_total, int64_t *nblocks);
+
+/* Distributed loads (compute_bc_vals!, src/bc.jl:116-136,175-194):
+ * F (ndofs, eq_id order) += the integrated facet / body forces at time t. */
+int amr_assemble_loads(amr_model *m, const amr_load *loads, int32_t nloads, double t, double *F);
+
+/* solve_system!(K, U, F, nu) (src/solver.jl:5-79) on the last assembled K:
+ * in: U[nu:] prescribed values, F[:nu] natural values; out: U[:nu] and the
+ * reactions F[nu:] = K21 U1 + K22 U2. */
+int amr_solve(amr_model *m, double *U, double *F, const amr_solve_opts *opts, amr_solve_stats *stats);
+
+/* mech_stage_solver! (src/mech/mech-solver.jl:186-492) on the device for one
+ * stage: Uex / Fex are the stage's essential values and natural loads from
+ * get_bc_vals (ndofs, eq_id order).  On return U and F (ndofs) hold the
+ * stage's accumulated displacements and internal forces (dof.vals updates,
+ * :394-397), IP states are committed. */
+int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params *p, double *U,
+                  double *F, amr_stage_stats *stats);
+
+/* Default parameter blocks (the reference's KwArgInfo defaults). */
+void amr_default_solve_opts(amr_solve_opts *o);
+void amr_default_stage_params(amr_stage_params *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,104 @@
+"""Host-side logic (no GPU): the C-ABI library's exports, the structured mesher,
+expression evaluation and DOF numbering, each checked against the oracle."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+import amaru_gpu as A
+from amaru_gpu import _lib
+from amaru_gpu.expr import affine_coefficients, evaluate
+from amaru_gpu.model import number_dofs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "amaru_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(amr_[A-Za-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    assert os.path.exists(_lib.LIB_PATH), "build() must have produced libamaru_gpu.so"
+    so = ctypes.CDLL(_lib.LIB_PATH)
+    names = _header_functions()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(so, n), n
+    assert sorted(_lib.SIGNATURES) == names
+
+
+@pytest.mark.parametrize("shape,n", [(A.HEX8, (3, 2, 2)), (A.HEX20, (3, 2, 2)), (A.TET10, (2, 2, 2)),
+                                     (A.TET4, (2, 2, 1)), (A.QUAD8, (3, 2)), (A.QUAD4, (3, 2)), (A.QUAD9, (2, 2)),
+                                     (A.TRI3, (2, 2)), (A.TRI6, (2, 2))])
+def test_mesher_matches_oracle(shape, n):
+    """Node numbering, connectivity and outer facets equal the restated split_block!/synchronize!."""
+    if len(n) == 3:
+        bm = A.Block([[0, 0, 0], [1, 0.5, 0.7]], nx=n[0], ny=n[1], nz=n[2], cellshape=shape)
+        bo = O.Block([[0, 0, 0], [1, 0.5, 0.7]], nx=n[0], ny=n[1], nz=n[2], cellshape=shape)
+    else:
+        bm = A.Block([[0, 0], [1, 0.5]], nx=n[0], ny=n[1], cellshape=shape)
+        bo = O.Block([[0, 0], [1, 0.5]], nx=n[0], ny=n[1], cellshape=shape)
+    mm, mo = A.Mesh(bm), O.Mesh(bo)
+    np.testing.assert_allclose(mm.coords, mo.coords, rtol=0, atol=1e-15)
+    assert (mm.conn == np.array([v for c in mo.elems for v in c.nodes])).all()
+    assert [list(r[r >= 0]) for r in mm.face_nodes] == [f.nodes for f in mo.faces]
+    assert sorted(map(lambda r: tuple(sorted(r)), mm.edge_nodes.tolist())) == \
+        sorted(tuple(sorted(e.nodes)) for e in mo.edges)
+
+
+@pytest.mark.parametrize("shape,n,nodes", [(A.HEX8, (10, 10, 10), 1331), (A.HEX20, (10, 10, 10), 4961),
+                                           (A.TET10, (10, 10, 10), 9261), (A.QUAD8, (10, 10), 341),
+                                           (A.TRI6, (10, 10), 441), (A.TRI3, (10, 10), 221)])
+def test_mesher_node_counts(shape, n, nodes):
+    """test/mesh/structured.jl node counts."""
+    if len(n) == 3:
+        b = A.Block([[0, 0, 0], [1, 1, 1]], nx=n[0], ny=n[1], nz=n[2], cellshape=shape)
+    else:
+        b = A.Block([[0, 0], [1, 1]], nx=n[0], ny=n[1], cellshape=shape)
+    assert len(A.Mesh(b).coords) == nodes
+
+
+def test_config_mesh_counts():
+    """Mesh sizes of the benchmark workloads (HEX8 20x4x4, HEX20 100x40x40 is checked by formula)."""
+    m = A.Mesh(A.Block([[0, 0, 0], [1.0, 0.2, 0.2]], nx=20, ny=4, nz=4, cellshape=A.HEX8))
+    assert len(m.coords) == 525 and len(m.shape) == 320
+    m = A.Mesh(A.Block([[0, 0, 0], [10, 4, 4]], nx=10, ny=4, nz=4, cellshape=A.HEX20))
+    nx, ny, nz = 10, 4, 4
+    full = (2 * nx + 1) * (2 * ny + 1) * (2 * nz + 1)
+    assert len(m.coords) == full - (nx * ny * (nz + 1) + nx * nz * (ny + 1) + ny * nz * (nx + 1)) - nx * ny * nz
+
+
+@pytest.mark.parametrize("expr,pt,want", [("x==0 && y==0", (0, 0, 0), True), ("x==0 && y==0", (0, 1e-7, 0), True),
+                                          ("x==0 || y==1", (2, 1, 0), True), ("x>=0.5", (0.4999999, 0, 0), True),
+                                          ("x>0.5", (0.5000005, 0, 0), False), ("3*z", (0, 0, 2.0), 6.0),
+                                          ("x^2+1", (2.0, 0, 0), 5.0)])
+def test_expressions_match_oracle(expr, pt, want):
+    x, y, z = pt
+    assert evaluate(expr, x=np.array([x]), y=np.array([y]), z=np.array([z]))[0] == want
+    assert O.evaluate(expr, x=x, y=y, z=z, t=0.0) == want
+
+
+def test_affine_loads():
+    assert affine_coefficients("3*z", 3) == [0.0, 0.0, 0.0, 3.0, 0.0]
+    assert affine_coefficients(-10.0, 3)[0] == -10.0
+    with pytest.raises(NotImplementedError):
+        affine_coefficients("x*x", 3)
+
+
+def test_dof_numbering_matches_oracle():
+    """configure_dofs!: unknowns first, prescribed last, node order then component order."""
+    mesh = O.Mesh(O.Block([[0, 0, 0], [1, 1, 1]], nx=2, ny=2, nz=1, cellshape=O.HEX8))
+    model = O.FEModel(mesh, [("all", O.LinearElastic(E=1.0, nu=0.3))])
+    bcs = [("z==0", O.NodeBC(ux=0, uz=0)), ("x==1", O.NodeBC(uy=0))]
+    dofs, nu, _ = O.configure_dofs(model, bcs)
+    presc = np.zeros((len(mesh.coords), 3), dtype=bool)
+    for e, k in dofs[nu:]:
+        presc[e, k] = True
+    eq, ndofs, nu2, dn, dk = number_dofs(np.arange(len(mesh.coords)), presc, len(mesh.coords))
+    assert nu2 == nu and ndofs == len(dofs)
+    assert (eq == model.eq_id).all()
