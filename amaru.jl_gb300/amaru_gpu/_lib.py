@@ -21,6 +21,7 @@ D3, PLANESTRAIN, PLANESTRESS, AXISYMMETRIC = 0, 1, 2, 3
 LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
 LOAD_FACET, LOAD_BODY = 0, 1
 SOLVER_MIXED, SOLVER_FP64 = 0, 1
+ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
 
 
 class AmrError(RuntimeError):
@@ -70,6 +71,7 @@ SIGNATURES = {
     "amr_create_error": (C.c_char_p, []),
     "amr_set_dofs": (C.c_int, [P, P, C.c_int64, C.c_int64]),
     "amr_set_youngs": (C.c_int, [P, P]),
+    "amr_set_assembly": (C.c_int, [P, C.c_int32]),
     "amr_assemble_K": (C.c_int, [P]),
     "amr_get_K_nnz": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_get_K_csc": (C.c_int, [P, P, P, P]),
@@ -191,6 +193,9 @@ class DeviceModel:
 
     def assemble_K(self):
         check(self.h, lib().amr_assemble_K(self.h))
+
+    def set_assembly(self, mode):
+        check(self.h, lib().amr_set_assembly(self.h, mode))
 
     def K_csc(self):
         """K as a scipy CSC matrix in eq_id order with the reference's stored-entry pattern."""

@@ -240,10 +240,17 @@ class FEModel:
         return U, F
 
     # ---- the solver-level plugin functions the library replaces
-    def mount_K(self):
-        """mount_K(elems, ndofs) (src/mech/mech-solver.jl:78-110): device assembly, reference CSC layout."""
-        self.dev.assemble_K()
-        return self.dev.K_csc()
+    def mount_K(self, reference_order=True):
+        """mount_K(elems, ndofs) (src/mech/mech-solver.jl:78-110): device assembly, exported in the
+        reference's CSC layout.  reference_order=True evaluates K_e in the reference's operation order,
+        so the stored-entry pattern follows the reference's |Ke_ij| >= eps() decisions; False uses the
+        fast pair-tensor kernel of the Newton loop."""
+        self.dev.set_assembly(L.ASSEMBLY_REFERENCE if reference_order else L.ASSEMBLY_FAST)
+        try:
+            self.dev.assemble_K()
+            return self.dev.K_csc()
+        finally:
+            self.dev.set_assembly(L.ASSEMBLY_FAST)
 
     def update_state(self, dU):
         """update_state!(elems, dU, t) (src/mech/mech-solver.jl:124-144): returns dFin."""

@@ -31,11 +31,13 @@ def _compile(src, verbose=False):
     obj = os.path.join(OUT_DIR, src + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), _headers()):
         return obj
-    cmd = [NVCC, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", SRC,
+    # host code without FMA contraction: the shape tables must be bitwise reproducible on x86 and Arm
+    cmd = [NVCC, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE,
+           "-I", SRC,
            "--expt-relaxed-constexpr", "-c", path, "-o", obj + ".tmp"]
     if src.endswith(".cpp"):
-        cmd = [NVCC, "-std=c++17", "-O3", "-x", "cu", *ARCH, "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", SRC, "-c",
-               path, "-o", obj + ".tmp"]
+        cmd = [NVCC, "-std=c++17", "-O3", "-x", "cu", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off", "-I",
+               INCLUDE, "-I", SRC, "-c", path, "-o", obj + ".tmp"]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -97,6 +97,7 @@ struct amr_model {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
     bool any_plastic = false;
+    int assembly_mode = AMR_ASSEMBLY_FAST;
 };
 
 // helpers

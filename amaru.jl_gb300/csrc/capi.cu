@@ -359,6 +359,15 @@ int amr_set_youngs(amr_model *m, const double *E) {
     });
 }
 
+int amr_set_assembly(amr_model *m, int32_t mode) {
+    return guarded(m, [&] {
+        if (mode != AMR_ASSEMBLY_FAST && mode != AMR_ASSEMBLY_REFERENCE) throw AmrError(AMR_EINVAL, "bad assembly mode");
+        if (m->assembly_mode != mode) m->K_valid = false;
+        m->assembly_mode = mode;
+        return AMR_OK;
+    });
+}
+
 int amr_assemble_K(amr_model *m) {
     return guarded(m, [&] {
         assemble(m);

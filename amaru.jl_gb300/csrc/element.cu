@@ -16,8 +16,11 @@
 //     T_ab = sum_ip w_ip g_a g_b^T,   P_ab = sum_ip w_ip gamma_ip (S g_a)(S g_b)^T,
 // with g = dN/dX at the IP, w_ip = detJ * weight * thickness and S the symmetric
 // tensor of m.  This is B^T D B written without the zeros of B.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <type_traits>
+#include <vector>
 
 #include "amr_internal.h"
 
@@ -440,6 +443,158 @@ __global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G
 }
 
 // ---------------------------------------------------------------------------
+// Reference-order stiffness: K_e = sum_ip coef * B^T (D B) evaluated exactly in
+// the order of elem_stiffness (src/mech/elem/mech-solid.jl:142-158): J = C^T dN/dR,
+// cofactor inverse, dN/dX, DB = D*B and K += coef*(B^T DB) with row-sequential
+// sums, every product and sum rounded separately (no FMA contraction).  With
+// the same dN/dR tables this reproduces the CPU restatement bit for bit, so the
+// |K_ij| >= eps() decisions of entries that are zero only by cancellation come
+// out as the reference's arithmetic makes them.  Used for the parity / export
+// path; the fast kernel above serves the Newton loop.
+// ---------------------------------------------------------------------------
+#define RMUL __dmul_rn
+#define RADD __dadd_rn
+#define RSUB __dsub_rn
+#define RDIV __ddiv_rn
+
+// B[l][(b,d)] of setB (mech-solid.jl:82-121) from g = dN/dX of node b
+template <int DIM>
+__device__ __forceinline__ double ref_B(int l, int d, const double *g) {
+    if (DIM == 3) {
+        switch (l) {
+        case 0: return d == 0 ? g[0] : 0.0;
+        case 1: return d == 1 ? g[1] : 0.0;
+        case 2: return d == 2 ? g[2] : 0.0;
+        case 3: return d == 1 ? RDIV(g[2], SQ2) : (d == 2 ? RDIV(g[1], SQ2) : 0.0);
+        case 4: return d == 0 ? RDIV(g[2], SQ2) : (d == 2 ? RDIV(g[0], SQ2) : 0.0);
+        default: return d == 0 ? RDIV(g[1], SQ2) : (d == 1 ? RDIV(g[0], SQ2) : 0.0);
+        }
+    }
+    switch (l) {
+    case 0: return d == 0 ? g[0] : 0.0;
+    case 1: return d == 1 ? g[1] : 0.0;
+    case 5: return d == 0 ? RDIV(g[1], SQ2) : RDIV(g[0], SQ2);
+    default: return 0.0;
+    }
+}
+
+template <int DIM, int NEN>
+__global__ void __launch_bounds__(256) stiffness_ref_kernel(ModelArgs M, GroupArgs G, double *Kel, const double *st,
+                                                            int32_t *status) {
+    constexpr int ND = NEN * DIM;
+    constexpr int NE = (ND * ND + 255) / 256;
+    __shared__ double sC[ND], sG[ND], sD[36], sDB[6 * ND], sIJ[9], sCoef;
+    const int64_t e = G.first + blockIdx.x;
+    const int nip = G.nip;
+    const bool ps = (M.stressmodel == AMR_PLANESTRESS);
+    for (int t = threadIdx.x; t < ND; t += blockDim.x) {
+        int32_t node = M.conn[M.conn_ptr[e] + t / DIM];
+        sC[t] = M.coords[3 * (int64_t)node + t % DIM];
+    }
+    double acc[NE];
+#pragma unroll
+    for (int q = 0; q < NE; q++) acc[q] = 0.0;
+    const double *par = M.mat_par + 8 * e;
+    __syncthreads();
+    for (int ip = 0; ip < nip; ip++) {
+        const double *dNdR = G.tab + ip * ND;
+        if (threadIdx.x == 0) {
+            double J[9];
+            for (int a = 0; a < DIM; a++)
+                for (int b = 0; b < DIM; b++) {
+                    double s = 0.0;
+                    for (int i = 0; i < NEN; i++) s = RADD(s, RMUL(sC[i * DIM + a], dNdR[i * DIM + b]));
+                    J[a * DIM + b] = s;
+                }
+            double det;
+            if (DIM == 2) {
+                det = RSUB(RMUL(J[0], J[3]), RMUL(J[1], J[2]));
+                sIJ[0] = RDIV(J[3], det); sIJ[1] = RDIV(-J[1], det); sIJ[2] = RDIV(-J[2], det); sIJ[3] = RDIV(J[0], det);
+            } else {
+                double c0 = RSUB(RMUL(J[4], J[8]), RMUL(J[5], J[7]));
+                double c1 = RSUB(RMUL(J[3], J[8]), RMUL(J[5], J[6]));
+                double c2 = RSUB(RMUL(J[3], J[7]), RMUL(J[4], J[6]));
+                det = RADD(RSUB(RMUL(J[0], c0), RMUL(J[1], c1)), RMUL(J[2], c2));
+                sIJ[0] = RDIV(c0, det);
+                sIJ[1] = RDIV(RSUB(RMUL(J[2], J[7]), RMUL(J[1], J[8])), det);
+                sIJ[2] = RDIV(RSUB(RMUL(J[1], J[5]), RMUL(J[2], J[4])), det);
+                sIJ[3] = RDIV(RSUB(RMUL(J[5], J[6]), RMUL(J[3], J[8])), det);
+                sIJ[4] = RDIV(RSUB(RMUL(J[0], J[8]), RMUL(J[2], J[6])), det);
+                sIJ[5] = RDIV(RSUB(RMUL(J[2], J[3]), RMUL(J[0], J[5])), det);
+                sIJ[6] = RDIV(RSUB(RMUL(J[3], J[7]), RMUL(J[4], J[6])), det);
+                sIJ[7] = RDIV(RSUB(RMUL(J[1], J[6]), RMUL(J[0], J[7])), det);
+                sIJ[8] = RDIV(RSUB(RMUL(J[0], J[4]), RMUL(J[1], J[3])), det);
+            }
+            if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
+            sCoef = RMUL(RMUL(det, G.tab[nip * ND + ip]), M.thickness);
+            // D: calcDe (linear-elastic.jl:98-119), plastic part as De - gamma m m^T
+            double E = par[0], nu = par[1];
+            for (int q = 0; q < 36; q++) sD[q] = 0.0;
+            if (ps) {
+                double c = RDIV(E, RSUB(1.0, RMUL(nu, nu)));
+                sD[0] = c; sD[1] = RMUL(c, nu); sD[6] = RMUL(c, nu); sD[7] = c;
+                double sh = RMUL(c, RSUB(1.0, nu));
+                sD[21] = sh; sD[28] = sh; sD[35] = sh;
+            } else {
+                double c = RDIV(E, RMUL(RADD(1.0, nu), RSUB(1.0, RMUL(2.0, nu))));
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) sD[6 * i + j] = (i == j) ? RMUL(c, RSUB(1.0, nu)) : RMUL(c, nu);
+                double sh = RMUL(c, RSUB(1.0, RMUL(2.0, nu)));
+                sD[21] = sh; sD[28] = sh; sD[35] = sh;
+            }
+            int64_t gi = M.ip_ptr[e] + ip;
+            double sig[6], m[6], lam, mu;
+            for (int i = 0; i < 6; i++) sig[i] = st[i * M.nip_total + gi];
+            lame(E, nu, ps, lam, mu);
+            double gam = plastic_tangent(M.mat_type[e], par, ps, sig, st[AMR_ST_EPA * M.nip_total + gi],
+                                         st[AMR_ST_DL * M.nip_total + gi], lam, mu, m);
+            if (gam != 0.0)
+                for (int i = 0; i < 6; i++)
+                    for (int j = 0; j < 6; j++) sD[6 * i + j] -= gam * m[i] * m[j];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < ND; t += blockDim.x) {  // dNdX = dNdR * inv(J)
+            int i = t / DIM, b = t % DIM;
+            double s = 0.0;
+            for (int a = 0; a < DIM; a++) s = RADD(s, RMUL(dNdR[i * DIM + a], sIJ[a * DIM + b]));
+            sG[t] = s;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < 6 * ND; t += blockDim.x) {  // DB = D * B
+            int k = t / ND, j = t % ND;
+            const double *gb = sG + (j / DIM) * DIM;
+            double s = 0.0;
+            for (int l = 0; l < 6; l++) s = RADD(s, RMUL(sD[6 * k + l], ref_B<DIM>(l, j % DIM, gb)));
+            sDB[t] = s;
+        }
+        __syncthreads();
+        const double coef = sCoef;
+#pragma unroll
+        for (int q = 0; q < NE; q++) {  // K += coef * B' * DB
+            int idx = threadIdx.x + q * 256;
+            if (idx < ND * ND) {
+                int i = idx / ND, j = idx % ND;
+                const double *gi = sG + (i / DIM) * DIM;
+                double s = 0.0;
+                for (int k = 0; k < 6; k++) s = RADD(s, RMUL(ref_B<DIM>(k, i % DIM, gi), sDB[k * ND + j]));
+                acc[q] = RADD(acc[q], RMUL(coef, s));
+            }
+        }
+        __syncthreads();
+    }
+    const int64_t base = M.kel_ptr[e];
+#pragma unroll
+    for (int q = 0; q < NE; q++) {
+        int idx = threadIdx.x + q * 256;
+        if (idx < ND * ND) {
+            int i = idx / ND, j = idx % ND;
+            int a = i / DIM, c = i % DIM, b = j / DIM, d = j % DIM;
+            Kel[(base + (int64_t)a * NEN + b) * DIM * DIM + c * DIM + d] = acc[q];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Gather: warp per node row, lane per nonzero block.  Contributions are summed
 // in element order skipping |Ke_ij| < eps() (the mount_K drop rule); the keep
 // bits record which scalar entries the reference's sparse() would store.
@@ -481,7 +636,7 @@ __global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *br
 #pragma unroll
             for (int q = 0; q < BB; q++) {
                 double x = src[q];
-                if (fabs(x) >= DBL_EPSILON) { v[q] += x; kb |= 1u << q; }
+                if (!(fabs(x) < DBL_EPSILON)) { v[q] += x; kb |= 1u << q; }  // NaN is pushed, as in mount_K
             }
         }
         int32_t j = bcol[k];
@@ -720,6 +875,13 @@ void launch_stiff(amr_model *m, const AmrGroup &g) {
 }
 
 template <int DIM, int NEN>
+void launch_stiff_ref(amr_model *m, const AmrGroup &g) {
+    GroupArgs ga{g.tab, g.nip, g.first, g.count};
+    stiffness_ref_kernel<DIM, NEN><<<(unsigned)g.count, 256, 0, m->stream>>>(margs(m), ga, m->Kel, m->st, m->d_status);
+    AMR_CUDA(cudaGetLastError());
+}
+
+template <int DIM, int NEN>
 void launch_internal(amr_model *m, const AmrGroup &g, const double *dU) {
     GroupArgs ga{g.tab, g.nip, g.first, g.count};
     int epb = (g.nip * 1 >= 16) ? 4 : 16;
@@ -766,9 +928,14 @@ int amr_check_status(amr_model *m) {
 
 void amr_stiffness(amr_model *m) {
     for (const AmrGroup &g : m->groups) {
-        dispatch(
-            m, g, [&](auto n) { launch_stiff<3, decltype(n)::value>(m, g); },
-            [&](auto n) { launch_stiff<2, decltype(n)::value>(m, g); });
+        if (m->assembly_mode == AMR_ASSEMBLY_REFERENCE)
+            dispatch(
+                m, g, [&](auto n) { launch_stiff_ref<3, decltype(n)::value>(m, g); },
+                [&](auto n) { launch_stiff_ref<2, decltype(n)::value>(m, g); });
+        else
+            dispatch(
+                m, g, [&](auto n) { launch_stiff<3, decltype(n)::value>(m, g); },
+                [&](auto n) { launch_stiff<2, decltype(n)::value>(m, g); });
     }
     unsigned grid = nblk(m->nnodes * 32, 256);
     if (m->B == 3)

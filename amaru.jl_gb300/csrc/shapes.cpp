@@ -1,12 +1,7 @@
 // Shape functions and quadrature rules of the isoparametric cells on the GPU path.
 //
-// The functions are written in generic form -- tensor products of 1-D
-// Lagrange polynomials, the serendipity corner/mid-side rules and barycentric
-// coordinates for simplices -- over the node tables of Amaru's cells
-// (src/shape/solids2d.jl, src/shape/solids3d.jl, src/shape/lines.jl), so the
-// local node order matches Amaru's.  They only feed host-built per-shape
-// tables (dN/dR at the integration points); no shape function is evaluated
-// on the device.
+// They only feed host-built per-shape tables (N and dN/dR at the integration
+// points); no shape function is evaluated on the device.
 #include <cmath>
 #include <cstring>
 
@@ -15,157 +10,204 @@
 namespace amr {
 namespace {
 
-// natural coordinates of the nodes, Amaru's local order
-const double kHex[20][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, 1, 1},
-                            {-1, 1, 1},   {0, -1, -1}, {1, 0, -1}, {0, 1, -1}, {-1, 0, -1}, {0, -1, 1}, {1, 0, 1},
-                            {0, 1, 1},    {-1, 0, 1},  {-1, -1, 0}, {1, -1, 0}, {1, 1, 0},  {-1, 1, 0}};
-const double kQuad[9][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}, {0, -1}, {1, 0}, {0, 1}, {-1, 0}, {0, 0}};
-// mid-edge nodes of the simplices as pairs of vertices
-const int kTet10Edges[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
-const int kTri6Edges[3][2] = {{0, 1}, {1, 2}, {2, 0}};
-
-// 1-D quadratic Lagrange basis on nodes {-1, 0, 1}: value and derivative at x for node c
-inline void lag2(double c, double x, double &v, double &d) {
-    if (c < -0.5) { v = 0.5 * x * (x - 1.0); d = x - 0.5; }
-    else if (c > 0.5) { v = 0.5 * x * (x + 1.0); d = x + 0.5; }
-    else { v = 1.0 - x * x; d = -2.0 * x; }
-}
-
-// barycentric coordinates and their derivatives w.r.t. (r,s[,t])
-void bary(int dim, const double *R, double *L, double *dL) {
-    double sum = 0.0;
-    for (int k = 0; k < dim; k++) sum += R[k];
-    L[0] = 1.0 - sum;
-    for (int k = 0; k < dim; k++) dL[0 * dim + k] = -1.0;
-    for (int i = 1; i <= dim; i++) {
-        L[i] = R[i - 1];
-        for (int k = 0; k < dim; k++) dL[i * dim + k] = (k == i - 1) ? 1.0 : 0.0;
-    }
-}
-
-// quadratic simplex (TRI6 / TET10): corners L(2L-1), edges 4 La Lb
-void simplex2(int dim, const int (*edges)[2], int nedges, const double *R, double *N, double *D) {
-    double L[4], dL[12];
-    bary(dim, R, L, dL);
-    for (int i = 0; i <= dim; i++) {
-        if (N) N[i] = L[i] * (2.0 * L[i] - 1.0);
-        if (D)
-            for (int k = 0; k < dim; k++) D[i * dim + k] = (4.0 * L[i] - 1.0) * dL[i * dim + k];
-    }
-    for (int e = 0; e < nedges; e++) {
-        int a = edges[e][0], b = edges[e][1], i = dim + 1 + e;
-        if (N) N[i] = 4.0 * L[a] * L[b];
-        if (D)
-            for (int k = 0; k < dim; k++) D[i * dim + k] = 4.0 * (dL[a * dim + k] * L[b] + L[a] * dL[b * dim + k]);
-    }
-}
-
-// serendipity quadratic brick / quad in `dim` dimensions over the node table
-void serendipity(int dim, int nn, const double *X, int stride, const double *R, double *N, double *D) {
-    for (int i = 0; i < nn; i++) {
-        const double *c = X + i * stride;
-        bool corner = true;
-        for (int k = 0; k < dim; k++) corner = corner && (c[k] != 0.0);
-        double f[3], df[3];
-        if (corner) {
-            // prod (1 + x_k c_k) * (sum x_k c_k - (dim-1)) / 2^dim
-            double lin = 0.0;
-            for (int k = 0; k < dim; k++) { f[k] = 1.0 + R[k] * c[k]; lin += R[k] * c[k]; }
-            double scale = (dim == 3) ? 0.125 : 0.25;
-            double g = lin - (dim - 1);
-            double p = 1.0;
-            for (int k = 0; k < dim; k++) p *= f[k];
-            if (N) N[i] = scale * p * g;
-            if (D)
-                for (int k = 0; k < dim; k++) {
-                    double pk = 1.0;
-                    for (int l = 0; l < dim; l++)
-                        if (l != k) pk *= f[l];
-                    D[i * dim + k] = scale * (c[k] * pk * g + p * c[k]);
-                }
-        } else {
-            // mid-side: (1 - x_m^2) along the zero coordinate m, linear in the others
-            double scale = (dim == 3) ? 0.25 : 0.5;
-            for (int k = 0; k < dim; k++) {
-                if (c[k] == 0.0) { f[k] = 1.0 - R[k] * R[k]; df[k] = -2.0 * R[k]; }
-                else { f[k] = 1.0 + R[k] * c[k]; df[k] = c[k]; }
-            }
-            double p = 1.0;
-            for (int k = 0; k < dim; k++) p *= f[k];
-            if (N) N[i] = scale * p;
-            if (D)
-                for (int k = 0; k < dim; k++) {
-                    double pk = df[k];
-                    for (int l = 0; l < dim; l++)
-                        if (l != k) pk *= f[l];
-                    D[i * dim + k] = scale * pk;
-                }
-        }
-    }
-}
-
-// multilinear cells (QUAD4 / HEX8): prod (1 + x_k c_k) / 2
-void multilinear(int dim, int nn, const double *X, int stride, const double *R, double *N, double *D) {
-    for (int i = 0; i < nn; i++) {
-        const double *c = X + i * stride;
-        double f[3];
-        for (int k = 0; k < dim; k++) f[k] = 0.5 * (1.0 + R[k] * c[k]);
-        if (N) {
-            double p = 1.0;
-            for (int k = 0; k < dim; k++) p *= f[k];
-            N[i] = p;
-        }
-        if (D)
-            for (int k = 0; k < dim; k++) {
-                double pk = 0.5 * c[k];
-                for (int l = 0; l < dim; l++)
-                    if (l != k) pk *= f[l];
-                D[i * dim + k] = pk;
-            }
-    }
-}
-
+// Shape functions and derivatives at a point.  The derivative tables of the
+// element kernels must carry bitwise the values Amaru computes at each
+// integration point: where a derivative is mathematically zero only by
+// cancellation (e.g. 4 - 8r - 4s - 4t of TET10 at a Gauss point), the exact
+// zero or residue it evaluates to decides which entries of K_e survive the
+// |K_ij| >= eps() drop rule of mount_K.  So the polynomials are evaluated in
+// the expanded forms of src/shape/solids2d.jl, solids3d.jl and lines.jl.
 void eval(int shape, const double *R, double *N, double *D) {
+    const double r = R[0], s = R[1], t = R[2];
     switch (shape) {
-    case AMR_LIN2: {
-        if (N) { N[0] = 0.5 * (1.0 - R[0]); N[1] = 0.5 * (1.0 + R[0]); }
+    case AMR_LIN2:
+        if (N) { N[0] = 0.5 * (1 - r); N[1] = 0.5 * (1 + r); }
         if (D) { D[0] = -0.5; D[1] = 0.5; }
         return;
-    }
-    case AMR_LIN3: {  // nodes at -1, 1, 0
-        const double c[3] = {-1.0, 1.0, 0.0};
-        for (int i = 0; i < 3; i++) {
-            double v, d;
-            lag2(c[i], R[0], v, d);
-            if (N) N[i] = v;
-            if (D) D[i] = d;
+    case AMR_LIN3:
+        if (N) { N[0] = 0.5 * (r * r - r); N[1] = 0.5 * (r * r + r); N[2] = 1.0 - r * r; }
+        if (D) { D[0] = r - 0.5; D[1] = r + 0.5; D[2] = -2.0 * r; }
+        return;
+    case AMR_TRI3:
+        if (N) { N[0] = 1.0 - r - s; N[1] = r; N[2] = s; }
+        if (D) { const double d[6] = {-1.0, -1.0, 1.0, 0.0, 0.0, 1.0}; std::memcpy(D, d, sizeof d); }
+        return;
+    case AMR_TRI6: {
+        const double rs = r + s;
+        if (N) {
+            N[0] = 1.0 - rs * (3.0 - 2.0 * rs); N[1] = r * (2.0 * r - 1.0); N[2] = s * (2.0 * s - 1.0);
+            N[3] = 4.0 * r * (1.0 - rs); N[4] = 4.0 * r * s; N[5] = 4.0 * s * (1.0 - rs);
+        }
+        if (D) {
+            const double d[12] = {-3.0 + 4.0 * rs, -3.0 + 4.0 * rs, 4.0 * r - 1.0, 0.0, 0.0, 4.0 * s - 1.0,
+                                  4.0 - 8.0 * r - 4.0 * s, -4.0 * r, 4.0 * s, 4.0 * r, -4.0 * s, 4.0 - 4.0 * r - 8.0 * s};
+            std::memcpy(D, d, sizeof d);
         }
         return;
     }
-    case AMR_TRI3: case AMR_TET4: {
-        int dim = (shape == AMR_TRI3) ? 2 : 3;
-        double L[4], dL[12];
-        bary(dim, R, L, dL);
-        for (int i = 0; i <= dim; i++) {
-            if (N) N[i] = L[i];
-            if (D)
-                for (int k = 0; k < dim; k++) D[i * dim + k] = dL[i * dim + k];
+    case AMR_QUAD4:
+        if (N) {
+            N[0] = 0.25 * (1.0 - r - s + r * s); N[1] = 0.25 * (1.0 + r - s - r * s);
+            N[2] = 0.25 * (1.0 + r + s + r * s); N[3] = 0.25 * (1.0 - r + s - r * s);
+        }
+        if (D) {
+            const double d[8] = {0.25 * (-1.0 + s), 0.25 * (-1.0 + r), 0.25 * (+1.0 - s), 0.25 * (-1.0 - r),
+                                 0.25 * (+1.0 + s), 0.25 * (+1.0 + r), 0.25 * (-1.0 - s), 0.25 * (+1.0 - r)};
+            std::memcpy(D, d, sizeof d);
+        }
+        return;
+    case AMR_QUAD8: {
+        const double rp = 1.0 + r, rm = 1.0 - r, sp = 1.0 + s, sm = 1.0 - s;
+        if (N) {
+            N[0] = 0.25 * rm * sm * (rm + sm - 3.0); N[1] = 0.25 * rp * sm * (rp + sm - 3.0);
+            N[2] = 0.25 * rp * sp * (rp + sp - 3.0); N[3] = 0.25 * rm * sp * (rm + sp - 3.0);
+            N[4] = 0.50 * sm * (1.0 - r * r); N[5] = 0.50 * rp * (1.0 - s * s);
+            N[6] = 0.50 * sp * (1.0 - r * r); N[7] = 0.50 * rm * (1.0 - s * s);
+        }
+        if (D) {
+            const double d[16] = {-0.25 * sm * (rm + rm + sm - 3.0), -0.25 * rm * (sm + rm + sm - 3.0),
+                                  0.25 * sm * (rp + rp + sm - 3.0),  -0.25 * rp * (sm + rp + sm - 3.0),
+                                  0.25 * sp * (rp + rp + sp - 3.0),  0.25 * rp * (sp + rp + sp - 3.0),
+                                  -0.25 * sp * (rm + rm + sp - 3.0), 0.25 * rm * (sp + rm + sp - 3.0),
+                                  -r * sm,                           -0.50 * (1.0 - r * r),
+                                  0.50 * (1.0 - s * s),              -s * rp,
+                                  -r * sp,                           0.50 * (1.0 - r * r),
+                                  -0.5 * (1.0 - s * s),              -s * rm};
+            std::memcpy(D, d, sizeof d);
         }
         return;
     }
-    case AMR_TRI6: simplex2(2, kTri6Edges, 3, R, N, D); return;
-    case AMR_TET10: simplex2(3, kTet10Edges, 6, R, N, D); return;
-    case AMR_QUAD4: multilinear(2, 4, &kQuad[0][0], 2, R, N, D); return;
-    case AMR_HEX8: multilinear(3, 8, &kHex[0][0], 3, R, N, D); return;
-    case AMR_QUAD8: serendipity(2, 8, &kQuad[0][0], 2, R, N, D); return;
-    case AMR_HEX20: serendipity(3, 20, &kHex[0][0], 3, R, N, D); return;
     case AMR_QUAD9: {
-        for (int i = 0; i < 9; i++) {
-            double v0, d0, v1, d1;
-            lag2(kQuad[i][0], R[0], v0, d0);
-            lag2(kQuad[i][1], R[1], v1, d1);
-            if (N) N[i] = v0 * v1;
-            if (D) { D[2 * i] = d0 * v1; D[2 * i + 1] = v0 * d1; }
+        const double rp = r + 1.0, rm = r - 1.0, sp = s + 1.0, sm = s - 1.0;
+        if (N) {
+            N[0] = 0.25 * r * s * sm * rm; N[1] = 0.25 * r * s * sm * rp; N[2] = 0.25 * r * s * sp * rp;
+            N[3] = 0.25 * r * s * sp * rm; N[4] = -0.50 * s * sm * rp * rm; N[5] = -0.50 * r * sp * sm * rp;
+            N[6] = -0.50 * s * sp * rp * rm; N[7] = -0.50 * r * sp * sm * rm; N[8] = sp * sm * rp * rm;
+        }
+        if (D) {
+            const double d[18] = {(r + rm) * s * sm / 4.0,         r * rm * (s + sm) / 4.0,
+                                  (r + rp) * s * sm / 4.0,         r * rp * (s + sm) / 4.0,
+                                  (r + rp) * s * sp / 4.0,         r * rp * (s + sp) / 4.0,
+                                  (r + rm) * s * sp / 4.0,         r * rm * (s + sp) / 4.0,
+                                  -(r + r) * s * (sm) / 2.0,       -(r * r - 1.0) * (s + sm) / 2.0,
+                                  -(r + rp) * (s * s - 1.0) / 2.0, -r * rp * (s + s) / 2.0,
+                                  -(r + r) * s * (sp) / 2.0,       -(r * r - 1.0) * (s + sp) / 2.0,
+                                  -(r + rm) * (s * s - 1.0) / 2.0, -r * rm * (s + s) / 2.0,
+                                  2.0 * r * (s * s - 1.0),         2.0 * s * (r * r - 1.0)};
+            std::memcpy(D, d, sizeof d);
+        }
+        return;
+    }
+    case AMR_TET4:
+        if (N) { N[0] = 1.0 - r - s - t; N[1] = r; N[2] = s; N[3] = t; }
+        if (D) {
+            const double d[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+            std::memcpy(D, d, sizeof d);
+        }
+        return;
+    case AMR_TET10: {
+        const double u = 1.0 - r - s - t;
+        if (N) {
+            N[0] = u * (2.0 * u - 1.0); N[1] = r * (2.0 * r - 1.0); N[2] = s * (2.0 * s - 1.0);
+            N[3] = t * (2.0 * t - 1.0); N[4] = 4.0 * u * r; N[5] = 4.0 * r * s; N[6] = 4.0 * s * u;
+            N[7] = 4.0 * u * t; N[8] = 4.0 * r * t; N[9] = 4.0 * s * t;
+        }
+        if (D) {
+            const double c = 4.0 * (r + s + t) - 3.0;
+            const double d[30] = {c, c, c,
+                                  4.0 * r - 1.0, 0.0, 0.0,
+                                  0.0, 4.0 * s - 1.0, 0.0,
+                                  0.0, 0.0, 4.0 * t - 1.0,
+                                  4.0 - 8.0 * r - 4.0 * s - 4.0 * t, -4.0 * r, -4.0 * r,
+                                  4.0 * s, 4.0 * r, 0.0,
+                                  -4.0 * s, 4.0 - 4.0 * r - 8.0 * s - 4.0 * t, -4.0 * s,
+                                  -4.0 * t, -4.0 * t, 4.0 - 4.0 * r - 4.0 * s - 8.0 * t,
+                                  4.0 * t, 0.0, 4.0 * r,
+                                  0.0, 4.0 * t, 4.0 * s};
+            std::memcpy(D, d, sizeof d);
+        }
+        return;
+    }
+    case AMR_HEX8: {
+        if (N) {
+            N[0] = 0.125 * (1.0 - r - s + r * s - t + s * t + r * t - r * s * t);
+            N[1] = 0.125 * (1.0 + r - s - r * s - t + s * t - r * t + r * s * t);
+            N[2] = 0.125 * (1.0 + r + s + r * s - t - s * t - r * t - r * s * t);
+            N[3] = 0.125 * (1.0 - r + s - r * s - t - s * t + r * t + r * s * t);
+            N[4] = 0.125 * (1.0 - r - s + r * s + t - s * t - r * t + r * s * t);
+            N[5] = 0.125 * (1.0 + r - s - r * s + t - s * t + r * t - r * s * t);
+            N[6] = 0.125 * (1.0 + r + s + r * s + t + s * t + r * t + r * s * t);
+            N[7] = 0.125 * (1.0 - r + s - r * s + t + s * t - r * t - r * s * t);
+        }
+        if (D) {
+            const double st = s * t, rt = r * t, rs = r * s;
+            const double d[24] = {-1.0 + s + t - st, -1.0 + r + t - rt, -1.0 + r + s - rs,
+                                  +1.0 - s - t + st, -1.0 - r + t + rt, -1.0 - r + s + rs,
+                                  +1.0 + s - t - st, +1.0 + r - t - rt, -1.0 - r - s - rs,
+                                  -1.0 - s + t + st, +1.0 - r - t + rt, -1.0 + r - s + rs,
+                                  -1.0 + s - t + st, -1.0 + r - t + rt, +1.0 - r - s + rs,
+                                  +1.0 - s + t - st, -1.0 - r - t - rt, +1.0 + r - s - rs,
+                                  +1.0 + s + t + st, +1.0 + r + t + rt, +1.0 + r + s + rs,
+                                  -1.0 - s - t - st, +1.0 - r + t - rt, +1.0 - r + s - rs};
+            for (int i = 0; i < 24; i++) D[i] = 0.125 * d[i];
+        }
+        return;
+    }
+    case AMR_HEX20: {
+        const double rp = 1.0 + r, rm = 1.0 - r, sp = 1.0 + s, sm = 1.0 - s, tp = 1.0 + t, tm = 1.0 - t;
+        if (N) {
+            N[0] = 0.125 * rm * sm * tm * (-r - s - t - 2.0); N[1] = 0.125 * rp * sm * tm * (r - s - t - 2.0);
+            N[2] = 0.125 * rp * sp * tm * (r + s - t - 2.0);  N[3] = 0.125 * rm * sp * tm * (-r + s - t - 2.0);
+            N[4] = 0.125 * rm * sm * tp * (-r - s + t - 2.0); N[5] = 0.125 * rp * sm * tp * (r - s + t - 2.0);
+            N[6] = 0.125 * rp * sp * tp * (r + s + t - 2.0);  N[7] = 0.125 * rm * sp * tp * (-r + s + t - 2.0);
+            N[8] = 0.25 * (1.0 - r * r) * sm * tm;  N[9] = 0.25 * rp * (1.0 - s * s) * tm;
+            N[10] = 0.25 * (1.0 - r * r) * sp * tm; N[11] = 0.25 * rm * (1.0 - s * s) * tm;
+            N[12] = 0.25 * (1.0 - r * r) * sm * tp; N[13] = 0.25 * rp * (1.0 - s * s) * tp;
+            N[14] = 0.25 * (1.0 - r * r) * sp * tp; N[15] = 0.25 * rm * (1.0 - s * s) * tp;
+            N[16] = 0.25 * rm * sm * (1.0 - t * t); N[17] = 0.25 * rp * sm * (1.0 - t * t);
+            N[18] = 0.25 * rp * sp * (1.0 - t * t); N[19] = 0.25 * rm * sp * (1.0 - t * t);
+        }
+        if (D) {
+            double *d = D;
+            // d/dr
+            d[0] = -0.125 * sm * tm * (-r - s - t - 2) - 0.125 * rm * sm * tm;
+            d[3] = 0.125 * sm * tm * (r - s - t - 2) + 0.125 * rp * sm * tm;
+            d[6] = 0.125 * sp * tm * (r + s - t - 2) + 0.125 * rp * sp * tm;
+            d[9] = -0.125 * sp * tm * (-r + s - t - 2) - 0.125 * rm * sp * tm;
+            d[12] = -0.125 * sm * tp * (-r - s + t - 2) - 0.125 * rm * sm * tp;
+            d[15] = 0.125 * sm * tp * (r - s + t - 2) + 0.125 * rp * sm * tp;
+            d[18] = 0.125 * sp * tp * (r + s + t - 2) + 0.125 * rp * sp * tp;
+            d[21] = -0.125 * sp * tp * (-r + s + t - 2) - 0.125 * rm * sp * tp;
+            d[24] = -0.5 * r * sm * tm;  d[27] = 0.25 * (1 - s * s) * tm; d[30] = -0.5 * r * sp * tm;
+            d[33] = -0.25 * (1 - s * s) * tm; d[36] = -0.5 * r * sm * tp; d[39] = 0.25 * (1 - s * s) * tp;
+            d[42] = -0.5 * r * sp * tp; d[45] = -0.25 * (1 - s * s) * tp; d[48] = -0.25 * sm * (1 - t * t);
+            d[51] = 0.25 * sm * (1 - t * t); d[54] = 0.25 * sp * (1 - t * t); d[57] = -0.25 * sp * (1 - t * t);
+            // d/ds
+            d[1] = -0.125 * rm * tm * (-r - s - t - 2) - 0.125 * rm * sm * tm;
+            d[4] = -0.125 * rp * tm * (r - s - t - 2) - 0.125 * rp * sm * tm;
+            d[7] = 0.125 * rp * tm * (r + s - t - 2) + 0.125 * rp * sp * tm;
+            d[10] = 0.125 * rm * tm * (-r + s - t - 2) + 0.125 * rm * sp * tm;
+            d[13] = -0.125 * rm * tp * (-r - s + t - 2) - 0.125 * rm * sm * tp;
+            d[16] = -0.125 * rp * tp * (r - s + t - 2) - 0.125 * rp * sm * tp;
+            d[19] = 0.125 * rp * tp * (r + s + t - 2) + 0.125 * rp * sp * tp;
+            d[22] = 0.125 * rm * tp * (-r + s + t - 2) + 0.125 * rm * sp * tp;
+            d[25] = -0.25 * (1 - r * r) * tm; d[28] = -0.5 * s * rp * tm; d[31] = 0.25 * (1 - r * r) * tm;
+            d[34] = -0.5 * s * rm * tm; d[37] = -0.25 * (1 - r * r) * tp; d[40] = -0.5 * s * rp * tp;
+            d[43] = 0.25 * (1 - r * r) * tp; d[46] = -0.5 * s * rm * tp; d[49] = -0.25 * rm * (1 - t * t);
+            d[52] = -0.25 * rp * (1 - t * t); d[55] = 0.25 * rp * (1 - t * t); d[58] = 0.25 * rm * (1 - t * t);
+            // d/dt
+            d[2] = -0.125 * rm * sm * (-r - s - t - 2) - 0.125 * rm * sm * tm;
+            d[5] = -0.125 * rp * sm * (r - s - t - 2) - 0.125 * rp * sm * tm;
+            d[8] = -0.125 * rp * sp * (r + s - t - 2) - 0.125 * rp * sp * tm;
+            d[11] = -0.125 * rm * sp * (-r + s - t - 2) - 0.125 * rm * sp * tm;
+            d[14] = 0.125 * rm * sm * (-r - s + t - 2) + 0.125 * rm * sm * tp;
+            d[17] = 0.125 * rp * sm * (r - s + t - 2) + 0.125 * rp * sm * tp;
+            d[20] = 0.125 * rp * sp * (r + s + t - 2) + 0.125 * rp * sp * tp;
+            d[23] = 0.125 * rm * sp * (-r + s + t - 2) + 0.125 * rm * sp * tp;
+            d[26] = -0.25 * (1 - r * r) * sm; d[29] = -0.25 * rp * (1 - s * s); d[32] = -0.25 * (1 - r * r) * sp;
+            d[35] = -0.25 * rm * (1 - s * s); d[38] = 0.25 * (1 - r * r) * sm; d[41] = 0.25 * rp * (1 - s * s);
+            d[44] = 0.25 * (1 - r * r) * sp; d[47] = 0.25 * rm * (1 - s * s); d[50] = -0.5 * t * rm * sm;
+            d[53] = -0.5 * t * rp * sm; d[56] = -0.5 * t * rp * sp; d[59] = -0.5 * t * rm * sp;
         }
         return;
     }

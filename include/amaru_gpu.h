@@ -151,6 +151,16 @@ int amr_set_youngs(amr_model *m, const double *E);
 
 /* ---- element / assembly operations (the drop-in for mount_K) ---- */
 
+/* Element-stiffness arithmetic of amr_assemble_K.
+ * AMR_ASSEMBLY_FAST (default): per node pair, K_ab = lambda T + mu T^T + mu tr(T) I - P
+ *   with FMA accumulation; the form the Newton loop uses.
+ * AMR_ASSEMBLY_REFERENCE: B^T (D B) in the operation order of elem_stiffness
+ *   (src/mech/elem/mech-solid.jl:142-158) without FMA contraction, so entries that
+ *   are zero only by cancellation fall under the |Ke_ij| >= eps() rule as the
+ *   reference's own arithmetic decides; used to export K in the reference layout. */
+enum { AMR_ASSEMBLY_FAST = 0, AMR_ASSEMBLY_REFERENCE = 1 };
+int amr_set_assembly(amr_model *m, int32_t mode);
+
 /* mount_K (src/mech/mech-solver.jl:78-110): element stiffness
  * (src/mech/elem/mech-solid.jl:124-166) with the tangent of each IP's current
  * state, deterministic assembly into the device pattern. */

@@ -55,7 +55,8 @@ def build(force=False):
         return LIB_PATH
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src,
+                           "-lm"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
