@@ -22,6 +22,7 @@ LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
 LOAD_FACET, LOAD_BODY = 0, 1
 SOLVER_MIXED, SOLVER_FP64 = 0, 1
 ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
+KERNEL_SPMV32, KERNEL_RESIDUAL64 = 0, 1
 
 
 class AmrError(RuntimeError):
@@ -59,7 +60,8 @@ class StageParams(C.Structure):
 
 class StageStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("increments", C.c_int32), ("iterations", C.c_int32),
-                ("krylov_iterations", C.c_int32), ("residue", C.c_double), ("T", C.c_double)]
+                ("krylov_iterations", C.c_int32), ("residue", C.c_double), ("T", C.c_double),
+                ("seconds", C.c_double), ("solve_seconds", C.c_double)]
 
 
 # Every exported entry point of include/amaru_gpu.h with its ctypes signature.
@@ -84,6 +86,9 @@ SIGNATURES = {
     "amr_assemble_loads": (C.c_int, [P, C.POINTER(Load), C.c_int32, C.c_double, P]),
     "amr_solve": (C.c_int, [P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
     "amr_stage_run": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
+    "amr_stage_run_dev": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
+    "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_default_solve_opts": (None, [C.POINTER(SolveOpts)]),
     "amr_default_stage_params": (None, [C.POINTER(StageParams)]),
 }
@@ -257,6 +262,23 @@ class DeviceModel:
         st = StageStats()
         rc = lib().amr_stage_run(self.h, ptr(Uex), ptr(Fex), C.byref(params), ptr(U), ptr(F), C.byref(st))
         return rc, U, F, st
+
+    def stage_run_dev(self, d_Uex, d_Fex, params, d_U, d_F):
+        """Device-pointer variant: arguments are raw CUDA device addresses (ints) of ndofs doubles."""
+        st = StageStats()
+        rc = lib().amr_stage_run_dev(self.h, C.c_void_p(d_Uex), C.c_void_p(d_Fex), C.byref(params), C.c_void_p(d_U),
+                                     C.c_void_p(d_F), C.byref(st))
+        return rc, st
+
+    def time_kernel(self, which, reps):
+        t, b = C.c_double(), C.c_double()
+        check(self.h, lib().amr_time_kernel(self.h, which, reps, C.byref(t), C.byref(b)))
+        return t.value, b.value
+
+    def launch_count(self):
+        n = C.c_int64()
+        check(self.h, lib().amr_launch_count(self.h, C.byref(n)))
+        return n.value
 
     def last_error(self):
         buf = C.create_string_buffer(1024)

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -101,6 +102,9 @@ struct amr_model {
 };
 
 // helpers
+// process-wide count of kernel launches by this library (reported by amr_launch_count)
+extern std::atomic<long long> amr_g_launches;
+#define AMR_COUNT(n) amr_g_launches.fetch_add((n), std::memory_order_relaxed)
 #define AMR_CUDA(call)                                                                 \
     do {                                                                               \
         cudaError_t e_ = (call);                                                       \

@@ -10,6 +10,9 @@
 
 #include "amr_internal.h"
 
+std::atomic<long long> amr_g_launches{0};
+double amr_time_solver_kernel(amr_model *m, int which, int reps);
+
 namespace {
 
 thread_local std::string g_create_error;
@@ -44,6 +47,7 @@ __global__ void k_free_mask(int64_t nnodes, int B, const int64_t *eq_id, int64_t
 void vec(amr_model *m, int op, double a, const double *x, double b, const double *y, double *o) {
     int64_t n = m->nnodes * m->B;
     k_vec<<<nblk(n, 256), 256, 0, m->stream>>>(n, op, a, x, b, y, o, m->free_mask);
+    AMR_COUNT(1);
 }
 
 void upload(void *d, const void *h, size_t bytes, cudaStream_t s) {
@@ -335,6 +339,7 @@ int amr_set_dofs(amr_model *m, const int64_t *eq_id, int64_t ndofs, int64_t nu) 
         upload(m->eq_id, eq_id, 3 * m->nnodes * sizeof(int64_t), m->stream);
         int64_t nt = m->nnodes * m->B;
         k_free_mask<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->eq_id, nu, m->free_mask);
+        AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
         AMR_CUDA(cudaStreamSynchronize(m->stream));
         m->dofs_set = true;
@@ -572,6 +577,57 @@ int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_
     });
 }
 
+int amr_stage_run_dev(amr_model *m, const double *d_Uex, const double *d_Fex, const amr_stage_params *p,
+                      double *d_U, double *d_F, amr_stage_stats *stats) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        amr_stage_params prm;
+        amr_default_stage_params(&prm);
+        if (p) prm = *p;
+        double *uex = m->vtmp[2], *fex = m->vtmp[3], *u = m->vtmp[4], *f = m->vtmp[5];
+        amr_eq_to_nm(m, d_Uex, uex);
+        amr_eq_to_nm(m, d_Fex, fex);
+        int rc = amr_stage_device(m, uex, fex, prm, u, f, stats);
+        if (rc == AMR_OK || rc == AMR_ESTAGE) {
+            amr_nm_to_eq(m, u, d_U);
+            amr_nm_to_eq(m, f, d_F);
+            AMR_CUDA(cudaStreamSynchronize(m->stream));
+        }
+        return rc;
+    });
+}
+
+int amr_launch_count(const amr_model *m, int64_t *count) {
+    if (!count) return AMR_EINVAL;
+    (void)m;
+    *count = amr_g_launches.load();
+    return AMR_OK;
+}
+
+int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch) {
+    return guarded(m, [&] {
+        if (!m->K_valid) throw AmrError(AMR_EINVAL, "assemble K first");
+        if (reps < 1) throw AmrError(AMR_EINVAL, "reps must be >= 1");
+        const double nb = (double)m->nblocks, nn = (double)m->nnodes, B = m->B, BB = m->BB;
+        double t = 0.0, bytes = 0.0;
+        switch (kernel) {
+        case AMR_KERNEL_SPMV32:  // K32 blocks + block columns + row pointers; z, p read, p, q written
+            t = amr_time_solver_kernel(m, AMR_KERNEL_SPMV32, reps);
+            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 4.0;
+            break;
+        case AMR_KERNEL_RESIDUAL64:  // K64 blocks + columns + row pointers; u, b read; r32, z written; Minv read
+            t = amr_time_solver_kernel(m, AMR_KERNEL_RESIDUAL64, reps);
+            bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 + 8.0 + 4.0 + 4.0 + 1.0) + nn * BB * 4.0;
+            break;
+        default:
+            throw AmrError(AMR_EINVAL, "kernel not timed by this entry point");
+        }
+        if (avg_seconds) *avg_seconds = t;
+        if (bytes_per_launch) *bytes_per_launch = bytes;
+        return AMR_OK;
+    });
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -592,6 +648,10 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
     };
     int status = AMR_OK;
     amr_stage_stats st{};
+    cudaEvent_t t0, t1;
+    AMR_CUDA(cudaEventCreate(&t0));
+    AMR_CUDA(cudaEventCreate(&t1));
+    AMR_CUDA(cudaEventRecord(t0, s));
     try {
         for (double *x : {U, F, R, dUa, dUi, Rc, dFin}) AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
         double tol = p.tol, rtol = p.rtol, dTmin = p.dTmin;
@@ -606,6 +666,9 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
         double T = 0.0, dT = 1.0 / nincs, dTbk = 0.0;
         if (autoinc) dT = std::min({dT, p.dTmax, dTcheck, p.dT0});
         const double p1 = 1.0, q11 = 1.0;
+        // every stage mounts K at least once (the reference mounts it at every iteration;
+        // a state-independent K is reused across the iterations of the stage only)
+        m->K_valid = false;
         // committed states = current states at stage start
         AMR_CUDA(cudaMemcpyAsync(m->stbk, m->st, (size_t)AMR_NST * m->nip_total * sizeof(double),
                                  cudaMemcpyDeviceToDevice, s));
@@ -632,6 +695,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 vec(m, V_SET_AXPBY, q11, R, 0.0, nullptr, Rtr);
                 AmrSolveResult sr = amr_solve_device(m, dUitr, Rtr, reac, p.linear);
                 st.krylov_iterations += sr.iterations;
+                st.solve_seconds += sr.seconds;
                 if (sr.status) { syserror = true; sysmsg = "solve_system!: Krylov solver did not converge"; break; }
                 double umax = amr_norm_inf(m, dUitr, m->free_mask);
                 if (!(umax <= 1e8)) { syserror = true; sysmsg = "solve_system!: Possible syngular matrix"; break; }
@@ -704,11 +768,19 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
         }
         st.T = T;
         st.status = status;
-        AMR_CUDA(cudaStreamSynchronize(s));
+        AMR_CUDA(cudaEventRecord(t1, s));
+        AMR_CUDA(cudaEventSynchronize(t1));
+        float ms = 0.f;
+        AMR_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+        st.seconds = ms * 1e-3;
     } catch (...) {
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
         release();
         throw;
     }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
     release();
     if (stats) *stats = st;
     return status;

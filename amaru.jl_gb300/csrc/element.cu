@@ -871,6 +871,7 @@ void launch_stiff(amr_model *m, const AmrGroup &g) {
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     unsigned grid = nblk(g.count, epb);
     stiffness_kernel<DIM, NEN><<<grid, threads, smem, m->stream>>>(margs(m), ga, epb, m->Kel, m->st, m->d_status);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }
 
@@ -878,6 +879,7 @@ template <int DIM, int NEN>
 void launch_stiff_ref(amr_model *m, const AmrGroup &g) {
     GroupArgs ga{g.tab, g.nip, g.first, g.count};
     stiffness_ref_kernel<DIM, NEN><<<(unsigned)g.count, 256, 0, m->stream>>>(margs(m), ga, m->Kel, m->st, m->d_status);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }
 
@@ -894,6 +896,7 @@ void launch_internal(amr_model *m, const AmrGroup &g, const double *dU) {
     unsigned grid = nblk(g.count, epb);
     internal_kernel<DIM, NEN><<<grid, threads, smem, m->stream>>>(margs(m), ga, epb, dU, m->stbk, m->st, m->Fel,
                                                                   m->d_status);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }
 
@@ -938,14 +941,16 @@ void amr_stiffness(amr_model *m) {
                 [&](auto n) { launch_stiff<2, decltype(n)::value>(m, g); });
     }
     unsigned grid = nblk(m->nnodes * 32, 256);
-    if (m->B == 3)
+    if (m->B == 3) {
         gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
                                                       m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
                                                       m->Minv32, m->Minv64, m->d_status);
-    else
+    } else {
         gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
                                                       m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
                                                       m->Minv32, m->Minv64, m->d_status);
+    }
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }
 
@@ -958,6 +963,7 @@ void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm) {
     int64_t nt = m->nnodes * m->B;
     node_gather_kernel<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->inc_ptr, m->inc, m->conn_ptr,
                                                              m->fel_ptr, m->Fel, dFin_nm, 0, m->d_status);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }
 
@@ -1031,8 +1037,10 @@ void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double
         load_kernel<<<nblk(L.nitems, 128), 128, 0, s>>>(L.kind, L.dir, L.edge_key, np, fd, nq, dtab, ditems, L.nitems,
                                                         m->conn, m->conn_ptr, dinv, m->coords, m->ndim,
                                                         m->stressmodel, m->thickness, dcf, t, Fst);
+        AMR_COUNT(1);
         int64_t nt = m->nnodes * m->B;
         load_gather_kernel<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, m->B, dptr, dlst, np, Fst, F_nm);
+        AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
         AMR_CUDA(cudaStreamSynchronize(s));
         amr_free(dtab); amr_free(dcf); amr_free(Fst); amr_free(ditems); amr_free(dptr); amr_free(dlst);

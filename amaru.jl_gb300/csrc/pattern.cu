@@ -203,11 +203,14 @@ void amr_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s) {
     amr_alloc(&sums, nb);
     amr_alloc(&soff, nb + 1);
     scan_blocks<<<(unsigned)nb, kScanBlock, 0, s>>>(in, out, sums, n);
+    AMR_COUNT(1);
     if (nb > 1) {
         amr_scan_i64(sums, soff, nb, s);
         scan_add<<<nblk(n, 256), 256, 0, s>>>(out, soff, n);
+        AMR_COUNT(1);
     }
     set_total<<<1, 1, 0, s>>>(out, in, n);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
     AMR_CUDA(cudaStreamSynchronize(s));
     amr_free(sums);
@@ -226,13 +229,16 @@ void amr_build_pattern(amr_model *m) {
     AMR_CUDA(cudaMemcpyAsync(inv, m->inv_perm.data(), m->nelems * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaMemsetAsync(cnt, 0, m->nnodes * sizeof(int64_t), s));
     inc_count<<<nblk(nconn, 256), 256, 0, s>>>(m->conn, nconn, cnt);
+    AMR_COUNT(1);
     amr_alloc(&m->inc_ptr, m->nnodes + 1);
     amr_scan_i64(cnt, m->inc_ptr, m->nnodes, s);
     m->ninc = nconn;
     amr_alloc(&m->inc, nconn);
     AMR_CUDA(cudaMemsetAsync(cnt, 0, m->nnodes * sizeof(int64_t), s));
     inc_fill<<<nblk(m->nelems, 128), 128, 0, s>>>(m->conn, m->conn_ptr, m->nelems, perm, m->inc_ptr, cnt, m->inc);
+    AMR_COUNT(1);
     inc_sort<<<nblk(m->nnodes, 128), 128, 0, s>>>(m->inc_ptr, m->inc, m->nnodes, inv);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 
     // 2. node-block pattern
@@ -242,6 +248,7 @@ void amr_build_pattern(amr_model *m) {
     unsigned gp = nblk(m->nnodes, kPatWarps);
     pattern_rows<<<gp, kPatWarps * 32, 0, s>>>(m->conn, m->conn_ptr, m->inc_ptr, m->inc, m->nnodes, nullptr, cnt,
                                                nullptr, overflow);
+    AMR_COUNT(1);
     int32_t hov = 0;
     AMR_CUDA(cudaMemcpyAsync(&hov, overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaStreamSynchronize(s));
@@ -254,6 +261,7 @@ void amr_build_pattern(amr_model *m) {
     amr_alloc(&m->bcol, m->nblocks);
     pattern_rows<<<gp, kPatWarps * 32, 0, s>>>(m->conn, m->conn_ptr, m->inc_ptr, m->inc, m->nnodes, m->brow_ptr,
                                                nullptr, m->bcol, overflow);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 
     // 3. contributions, element order per block
@@ -263,6 +271,7 @@ void amr_build_pattern(amr_model *m) {
     unsigned gc = nblk(m->nnodes * 32, 256);
     contrib_rows<<<gc, 256, 0, s>>>(m->conn, m->conn_ptr, m->kel_ptr, m->inc_ptr, m->inc, m->nnodes, m->brow_ptr,
                                     m->bcol, bcnt, nullptr, nullptr);
+    AMR_COUNT(1);
     amr_alloc(&m->contrib_ptr, m->nblocks + 1);
     amr_scan_i64(bcnt, m->contrib_ptr, m->nblocks, s);
     AMR_CUDA(cudaMemcpyAsync(&m->ncontrib, m->contrib_ptr + m->nblocks, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -271,6 +280,7 @@ void amr_build_pattern(amr_model *m) {
     AMR_CUDA(cudaMemsetAsync(bcnt, 0, m->nblocks * sizeof(int64_t), s));
     contrib_rows<<<gc, 256, 0, s>>>(m->conn, m->conn_ptr, m->kel_ptr, m->inc_ptr, m->inc, m->nnodes, m->brow_ptr,
                                     m->bcol, bcnt, m->contrib_ptr, m->contrib);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
     // host copy of the pattern (export in the reference layout)
     m->h_brow_ptr.resize(m->nnodes + 1);

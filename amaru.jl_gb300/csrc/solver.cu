@@ -511,6 +511,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     unsigned g = (unsigned)w->grid;
     k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac, w->r32,
                                        w->z32, m->Minv32, w->ctl, w->partials, 1, tol2);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
     int cur = 0;
     int every = o.refine_every > 0 ? o.refine_every : 32;
@@ -527,17 +528,21 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
         for (int it = 0; it < nit; it++) {
             k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->p32[cur],
                                                w->p32[cur ^ 1], w->q32, w->ctl, w->partials);
+            AMR_COUNT(1);
             k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[cur ^ 1], w->q32, w->x32, w->r32, w->z32,
                                                  w->ctl, w->partials, stop_rr);
+            AMR_COUNT(1);
             cur ^= 1;
         }
         AMR_CUDA(cudaGetLastError());
         res.iterations += nit;
         // fold the FP32 correction into the FP64 solution and refresh the true residual
         k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
+        AMR_COUNT(1);
         AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
         k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac,
                                            w->r32, w->z32, m->Minv32, w->ctl, w->partials, 0, tol2);
+        AMR_COUNT(1);
         res.refinements++;
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
@@ -567,6 +572,7 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
         AMR_CUDA(cudaMemsetAsync(cnt, 0, nu * sizeof(int64_t), s));
         int64_t nt = m->nnodes * B;
         k_csr_count<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, cnt);
+        AMR_COUNT(1);
         amr_alloc(&w->crp, nu + 1);
         amr_scan_i64(cnt, w->crp, nu, s);
         AMR_CUDA(cudaMemcpy(&w->csr_nnz, w->crp + nu, sizeof(int64_t), cudaMemcpyDeviceToHost));
@@ -575,6 +581,7 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
         amr_alloc(&w->cval, w->csr_nnz);
         k_csr_fill<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, m->nblocks, w->crp,
                                                  w->ccol, w->csrc);
+        AMR_COUNT(1);
         amr_free(cnt);
         amr_alloc(&w->dinv, nu); amr_alloc(&w->cx, nu); amr_alloc(&w->cr, nu); amr_alloc(&w->cz, nu);
         amr_alloc(&w->cp[0], nu); amr_alloc(&w->cp[1], nu); amr_alloc(&w->cq, nu); amr_alloc(&w->cb, nu);
@@ -584,15 +591,20 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
     }
     // values of the last assembly (part of assembly for this path, not of the solve time)
     k_csr_values<<<nblk(w->csr_nnz, 256), 256, 0, s>>>(w->csr_nnz, w->csrc, m->K64, w->cval);
+    AMR_COUNT(1);
     k_csr_diag<<<nblk(nu, 256), 256, 0, s>>>(nu, w->crp, w->ccol, w->cval, w->dinv);
+    AMR_COUNT(1);
     // b_red = b - K12 u2: tmp = K64 x (x holds prescribed values, zero at free slots on entry)
     int64_t nt = m->nnodes * B;
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, x,
                                                          w->tmp);
+    AMR_COUNT(1);
     // cb = b - K12 u2 on the free eq rows (b and K64 x scattered to eq order)
     k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, (double *)b, w->cb, 1);
+    AMR_COUNT(1);
     k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, w->tmp, w->cq, 1);
+    AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
     double tol2 = o.rtol * o.rtol;
     AMR_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), s));
@@ -600,6 +612,7 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
     unsigned g = (unsigned)w->grid;
     amr_axpy_d(nu, -1.0, w->cq, w->cb, s);
     k_csr_init<<<g, kThreads, 0, s>>>(nu, w->cb, w->dinv, w->cr, w->cz, w->cx, w->ctl, w->partials);
+    AMR_COUNT(1);
     int cur = 0;
     int every = o.refine_every > 0 ? o.refine_every : 32;
     for (;;) {
@@ -613,8 +626,10 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
         for (int it = 0; it < nit; it++) {
             k_csr_spmv<<<g, kThreads, 0, s>>>(nu, w->crp, w->ccol, w->cval, w->cz, w->cp[cur], w->cp[cur ^ 1], w->cq,
                                               w->ctl, w->partials);
+            AMR_COUNT(1);
             k_csr_update<<<g, kThreads, 0, s>>>(nu, w->dinv, w->cp[cur ^ 1], w->cq, w->cx, w->cr, w->cz, w->ctl,
                                                 w->partials, tol2);
+            AMR_COUNT(1);
             cur ^= 1;
         }
         AMR_CUDA(cudaGetLastError());
@@ -627,8 +642,10 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
     res.seconds = ms * 1e-3;
     // x (node-major) free slots <- cx ; reactions and the true residual from the BSR FP64 matrix
     k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, x, w->cx, 0);
+    AMR_COUNT(1);
     k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, x,
                                                          w->tmp);
+    AMR_COUNT(1);
     double rr = amr_masked_residual(m, b, w->tmp, reac);
     Ctl c = *w->h_ctl;
     res.rel_residual = c.bnorm2 > 0 ? std::sqrt(rr / c.bnorm2) : 0.0;
@@ -696,6 +713,7 @@ __global__ void k_absmax(int64_t n, const double *v, const uint8_t *fm, double *
 void amr_axpy_d(int64_t n, double a, const double *x, double *y, cudaStream_t s) {
     if (n <= 0) return;
     k_axpy<<<nblk(n, 256), 256, 0, s>>>(n, a, x, y);
+    AMR_COUNT(1);
 }
 
 double amr_masked_residual(amr_model *m, const double *b, const double *Kx, double *reac) {
@@ -703,6 +721,7 @@ double amr_masked_residual(amr_model *m, const double *b, const double *Kx, doub
     double *out = (double *)(w->partials + 3 * (size_t)w->grid);
     k_masked_res<<<w->grid, kThreads, 0, m->stream>>>(w->n, m->free_mask, b, Kx, reac, w->partials, &w->ctl->ticket[3],
                                                       out);
+    AMR_COUNT(1);
     double h = 0.0;
     AMR_CUDA(cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     AMR_CUDA(cudaStreamSynchronize(m->stream));
@@ -713,6 +732,7 @@ double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask) {
     AmrSolveWork *w = work(m);
     double *out = (double *)(w->partials + 3 * (size_t)w->grid);
     k_absmax<<<w->grid, kThreads, 0, m->stream>>>(w->n, v, mask, w->partials, &w->ctl->ticket[3], out);
+    AMR_COUNT(1);
     double h = 0.0;
     AMR_CUDA(cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     AMR_CUDA(cudaStreamSynchronize(m->stream));
@@ -723,15 +743,66 @@ void amr_eq_to_nm(amr_model *m, const double *d_eq, double *d_nm) {
     int64_t nt = m->nnodes * m->B;
     AMR_CUDA(cudaMemsetAsync(d_nm, 0, nt * sizeof(double), m->stream));
     k_scatter_eq<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->eq_id, m->ndofs, d_nm, (double *)d_eq, 0);
+    AMR_COUNT(1);
 }
 
 void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq) {
     int64_t nt = m->nnodes * m->B;
     k_scatter_eq<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->eq_id, m->ndofs, (double *)d_nm, d_eq, 1);
+    AMR_COUNT(1);
 }
 
 AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
     if (o.method == AMR_SOLVER_FP64)
         return m->B == 3 ? solve_fp64_csr<3>(m, x, b, reac, o) : solve_fp64_csr<2>(m, x, b, reac, o);
     return m->B == 3 ? solve_mixed<3>(m, x, b, reac, o) : solve_mixed<2>(m, x, b, reac, o);
+}
+
+// ---- kernel timing for the roofline report (CUDA events on the handle's stream) ----
+template <int B>
+static double time_spmv32(amr_model *m, int reps) {
+    AmrSolveWork *w = work(m);
+    cudaStream_t s = m->stream;
+    unsigned g = (unsigned)w->grid;
+    Ctl c{};
+    c.rz = 1.0;
+    c.beta = 0.5;
+    AMR_CUDA(cudaMemcpyAsync(w->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    for (int i = 0; i < reps; i++) {
+        k_spmv32<B><<<g, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->p32[i & 1],
+                                           w->p32[(i & 1) ^ 1], w->q32, w->ctl, w->partials);
+        AMR_COUNT(1);
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    return ms * 1e-3 / reps;
+}
+
+template <int B>
+static double time_residual64(amr_model *m, int reps) {
+    AmrSolveWork *w = work(m);
+    cudaStream_t s = m->stream;
+    unsigned g = (unsigned)w->grid;
+    double *u = m->vtmp[5], *b = m->vtmp[6];
+    AMR_CUDA(cudaMemsetAsync(u, 0, w->n * sizeof(double), s));
+    AMR_CUDA(cudaMemsetAsync(b, 0, w->n * sizeof(double), s));
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    for (int i = 0; i < reps; i++) {
+        k_refine<B><<<g, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, u,
+                                           nullptr, w->r32, w->z32, m->Minv32, w->ctl, w->partials, 1, 1e-16);
+        AMR_COUNT(1);
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    return ms * 1e-3 / reps;
+}
+
+double amr_time_solver_kernel(amr_model *m, int which, int reps) {
+    if (which == AMR_KERNEL_SPMV32) return m->B == 3 ? time_spmv32<3>(m, reps) : time_spmv32<2>(m, reps);
+    return m->B == 3 ? time_residual64<3>(m, reps) : time_residual64<2>(m, reps);
 }

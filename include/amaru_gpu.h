@@ -126,6 +126,8 @@ typedef struct {
     int32_t krylov_iterations;
     double residue;          /* last Newton residue ||R||inf */
     double T;                /* pseudo-time reached */
+    double seconds;          /* device time of the stage (CUDA events on the handle's stream) */
+    double solve_seconds;    /* device time spent in the linear solves */
 } amr_stage_stats;
 
 /* ---- lifecycle ---- */
@@ -199,6 +201,22 @@ int amr_solve(amr_model *m, double *U, double *F, const amr_solve_opts *opts, am
  * :394-397), IP states are committed. */
 int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params *p, double *U,
                   double *F, amr_stage_stats *stats);
+
+/* amr_stage_run with device-resident vectors: d_Uex, d_Fex, d_U, d_F are device
+ * pointers to ndofs doubles in eq_id order (for callers that keep their loads
+ * and results on the GPU across stages). */
+int amr_stage_run_dev(amr_model *m, const double *d_Uex, const double *d_Fex, const amr_stage_params *p,
+                      double *d_U, double *d_F, amr_stage_stats *stats);
+
+/* ---- diagnostics (no counterpart in the reference) ---- */
+/* Average device time of one launch of a hot kernel over `reps` launches,
+ * timed with CUDA events on the handle's stream, and its algorithmic bytes
+ * per launch.  Needs a preceding amr_assemble_K (and a solve for the SpMV). */
+enum { AMR_KERNEL_SPMV32 = 0, AMR_KERNEL_RESIDUAL64 = 1, AMR_KERNEL_STIFFNESS = 2, AMR_KERNEL_GATHER = 3,
+       AMR_KERNEL_INTERNAL = 4 };
+int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch);
+/* Number of kernels this handle has launched since it was created. */
+int amr_launch_count(const amr_model *m, int64_t *count);
 
 /* Default parameter blocks (the reference's KwArgInfo defaults). */
 void amr_default_solve_opts(amr_solve_opts *o);
