@@ -367,8 +367,7 @@ int amr_set_youngs(amr_model *m, const double *E) {
 int amr_set_assembly(amr_model *m, int32_t mode) {
     return guarded(m, [&] {
         if (mode != AMR_ASSEMBLY_FAST && mode != AMR_ASSEMBLY_REFERENCE) throw AmrError(AMR_EINVAL, "bad assembly mode");
-        if (m->assembly_mode != mode) m->K_valid = false;
-        m->assembly_mode = mode;
+        m->assembly_mode = mode;  // applies to the next assembly; the current K stays valid
         return AMR_OK;
     });
 }
@@ -611,9 +610,9 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
         const double nb = (double)m->nblocks, nn = (double)m->nnodes, B = m->B, BB = m->BB;
         double t = 0.0, bytes = 0.0;
         switch (kernel) {
-        case AMR_KERNEL_SPMV32:  // K32 blocks + block columns + row pointers; z, p read, p, q written
+        case AMR_KERNEL_SPMV32:  // K32 blocks + block columns + row pointers; p read once, q written
             t = amr_time_solver_kernel(m, AMR_KERNEL_SPMV32, reps);
-            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 4.0;
+            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 2.0;
             break;
         case AMR_KERNEL_RESIDUAL64:  // K64 blocks + columns + row pointers; u, b read; r32, z written; Minv read
             t = amr_time_solver_kernel(m, AMR_KERNEL_RESIDUAL64, reps);

@@ -23,8 +23,8 @@
 namespace {
 
 struct Ctl {
-    double rz, pq, alpha, beta, rr, rr_true, bnorm2;
-    int32_t stop, converged, breakdown, pad;
+    double rz, pq, alpha, beta, rr, rr_true, bnorm2, gold, aold;
+    int32_t stop, converged, breakdown, iters, first, pad;
     unsigned int ticket[4];
 };
 
@@ -99,89 +99,119 @@ __device__ bool grid_sum(double (&v)[NV], double *partials, unsigned int *ticket
 }
 
 // ---------------------------------------------------------------------------
-// Mixed path kernels (BSR, B x B blocks, SoA values [BB][nblocks])
+// Mixed path kernels (BSR, B x B blocks, SoA values [BB][nblocks]).
+// Preconditioned CG in three launches per iteration: p = z + beta p, then
+// q = K32 p with pq = p.q and alpha = gamma / pq, then the vector updates
+// with gamma = r.z and beta.  Keeping the direction update out of the SpMV
+// lets the SpMV gather a single vector.
 // ---------------------------------------------------------------------------
-// p_new = z + beta p_old (own rows), q = K32 p_new, pq = p_new . q
+template <int B>
+__global__ void k_pupdate32(int64_t n, const float *__restrict__ z, float *__restrict__ p, const Ctl *ctl) {
+    if (ctl->stop) return;
+    const float beta = ctl->first ? 0.0f : (float)ctl->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * B; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fmaf(beta, p[i], z[i]);
+}
+
+// q = K32 p ; pq = p.q ; alpha = gamma / pq
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_spmv32(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
                                                      const int32_t *__restrict__ cj, const float *__restrict__ A,
-                                                     const float *__restrict__ z, const float *__restrict__ pold,
-                                                     float *__restrict__ pnew, float *__restrict__ q, Ctl *ctl,
+                                                     const float *__restrict__ z, float *__restrict__ sv, Ctl *ctl,
                                                      double *partials) {
     if (ctl->stop) return;
-    const float beta = (float)ctl->beta;
     int lane = threadIdx.x & 31;
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    double dot = 0.0;
+    // FP32 partial dot per thread: per-row FP64 arithmetic would saturate this GPU's narrow FP64 pipe
+    float dot = 0.0f;
     for (int64_t n = warp; n < nn; n += nw) {
         float acc[B];
 #pragma unroll
         for (int c = 0; c < B; c++) acc[c] = 0.0f;
-        for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
-            int64_t j = cj[k];
-            float pj[B];
+        const int64_t k1 = rp[n + 1];
+        int64_t k = rp[n] + lane;
+        for (; k + 32 < k1; k += 64) {  // two blocks per lane in flight; the matrix streams (evict-first)
+            const int64_t j0 = __ldcs(cj + k), j1 = __ldcs(cj + k + 32);
+            float a0[B * B], a1[B * B], z0[B], z1[B];
 #pragma unroll
-            for (int d = 0; d < B; d++) pj[d] = fmaf(beta, pold[j * B + d], z[j * B + d]);
+            for (int q = 0; q < B * B; q++) {
+                a0[q] = __ldcs(A + (int64_t)q * nb + k);
+                a1[q] = __ldcs(A + (int64_t)q * nb + k + 32);
+            }
+#pragma unroll
+            for (int d = 0; d < B; d++) { z0[d] = __ldg(z + j0 * B + d); z1[d] = __ldg(z + j1 * B + d); }
 #pragma unroll
             for (int c = 0; c < B; c++)
 #pragma unroll
-                for (int d = 0; d < B; d++) acc[c] = fmaf(A[(int64_t)(c * B + d) * nb + k], pj[d], acc[c]);
+                for (int d = 0; d < B; d++) acc[c] = fmaf(a1[c * B + d], z1[d], fmaf(a0[c * B + d], z0[d], acc[c]));
+        }
+        if (k < k1) {
+            const int64_t j0 = __ldcs(cj + k);
+            float z0[B];
+#pragma unroll
+            for (int d = 0; d < B; d++) z0[d] = __ldg(z + j0 * B + d);
+#pragma unroll
+            for (int c = 0; c < B; c++)
+#pragma unroll
+                for (int d = 0; d < B; d++) acc[c] = fmaf(__ldcs(A + (int64_t)(c * B + d) * nb + k), z0[d], acc[c]);
         }
 #pragma unroll
         for (int c = 0; c < B; c++) acc[c] = warp_sumf(acc[c]);
         if (lane == 0) {
 #pragma unroll
             for (int c = 0; c < B; c++) {
-                float pn = fmaf(beta, pold[n * B + c], z[n * B + c]);
-                pnew[n * B + c] = pn;
-                q[n * B + c] = acc[c];
-                dot += (double)pn * (double)acc[c];
+                sv[n * B + c] = acc[c];
+                dot = fmaf(z[n * B + c], acc[c], dot);
             }
         }
     }
-    double v[1] = {dot}, tot[1];
+    double v[1] = {(double)dot}, tot[1];
     if (grid_sum<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
         ctl->pq = tot[0];
         if (!(tot[0] > 0.0)) { ctl->breakdown = 1; ctl->stop = 1; }
-        else ctl->alpha = ctl->rz / tot[0];
+        else { ctl->alpha = ctl->rz / tot[0]; ctl->first = 0; }
     }
 }
 
-// x += alpha p ; r -= alpha q ; z = Minv r ; rz, rr partials ; beta
+// x += alpha p ; r -= alpha q ; z = Minv r ; gamma = r.z, |r|^2 ; beta = gamma / gamma_old
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *__restrict__ Minv,
                                                        const float *__restrict__ p, const float *__restrict__ q,
                                                        float *__restrict__ x, float *__restrict__ r,
                                                        float *__restrict__ z, Ctl *ctl, double *partials,
-                                                       double stop_rr) {
+                                                       double stop_rr, double delta2) {
     if (ctl->stop) return;
     const float alpha = (float)ctl->alpha;
-    double rz = 0.0, rr = 0.0;
+    float rz = 0.0f, rr = 0.0f;
     for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
         float rv[B];
 #pragma unroll
         for (int c = 0; c < B; c++) {
-            x[n * B + c] = fmaf(alpha, p[n * B + c], x[n * B + c]);
-            rv[c] = fmaf(-alpha, q[n * B + c], r[n * B + c]);
-            r[n * B + c] = rv[c];
+            const int64_t i = n * B + c;
+            x[i] = fmaf(alpha, p[i], x[i]);
+            rv[c] = fmaf(-alpha, q[i], r[i]);
+            r[i] = rv[c];
         }
 #pragma unroll
         for (int c = 0; c < B; c++) {
-            float s = 0.0f;
+            float zz = 0.0f;
 #pragma unroll
-            for (int d = 0; d < B; d++) s = fmaf(Minv[n * B * B + c * B + d], rv[d], s);
-            z[n * B + c] = s;
-            rz += (double)rv[c] * (double)s;
-            rr += (double)rv[c] * (double)rv[c];
+            for (int d = 0; d < B; d++) zz = fmaf(Minv[n * B * B + c * B + d], rv[d], zz);
+            z[n * B + c] = zz;
+            rz = fmaf(rv[c], zz, rz);
+            rr = fmaf(rv[c], rv[c], rr);
         }
     }
-    double v[2] = {rz, rr}, tot[2];
+    double v[2] = {(double)rz, (double)rr}, tot[2];
     if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
         ctl->beta = tot[0] / ctl->rz;
         ctl->rz = tot[0];
         ctl->rr = tot[1];
-        if (!(tot[1] > stop_rr)) ctl->stop = 1;  // recursive residual small (or NaN): refresh now
+        ctl->iters += 1;
+        // reliable update: refresh the FP64 true residual once the recursive one has dropped by delta
+        // since the last refresh, or looks converged (or is NaN)
+        if (!(tot[1] > stop_rr) || tot[1] <= delta2 * ctl->rr_true) ctl->stop = 1;
     }
 }
 
@@ -444,7 +474,8 @@ double amr_masked_residual(amr_model *m, const double *b, const double *Kx, doub
 
 struct AmrSolveWork {
     int64_t n = 0;               // nnodes * B
-    float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32[2] = {nullptr, nullptr}, *q32 = nullptr;
+    float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32[2] = {nullptr, nullptr}, *q32 = nullptr,
+          *s32 = nullptr;
     double *partials = nullptr;
     Ctl *ctl = nullptr;
     Ctl *h_ctl = nullptr;        // pinned
@@ -466,6 +497,8 @@ static AmrSolveWork *work(amr_model *m) {
         w->n = n;
         amr_free(w->x32); amr_free(w->r32); amr_free(w->z32); amr_free(w->p32[0]); amr_free(w->p32[1]);
         amr_free(w->q32);
+        amr_free(w->s32);
+        amr_alloc(&w->s32, n);
         amr_alloc(&w->x32, n); amr_alloc(&w->r32, n); amr_alloc(&w->z32, n); amr_alloc(&w->p32[0], n);
         amr_alloc(&w->p32[1], n); amr_alloc(&w->q32, n);
         int dev = 0, sms = 148;
@@ -487,6 +520,7 @@ void amr_solver_free(amr_model *m) {
     AmrSolveWork *w = m->sw;
     if (!w) return;
     amr_free(w->x32); amr_free(w->r32); amr_free(w->z32); amr_free(w->p32[0]); amr_free(w->p32[1]); amr_free(w->q32);
+    amr_free(w->s32);
     amr_free(w->partials); amr_free(w->ctl);
     if (w->h_ctl) cudaFreeHost(w->h_ctl);
     amr_free(w->crp); amr_free(w->csrc); amr_free(w->ccol); amr_free(w->cval); amr_free(w->dinv); amr_free(w->cx);
@@ -503,9 +537,14 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     int64_t nn = m->nnodes;
     AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
     double tol2 = o.rtol * o.rtol;
-    AMR_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), s));
     AMR_CUDA(cudaMemsetAsync(w->x32, 0, w->n * sizeof(float), s));
     AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, w->n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w->q32, 0, w->n * sizeof(float), s));
+    {
+        Ctl c0{};
+        c0.first = 1;
+        AMR_CUDA(cudaMemcpyAsync(w->ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    }
     // free slots of x start at zero (the reduced system's initial guess)
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     unsigned g = (unsigned)w->grid;
@@ -513,37 +552,44 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
                                        w->z32, m->Minv32, w->ctl, w->partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
-    int cur = 0;
-    int every = o.refine_every > 0 ? o.refine_every : 32;
+    int every = o.refine_every > 0 ? o.refine_every : 32;  // iterations between host checks
     double stop_rr_rel = 0.25 * 0.25 * tol2;  // refresh early once the FP32 residual looks converged
+    const double delta2 = 1e-2;                // refresh after a 10x drop of the residual
+    int since = 0;
     for (;;) {
         AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
         AMR_CUDA(cudaStreamSynchronize(s));
         Ctl c = *w->h_ctl;
+        res.iterations = c.iters;
         if (c.bnorm2 == 0.0 || c.converged) break;
         if (c.breakdown) { res.status = AMR_ENOCONV; break; }
-        if (res.iterations >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        if (c.iters >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        if (c.stop || since >= 16 * every) {
+            // fold the FP32 correction into the FP64 solution and refresh the true residual
+            k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
+            AMR_COUNT(1);
+            AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
+            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+                                               reac, w->r32, w->z32, m->Minv32, w->ctl, w->partials, 0, tol2);
+            AMR_COUNT(1);
+            res.refinements++;
+            since = 0;
+            continue;
+        }
         double stop_rr = stop_rr_rel * c.bnorm2;
-        int nit = std::min(every, o.max_iters - res.iterations);
+        int nit = std::min(every, o.max_iters - c.iters);
         for (int it = 0; it < nit; it++) {
-            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->p32[cur],
-                                               w->p32[cur ^ 1], w->q32, w->ctl, w->partials);
+            k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
             AMR_COUNT(1);
-            k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[cur ^ 1], w->q32, w->x32, w->r32, w->z32,
-                                                 w->ctl, w->partials, stop_rr);
+            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->p32[0], w->q32,
+                                               w->ctl, w->partials);
             AMR_COUNT(1);
-            cur ^= 1;
+            k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[0], w->q32, w->x32, w->r32, w->z32, w->ctl,
+                                                 w->partials, stop_rr, delta2);
+            AMR_COUNT(1);
         }
         AMR_CUDA(cudaGetLastError());
-        res.iterations += nit;
-        // fold the FP32 correction into the FP64 solution and refresh the true residual
-        k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
-        AMR_COUNT(1);
-        AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
-        k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac,
-                                           w->r32, w->z32, m->Minv32, w->ctl, w->partials, 0, tol2);
-        AMR_COUNT(1);
-        res.refinements++;
+        since += nit;
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));
@@ -766,12 +812,12 @@ static double time_spmv32(amr_model *m, int reps) {
     unsigned g = (unsigned)w->grid;
     Ctl c{};
     c.rz = 1.0;
-    c.beta = 0.5;
+    c.first = 1;
     AMR_CUDA(cudaMemcpyAsync(w->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        k_spmv32<B><<<g, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->p32[i & 1],
-                                           w->p32[(i & 1) ^ 1], w->q32, w->ctl, w->partials);
+        k_spmv32<B><<<g, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->s32,
+                                           w->ctl, w->partials);
         AMR_COUNT(1);
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));

@@ -230,7 +230,7 @@ def run_ours(a):
                                                                              sizes["nblocks"] * 72 / 1e9),
                    "parallelism": "replicas (one model per GPU)", "setup_s": setup_s},
         "solve": dict(solve_cmp, step_solve_s=float(np.mean(solve_s)), step_krylov_iters=int(np.mean(kry))),
-        "roofline": {"bound": "hbm", "kernel": "k_spmv32 (FP32 BSR SpMV + fused p-update and dot)",
+        "roofline": {"bound": "hbm", "kernel": "k_spmv32 (FP32 BSR SpMV q = K p with fused p.q)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_kind, "traffic": traffic, "bytes_per_launch": spmv_b,
                      "avg_launch_s": spmv_t,
