@@ -98,6 +98,57 @@ __device__ bool grid_sum(double (&v)[NV], double *partials, unsigned int *ticket
     return true;
 }
 
+// As grid_sum, for FP32 per-thread values: the CTA-level tree runs in FP32 (the FP64 pipe of
+// this GPU is narrow enough that a per-CTA FP64 shuffle tree shows in a bandwidth-bound
+// kernel); each CTA's partial is widened once and the last CTA adds them in FP64.
+template <int NV>
+__device__ bool grid_sumf(float (&v)[NV], double *partials, unsigned int *ticket, double (&tot)[NV]) {
+    __shared__ float shf[NV][kThreads / 32];
+    __shared__ double sh[NV][kThreads / 32];
+    __shared__ bool last;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        float x = warp_sumf(v[i]);
+        if (lane == 0) shf[i][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            float x = (lane < (int)(blockDim.x >> 5)) ? shf[i][lane] : 0.0f;
+            x = warp_sumf(x);
+            if (lane == 0) partials[i * gridDim.x + blockIdx.x] = (double)x;
+        }
+        if (lane == 0) {
+            __threadfence();
+            unsigned int t = atomicAdd(ticket, 1u);
+            last = (t == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        acc[i] = 0.0;
+        for (unsigned j = threadIdx.x; j < gridDim.x; j += blockDim.x)
+            acc[i] += ((volatile double *)partials)[i * gridDim.x + j];
+    }
+    block_sum<NV>(acc, sh);
+    __shared__ double res[NV];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) res[i] = acc[i];
+        *ticket = 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; i++) tot[i] = res[i];
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // Mixed path kernels (BSR, B x B blocks, SoA values [BB][nblocks]).
 // Preconditioned CG in three launches per iteration: p = z + beta p, then
@@ -120,44 +171,46 @@ __global__ void __launch_bounds__(kThreads) k_spmv32(int64_t nn, int64_t nb, con
                                                      const float *__restrict__ z, float *__restrict__ sv, Ctl *ctl,
                                                      double *partials) {
     if (ctl->stop) return;
-    int lane = threadIdx.x & 31;
-    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    // a half-warp per block row, two blocks per lane in flight; the matrix streams (evict-first).
+    // Shuffles are masked to the half-warp, so the two halves of a warp may run different row counts.
+    constexpr int G = 16, U = 2;
+    const int lane = threadIdx.x % G;
+    const unsigned hmask = 0xffffu << (16 * ((threadIdx.x >> 4) & 1));
+    const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
     // FP32 partial dot per thread: per-row FP64 arithmetic would saturate this GPU's narrow FP64 pipe
     float dot = 0.0f;
-    for (int64_t n = warp; n < nn; n += nw) {
+    for (int64_t n = grp; n < nn; n += ng) {
         float acc[B];
 #pragma unroll
         for (int c = 0; c < B; c++) acc[c] = 0.0f;
-        const int64_t k1 = rp[n + 1];
-        int64_t k = rp[n] + lane;
-        for (; k + 32 < k1; k += 64) {  // two blocks per lane in flight; the matrix streams (evict-first)
-            const int64_t j0 = __ldcs(cj + k), j1 = __ldcs(cj + k + 32);
-            float a0[B * B], a1[B * B], z0[B], z1[B];
+        const int64_t k0 = rp[n], k1 = rp[n + 1];
+        for (int64_t kb = k0 + lane; kb < k1; kb += G * U) {
+            int32_t j[U];
+            float a[U][B * B];
 #pragma unroll
-            for (int q = 0; q < B * B; q++) {
-                a0[q] = __ldcs(A + (int64_t)q * nb + k);
-                a1[q] = __ldcs(A + (int64_t)q * nb + k + 32);
+            for (int u = 0; u < U; u++) {
+                const int64_t k = kb + u * G;
+                const bool ok = k < k1;
+                j[u] = ok ? __ldcs(cj + k) : 0;
+#pragma unroll
+                for (int q = 0; q < B * B; q++) a[u][q] = ok ? __ldcs(A + (int64_t)q * nb + k) : 0.0f;
             }
 #pragma unroll
-            for (int d = 0; d < B; d++) { z0[d] = __ldg(z + j0 * B + d); z1[d] = __ldg(z + j1 * B + d); }
+            for (int u = 0; u < U; u++) {
+                float xv[B];
 #pragma unroll
-            for (int c = 0; c < B; c++)
+                for (int d = 0; d < B; d++) xv[d] = __ldg(z + (int64_t)B * j[u] + d);
 #pragma unroll
-                for (int d = 0; d < B; d++) acc[c] = fmaf(a1[c * B + d], z1[d], fmaf(a0[c * B + d], z0[d], acc[c]));
-        }
-        if (k < k1) {
-            const int64_t j0 = __ldcs(cj + k);
-            float z0[B];
+                for (int c = 0; c < B; c++)
 #pragma unroll
-            for (int d = 0; d < B; d++) z0[d] = __ldg(z + j0 * B + d);
-#pragma unroll
-            for (int c = 0; c < B; c++)
-#pragma unroll
-                for (int d = 0; d < B; d++) acc[c] = fmaf(__ldcs(A + (int64_t)(c * B + d) * nb + k), z0[d], acc[c]);
+                    for (int d = B - 1; d >= 0; d--) acc[c] = fmaf(a[u][c * B + d], xv[d], acc[c]);
+            }
         }
 #pragma unroll
-        for (int c = 0; c < B; c++) acc[c] = warp_sumf(acc[c]);
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < B; c++) acc[c] += __shfl_down_sync(hmask, acc[c], o, G);
         if (lane == 0) {
 #pragma unroll
             for (int c = 0; c < B; c++) {
@@ -166,8 +219,9 @@ __global__ void __launch_bounds__(kThreads) k_spmv32(int64_t nn, int64_t nb, con
             }
         }
     }
-    double v[1] = {(double)dot}, tot[1];
-    if (grid_sum<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
+    float v[1] = {dot};
+    double tot[1];
+    if (grid_sumf<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
         ctl->pq = tot[0];
         if (!(tot[0] > 0.0)) { ctl->breakdown = 1; ctl->stop = 1; }
         else { ctl->alpha = ctl->rz / tot[0]; ctl->first = 0; }
@@ -203,8 +257,9 @@ __global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *
             rr = fmaf(rv[c], rv[c], rr);
         }
     }
-    double v[2] = {(double)rz, (double)rr}, tot[2];
-    if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
+    float v[2] = {rz, rr};
+    double tot[2];
+    if (grid_sumf<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
         ctl->beta = tot[0] / ctl->rz;
         ctl->rz = tot[0];
         ctl->rr = tot[1];
@@ -479,7 +534,7 @@ struct AmrSolveWork {
     double *partials = nullptr;
     Ctl *ctl = nullptr;
     Ctl *h_ctl = nullptr;        // pinned
-    int grid = 0;
+    int grid = 0, grid_spmv = 0;
     // plain FP64 CSR path
     int64_t csr_nnz = -1;
     int64_t *crp = nullptr, *csrc = nullptr;
@@ -505,8 +560,9 @@ static AmrSolveWork *work(amr_model *m) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         w->grid = sms * 8;
+        w->grid_spmv = sms * 8;
         amr_free(w->partials);
-        amr_alloc(&w->partials, 4 * (size_t)w->grid);
+        amr_alloc(&w->partials, (size_t)std::max(4 * w->grid, w->grid_spmv) + 8);
         if (!w->ctl) {
             amr_alloc(&w->ctl, 1);
             AMR_CUDA(cudaMemset(w->ctl, 0, sizeof(Ctl)));
@@ -581,7 +637,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
         for (int it = 0; it < nit; it++) {
             k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
             AMR_COUNT(1);
-            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->p32[0], w->q32,
+            k_spmv32<B><<<(unsigned)w->grid_spmv, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->p32[0], w->q32,
                                                w->ctl, w->partials);
             AMR_COUNT(1);
             k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[0], w->q32, w->x32, w->r32, w->z32, w->ctl,
@@ -816,7 +872,7 @@ static double time_spmv32(amr_model *m, int reps) {
     AMR_CUDA(cudaMemcpyAsync(w->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        k_spmv32<B><<<g, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->s32,
+        k_spmv32<B><<<(unsigned)w->grid_spmv, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->s32,
                                            w->ctl, w->partials);
         AMR_COUNT(1);
     }
