@@ -87,6 +87,7 @@ SIGNATURES = {
     "amr_solve": (C.c_int, [P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
     "amr_stage_run": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
     "amr_stage_run_dev": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
+    "amr_solve_noalloc": (C.c_int, [P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_default_solve_opts": (None, [C.POINTER(SolveOpts)]),

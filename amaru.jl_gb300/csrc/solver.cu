@@ -908,3 +908,225 @@ double amr_time_solver_kernel(amr_model *m, int which, int reps) {
     if (which == AMR_KERNEL_SPMV32) return m->B == 3 ? time_spmv32<3>(m, reps) : time_spmv32<2>(m, reps);
     return m->B == 3 ? time_residual64<3>(m, reps) : time_residual64<2>(m, reps);
 }
+
+// ===========================================================================
+// solve_system! with caller-owned device buffers and no device allocation.
+//
+// For callers that cannot allocate GPU memory while they solve: an embedding
+// that hands the library a fixed memory budget up front, a real-time loop
+// that must not enter the CUDA allocator, or code whose memory pool forbids
+// growth.  All scratch of the mixed-precision solve -- the node-major FP64
+// work vectors, the FP32 Krylov vectors, the per-CTA reduction partials and
+// the control block -- lives in one file-scope device array of fixed size.
+// The model itself (pattern, K, masks) is created and assembled beforehand by
+// the ordinary entry points, which do allocate.
+// ===========================================================================
+namespace {
+
+// node-major slots (nnodes x ndim) the scratch array serves
+constexpr int64_t kNoAllocMaxSlots = int64_t(1) << 18;  // 262 144 (e.g. 87 381 nodes in 3-D)
+constexpr int64_t kNoAllocPartials = 8192;              // doubles of CTA partials
+constexpr size_t kNoAllocAlign = 256;
+constexpr size_t align_up(size_t v) { return (v + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+constexpr size_t kNoAllocBytes = 3 * align_up(sizeof(double) * kNoAllocMaxSlots) +  // x, b, reactions (FP64)
+                                 5 * align_up(sizeof(float) * kNoAllocMaxSlots) +   // x32 r32 z32 p32 q32
+                                 align_up(sizeof(double) * kNoAllocPartials) + align_up(sizeof(Ctl));
+
+// The scratch.  Every GPU that loads the library holds these ~11.5 MB until the process exits.
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+void *g_noalloc_addr[kMaxDevices] = {nullptr};
+std::atomic<int> g_noalloc_lock{0};
+
+// Device address of g_noalloc_scratch for the current device, looked up once per device.
+// (In host code the symbol name is only a host-side stand-in, not a device address.)
+void *noalloc_base() {
+    int dev = 0;
+    AMR_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw AmrError(AMR_EINVAL, "device ordinal out of range");
+    while (g_noalloc_lock.exchange(1)) {
+    }
+    void *p = g_noalloc_addr[dev];
+    cudaError_t e = cudaSuccess;
+    if (!p) {
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e == cudaSuccess) g_noalloc_addr[dev] = p;
+    }
+    g_noalloc_lock.store(0);
+    if (e != cudaSuccess)
+        throw AmrError(AMR_ECUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    return p;
+}
+
+struct NoAllocView {
+    double *x, *b, *reac, *partials;
+    float *x32, *r32, *z32, *p32, *q32;
+    Ctl *ctl;
+};
+
+NoAllocView noalloc_view(void *base) {
+    unsigned char *c = (unsigned char *)base;
+    NoAllocView v;
+    size_t d = align_up(sizeof(double) * kNoAllocMaxSlots), f = align_up(sizeof(float) * kNoAllocMaxSlots);
+    v.x = (double *)c; c += d;
+    v.b = (double *)c; c += d;
+    v.reac = (double *)c; c += d;
+    v.x32 = (float *)c; c += f;
+    v.r32 = (float *)c; c += f;
+    v.z32 = (float *)c; c += f;
+    v.p32 = (float *)c; c += f;
+    v.q32 = (float *)c; c += f;
+    v.partials = (double *)c; c += align_up(sizeof(double) * kNoAllocPartials);
+    v.ctl = (Ctl *)c;
+    return v;
+}
+
+// node-major <- eq_id entries in [nu, ndofs) (prescribed values), 0 elsewhere
+__global__ void k_gather_prescribed(int64_t nnodes, int B, const int64_t *eq_id, int64_t nu, int64_t ndofs,
+                                    const double *eq, double *nm) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t e = eq_id[(t / B) * 3 + t % B];
+    nm[t] = (e >= nu && e < ndofs) ? eq[e] : 0.0;
+}
+
+// eq_id entries in [nu, ndofs) <- node-major values (the reactions of solve_system!)
+__global__ void k_scatter_prescribed(int64_t nnodes, int B, const int64_t *eq_id, int64_t nu, int64_t ndofs,
+                                     const double *nm, double *eq) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * B) return;
+    int64_t e = eq_id[(t / B) * 3 + t % B];
+    if (e >= nu && e < ndofs) eq[e] = nm[t];
+}
+
+template <int B>
+AmrSolveResult solve_mixed_noalloc(amr_model *m, const NoAllocView &w, int grid, const amr_solve_opts &o) {
+    cudaStream_t s = m->stream;
+    const int64_t nn = m->nnodes, n = nn * B;
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    const double tol2 = o.rtol * o.rtol;
+    // everything that must start at zero is cleared here: the array keeps the previous call's contents
+    AMR_CUDA(cudaMemsetAsync(w.x32, 0, n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w.p32, 0, n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w.q32, 0, n * sizeof(float), s));
+    Ctl hc{};
+    hc.first = 1;
+    AMR_CUDA(cudaMemcpyAsync(w.ctl, &hc, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    const unsigned g = (unsigned)grid;
+    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x, w.reac,
+                                       w.r32, w.z32, m->Minv32, w.ctl, w.partials, 1, tol2);
+    AMR_COUNT(1);
+    AMR_CUDA(cudaGetLastError());
+    const int every = o.refine_every > 0 ? o.refine_every : 32;
+    const double stop_rr_rel = 0.25 * 0.25 * tol2;
+    const double delta2 = 1e-2;
+    int since = 0;
+    for (;;) {
+        AMR_CUDA(cudaMemcpyAsync(&hc, w.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));  // pageable: no pinned buffer
+        AMR_CUDA(cudaStreamSynchronize(s));
+        res.iterations = hc.iters;
+        if (hc.bnorm2 == 0.0 || hc.converged) break;
+        if (hc.breakdown) { res.status = AMR_ENOCONV; break; }
+        if (hc.iters >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        if (hc.stop || since >= 16 * every) {
+            k_fold<B><<<nblk(n, 256), 256, 0, s>>>(nn, m->free_mask, w.x32, w.x);
+            AMR_COUNT(1);
+            AMR_CUDA(cudaMemsetAsync(&w.ctl->stop, 0, sizeof(int32_t), s));
+            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x,
+                                               w.reac, w.r32, w.z32, m->Minv32, w.ctl, w.partials, 0, tol2);
+            AMR_COUNT(1);
+            res.refinements++;
+            since = 0;
+            continue;
+        }
+        const double stop_rr = stop_rr_rel * hc.bnorm2;
+        const int nit = std::min(every, o.max_iters - hc.iters);
+        for (int it = 0; it < nit; it++) {
+            k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w.z32, w.p32, w.ctl);
+            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w.p32, w.q32, w.ctl,
+                                               w.partials);
+            k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w.p32, w.q32, w.x32, w.r32, w.z32, w.ctl, w.partials,
+                                                 stop_rr, delta2);
+            AMR_COUNT(3);
+        }
+        AMR_CUDA(cudaGetLastError());
+        since += nit;
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    res.seconds = ms * 1e-3;
+    res.rel_residual = hc.bnorm2 > 0 ? std::sqrt(hc.rr_true / hc.bnorm2) : 0.0;
+    return res;
+}
+
+}  // namespace
+
+extern "C" int amr_solve_noalloc(amr_model *m, double *d_U, double *d_F, const amr_solve_opts *opts,
+                                 amr_solve_stats *stats) {
+    if (!m) return AMR_EINVAL;
+    try {
+        m->err.clear();
+        if (!m->dofs_set) throw AmrError(AMR_EINVAL, "amr_set_dofs must be called first");
+        if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+        if (!d_U || !d_F) throw AmrError(AMR_EINVAL, "null device buffer");
+        const int64_t n = m->nnodes * m->B;
+        if (n > kNoAllocMaxSlots)
+            throw AmrError(AMR_EINVAL, "amr_solve_noalloc serves models of at most " + std::to_string(kNoAllocMaxSlots) +
+                                           " node-DOF slots (nnodes x ndim); this model has " + std::to_string(n) +
+                                           ": use amr_solve");
+        int dev = 0, sms = 0;
+        AMR_CUDA(cudaGetDevice(&dev));
+        AMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int grid = sms * 8;
+        if (2 * grid + 8 > kNoAllocPartials) throw AmrError(AMR_EUNSUPPORTED, "too many SMs for the reduction scratch");
+        amr_solve_opts o;
+        amr_default_solve_opts(&o);
+        if (opts) o = *opts;
+        if (o.method != AMR_SOLVER_MIXED) throw AmrError(AMR_EINVAL, "amr_solve_noalloc runs the mixed-precision solver");
+        const NoAllocView w = noalloc_view(noalloc_base());
+        cudaStream_t s = m->stream;
+        const int64_t nt = n;
+        // x: prescribed values at prescribed slots, 0 at free slots; b: natural values at free slots
+        AMR_CUDA(cudaMemsetAsync(w.x, 0, nt * sizeof(double), s));
+        AMR_CUDA(cudaMemsetAsync(w.b, 0, nt * sizeof(double), s));
+        AMR_CUDA(cudaMemsetAsync(w.reac, 0, nt * sizeof(double), s));
+        k_gather_prescribed<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, m->B, m->eq_id, m->nu, m->ndofs, d_U, w.x);
+        k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, m->B, m->eq_id, m->ndofs, w.b, d_F, 0);
+        AMR_COUNT(2);
+        AMR_CUDA(cudaGetLastError());
+        AmrSolveResult r = m->B == 3 ? solve_mixed_noalloc<3>(m, w, grid, o) : solve_mixed_noalloc<2>(m, w, grid, o);
+        if (stats) {
+            stats->iterations = r.iterations;
+            stats->refinements = r.refinements;
+            stats->rel_residual = r.rel_residual;
+            stats->seconds = r.seconds;
+        }
+        if (r.status) throw AmrError(r.status, "solve_system!: Krylov solver did not converge");
+        // |U1|max > 1e8 check of solve_system! (src/solver.jl:68-71), partials as scratch
+        double *out = w.partials + (kNoAllocPartials - 1);
+        k_absmax<<<grid, kThreads, 0, s>>>(nt, w.x, m->free_mask, w.partials, &w.ctl->ticket[3], out);
+        AMR_COUNT(1);
+        double umax = 0.0;
+        AMR_CUDA(cudaMemcpyAsync(&umax, out, sizeof(double), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        if (std::isnan(umax) || std::isinf(umax)) throw AmrError(AMR_ENAN, "solve_system!: NaN values in the solution");
+        if (umax > 1e8) throw AmrError(AMR_ESINGULAR, "solve_system!: Possible syngular matrix");
+        // U[:nu] <- solution, F[nu:] <- reactions
+        k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, m->B, m->eq_id, m->nu, w.x, d_U, 1);
+        k_scatter_prescribed<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, m->B, m->eq_id, m->nu, m->ndofs, w.reac, d_F);
+        AMR_COUNT(2);
+        AMR_CUDA(cudaGetLastError());
+        AMR_CUDA(cudaStreamSynchronize(s));
+        return AMR_OK;
+    } catch (const AmrError &e) {
+        m->err = e.msg;
+        return e.code;
+    } catch (const std::exception &e) {
+        m->err = e.what();
+        return AMR_EINVAL;
+    }
+}

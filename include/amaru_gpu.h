@@ -202,6 +202,22 @@ int amr_solve(amr_model *m, double *U, double *F, const amr_solve_opts *opts, am
 int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params *p, double *U,
                   double *F, amr_stage_stats *stats);
 
+/* amr_solve for callers that cannot allocate GPU memory while they solve (a host
+ * application that gives the library a fixed memory budget up front, a real-time
+ * loop that must stay out of the CUDA allocator, a memory pool that may not grow).
+ * No counterpart in the reference: Amaru allocates freely in solve_system!.
+ * Same semantics as amr_solve on the last assembled K, mixed-precision solver only,
+ * but d_U and d_F are caller-owned DEVICE buffers of ndofs doubles (eq_id order):
+ * in: d_U[nu:] prescribed values, d_F[:nu] natural values; out: d_U[:nu] and the
+ * reactions d_F[nu:].  The call allocates nothing: all scratch lives in one static
+ * device array of about 11.5 MB that every GPU loading the library holds until the
+ * process exits, which limits the model to nnodes x ndim <= 262 144 (larger models
+ * get AMR_EINVAL; use amr_solve).  The first call on each device looks up that
+ * array's device address (cudaGetSymbolAddress), so make it before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the GPU
+ * (other handles, other streams, other threads) race and must be serialized. */
+int amr_solve_noalloc(amr_model *m, double *d_U, double *d_F, const amr_solve_opts *opts, amr_solve_stats *stats);
+
 /* amr_stage_run with device-resident vectors: d_Uex, d_Fex, d_U, d_F are device
  * pointers to ndofs doubles in eq_id order (for callers that keep their loads
  * and results on the GPU across stages). */
