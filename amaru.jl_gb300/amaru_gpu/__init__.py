@@ -10,5 +10,5 @@ from ._lib import (AmrError, HEX8, HEX20, LIN2, LIN3, QUAD4, QUAD8, QUAD9, TET4,
                    SOLVER_FP64, SOLVER_MIXED, lib)
 from .expr import evaluate  # noqa: F401
 from .mesh import Block, Mesh  # noqa: F401
-from .model import (BodyC, DruckerPrager, EdgeBC, ElemBC, FaceBC, FEModel, LinearElastic,  # noqa: F401
+from .model import (BatchAnalysis, BodyC, DruckerPrager, EdgeBC, ElemBC, FaceBC, FEModel, LinearElastic,  # noqa: F401
                     MechAnalysis, MechContext, MechSolid, NodeBC, SurfaceBC, VonMises)

@@ -64,6 +64,16 @@ class StageStats(C.Structure):
                 ("seconds", C.c_double), ("solve_seconds", C.c_double)]
 
 
+MAX_TUNED_GROUPS = 8
+
+
+class Tuning(C.Structure):
+    _fields_ = [("ngroups", C.c_int32), ("shape", C.c_int32 * MAX_TUNED_GROUPS),
+                ("stiffness_epb", C.c_int32 * MAX_TUNED_GROUPS), ("internal_epb", C.c_int32 * MAX_TUNED_GROUPS),
+                ("batch_threads", C.c_int32), ("batch_ctas_per_sm", C.c_int32),
+                ("stiffness_seconds", C.c_double), ("internal_seconds", C.c_double)]
+
+
 # Every exported entry point of include/amaru_gpu.h with its ctypes signature.
 P = C.c_void_p
 SIGNATURES = {
@@ -88,6 +98,9 @@ SIGNATURES = {
     "amr_stage_run": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
     "amr_stage_run_dev": (C.c_int, [P, P, P, C.POINTER(StageParams), P, P, C.POINTER(StageStats)]),
     "amr_solve_noalloc": (C.c_int, [P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
+    "amr_set_parts": (C.c_int, [P, C.c_int64, P]),
+    "amr_get_part_stats": (C.c_int, [P, C.c_int64, P]),
+    "amr_autotune": (C.c_int, [P, C.POINTER(Tuning)]),
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_default_solve_opts": (None, [C.POINTER(SolveOpts)]),
@@ -270,6 +283,22 @@ class DeviceModel:
         rc = lib().amr_stage_run_dev(self.h, C.c_void_p(d_Uex), C.c_void_p(d_Fex), C.byref(params), C.c_void_p(d_U),
                                      C.c_void_p(d_F), C.byref(st))
         return rc, st
+
+    def set_parts(self, node_ptr):
+        """Declares the handle a batch of independent parts (node ranges node_ptr[i]..node_ptr[i+1]-1)."""
+        a = np.ascontiguousarray(node_ptr, dtype=np.int64)
+        self.nparts = len(a) - 1 if len(a) else 0
+        check(self.h, lib().amr_set_parts(self.h, self.nparts, ptr(a) if len(a) else None))
+
+    def part_stats(self):
+        out = (StageStats * self.nparts)()
+        check(self.h, lib().amr_get_part_stats(self.h, self.nparts, C.cast(out, C.c_void_p)))
+        return list(out)
+
+    def autotune(self):
+        t = Tuning()
+        check(self.h, lib().amr_autotune(self.h, C.byref(t)))
+        return t
 
     def time_kernel(self, which, reps):
         t, b = C.c_double(), C.c_double()

@@ -97,6 +97,43 @@ class Mesh:
         self.tags = np.array(tags, dtype=object)
         self._facets()
 
+    @classmethod
+    def join(cls, meshes):
+        """Meshes side by side as one mesh, without merging any nodes: mesh i's nodes and
+        elements follow those of meshes 0..i-1.  Returns (mesh, node offsets, element offsets);
+        the offsets have len(meshes)+1 entries."""
+        meshes = list(meshes)
+        if not meshes:
+            raise ValueError("Mesh.join needs at least one mesh")
+        noff = np.zeros(len(meshes) + 1, dtype=np.int64)
+        eoff = np.zeros(len(meshes) + 1, dtype=np.int64)
+        noff[1:] = np.cumsum([len(m.coords) for m in meshes])
+        eoff[1:] = np.cumsum([len(m.shape) for m in meshes])
+
+        def shift(a, o):
+            return np.where(a >= 0, a + o, a)
+
+        out = cls.__new__(cls)
+        out.ndim = max(m.ndim for m in meshes)
+        out.coords = np.concatenate([m.coords for m in meshes], axis=0)
+        out.shape = np.concatenate([m.shape for m in meshes])
+        out.conn_list = [c + noff[i] for i, m in enumerate(meshes) for c in m.conn_list]
+        out.conn_ptr = np.zeros(len(out.shape) + 1, dtype=np.int64)
+        out.conn_ptr[1:] = np.cumsum(np.concatenate([np.diff(m.conn_ptr) for m in meshes]))
+        out.conn = np.concatenate([m.conn + noff[i] for i, m in enumerate(meshes)])
+        out.tags = np.concatenate([m.tags for m in meshes])
+        out.faces = []
+        w = max(m.face_nodes.shape[1] for m in meshes)
+        out.face_nodes = np.concatenate([np.pad(shift(m.face_nodes, noff[i]), ((0, 0), (0, w - m.face_nodes.shape[1])),
+                                                constant_values=-1) for i, m in enumerate(meshes)])
+        out.face_shape = np.concatenate([m.face_shape for m in meshes])
+        out.face_owner = np.concatenate([m.face_owner + eoff[i] for i, m in enumerate(meshes)])
+        w = max(m.edge_nodes.shape[1] for m in meshes)
+        out.edge_nodes = np.concatenate([np.pad(shift(m.edge_nodes, noff[i]), ((0, 0), (0, w - m.edge_nodes.shape[1])),
+                                                constant_values=-1) for i, m in enumerate(meshes)])
+        out.edge_shape = np.concatenate([m.edge_shape for m in meshes])
+        return out, noff, eoff
+
     # -- node creation with de-duplication on block boundaries
     def _add_nodes(self, C, boundary):
         ids = np.empty(len(C), dtype=np.int64)

@@ -114,7 +114,8 @@ class FEModel:
     matbinds: list of (filter, MechSolid, MaterialType, params-dict) or (filter, material instance);
     filter is a tag, an expression over the element's nodes, or "all"."""
 
-    def __init__(self, mesh, matbinds, ctx=None, thickness=1.0, nips=0, E=None):
+    def __init__(self, mesh, matbinds, ctx=None, thickness=1.0, nips=0, E=None, device=True):
+        """device=False keeps the model on the host only, to be joined with others (FEModel.join)."""
         ctx = ctx or MechContext()
         self.mesh = mesh
         self.ndim = mesh.ndim
@@ -144,8 +145,14 @@ class FEModel:
         if E is not None:
             self.mat_params[:, 0] = E
         self.nips = np.full(ne, nips, dtype=np.int32)
-        self.dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, mesh.coords, mesh.shape, self.nips,
-                                 mesh.conn_ptr, mesh.conn, self.mat_type, self.mat_params)
+        self.dev = None
+        if device:
+            self.dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, mesh.coords, mesh.shape, self.nips,
+                                     mesh.conn_ptr, mesh.conn, self.mat_type, self.mat_params)
+        self._host_fields()
+
+    def _host_fields(self):
+        mesh = self.mesh
         self.nnodes = len(mesh.coords)
         self.U = np.zeros((self.nnodes, self.ndim))  # dof.vals of the displacement keys
         self.F = np.zeros((self.nnodes, self.ndim))  # dof.vals of the natural keys
@@ -153,6 +160,28 @@ class FEModel:
         self.ndofs = self.nu = 0
         self.active_nodes = np.unique(mesh.conn)
         self._dof_names = ["ux", "uy", "uz"][: self.ndim]
+
+    @classmethod
+    def join(cls, models):
+        """One device model holding independent models side by side, each a part (amr_set_parts):
+        the batched solver and stage driver then run every part as if it were alone."""
+        models = list(models)
+        m0 = models[0]
+        for m in models:
+            if (m.ndim, m.stressmodel, m.thickness) != (m0.ndim, m0.stressmodel, m0.thickness):
+                raise ValueError("joined models must share ndim, stress model and thickness")
+        mesh, noff, eoff = Mesh.join([m.mesh for m in models])
+        out = cls.__new__(cls)
+        out.mesh, out.ndim, out.stressmodel, out.thickness = mesh, m0.ndim, m0.stressmodel, m0.thickness
+        out.mat_type = np.concatenate([m.mat_type for m in models])
+        out.mat_params = np.concatenate([m.mat_params for m in models])
+        out.nips = np.concatenate([m.nips for m in models])
+        out.dev = L.DeviceModel(out.ndim, out.stressmodel, out.thickness, mesh.coords, mesh.shape, out.nips,
+                                mesh.conn_ptr, mesh.conn, out.mat_type, out.mat_params)
+        out._host_fields()
+        out.node_offsets, out.elem_offsets = noff, eoff
+        out.dev.set_parts(noff)
+        return out
 
     def changequadrature(self, n):
         """changequadrature!(elems, n) (src/element.jl:185-188): rebuilds the device model."""
@@ -186,7 +215,7 @@ class FEModel:
             sel = mesh.select_cells(enodes, filt)
         return sel, enodes[sel]
 
-    def configure_dofs(self, bcs):
+    def _prescribed(self, bcs):
         presc = np.zeros((self.nnodes, self.ndim), dtype=bool)
         setup = []
         for filt, bc in bcs:
@@ -197,9 +226,14 @@ class FEModel:
                 if key in self._dof_names:
                     presc[nodes, self._dof_names.index(key)] = True
             setup.append((bc, sel, objs, nodes))
+        return presc, setup
+
+    def configure_dofs(self, bcs):
+        presc, setup = self._prescribed(bcs)
         self.eq_id, self.ndofs, self.nu, self.dof_node, self.dof_comp = number_dofs(self.active_nodes, presc,
                                                                                    self.nnodes)
-        self.dev.set_dofs(self.eq_id, self.ndofs, self.nu)
+        if self.dev is not None:
+            self.dev.set_dofs(self.eq_id, self.ndofs, self.nu)
         return setup
 
     # ---- get_bc_vals (src/bc.jl:237-249)
@@ -312,3 +346,111 @@ class MechAnalysis:
                 return False, model.dev.last_error()
             st.status = "done"
         return True, ""
+
+
+def _shift_setup(setup, noff, eoff):
+    """A part's BC selections in the joined model's node and element numbering."""
+    def sh(a):
+        a = np.asarray(a)
+        return np.where(a >= 0, a + noff, a)
+    out = []
+    for bc, sel, objs, nodes in setup:
+        if isinstance(bc, NodeBC):
+            out.append((bc, sh(sel), sh(objs), sh(nodes)))
+        elif isinstance(bc, (SurfaceBC, EdgeBC)):
+            out.append((bc, sel, (sh(objs[0]), objs[1]), sh(nodes)))
+        else:
+            out.append((bc, np.asarray(sel) + eoff, sh(objs), sh(nodes)))
+    return out
+
+
+class BatchAnalysis:
+    """Independent staged analyses run together on one device handle.
+
+    models: FEModel instances built with device=False, one per part; they are joined
+    (FEModel.join) into one device model.  Each part runs its own mech_stage_solver!
+    (src/mech/mech-solver.jl:186-492): its own increments, Newton iterations, residue
+    checks and failure handling, with its DOFs numbered as if it were alone.  Every
+    kernel launch serves all parts at once."""
+
+    def __init__(self, models):
+        self.models = list(models)
+        self.joined = FEModel.join(self.models)
+        self.stages = []
+        self.stats = []
+        self.part_stats = []
+
+    def addstage(self, bcs, nincs=1, nouts=0):
+        """bcs: one BC list for every part, or a list with one BC list per part."""
+        if bcs and isinstance(bcs[0], list):
+            if len(bcs) != len(self.models):
+                raise ValueError("one BC list per part")
+            per = [list(b) for b in bcs]
+        else:
+            per = [list(bcs)] * len(self.models)
+        self.stages.append(Stage(per, nincs, nouts))
+
+    def configure(self, bcs_per_part):
+        """configure_dofs! and get_bc_vals for every part: each part's DOFs numbered as if it were
+        alone, the joined model's numbering (all unknowns first) on the device; returns (Uex, Fex)."""
+        J = self.joined
+        pres, setup = [], []
+        for i, (m, bcs) in enumerate(zip(self.models, bcs_per_part)):
+            p, su = m._prescribed(bcs)
+            m.eq_id, m.ndofs, m.nu, m.dof_node, m.dof_comp = number_dofs(m.active_nodes, p, m.nnodes)
+            pres.append(p)
+            setup += _shift_setup(su, J.node_offsets[i], J.elem_offsets[i])
+        J.eq_id, J.ndofs, J.nu, J.dof_node, J.dof_comp = number_dofs(J.active_nodes, np.concatenate(pres), J.nnodes)
+        J.dev.set_dofs(J.eq_id, J.ndofs, J.nu)
+        return J.get_bc_vals(setup)
+
+    def split(self, V):
+        """A joined eq_id-ordered vector as one node-major (nnodes, ndim) array per part."""
+        J = self.joined
+        Vn = np.zeros((J.nnodes, J.ndim))
+        Vn[J.dof_node, J.dof_comp] = V
+        return [Vn[J.node_offsets[i]:J.node_offsets[i + 1]] for i in range(len(self.models))]
+
+    def autotune(self):
+        """Picks the element kernels' and the batched solver's launch shapes on this batch (amr_autotune);
+        results do not depend on them."""
+        pending = [st for st in self.stages if st.status != "done"]
+        if pending:
+            self.configure(pending[0].bcs)
+        self.joined.dev.assemble_K()
+        return self.joined.dev.autotune()
+
+    def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
+              autoinc=False, quiet=True, linear_rtol=1e-8, refine_every=32, max_iters=20000):
+        """solve!(ana; args...) for every part; returns a list of (success, message), one per part."""
+        if not (1 <= maxits <= 10):
+            raise ValueError("maxits must be in 1..10")
+        J = self.joined
+        lin = L.default_solve_opts(method=L.SOLVER_MIXED, rtol=linear_rtol, refine_every=refine_every,
+                                   max_iters=max_iters)
+        result = [(True, "")] * len(self.models)
+        failed = np.zeros(len(self.models), dtype=bool)
+        for st in self.stages:
+            if st.status == "done":
+                continue
+            Uex, Fex = self.configure(st.bcs)
+            p = L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,
+                                       scheme={"FE": 0, "ME": 1, "BE": 2, "Ralston": 3}[scheme], maxits=maxits,
+                                       autoinc=int(autoinc), nincs=st.nincs, nouts=st.nouts, linear=lin)
+            rc, U, F, stats = J.dev.stage_run(Uex, Fex, p)
+            if rc not in (0, -11):
+                raise L.AmrError(rc, J.dev.last_error())
+            self.stats.append(stats)
+            ps = J.dev.part_stats()
+            self.part_stats.append(ps)
+            Us, Fs = self.split(U), self.split(F)
+            for i, m in enumerate(self.models):
+                if failed[i]:
+                    continue
+                m.U += Us[i]
+                m.F += Fs[i]
+                if ps[i].status != 0:
+                    failed[i] = True
+                    result[i] = (False, "Solver did not converge.")
+            st.status = "done"
+        return result

@@ -31,9 +31,11 @@ struct AmrGroup {             // elements sharing (shape, quadrature)
     int64_t first = 0, count = 0;  // range in the sorted element order
     double *tab = nullptr;    // device: [nip][nen*ndim] dN/dR, then [nip] w, then [nip][nen] N
     int epb = 1;              // elements per CTA for the stiffness kernel (autotuned)
+    int epb_int = 0;          // elements per CTA for the internal-force kernel (0: by quadrature size)
 };
 
 struct AmrSolveWork;          // solver workspace (solver.cu)
+struct AmrBatch;              // independent parts solved together (batch.cu)
 
 struct amr_model {
     int ndim = 3, B = 3, BB = 9, stressmodel = 0;
@@ -94,6 +96,12 @@ struct amr_model {
     // scratch
     double *vtmp[8] = {nullptr};    // node-major FP64 vectors (nnodes*B)
     AmrSolveWork *sw = nullptr;
+    AmrBatch *batch = nullptr;
+    // per-part masks read by the element kernels while a batched stage runs (null otherwise)
+    const int32_t *bp_elem_part = nullptr;  // sorted element -> part
+    const int32_t *bp_node_part = nullptr;  // node -> part
+    const uint8_t *bp_active = nullptr;     // part -> takes part in this Newton iteration
+    int32_t *bp_err = nullptr;              // part -> first error code of this iteration
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
@@ -140,6 +148,7 @@ void amr_build_pattern(amr_model *m);
 void amr_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);  // exclusive, out has n+1
 // element.cu
 void amr_stiffness(amr_model *m);                       // Kel + gather into K64/K32/Minv
+void amr_stiffness_elements(amr_model *m);              // Kel only (element kernels)
 void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm);  // node-major device vectors
 void amr_apply_dofs(amr_model *m);                      // masks after amr_set_dofs
 void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double *F_nm);  // F_nm += (device)
@@ -158,6 +167,14 @@ void amr_solver_free(amr_model *m);
 double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask_or_null);
 void amr_eq_to_nm(amr_model *m, const double *d_eq, double *d_nm);  // scatter eq_id-ordered -> node-major (0 elsewhere)
 void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq);
+// batch.cu: independent parts (contiguous node ranges, no element spanning two)
+void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *node_ptr);
+void amr_batch_free(amr_model *m);
+AmrSolveResult amr_batch_solve(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o);
+int amr_batch_stage(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p, double *U_nm,
+                    double *F_nm, amr_stage_stats *stats);
+void amr_batch_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *out);
+void amr_autotune_model(amr_model *m, amr_tuning *out);
 // stage.cpp-equivalent (capi.cu)
 int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
                      double *U_nm, double *F_nm, amr_stage_stats *stats);

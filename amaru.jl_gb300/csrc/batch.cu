@@ -1,0 +1,1063 @@
+// Batches of independent models: many FE models of uneven size joined into one
+// handle, each a contiguous range of nodes ("part") with no element joining two.
+//
+// * Solve (solve_system!, src/solver.jl:5-79, once per part): one persistent
+//   kernel.  CTAs take parts from an integer work counter, largest first, and
+//   run the part's whole mixed-precision solve -- FP32 block-Jacobi PCG on the
+//   part's rows of K32 with FP64 true-residual refreshes from K64 -- with
+//   CTA barriers and fixed-order CTA reductions only.  No CTA waits on another.
+//   The CTA size is fixed, so a part's arithmetic, and its result, is the same
+//   whichever CTA takes it and whatever else is in the batch.
+// * Stage (mech_stage_solver!, src/mech/mech-solver.jl:186-492, once per part):
+//   each part keeps its own increment and Newton state (T, dT, iteration,
+//   residue, status) on the device.  One Newton iteration of every part that is
+//   still running is a fixed sequence of kernels -- per-part control, the
+//   vector updates, the batched solve, the element update of the active parts,
+//   the per-part residue, the commit or restore -- captured once as a CUDA graph
+//   and replayed until every part has finished its stage.
+// * Autotuner: elements per CTA of the element kernels and resident CTAs per SM
+//   of the batched solve, timed on the model itself.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <functional>
+#include <numeric>
+
+#include "amr_internal.h"
+
+namespace {
+
+constexpr int kPartThreads = 512;  // fixed: the reduction order of a part depends on it
+constexpr int kWarps = kPartThreads / 32;
+
+struct PartStat {
+    int32_t iters, refreshes, status, pad;
+    double rel_residual, umax;
+};
+
+enum { PH_START = 0, PH_ITER = 1, PH_DONE = 2 };
+enum { ACT_NONE = 0, ACT_COMMIT = 1, ACT_RESTORE = 2 };
+
+// per-part Newton / increment state of a batched stage
+struct PartCtl {
+    double T, dT, dTbk, Tcheck, acr, cR, res, res1, lastres, err;
+    int32_t phase, it, increments, iterations, krylov, status, start, syserr, action, pad;
+};
+
+struct StageP {
+    double tol, rtol, rspan, dTmin, dTmax, dTcheck;
+    int32_t maxits, autoinc;
+};
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// what the host reads after each Newton iteration of a batched stage
+struct StepInfo {
+    unsigned long long t0, t1;  // %globaltimer span of the batched solve (ns): first CTA start, last CTA end
+    int32_t remaining, pad;     // parts still running their stage
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// CTA-wide sums: FP32 partials per thread, FP32 warp trees, the warps' sums
+// added in FP64 in warp order.  Every thread receives the totals.
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ void cta_sum(const float (&v)[NV], double (&out)[NV], float *sh, double *shd) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        float x = v[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[i * kWarps + w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int q = 0; q < kWarps; q++) s += (double)sh[threadIdx.x * kWarps + q];
+        shd[threadIdx.x] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; i++) out[i] = shd[i];
+    __syncthreads();
+}
+
+__device__ double cta_max(double v, double *shd) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) shd[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int q = 0; q < kWarps; q++) m = fmax(m, shd[q]);
+        shd[kWarps] = m;
+    }
+    __syncthreads();
+    double r = shd[kWarps];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ double absnan(double x) {  // |x|, NaN as +inf (as the whole-model norm)
+    double a = fabs(x);
+    return isnan(a) ? INFINITY : a;
+}
+
+// q = K32 p on rows [n0, n1), a half-warp per row, two rows per half-warp in flight.
+// Returns this thread's part of p.q.
+template <int B>
+__device__ float part_spmv32(int64_t n0, int64_t n1, int64_t nb, const int64_t *__restrict__ rp,
+                             const int32_t *__restrict__ cj, const float *__restrict__ A, const float *__restrict__ p,
+                             float *__restrict__ q) {
+    constexpr int G = 16;
+    const int lane = threadIdx.x & (G - 1);
+    const int hw = threadIdx.x / G, nhw = kPartThreads / G;
+    const unsigned hmask = 0xffffu << (16 * (hw & 1));
+    float dot = 0.0f;
+    for (int64_t base = n0 + hw; base < n1; base += 2 * nhw) {
+        const int64_t r1 = base + nhw;
+        const bool two = r1 < n1;
+        float acc0[B], acc1[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc0[c] = acc1[c] = 0.0f;
+        const int64_t a0 = rp[base], e0 = rp[base + 1];
+        const int64_t a1 = two ? rp[r1] : 0, e1 = two ? rp[r1 + 1] : 0;
+        const int64_t len = max(e0 - a0, e1 - a1);
+        for (int64_t k = lane; k < len; k += G) {
+            if (a0 + k < e0) {
+                const int64_t kk = a0 + k, j = cj[kk];
+                float xv[B];
+#pragma unroll
+                for (int d = 0; d < B; d++) xv[d] = p[j * B + d];
+#pragma unroll
+                for (int c = 0; c < B; c++)
+#pragma unroll
+                    for (int d = 0; d < B; d++) acc0[c] = fmaf(__ldcs(A + (int64_t)(c * B + d) * nb + kk), xv[d], acc0[c]);
+            }
+            if (a1 + k < e1) {
+                const int64_t kk = a1 + k, j = cj[kk];
+                float xv[B];
+#pragma unroll
+                for (int d = 0; d < B; d++) xv[d] = p[j * B + d];
+#pragma unroll
+                for (int c = 0; c < B; c++)
+#pragma unroll
+                    for (int d = 0; d < B; d++) acc1[c] = fmaf(__ldcs(A + (int64_t)(c * B + d) * nb + kk), xv[d], acc1[c]);
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                acc0[c] += __shfl_down_sync(hmask, acc0[c], o, G);
+                acc1[c] += __shfl_down_sync(hmask, acc1[c], o, G);
+            }
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                q[base * B + c] = acc0[c];
+                dot = fmaf(p[base * B + c], acc0[c], dot);
+            }
+            if (two) {
+#pragma unroll
+                for (int c = 0; c < B; c++) {
+                    q[r1 * B + c] = acc1[c];
+                    dot = fmaf(p[r1 * B + c], acc1[c], dot);
+                }
+            }
+        }
+    }
+    return dot;
+}
+
+// FP64 true residual on rows [n0, n1): r = b - K64 u at free slots (0 at prescribed ones),
+// reactions K64 u at prescribed slots, r32 = r, z = Minv r32; adds r.z and |r|^2 (FP32) to rz, rr.
+template <int B>
+__device__ void part_residual64(int64_t n0, int64_t n1, int64_t nb, const int64_t *__restrict__ rp,
+                                const int32_t *__restrict__ cj, const double *__restrict__ A,
+                                const uint8_t *__restrict__ fm, const double *__restrict__ b,
+                                const double *__restrict__ u, double *__restrict__ reac, float *__restrict__ r32,
+                                float *__restrict__ z, const float *__restrict__ Minv, float &rz, float &rr) {
+    constexpr int G = 16;
+    const int lane = threadIdx.x & (G - 1);
+    const int hw = threadIdx.x / G, nhw = kPartThreads / G;
+    const unsigned hmask = 0xffffu << (16 * (hw & 1));
+    for (int64_t n = n0 + hw; n < n1; n += nhw) {
+        double acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0;
+        for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += G) {
+            const int64_t j = cj[k];
+#pragma unroll
+            for (int c = 0; c < B; c++)
+#pragma unroll
+                for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u[j * B + d], acc[c]);
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < B; c++) acc[c] += __shfl_down_sync(hmask, acc[c], o, G);
+        if (lane == 0) {
+            float rv[B];
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                double res = 0.0;
+                if (fm[n * B + c]) res = b[n * B + c] - acc[c];
+                else reac[n * B + c] = acc[c];
+                rv[c] = (float)res;
+                r32[n * B + c] = rv[c];
+                rr = fmaf(rv[c], rv[c], rr);
+            }
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                float s = 0.0f;
+#pragma unroll
+                for (int d = 0; d < B; d++) s = fmaf(Minv[n * B * B + c * B + d], rv[d], s);
+                z[n * B + c] = s;
+                rz = fmaf(rv[c], s, rz);
+            }
+        }
+    }
+}
+
+struct PcgArgs {
+    int64_t nparts;
+    const int64_t *part_ptr;  // node ranges
+    const int64_t *order;     // parts, most nodes first
+    const uint8_t *active;    // null: every part
+    int64_t nb;
+    const int64_t *rp;
+    const int32_t *cj;
+    const float *K32;
+    const double *K64;
+    const float *Minv;
+    const uint8_t *fm;
+    const double *b;
+    double *x;  // in: prescribed values at prescribed slots, 0 at free ones; out: solution
+    double *reac;
+    float *x32, *r32, *z32, *p32, *q32;
+    PartStat *stat;
+    unsigned long long *counter;
+    StepInfo *step;  // null: no timing
+    double tol2;
+    int max_iters, force_every;
+};
+
+// One CTA solves one part at a time: PCG with reliable updates, as the whole-model
+// mixed solver (restart-free; refresh when the recursive residual has dropped 100x
+// since the last refresh or looks converged; convergence judged on the FP64 residual).
+template <int B>
+__global__ void __launch_bounds__(kPartThreads, 2) k_part_pcg(PcgArgs a) {
+    __shared__ float sh[2 * kWarps];
+    __shared__ double shd[kWarps + 1];
+    __shared__ long long s_part;
+    if (a.step && threadIdx.x == 0) atomicMin(&a.step->t0, global_ns());
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long t = atomicAdd(a.counter, 1ULL);
+            s_part = (t < (unsigned long long)a.nparts) ? (long long)a.order[t] : -1;
+        }
+        __syncthreads();
+        const long long part = s_part;
+        __syncthreads();
+        if (part < 0) {
+            if (a.step && threadIdx.x == 0) atomicMax(&a.step->t1, global_ns());
+            return;
+        }
+        if (a.active && !a.active[part]) continue;
+        const int64_t n0 = a.part_ptr[part], n1 = a.part_ptr[part + 1];
+        const int64_t i0 = n0 * B, i1 = n1 * B;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) {
+            a.x32[i] = 0.0f;
+            a.p32[i] = 0.0f;
+        }
+        __syncthreads();
+        float rz = 0.0f, rr = 0.0f;
+        part_residual64<B>(n0, n1, a.nb, a.rp, a.cj, a.K64, a.fm, a.b, a.x, a.reac, a.r32, a.z32, a.Minv, rz, rr);
+        __syncthreads();
+        double t2[2];
+        cta_sum<2>({rz, rr}, t2, sh, shd);
+        double gam = t2[0], rr_true = t2[1];
+        const double bnorm2 = rr_true;
+        const double stop_rr = 0.0625 * a.tol2 * bnorm2;
+        int iters = 0, refreshes = 0, status = 0, since = 0;
+        bool first = true, done = !(bnorm2 > 0.0) || rr_true <= a.tol2 * bnorm2;
+        double beta = 0.0;
+        if (isnan(rr_true)) { status = AMR_ENOCONV; done = true; }
+        while (!done) {
+            if (iters >= a.max_iters) { status = AMR_ENOCONV; break; }
+            const float bf = first ? 0.0f : (float)beta;
+            for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) a.p32[i] = fmaf(bf, a.p32[i], a.z32[i]);
+            __syncthreads();
+            const float pq = part_spmv32<B>(n0, n1, a.nb, a.rp, a.cj, a.K32, a.p32, a.q32);
+            __syncthreads();
+            double t1[1];
+            cta_sum<1>({pq}, t1, sh, shd);
+            if (!(t1[0] > 0.0)) { status = AMR_ENOCONV; break; }
+            const float af = (float)(gam / t1[0]);
+            first = false;
+            float rzl = 0.0f, rrl = 0.0f;
+            for (int64_t n = n0 + threadIdx.x; n < n1; n += kPartThreads) {
+                float rv[B];
+#pragma unroll
+                for (int c = 0; c < B; c++) {
+                    const int64_t i = n * B + c;
+                    a.x32[i] = fmaf(af, a.p32[i], a.x32[i]);
+                    rv[c] = fmaf(-af, a.q32[i], a.r32[i]);
+                    a.r32[i] = rv[c];
+                }
+#pragma unroll
+                for (int c = 0; c < B; c++) {
+                    float s = 0.0f;
+#pragma unroll
+                    for (int d = 0; d < B; d++) s = fmaf(a.Minv[n * B * B + c * B + d], rv[d], s);
+                    a.z32[n * B + c] = s;
+                    rzl = fmaf(rv[c], s, rzl);
+                    rrl = fmaf(rv[c], rv[c], rrl);
+                }
+            }
+            __syncthreads();
+            cta_sum<2>({rzl, rrl}, t2, sh, shd);
+            beta = t2[0] / gam;
+            gam = t2[0];
+            iters++;
+            since++;
+            if (!(t2[1] > stop_rr) || t2[1] <= 1e-2 * rr_true || since >= a.force_every) {
+                for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) {
+                    if (a.fm[i]) a.x[i] += (double)a.x32[i];
+                    a.x32[i] = 0.0f;
+                }
+                __syncthreads();
+                rz = 0.0f;
+                rr = 0.0f;
+                part_residual64<B>(n0, n1, a.nb, a.rp, a.cj, a.K64, a.fm, a.b, a.x, a.reac, a.r32, a.z32, a.Minv, rz,
+                                   rr);
+                __syncthreads();
+                cta_sum<2>({rz, rr}, t2, sh, shd);
+                gam = t2[0];
+                rr_true = t2[1];
+                refreshes++;
+                since = 0;
+                if (isnan(rr_true)) { status = AMR_ENOCONV; break; }
+                if (rr_true <= a.tol2 * bnorm2) done = true;
+            }
+        }
+        double um = 0.0;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads)
+            if (a.fm[i]) um = fmax(um, absnan(a.x[i]));
+        um = cta_max(um, shd);
+        if (threadIdx.x == 0) {
+            a.stat[part].iters = iters;
+            a.stat[part].refreshes = refreshes;
+            a.stat[part].status = status;
+            a.stat[part].rel_residual = bnorm2 > 0.0 ? sqrt(rr_true / bnorm2) : 0.0;
+            a.stat[part].umax = um;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched stage: per-part control and per-slot vector kernels.  The vector
+// arithmetic is that of the whole-model stage driver, slot by slot.
+// ---------------------------------------------------------------------------
+__device__ double round_sig3_d(double x) {  // round(x, sigdigits=3)
+    if (x == 0.0 || !isfinite(x)) return x;
+    const double e = floor(log10(fabs(x)));
+    const double sc = pow(10.0, 2.0 - e);
+    return round(x * sc) / sc;
+}
+
+__global__ void k_ctl_begin(int64_t np, PartCtl *c, uint8_t *active, int32_t *perr, StageP p) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    PartCtl q = c[i];
+    perr[i] = 0;
+    q.action = ACT_NONE;
+    if (q.phase == PH_DONE) {
+        active[i] = 0;
+        c[i] = q;
+        return;
+    }
+    if (q.phase == PH_START) {
+        const double dTcr = fmin(p.rspan, 1.0 - q.T);
+        q.acr = fmin(q.dT / dTcr, 1.0);
+        q.cR = (q.T < 1.0 - p.rspan) ? q.acr : 0.0;
+        q.start = 1;
+        q.it = 0;
+        q.res = q.res1 = q.err = 0.0;
+        q.phase = PH_ITER;
+    } else {
+        q.start = 0;
+    }
+    q.syserr = 0;
+    q.it += 1;
+    q.lastres = q.res;
+    active[i] = 1;
+    c[i] = q;
+}
+
+struct SlotArgs {
+    int64_t n;
+    int B;
+    const int32_t *node_part;
+    const PartCtl *c;
+    const uint8_t *active;
+    const uint8_t *fm;
+    const double *Uex, *Fex;
+    double *U, *F, *R, *Rc, *dUa, *dUi, *dUitr, *Rtr, *dUt, *dFin, *dFex;
+};
+
+__global__ void k_slot_begin(SlotArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    const int32_t p = a.node_part[t / a.B];
+    if (!a.active[p]) return;
+    const PartCtl &q = a.c[p];
+    if (q.start) {
+        const double f = q.dT * a.Fex[t] + q.cR * a.Rc[t];
+        a.dFex[t] = f;
+        a.R[t] = f;
+        a.dUa[t] = 0.0;
+        a.dUi[t] = q.dT * a.Uex[t] + 0.0;
+    } else {
+        a.dUi[t] = 0.0;
+    }
+    a.dUitr[t] = a.fm[t] ? 0.0 : a.dUi[t];
+    a.Rtr[t] = 1.0 * a.R[t] + 0.0;
+}
+
+__global__ void k_ctl_mid(int64_t np, PartCtl *c, const PartStat *st, uint8_t *active) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np || !active[i]) return;
+    c[i].krylov += st[i].iters;
+    if (st[i].status) {
+        c[i].syserr = 1;  // Krylov solver did not converge
+        active[i] = 0;
+    } else if (!(st[i].umax <= 1e8)) {
+        c[i].syserr = 2;  // possible singular matrix
+        active[i] = 0;
+    }
+}
+
+__global__ void k_slot_mid(SlotArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    if (!a.active[a.node_part[t / a.B]]) return;
+    a.dUt[t] = 1.0 * a.dUa[t] + 1.0 * a.dUitr[t];
+}
+
+__global__ void k_slot_post(SlotArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    if (!a.active[a.node_part[t / a.B]]) return;
+    const double di = a.dUitr[t];
+    a.dUi[t] = di;
+    a.dUa[t] = 1.0 * a.dUa[t] + 1.0 * di;
+    const double r = 1.0 * a.dFex[t] + -1.0 * a.dFin[t];
+    a.R[t] = a.fm[t] ? r : 0.0;
+}
+
+// residue max|R|, and |dUi|, |dUa| of each active part (CTA per part)
+__global__ void __launch_bounds__(kPartThreads) k_part_norms(int64_t np, int B, const int64_t *part_ptr,
+                                                             const uint8_t *active, const double *R,
+                                                             const double *dUi, const double *dUa, PartCtl *c) {
+    __shared__ double shd[kWarps + 1];
+    for (int64_t p = blockIdx.x; p < np; p += gridDim.x) {
+        if (!active[p]) continue;
+        const int64_t i0 = part_ptr[p] * B, i1 = part_ptr[p + 1] * B;
+        double r = 0.0, ui = 0.0, ua = 0.0;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+            r = fmax(r, absnan(R[i]));
+            ui = fmax(ui, absnan(dUi[i]));
+            ua = fmax(ua, absnan(dUa[i]));
+        }
+        r = cta_max(r, shd);
+        ui = cta_max(ui, shd);
+        ua = cta_max(ua, shd);
+        if (threadIdx.x == 0) {
+            c[p].res = r;
+            c[p].err = ui / ua;
+        }
+    }
+}
+
+__global__ void k_ctl_end(int64_t np, PartCtl *c, const int32_t *perr, StageP p, StepInfo *step) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    PartCtl q = c[i];
+    if (q.phase != PH_ITER) return;
+    const double eps = DBL_EPSILON;
+    bool conv = false, fail = false;
+    if (q.syserr) {
+        fail = true;
+    } else if (perr[i]) {
+        q.syserr = 3;  // return mapping failed / NaN internal forces
+        fail = true;
+    } else {
+        q.iterations++;
+        if (q.it == 1) q.res1 = q.res;
+        if (q.res < p.tol) conv = true;
+        else if (q.err < p.rtol) conv = true;
+        else if (isnan(q.res)) fail = true;
+        else if (q.it > 1 && q.res > q.lastres) fail = true;
+        else if (q.it >= p.maxits) fail = true;
+    }
+    if (conv) {
+        q.action = ACT_COMMIT;
+        q.T += q.dT;
+        q.increments++;
+        if (q.T > q.Tcheck - p.dTmin) q.Tcheck += p.dTcheck;
+        if (p.autoinc) {
+            if (q.dTbk > 0.0) {
+                q.dT = fmin(q.dTbk, q.Tcheck - q.T);
+                q.dTbk = 0.0;
+            } else {
+                double f = 1.0 + tanh(log10(p.tol / (q.res1 + eps)));
+                f = fmax(f, 1.1);
+                const double dTtr = fmin(fmin(f * q.dT, p.dTmax), 1.0 - q.T);
+                if (q.T + dTtr > q.Tcheck - p.dTmin) {
+                    q.dTbk = q.dT;
+                    q.dT = q.Tcheck - q.T;
+                } else {
+                    q.dT = dTtr;
+                    q.dTbk = 0.0;
+                }
+            }
+        }
+        q.phase = (q.T < 1.0 - p.dTmin) ? PH_START : PH_DONE;
+    } else if (fail) {
+        q.action = ACT_RESTORE;
+        if (p.autoinc) {
+            double f = 1.0 + tanh(log10(p.tol / (q.res1 + eps)));
+            f = fmin(fmax(f, 0.2), 0.9);
+            if (q.syserr) f = 0.7;
+            q.dT = round_sig3_d(f * q.dT);
+            if (q.dT < p.dTmin) {
+                q.status = AMR_ESTAGE;
+                q.phase = PH_DONE;
+            } else {
+                q.phase = PH_START;
+            }
+        } else {
+            q.status = AMR_ESTAGE;
+            q.phase = PH_DONE;
+        }
+    }
+    if (q.phase != PH_DONE) atomicAdd(&step->remaining, 1);
+    c[i] = q;
+}
+
+__global__ void k_slot_commit(SlotArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    const PartCtl &q = a.c[a.node_part[t / a.B]];
+    if (q.action != ACT_COMMIT) return;
+    a.U[t] = 1.0 * a.U[t] + 1.0 * a.dUa[t];
+    a.F[t] = 1.0 * a.F[t] + 1.0 * a.dFin[t];
+    a.Rc[t] = (1.0 - q.acr) * a.Rc[t] + 1.0 * a.R[t];
+}
+
+// StateBk <- State for committing parts, State <- StateBk for failing ones
+__global__ void k_ip_commit(int64_t nip, const int32_t *ip_part, const PartCtl *c, double *st, double *stbk) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nip) return;
+    const int32_t act = c[ip_part[g]].action;
+    if (act == ACT_COMMIT) {
+        for (int f = 0; f < AMR_NST; f++) stbk[f * nip + g] = st[f * nip + g];
+    } else if (act == ACT_RESTORE) {
+        for (int f = 0; f < AMR_NST; f++) st[f * nip + g] = stbk[f * nip + g];
+    }
+}
+
+}  // namespace
+
+struct AmrBatch {
+    int64_t nparts = 0;
+    std::vector<int64_t> h_ptr;
+    int64_t *part_ptr = nullptr, *order = nullptr;
+    int32_t *node_part = nullptr, *elem_part = nullptr, *ip_part = nullptr;
+    PartStat *stat = nullptr;
+    PartCtl *ctl = nullptr;
+    uint8_t *active = nullptr;
+    int32_t *perr = nullptr;
+    StepInfo *step = nullptr, *h_step = nullptr;
+    unsigned long long *counter = nullptr;
+    float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+    int ctas_per_sm = 2;
+    std::vector<PartCtl> h_ctl;
+    std::vector<PartStat> h_stat;
+    double stage_seconds = 0.0, stage_solve_seconds = 0.0;
+    bool have_stage = false;
+};
+
+void amr_batch_free(amr_model *m) {
+    AmrBatch *b = m->batch;
+    if (!b) return;
+    amr_free(b->part_ptr); amr_free(b->order); amr_free(b->node_part); amr_free(b->elem_part);
+    amr_free(b->ip_part); amr_free(b->stat); amr_free(b->ctl); amr_free(b->active); amr_free(b->perr);
+    amr_free(b->step); amr_free(b->counter);
+    amr_free(b->x32); amr_free(b->r32); amr_free(b->z32); amr_free(b->p32); amr_free(b->q32);
+    if (b->h_step) cudaFreeHost(b->h_step);
+    delete b;
+    m->batch = nullptr;
+}
+
+void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *ptr) {
+    if (nparts < 1) throw AmrError(AMR_EINVAL, "nparts must be >= 1");
+    if (!ptr) throw AmrError(AMR_EINVAL, "null node_ptr");
+    if (nparts > INT32_MAX) throw AmrError(AMR_EINVAL, "too many parts");
+    if (ptr[0] != 0 || ptr[nparts] != m->nnodes) throw AmrError(AMR_EINVAL, "parts must cover nodes 0..nnodes-1");
+    for (int64_t i = 0; i < nparts; i++)
+        if (ptr[i + 1] <= ptr[i]) throw AmrError(AMR_EINVAL, "parts must be non-empty node ranges in increasing order");
+    std::vector<int32_t> npart(m->nnodes);
+    for (int64_t i = 0; i < nparts; i++)
+        for (int64_t n = ptr[i]; n < ptr[i + 1]; n++) npart[n] = (int32_t)i;
+    std::vector<int32_t> epart(m->nelems);
+    for (int64_t s = 0; s < m->nelems; s++) {  // sorted element order
+        const int32_t q = npart[m->h_conn[m->h_conn_ptr[s]]];
+        for (int64_t k = m->h_conn_ptr[s]; k < m->h_conn_ptr[s + 1]; k++)
+            if (npart[m->h_conn[k]] != q)
+                throw AmrError(AMR_EINVAL, "element " + std::to_string(m->perm[s] + 1) + " joins two parts");
+        epart[s] = q;
+    }
+    std::vector<int32_t> ipart(m->nip_total);
+    for (int64_t s = 0; s < m->nelems; s++)
+        for (int64_t g = m->h_ip_ptr[s]; g < m->h_ip_ptr[s + 1]; g++) ipart[g] = epart[s];
+    std::vector<int64_t> order(nparts);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t x, int64_t y) { return ptr[x + 1] - ptr[x] > ptr[y + 1] - ptr[y]; });
+    amr_batch_free(m);
+    AmrBatch *b = new AmrBatch();
+    m->batch = b;
+    try {
+        b->nparts = nparts;
+        b->h_ptr.assign(ptr, ptr + nparts + 1);
+        const int64_t n = m->nnodes * m->B;
+        amr_alloc(&b->part_ptr, nparts + 1);
+        amr_alloc(&b->order, nparts);
+        amr_alloc(&b->node_part, m->nnodes);
+        amr_alloc(&b->elem_part, m->nelems);
+        amr_alloc(&b->ip_part, m->nip_total);
+        amr_alloc(&b->stat, nparts);
+        amr_alloc(&b->ctl, nparts);
+        amr_alloc(&b->active, nparts);
+        amr_alloc(&b->perr, nparts);
+        amr_alloc(&b->step, 1);
+        amr_alloc(&b->counter, 1);
+        amr_alloc(&b->x32, n); amr_alloc(&b->r32, n); amr_alloc(&b->z32, n); amr_alloc(&b->p32, n);
+        amr_alloc(&b->q32, n);
+        AMR_CUDA(cudaMallocHost((void **)&b->h_step, sizeof(StepInfo)));
+        AMR_CUDA(cudaMemcpy(b->part_ptr, ptr, (nparts + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+        AMR_CUDA(cudaMemcpy(b->order, order.data(), nparts * sizeof(int64_t), cudaMemcpyHostToDevice));
+        AMR_CUDA(cudaMemcpy(b->node_part, npart.data(), npart.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        AMR_CUDA(cudaMemcpy(b->elem_part, epart.data(), epart.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        AMR_CUDA(cudaMemcpy(b->ip_part, ipart.data(), ipart.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        b->h_ctl.resize(nparts);
+        b->h_stat.resize(nparts);
+    } catch (...) {
+        amr_batch_free(m);
+        throw;
+    }
+}
+
+namespace {
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    AMR_CUDA(cudaGetDevice(&dev));
+    AMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return sms;
+}
+
+PcgArgs pcg_args(amr_model *m, double *x, const double *b_, double *reac, const amr_solve_opts &o,
+                 const uint8_t *active) {
+    AmrBatch *b = m->batch;
+    PcgArgs a;
+    a.nparts = b->nparts; a.part_ptr = b->part_ptr; a.order = b->order; a.active = active;
+    a.nb = m->nblocks; a.rp = m->brow_ptr; a.cj = m->bcol; a.K32 = m->K32; a.K64 = m->K64; a.Minv = m->Minv32;
+    a.fm = m->free_mask; a.b = b_; a.x = x; a.reac = reac;
+    a.x32 = b->x32; a.r32 = b->r32; a.z32 = b->z32; a.p32 = b->p32; a.q32 = b->q32;
+    a.stat = b->stat; a.counter = b->counter; a.step = nullptr; a.tol2 = o.rtol * o.rtol; a.max_iters = o.max_iters;
+    a.force_every = 16 * (o.refine_every > 0 ? o.refine_every : 32);
+    return a;
+}
+
+void launch_pcg(amr_model *m, const PcgArgs &a, int ctas_per_sm) {
+    AmrBatch *b = m->batch;
+    AMR_CUDA(cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), m->stream));
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(b->nparts, (int64_t)device_sms() * ctas_per_sm));
+    if (m->B == 3) k_part_pcg<3><<<grid, kPartThreads, 0, m->stream>>>(a);
+    else k_part_pcg<2><<<grid, kPartThreads, 0, m->stream>>>(a);
+    AMR_COUNT(1);
+    AMR_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+AmrSolveResult amr_batch_solve(amr_model *m, double *x, const double *b_, double *reac, const amr_solve_opts &o) {
+    AmrBatch *b = m->batch;
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    AMR_CUDA(cudaEventRecord(m->ev0, m->stream));
+    launch_pcg(m, pcg_args(m, x, b_, reac, o, nullptr), b->ctas_per_sm);
+    AMR_CUDA(cudaEventRecord(m->ev1, m->stream));
+    AMR_CUDA(cudaMemcpyAsync(b->h_stat.data(), b->stat, b->nparts * sizeof(PartStat), cudaMemcpyDeviceToHost,
+                             m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    res.seconds = ms * 1e-3;
+    for (const PartStat &s : b->h_stat) {
+        res.iterations = std::max(res.iterations, s.iters);
+        res.refinements = std::max(res.refinements, s.refreshes);
+        res.rel_residual = std::max(res.rel_residual, s.rel_residual);
+        if (s.status && !res.status) res.status = s.status;
+    }
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// Batched mech_stage_solver!
+// ---------------------------------------------------------------------------
+namespace {
+
+// sets the element kernels' per-part masks for the duration of a batched stage
+struct MaskScope {
+    amr_model *m;
+    MaskScope(amr_model *m_, AmrBatch *b) : m(m_) {
+        m->bp_elem_part = b->elem_part;
+        m->bp_node_part = b->node_part;
+        m->bp_active = b->active;
+        m->bp_err = b->perr;
+    }
+    ~MaskScope() {
+        m->bp_elem_part = nullptr;
+        m->bp_node_part = nullptr;
+        m->bp_active = nullptr;
+        m->bp_err = nullptr;
+    }
+};
+
+struct GraphScope {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    ~GraphScope() {
+        if (x) cudaGraphExecDestroy(x);
+        if (g) cudaGraphDestroy(g);
+    }
+};
+
+}  // namespace
+
+int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params &prm, double *U,
+                    double *F, amr_stage_stats *stats) {
+    AmrBatch *b = m->batch;
+    cudaStream_t s = m->stream;
+    if (prm.scheme != AMR_SCHEME_FE) throw AmrError(AMR_EUNSUPPORTED, "only the FE predictor scheme is on the GPU path");
+    if (prm.maxits < 1 || prm.nincs < 1) throw AmrError(AMR_EINVAL, "bad stage parameters");
+    if (prm.linear.method != AMR_SOLVER_MIXED)
+        throw AmrError(AMR_EUNSUPPORTED, "batched stages use the mixed-precision solver");
+    const int64_t n = m->nnodes * m->B, np = b->nparts;
+    std::vector<double *> v(10, nullptr);
+    struct Release {
+        std::vector<double *> &v;
+        ~Release() {
+            for (auto &x : v) amr_free(x);
+        }
+    } release{v};
+    for (auto &x : v) amr_alloc(&x, n);
+    double *R = v[0], *dUa = v[1], *dUi = v[2], *Rc = v[3], *dFin = v[4], *dFex = v[5], *dUitr = v[6], *Rtr = v[7],
+           *reac = v[8], *dUt = v[9];
+    b->have_stage = false;
+    cudaEvent_t t0 = m->ev0, t1 = m->ev1;
+    AMR_CUDA(cudaEventRecord(t0, s));
+    for (double *x : {U, F, R, dUa, dUi, Rc, dFin, dFex, dUitr, Rtr, reac, dUt})
+        AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+    // stage parameters (src/solver.jl:128-140 for nouts)
+    int nincs = prm.nincs;
+    const bool saveouts = prm.nouts > 0, autoinc = prm.autoinc != 0;
+    if (saveouts && !autoinc) {
+        if (prm.nouts > nincs) nincs = prm.nouts;
+        if (nincs % prm.nouts != 0) nincs = nincs - (nincs % prm.nouts) + prm.nouts;
+    }
+    StageP sp;
+    sp.tol = prm.tol; sp.rtol = prm.rtol; sp.rspan = prm.rspan; sp.dTmin = prm.dTmin; sp.dTmax = prm.dTmax;
+    sp.dTcheck = saveouts ? 1.0 / prm.nouts : 1.0;
+    sp.maxits = prm.maxits; sp.autoinc = autoinc ? 1 : 0;
+    PartCtl c0{};
+    c0.T = 0.0;
+    c0.dT = 1.0 / nincs;
+    if (autoinc) c0.dT = std::min({c0.dT, prm.dTmax, sp.dTcheck, prm.dT0});
+    c0.Tcheck = sp.dTcheck;
+    c0.phase = PH_START;
+    std::fill(b->h_ctl.begin(), b->h_ctl.end(), c0);
+    AMR_CUDA(cudaMemcpyAsync(b->ctl, b->h_ctl.data(), np * sizeof(PartCtl), cudaMemcpyHostToDevice, s));
+    AMR_CUDA(cudaMemcpyAsync(m->stbk, m->st, (size_t)AMR_NST * m->nip_total * sizeof(double),
+                             cudaMemcpyDeviceToDevice, s));
+    // the element-force staging is read for every node: start it at zero
+    {
+        int64_t nfel = 0;
+        AMR_CUDA(cudaMemcpyAsync(&nfel, m->fel_ptr + m->nelems, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        AMR_CUDA(cudaMemsetAsync(m->Fel, 0, nfel * sizeof(double), s));
+    }
+    // every stage mounts K once; a state-dependent K is mounted in every Newton iteration (inside the graph)
+    m->K_valid = false;
+    amr_stiffness(m);
+    {
+        int rc = amr_check_status(m);
+        if (rc == AMR_ENEGJAC)
+            throw AmrError(rc, "Negative Jacobian determinant in cell " + std::to_string(m->perm[m->h_status[1]] + 1));
+        if (rc) throw AmrError(rc, "assembly failed");
+    }
+    m->K_valid = true;
+
+    SlotArgs sa;
+    sa.n = n; sa.B = m->B; sa.node_part = b->node_part; sa.c = b->ctl; sa.active = b->active; sa.fm = m->free_mask;
+    sa.Uex = Uex; sa.Fex = Fex; sa.U = U; sa.F = F; sa.R = R; sa.Rc = Rc; sa.dUa = dUa; sa.dUi = dUi;
+    sa.dUitr = dUitr; sa.Rtr = Rtr; sa.dUt = dUt; sa.dFin = dFin; sa.dFex = dFex;
+    PcgArgs pa = pcg_args(m, dUitr, Rtr, reac, prm.linear, b->active);
+    pa.step = b->step;
+    const unsigned gs = nblk(n, 256), gp = nblk(np, 128), gi = nblk(m->nip_total, 256);
+    const unsigned gn = (unsigned)std::min<int64_t>(np, (int64_t)device_sms() * 4);
+
+    MaskScope mask(m, b);
+    GraphScope gr;
+    // one Newton iteration of every running part
+    auto iteration = [&]() {
+        AMR_CUDA(cudaMemsetAsync(&b->step->t0, 0xff, sizeof(unsigned long long), s));
+        AMR_CUDA(cudaMemsetAsync(&b->step->t1, 0, sizeof(StepInfo) - sizeof(unsigned long long), s));
+        k_ctl_begin<<<gp, 128, 0, s>>>(np, b->ctl, b->active, b->perr, sp);
+        k_slot_begin<<<gs, 256, 0, s>>>(sa);
+        AMR_COUNT(2);
+        if (m->any_plastic) amr_stiffness(m);
+        launch_pcg(m, pa, b->ctas_per_sm);
+        k_ctl_mid<<<gp, 128, 0, s>>>(np, b->ctl, b->stat, b->active);
+        k_slot_mid<<<gs, 256, 0, s>>>(sa);
+        AMR_COUNT(2);
+        amr_update_elements(m, dUt, dFin);
+        k_slot_post<<<gs, 256, 0, s>>>(sa);
+        k_part_norms<<<gn, kPartThreads, 0, s>>>(np, m->B, b->part_ptr, b->active, R, dUi, dUa, b->ctl);
+        k_ctl_end<<<gp, 128, 0, s>>>(np, b->ctl, b->perr, sp, b->step);
+        k_slot_commit<<<gs, 256, 0, s>>>(sa);
+        k_ip_commit<<<gi, 256, 0, s>>>(m->nip_total, b->ip_part, b->ctl, m->st, m->stbk);
+        AMR_COUNT(5);
+        AMR_CUDA(cudaGetLastError());
+    };
+    // capture it once; count its kernels per replay instead of at capture
+    const long long before = amr_g_launches.load();
+    AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    try {
+        iteration();
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        throw;
+    }
+    AMR_CUDA(cudaStreamEndCapture(s, &gr.g));
+    const long long per_iter = amr_g_launches.load() - before;
+    AMR_COUNT(-per_iter);
+    AMR_CUDA(cudaGraphInstantiate(&gr.x, gr.g, 0));
+
+    double solve_s = 0.0;
+    int steps = 0;
+    const int max_steps = 1000000;
+    for (;;) {
+        AMR_CUDA(cudaGraphLaunch(gr.x, s));
+        AMR_COUNT(per_iter);
+        AMR_CUDA(cudaMemcpyAsync(b->h_step, b->step, sizeof(StepInfo), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        if (b->h_step->t1 > b->h_step->t0) solve_s += (double)(b->h_step->t1 - b->h_step->t0) * 1e-9;
+        steps++;
+        if (b->h_step->remaining == 0) break;
+        if (steps >= max_steps) throw AmrError(AMR_ESTAGE, "batched stage did not finish");
+    }
+    AMR_CUDA(cudaEventRecord(t1, s));
+    AMR_CUDA(cudaMemcpyAsync(b->h_ctl.data(), b->ctl, np * sizeof(PartCtl), cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaEventSynchronize(t1));
+    AMR_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+    // element kernels wrote their errors per part; leave the handle's own status clear
+    {
+        int32_t reset[2] = {0, INT32_MAX};
+        AMR_CUDA(cudaMemcpy(m->d_status, reset, sizeof reset, cudaMemcpyHostToDevice));
+    }
+    if (m->any_plastic) m->K_valid = false;  // K holds the tangent of some part's last trial state
+    b->stage_seconds = ms * 1e-3;
+    b->stage_solve_seconds = solve_s;
+    b->have_stage = true;
+    amr_stage_stats st{};
+    st.status = AMR_OK;
+    st.T = 1.0;
+    int64_t failed = -1;
+    for (int64_t i = 0; i < np; i++) {
+        const PartCtl &q = b->h_ctl[i];
+        if (q.status && failed < 0) failed = i;
+        st.increments = std::max(st.increments, q.increments);
+        st.krylov_iterations += q.krylov;
+        st.residue = std::max(st.residue, q.res);
+        st.T = std::min(st.T, q.T);
+    }
+    st.iterations = steps;
+    st.seconds = b->stage_seconds;
+    st.solve_seconds = solve_s;
+    int status = AMR_OK;
+    if (failed >= 0) {
+        status = AMR_ESTAGE;
+        st.status = status;
+        m->err = "part " + std::to_string(failed) + ": Solver did not converge.";
+    }
+    if (stats) *stats = st;
+    return status;
+}
+
+void amr_batch_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *out) {
+    const AmrBatch *b = m->batch;
+    if (!b) throw AmrError(AMR_EINVAL, "no parts set");
+    if (!b->have_stage) throw AmrError(AMR_EINVAL, "no batched stage has run");
+    if (nparts != b->nparts) throw AmrError(AMR_EINVAL, "nparts does not match the parts set");
+    for (int64_t i = 0; i < nparts; i++) {
+        const PartCtl &q = b->h_ctl[i];
+        amr_stage_stats &s = out[i];
+        s.status = q.status;
+        s.increments = q.increments;
+        s.iterations = q.iterations;
+        s.krylov_iterations = q.krylov;
+        s.residue = q.res;
+        s.T = q.T;
+        s.seconds = b->stage_seconds;
+        s.solve_seconds = b->stage_solve_seconds;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+namespace {
+
+double time_ms(amr_model *m, const std::function<void()> &f, int reps) {
+    f();  // warm-up (and attribute set-up)
+    AMR_CUDA(cudaEventRecord(m->ev0, m->stream));
+    for (int r = 0; r < reps; r++) f();
+    AMR_CUDA(cudaEventRecord(m->ev1, m->stream));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    return ms / reps;
+}
+
+int pairs_of(int nen) { return nen * (nen + 1) / 2; }
+
+}  // namespace
+
+void amr_autotune_model(amr_model *m, amr_tuning *out) {
+    if (!m->dofs_set) throw AmrError(AMR_EINVAL, "amr_set_dofs must be called first");
+    cudaStream_t s = m->stream;
+    const size_t nst = (size_t)AMR_NST * m->nip_total;
+    const int64_t n = m->nnodes * m->B;
+    double *st_save = nullptr, *dU = nullptr, *dF = nullptr;
+    struct Free {
+        double *&a, *&b, *&c;
+        ~Free() { amr_free(a); amr_free(b); amr_free(c); }
+    } fr{st_save, dU, dF};
+    amr_alloc(&st_save, nst);
+    amr_alloc(&dU, n);
+    amr_alloc(&dF, n);
+    AMR_CUDA(cudaMemcpyAsync(st_save, m->st, nst * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    AMR_CUDA(cudaMemsetAsync(dU, 0, n * sizeof(double), s));
+    const int saved_mode = m->assembly_mode;
+    m->assembly_mode = AMR_ASSEMBLY_FAST;
+    amr_tuning t{};
+    t.ngroups = (int32_t)std::min<size_t>(m->groups.size(), AMR_MAX_TUNED_GROUPS);
+    t.stiffness_seconds = 0.0;
+    t.internal_seconds = 0.0;
+    std::vector<AmrGroup> all = m->groups;
+    try {
+        for (size_t gi = 0; gi < m->groups.size(); gi++) {
+            // time this group's kernels alone: the other groups are taken out of the list meanwhile
+            AmrGroup g = all[gi];
+            const int np = pairs_of(g.nen), ndim = amr::shape_ndim(g.shape);
+            double best = 1e300;
+            int best_epb = g.epb;
+            for (int e : {1, 2, 3, 4, 6, 8}) {
+                if (e > 1 && e * np > 512) continue;
+                const size_t smem = sizeof(double) * (size_t)e * (g.nen * ndim + 2 * g.nip * g.nen * ndim + 2 * g.nip);
+                if (smem > 200 * 1024) continue;
+                g.epb = e;
+                m->groups.assign(1, g);
+                const double ms = time_ms(m, [&] { amr_stiffness_elements(m); }, 3);
+                if (ms < best) { best = ms; best_epb = e; }
+            }
+            g.epb = best_epb;
+            t.stiffness_seconds += best * 1e-3;
+            double besti = 1e300;
+            int best_int = g.epb_int;
+            for (int e : {1, 2, 4, 8, 16}) {
+                const size_t smem = sizeof(double) * (size_t)e * (2 * g.nen * ndim + g.nip * g.nen * ndim);
+                if (smem > 200 * 1024) continue;
+                g.epb_int = e;
+                m->groups.assign(1, g);
+                const double ms = time_ms(m, [&] { amr_update_elements(m, dU, dF); }, 3);
+                if (ms < besti) { besti = ms; best_int = e; }
+            }
+            g.epb_int = best_int;
+            t.internal_seconds += besti * 1e-3;
+            all[gi] = g;
+            if (gi < AMR_MAX_TUNED_GROUPS) {
+                t.shape[gi] = g.shape;
+                t.stiffness_epb[gi] = g.epb;
+                t.internal_epb[gi] = g.epb_int;
+            }
+        }
+    } catch (...) {
+        m->groups = all;
+        m->assembly_mode = saved_mode;
+        throw;
+    }
+    m->groups = all;
+    m->assembly_mode = saved_mode;
+    amr_check_status(m);  // a trial update with dU = 0 reports nothing the caller asked for
+    AMR_CUDA(cudaMemcpyAsync(m->st, st_save, nst * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    // batched solve: resident CTAs per SM, on a capped run of the assembled K with a unit load
+    if (m->batch && m->K_valid) {
+        AmrBatch *b = m->batch;
+        double *x = dU, *rhs = dF, *reac = nullptr;
+        amr_alloc(&reac, n);
+        struct FreeOne {
+            double *&p;
+            ~FreeOne() { amr_free(p); }
+        } fo{reac};
+        std::vector<double> ones(n, 1.0);
+        AMR_CUDA(cudaMemcpyAsync(rhs, ones.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        amr_solve_opts o;
+        amr_default_solve_opts(&o);
+        o.max_iters = 50;
+        double best = 1e300;
+        int best_k = b->ctas_per_sm;
+        for (int k : {1, 2, 3, 4}) {
+            const double ms = time_ms(m, [&] {
+                AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+                launch_pcg(m, pcg_args(m, x, rhs, reac, o, nullptr), k);
+            }, 2);
+            if (ms < best) { best = ms; best_k = k; }
+        }
+        b->ctas_per_sm = best_k;
+        AMR_CUDA(cudaStreamSynchronize(s));
+    }
+    t.batch_threads = kPartThreads;
+    t.batch_ctas_per_sm = m->batch ? m->batch->ctas_per_sm : 0;
+    if (out) *out = t;
+}

@@ -279,6 +279,7 @@ int amr_model_destroy(amr_model *m) {
     if (!m) return AMR_OK;
     if (m->stream) cudaStreamSynchronize(m->stream);
     amr_solver_free(m);
+    amr_batch_free(m);
     for (AmrGroup &g : m->groups) amr_free(g.tab);
     amr_free(m->coords); amr_free(m->conn); amr_free(m->conn_ptr); amr_free(m->mat_type); amr_free(m->mat_par);
     amr_free(m->ip_ptr); amr_free(m->kel_ptr); amr_free(m->inc_ptr); amr_free(m->inc); amr_free(m->brow_ptr);
@@ -596,6 +597,29 @@ int amr_stage_run_dev(amr_model *m, const double *d_Uex, const double *d_Fex, co
     });
 }
 
+int amr_set_parts(amr_model *m, int64_t nparts, const int64_t *node_ptr) {
+    return guarded(m, [&] {
+        if (nparts == 0) amr_batch_free(m);
+        else amr_batch_set(m, nparts, node_ptr);
+        return AMR_OK;
+    });
+}
+
+int amr_get_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *stats) {
+    if (!stats) return AMR_EINVAL;
+    return guarded(const_cast<amr_model *>(m), [&] {
+        amr_batch_part_stats(m, nparts, stats);
+        return AMR_OK;
+    });
+}
+
+int amr_autotune(amr_model *m, amr_tuning *out) {
+    return guarded(m, [&] {
+        amr_autotune_model(m, out);
+        return AMR_OK;
+    });
+}
+
 int amr_launch_count(const amr_model *m, int64_t *count) {
     if (!count) return AMR_EINVAL;
     (void)m;
@@ -634,6 +658,7 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
 // ---------------------------------------------------------------------------
 int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params &p, double *U,
                      double *F, amr_stage_stats *stats) {
+    if (m->batch) return amr_batch_stage(m, Uex, Fex, p, U, F, stats);  // each part its own stage
     int64_t n = m->nnodes * m->B;
     cudaStream_t s = m->stream;
     if (p.scheme != AMR_SCHEME_FE) throw AmrError(AMR_EUNSUPPORTED, "only the FE predictor scheme is on the GPU path");

@@ -47,7 +47,15 @@ struct ModelArgs {
     int64_t nip_total;
     int stressmodel;
     double thickness;
+    // batched stages: elements of inactive parts are skipped, errors are recorded per part
+    const int32_t *elem_part;
+    const uint8_t *part_active;
+    int32_t *part_err;
 };
+
+__device__ __forceinline__ bool elem_skipped(const ModelArgs &M, int64_t e) {
+    return M.part_active && !M.part_active[M.elem_part[e]];
+}
 
 __device__ __forceinline__ void set_status(int32_t *st, int code, int64_t elem) {
     atomicCAS(&st[0], 0, code);
@@ -703,6 +711,7 @@ __global__ void __launch_bounds__(256) internal_kernel(ModelArgs M, GroupArgs G,
     for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
         int el = t / nip, ip = t % nip;
         int64_t e = e0 + el;
+        if (elem_skipped(M, e)) continue;
         double g[NEN * DIM];
         double det = ip_geometry<DIM>(NEN, dNdR + ip * NEN * DIM, sC + el * NEN * DIM, g);
         const double *u = sU + el * NEN * DIM;
@@ -728,7 +737,8 @@ __global__ void __launch_bounds__(256) internal_kernel(ModelArgs M, GroupArgs G,
         for (int f = 0; f < AMR_NST; f++) s0[f] = stbk[f * M.nip_total + gi];
         int rc = material_update(M.mat_type[e], M.mat_par + 8 * e, ps, s0, s1, de, ds);
         if (rc) {
-            set_status(status, rc, e);
+            if (M.part_err) atomicCAS(&M.part_err[M.elem_part[e]], 0, rc);
+            else set_status(status, rc, e);
             for (int f = 0; f < AMR_NST; f++) s1[f] = s0[f];
             for (int i = 0; i < 6; i++) ds[i] = 0.0;
         }
@@ -745,6 +755,7 @@ __global__ void __launch_bounds__(256) internal_kernel(ModelArgs M, GroupArgs G,
     __syncthreads();
     for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
         int el = t / (NEN * DIM), q = t % (NEN * DIM);
+        if (elem_skipped(M, e0 + el)) continue;
         double s = 0.0;
         for (int ip = 0; ip < nip; ip++) s += sF[(el * nip + ip) * NEN * DIM + q];
         Fel[M.fel_ptr[e0 + el] + q] = s;
@@ -754,7 +765,8 @@ __global__ void __launch_bounds__(256) internal_kernel(ModelArgs M, GroupArgs G,
 // dFin[node] = sum over incident (element, local) in element order
 __global__ void node_gather_kernel(int64_t nnodes, int B, const int64_t *inc_ptr, const int64_t *inc,
                                    const int64_t *conn_ptr, const int64_t *fel_ptr, const double *Fel, double *out,
-                                   int accumulate, int32_t *status) {
+                                   int accumulate, int32_t *status, const int32_t *node_part,
+                                   const uint8_t *part_active, int32_t *part_err) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nnodes * B) return;
     int64_t n = t / B;
@@ -765,7 +777,13 @@ __global__ void node_gather_kernel(int64_t nnodes, int B, const int64_t *inc_ptr
         int a = (int)(inc[q] & 0xff);
         s += Fel[fel_ptr[e] + a * B + c];
     }
-    if (isnan(s)) set_status(status, AMR_ENAN, -1);
+    if (isnan(s)) {
+        if (part_err) {
+            if (part_active[node_part[n]]) atomicCAS(&part_err[node_part[n]], 0, AMR_ENAN);
+        } else {
+            set_status(status, AMR_ENAN, -1);
+        }
+    }
     out[t] = accumulate ? out[t] + s : s;
 }
 
@@ -855,6 +873,7 @@ ModelArgs margs(amr_model *m) {
     a.coords = m->coords; a.conn = m->conn; a.conn_ptr = m->conn_ptr; a.mat_type = m->mat_type;
     a.mat_par = m->mat_par; a.ip_ptr = m->ip_ptr; a.kel_ptr = m->kel_ptr; a.fel_ptr = m->fel_ptr;
     a.nip_total = m->nip_total; a.stressmodel = m->stressmodel; a.thickness = m->thickness;
+    a.elem_part = m->bp_elem_part; a.part_active = m->bp_active; a.part_err = m->bp_err;
     return a;
 }
 
@@ -886,7 +905,7 @@ void launch_stiff_ref(amr_model *m, const AmrGroup &g) {
 template <int DIM, int NEN>
 void launch_internal(amr_model *m, const AmrGroup &g, const double *dU) {
     GroupArgs ga{g.tab, g.nip, g.first, g.count};
-    int epb = (g.nip * 1 >= 16) ? 4 : 16;
+    int epb = g.epb_int > 0 ? g.epb_int : ((g.nip >= 16) ? 4 : 16);
     size_t smem = sizeof(double) * (size_t)epb * (2 * NEN * DIM + g.nip * NEN * DIM);
     int threads = std::max(epb * g.nip, epb * NEN * DIM);
     threads = ((threads + 31) / 32) * 32;
@@ -929,7 +948,7 @@ int amr_check_status(amr_model *m) {
     return code;
 }
 
-void amr_stiffness(amr_model *m) {
+void amr_stiffness_elements(amr_model *m) {
     for (const AmrGroup &g : m->groups) {
         if (m->assembly_mode == AMR_ASSEMBLY_REFERENCE)
             dispatch(
@@ -940,6 +959,10 @@ void amr_stiffness(amr_model *m) {
                 m, g, [&](auto n) { launch_stiff<3, decltype(n)::value>(m, g); },
                 [&](auto n) { launch_stiff<2, decltype(n)::value>(m, g); });
     }
+}
+
+void amr_stiffness(amr_model *m) {
+    amr_stiffness_elements(m);
     unsigned grid = nblk(m->nnodes * 32, 256);
     if (m->B == 3) {
         gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
@@ -962,7 +985,8 @@ void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm) {
     }
     int64_t nt = m->nnodes * m->B;
     node_gather_kernel<<<nblk(nt, 256), 256, 0, m->stream>>>(m->nnodes, m->B, m->inc_ptr, m->inc, m->conn_ptr,
-                                                             m->fel_ptr, m->Fel, dFin_nm, 0, m->d_status);
+                                                             m->fel_ptr, m->Fel, dFin_nm, 0, m->d_status,
+                                                             m->bp_node_part, m->bp_active, m->bp_err);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }

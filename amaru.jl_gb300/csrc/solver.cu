@@ -855,6 +855,7 @@ void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq) {
 }
 
 AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
+    if (m->batch && o.method == AMR_SOLVER_MIXED) return amr_batch_solve(m, x, b, reac, o);  // one CTA per part
     if (o.method == AMR_SOLVER_FP64)
         return m->B == 3 ? solve_fp64_csr<3>(m, x, b, reac, o) : solve_fp64_csr<2>(m, x, b, reac, o);
     return m->B == 3 ? solve_mixed<3>(m, x, b, reac, o) : solve_mixed<2>(m, x, b, reac, o);

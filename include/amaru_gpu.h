@@ -224,6 +224,38 @@ int amr_solve_noalloc(amr_model *m, double *d_U, double *d_F, const amr_solve_op
 int amr_stage_run_dev(amr_model *m, const double *d_Uex, const double *d_Fex, const amr_stage_params *p,
                       double *d_U, double *d_F, amr_stage_stats *stats);
 
+/* ---- batches of independent models ----
+ * Many independent FE models (each one a call of mech_stage_solver!,
+ * src/mech/mech-solver.jl:186-492, on its own FEModel) joined into one handle:
+ * part i owns the nodes node_ptr[i] .. node_ptr[i+1]-1 and no element joins two
+ * parts.  With parts set, amr_solve runs one persistent kernel in which each
+ * part's mixed-precision solve is done by one CTA (relative residual per part),
+ * and amr_stage_run / amr_stage_run_dev run each part's own Newton loop and
+ * increment control on the device, one Newton iteration of all parts per CUDA
+ * graph launch; assembly and internal forces stay one launch for all parts.  A
+ * part's result does not depend on the other parts in the batch.
+ * nparts = 0 clears the parts. */
+int amr_set_parts(amr_model *m, int64_t nparts, const int64_t *node_ptr);
+/* Per-part outcome of the last batched stage (nparts entries). */
+int amr_get_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *stats);
+
+/* Launch shapes picked by amr_autotune (no counterpart in the reference). */
+#define AMR_MAX_TUNED_GROUPS 8
+typedef struct {
+    int32_t ngroups;                            /* element groups (shape, quadrature) */
+    int32_t shape[AMR_MAX_TUNED_GROUPS];
+    int32_t stiffness_epb[AMR_MAX_TUNED_GROUPS];  /* elements per CTA, element stiffness */
+    int32_t internal_epb[AMR_MAX_TUNED_GROUPS];   /* elements per CTA, internal forces */
+    int32_t batch_threads;                      /* threads per CTA of the batched solve */
+    int32_t batch_ctas_per_sm;                  /* resident CTAs per SM of the batched solve */
+    double stiffness_seconds;                   /* best time of one assembly, all groups */
+    double internal_seconds;                    /* best time of one internal-force pass */
+} amr_tuning;
+/* Times the candidate launch shapes of the element kernels on this model (and of
+ * the batched solve when parts are set) and keeps the fastest.  Needs the DOFs
+ * set; leaves K, the IP states and the results of earlier calls unchanged. */
+int amr_autotune(amr_model *m, amr_tuning *out);
+
 /* ---- diagnostics (no counterpart in the reference) ---- */
 /* Average device time of one launch of a hot kernel over `reps` launches,
  * timed with CUDA events on the handle's stream, and its algorithmic bytes

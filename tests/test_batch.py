@@ -1,0 +1,158 @@
+"""Batches of independent models: many plane-strain QUAD8 rectangles of uneven size,
+each its own mech_stage_solver! (src/mech/mech-solver.jl:186-492), joined into one
+device handle (amr_set_parts) and run together.
+
+Checked here:
+* every part against the same model run alone through the whole-model path and
+  against the oracle (1e-6 of max|U| and of max|F|);
+* a part's result is bitwise the same alone (a batch of one) and in the mix;
+* elastoplastic parts over several increments, with Newton iteration counts equal
+  to the model run alone;
+* the batched solve_system! per part;
+* a part that fails its stage leaves the others untouched;
+* the autotuner changes launch shapes only, not results.
+"""
+import numpy as np
+import pytest
+
+import amaru_gpu as A
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+BOX = [[0, 0], [2.0, 1.0]]
+
+
+def _instances(seed, count, nmin, nmax):
+    """(n, E, nu) per model: n uniform in [nmin, nmax], E lognormal(ln 200e3, 0.2), nu uniform [0.2, 0.35]."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(nmin, nmax + 1)), float(np.exp(rng.normal(np.log(200e3), 0.2))),
+             float(rng.uniform(0.2, 0.35))) for _ in range(count)]
+
+
+def _gpu_model(n, mat, device):
+    mesh = A.Mesh(A.Block(BOX, nx=n, ny=n, cellshape=A.QUAD8))
+    return A.FEModel(mesh, [("all", mat)], A.MechContext(stressmodel="planestrain"), nips=9, device=device)
+
+
+def _bcs(mod, load):
+    return [("x==0", mod.SurfaceBC(ux=0, uy=0)), ("x==2", mod.SurfaceBC(tx=load))]
+
+
+def _linear(inst, device=False):
+    return [_gpu_model(n, A.LinearElastic(E=E, nu=nu), device) for n, E, nu in inst]
+
+
+def _close(a, b, tol=1e-6):
+    s = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() <= tol * s
+
+
+def test_batch_matches_each_model_alone_and_the_oracle():
+    inst = _instances(7, 6, 2, 12)
+    ba = A.BatchAnalysis(_linear(inst))
+    ba.addstage(_bcs(A, 1.0))
+    res = ba.solve()
+    assert all(ok for ok, _ in res)
+    for (n, E, nu), m in zip(inst, ba.models):
+        alone = _gpu_model(n, A.LinearElastic(E=E, nu=nu), True)
+        ana = A.MechAnalysis(alone)
+        ana.addstage(_bcs(A, 1.0))
+        assert ana.solve()[0]
+        assert _close(m.U, alone.U) and _close(m.F, alone.F)
+        mo = O.Mesh(O.Block(BOX, nx=n, ny=n, cellshape=A.QUAD8))
+        om = O.FEModel(mo, [("all", O.LinearElastic(E=E, nu=nu))], stressmodel="planestrain", nips=9)
+        ao = O.MechAnalysis(om)
+        ao.addstage(_bcs(O, 1.0))
+        assert ao.solve()[0]
+        assert _close(m.U, om.U) and _close(m.F, om.F)
+    st = ba.part_stats[0]
+    assert all(s.status == 0 and s.increments == 1 for s in st)
+
+
+def test_part_result_is_the_same_alone_and_in_the_mix():
+    inst = _instances(11, 9, 2, 14)
+    mix = A.BatchAnalysis(_linear(inst))
+    mix.addstage(_bcs(A, 1.0))
+    assert all(ok for ok, _ in mix.solve())
+    for k in (int(np.argmin([i[0] for i in inst])), int(np.argmax([i[0] for i in inst])), 3):
+        one = A.BatchAnalysis(_linear([inst[k]]))
+        one.addstage(_bcs(A, 1.0))
+        assert one.solve()[0][0]
+        assert np.array_equal(one.models[0].U, mix.models[k].U)
+        assert np.array_equal(one.models[0].F, mix.models[k].F)
+
+
+def test_elastoplastic_parts_over_increments():
+    inst = _instances(3, 4, 2, 6)
+    mats = [A.VonMises(E=E, nu=nu, fy=0.9, H=1e3) for _, E, nu in inst]
+    ba = A.BatchAnalysis([_gpu_model(n, mat, False) for (n, _, _), mat in zip(inst, mats)])
+    ba.addstage(_bcs(A, 1.0), nincs=5)
+    assert all(ok for ok, _ in ba.solve(tol=1e-6))
+    for k, ((n, E, nu), m) in enumerate(zip(inst, ba.models)):
+        alone = _gpu_model(n, A.VonMises(E=E, nu=nu, fy=0.9, H=1e3), True)
+        ana = A.MechAnalysis(alone)
+        ana.addstage(_bcs(A, 1.0), nincs=5)
+        assert ana.solve(tol=1e-6)[0]
+        assert ba.part_stats[0][k].iterations == ana.stats[0].iterations
+        assert _close(m.U, alone.U) and _close(m.F, alone.F)
+        assert alone.state()[:, 12].max() > 0  # the load yields the material
+    one = A.BatchAnalysis([_gpu_model(inst[2][0], A.VonMises(E=inst[2][1], nu=inst[2][2], fy=0.9, H=1e3), False)])
+    one.addstage(_bcs(A, 1.0), nincs=5)
+    assert one.solve(tol=1e-6)[0][0]
+    assert np.array_equal(one.models[0].U, ba.models[2].U)
+
+
+def test_batched_solve_system_per_part():
+    inst = _instances(5, 5, 2, 10)
+    ba = A.BatchAnalysis(_linear(inst))
+    Uex, Fex = ba.configure([_bcs(A, 1.0)] * len(inst))
+    J = ba.joined
+    J.dev.assemble_K()
+    U, F = Uex.copy(), Fex.copy()
+    st = J.solve_system(U, F, rtol=1e-10)
+    assert st.rel_residual <= 1e-10
+    Us, Fs = ba.split(U), ba.split(F)
+    for (n, E, nu), Ui, Fi in zip(inst, Us, Fs):
+        alone = _gpu_model(n, A.LinearElastic(E=E, nu=nu), True)
+        setup = alone.configure_dofs(_bcs(A, 1.0))
+        Ua, Fa = alone.get_bc_vals(setup)
+        alone.dev.assemble_K()
+        alone.solve_system(Ua, Fa, rtol=1e-10)
+        Un = np.zeros((alone.nnodes, 2))
+        Fn = np.zeros((alone.nnodes, 2))
+        Un[alone.dof_node, alone.dof_comp] = Ua
+        Fn[alone.dof_node, alone.dof_comp] = Fa
+        assert _close(Ui, Un) and _close(Fi, Fn)
+
+
+def test_failing_part_leaves_the_others_untouched():
+    inst = _instances(13, 4, 2, 6)
+    mats = [A.VonMises(E=E, nu=nu, fy=0.9, H=0.0) for _, E, nu in inst]
+    loads = [0.5, 50.0, 0.5, 0.5]  # part 1: far beyond the limit load of a perfectly plastic strip
+    ba = A.BatchAnalysis([_gpu_model(n, mat, False) for (n, _, _), mat in zip(inst, mats)])
+    ba.addstage([_bcs(A, q) for q in loads], nincs=2)
+    res = ba.solve(tol=1e-6, maxits=3)
+    assert not res[1][0] and all(res[k][0] for k in (0, 2, 3))
+    assert ba.part_stats[0][1].status == -11
+    rest = A.BatchAnalysis([_gpu_model(inst[k][0], mats[k], False) for k in (0, 2, 3)])
+    rest.addstage([_bcs(A, loads[k]) for k in (0, 2, 3)], nincs=2)
+    assert all(ok for ok, _ in rest.solve(tol=1e-6, maxits=3))
+    for j, k in enumerate((0, 2, 3)):
+        assert np.array_equal(rest.models[j].U, ba.models[k].U)
+
+
+def test_autotune_changes_launch_shapes_not_results():
+    inst = _instances(17, 12, 2, 16)
+    a = A.BatchAnalysis(_linear(inst))
+    a.addstage(_bcs(A, 1.0))
+    assert all(ok for ok, _ in a.solve())
+    b = A.BatchAnalysis(_linear(inst))
+    b.addstage(_bcs(A, 1.0))
+    t = b.autotune()
+    assert t.ngroups == 1 and t.shape[0] == A.QUAD8
+    assert t.stiffness_epb[0] >= 1 and t.internal_epb[0] >= 1 and 1 <= t.batch_ctas_per_sm <= 4
+    assert t.batch_threads == 512 and t.stiffness_seconds > 0 and t.internal_seconds > 0
+    assert all(ok for ok, _ in b.solve())
+    for ma, mb in zip(a.models, b.models):
+        assert np.array_equal(ma.U, mb.U) and np.array_equal(ma.F, mb.F)
