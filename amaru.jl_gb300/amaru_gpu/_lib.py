@@ -74,6 +74,26 @@ class Tuning(C.Structure):
                 ("stiffness_seconds", C.c_double), ("internal_seconds", C.c_double)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int32), ("pad", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("model", ModelDesc), ("eq_id", C.c_void_p), ("ndofs", C.c_int64), ("nu", C.c_int64),
+                ("Uex", C.c_void_p), ("Fex", C.c_void_p), ("loads", C.c_void_p), ("nloads", C.c_int32),
+                ("pad", C.c_int32), ("stage", StageParams)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("active_at_admit", C.c_int32), ("bytes", C.c_int64),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double), ("stage", StageStats)]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("queued", C.c_int64), ("active", C.c_int64), ("peak_active", C.c_int64), ("completed", C.c_int64),
+                ("active_bytes", C.c_int64), ("peak_bytes", C.c_int64), ("seconds", C.c_double)]
+
+
 # Every exported entry point of include/amaru_gpu.h with its ctypes signature.
 P = C.c_void_p
 SIGNATURES = {
@@ -101,6 +121,12 @@ SIGNATURES = {
     "amr_set_parts": (C.c_int, [P, C.c_int64, P]),
     "amr_get_part_stats": (C.c_int, [P, C.c_int64, P]),
     "amr_autotune": (C.c_int, [P, C.POINTER(Tuning)]),
+    "amr_estimate_bytes": (C.c_int, [C.POINTER(ModelDesc), C.POINTER(C.c_int64)]),
+    "amr_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "amr_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    "amr_server_wait": (C.c_int, [P, C.c_int64, P, P, C.POINTER(RequestResult), C.c_char_p, C.c_size_t]),
+    "amr_server_stats": (C.c_int, [P, C.POINTER(ServerInfo)]),
+    "amr_server_destroy": (C.c_int, [P]),
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_default_solve_opts": (None, [C.POINTER(SolveOpts)]),
@@ -163,20 +189,42 @@ def default_stage_params(**kw):
     return p
 
 
+def model_desc(ndim, stressmodel, thickness, coords, shape, nips, conn_ptr, conn, mat_type, mat_params):
+    """(ModelDesc, arrays it points into): keep the arrays alive while the desc is used."""
+    keep = [np.ascontiguousarray(coords, dtype=np.float64), np.ascontiguousarray(shape, dtype=np.int32),
+            np.ascontiguousarray(nips, dtype=np.int32), np.ascontiguousarray(conn_ptr, dtype=np.int64),
+            np.ascontiguousarray(conn, dtype=np.int64), np.ascontiguousarray(mat_type, dtype=np.int32),
+            np.ascontiguousarray(mat_params, dtype=np.float64)]
+    c, s, n, cp, cn, mt, mp = keep
+    d = ModelDesc()
+    d.ndim, d.stressmodel, d.thickness = ndim, stressmodel, thickness
+    d.nnodes, d.coords = c.shape[0], ptr(c)
+    d.nelems, d.shape, d.nips = s.shape[0], ptr(s), ptr(n)
+    d.conn_ptr, d.conn, d.mat_type, d.mat_params = ptr(cp), ptr(cn), ptr(mt), ptr(mp)
+    return d, keep
+
+
+def load_array(loads):
+    """(Load array, arrays it points into) from (kind, dir, edge_key, facet_shape, items, coef) tuples."""
+    arr = (Load * max(len(loads), 1))()
+    keep = []
+    for i, (kind, dr, edge, fshape, items, coef) in enumerate(loads):
+        it = np.ascontiguousarray(items, dtype=np.int64)
+        keep.append(it)
+        arr[i].kind, arr[i].dir, arr[i].edge_key, arr[i].facet_shape = kind, dr, edge, fshape
+        arr[i].nitems = it.shape[0] if it.ndim > 0 else 0
+        arr[i].items = ptr(it)
+        for k in range(5):
+            arr[i].coef[k] = coef[k]
+    return arr, keep
+
+
 class DeviceModel:
     """Owning wrapper of an amr_model handle."""
 
     def __init__(self, ndim, stressmodel, thickness, coords, shape, nips, conn_ptr, conn, mat_type, mat_params):
-        self._keep = [np.ascontiguousarray(coords, dtype=np.float64), np.ascontiguousarray(shape, dtype=np.int32),
-                      np.ascontiguousarray(nips, dtype=np.int32), np.ascontiguousarray(conn_ptr, dtype=np.int64),
-                      np.ascontiguousarray(conn, dtype=np.int64), np.ascontiguousarray(mat_type, dtype=np.int32),
-                      np.ascontiguousarray(mat_params, dtype=np.float64)]
-        c, s, n, cp, cn, mt, mp = self._keep
-        d = ModelDesc()
-        d.ndim, d.stressmodel, d.thickness = ndim, stressmodel, thickness
-        d.nnodes, d.coords = c.shape[0], ptr(c)
-        d.nelems, d.shape, d.nips = s.shape[0], ptr(s), ptr(n)
-        d.conn_ptr, d.conn, d.mat_type, d.mat_params = ptr(cp), ptr(cn), ptr(mt), ptr(mp)
+        d, self._keep = model_desc(ndim, stressmodel, thickness, coords, shape, nips, conn_ptr, conn, mat_type,
+                                   mat_params)
         h = C.c_void_p()
         check(None, lib().amr_model_create(C.byref(d), C.byref(h)))
         self.h = h
@@ -246,16 +294,7 @@ class DeviceModel:
         return s
 
     def assemble_loads(self, loads, F, t=0.0):
-        arr = (Load * max(len(loads), 1))()
-        keep = []
-        for i, (kind, dr, edge, fshape, items, coef) in enumerate(loads):
-            it = np.ascontiguousarray(items, dtype=np.int64)
-            keep.append(it)
-            arr[i].kind, arr[i].dir, arr[i].edge_key, arr[i].facet_shape = kind, dr, edge, fshape
-            arr[i].nitems = it.shape[0] if it.ndim > 0 else 0
-            arr[i].items = ptr(it)
-            for k in range(5):
-                arr[i].coef[k] = coef[k]
+        arr, keep = load_array(loads)
         F = np.ascontiguousarray(F, dtype=np.float64)
         check(self.h, lib().amr_assemble_loads(self.h, arr, len(loads), t, ptr(F)))
         return F

@@ -238,6 +238,14 @@ class FEModel:
 
     # ---- get_bc_vals (src/bc.jl:237-249)
     def get_bc_vals(self, setup, t=0.0):
+        U, F, loads = self.bc_vals(setup, t)
+        if loads:
+            F = self.dev.assemble_loads(loads, F, t)
+        return U, F
+
+    def bc_vals(self, setup, t=0.0):
+        """Essential values U, concentrated natural values F, and the distributed loads as
+        amr_load tuples still to be integrated into F (on the device)."""
         U = np.zeros(self.ndofs)
         F = np.zeros(self.ndofs)
         loads = []
@@ -269,9 +277,7 @@ class FEModel:
                         raise ValueError("body condition %s is not applicable" % key)
                     cf = affine_coefficients(val, self.ndim)
                     loads.append((L.LOAD_BODY, _DIR[key[1]], 0, 0, np.asarray(sel, dtype=np.int64), cf))
-        if loads:
-            F = self.dev.assemble_loads(loads, F, t)
-        return U, F
+        return U, F, loads
 
     # ---- the solver-level plugin functions the library replaces
     def mount_K(self, reference_order=True):

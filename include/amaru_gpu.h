@@ -239,6 +239,58 @@ int amr_set_parts(amr_model *m, int64_t nparts, const int64_t *node_ptr);
 /* Per-part outcome of the last batched stage (nparts entries). */
 int amr_get_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *stats);
 
+/* ---- serving (no counterpart in the reference: Amaru runs one analysis per call) ----
+ * A request is one mech_stage_solver! stage (src/mech/mech-solver.jl:186-492) of
+ * its own model: the model description, the DOF numbering of configure_dofs!,
+ * the stage's essential values and natural loads (get_bc_vals, src/bc.jl:237-249,
+ * with distributed loads as amr_load items evaluated at t = 0) and the stage
+ * parameters.  The server copies it at submit.  max_active worker slots run
+ * admitted requests concurrently, each on its own CUDA stream; requests are
+ * admitted in arrival order once a slot is free and amr_estimate_bytes of the
+ * request fits in hbm_budget_bytes beside the running ones (continuous
+ * batching).  A request's pattern, K, IP states and solution stay on the device
+ * across all increments of its stage.  Its result is the one it gets alone. */
+typedef struct amr_server amr_server;
+typedef struct {
+    double hbm_budget_bytes;  /* device memory the admitted requests may hold together */
+    int32_t max_active;       /* worker slots: requests on the device at once */
+    int32_t pad;
+} amr_server_config;
+typedef struct {
+    amr_model_desc model;
+    const int64_t *eq_id;     /* nnodes x 3, as amr_set_dofs */
+    int64_t ndofs, nu;
+    const double *Uex, *Fex;  /* ndofs each, eq_id order */
+    const amr_load *loads;    /* distributed loads added to Fex on the device */
+    int32_t nloads, pad;
+    amr_stage_params stage;
+} amr_request;
+typedef struct {
+    int32_t status;           /* AMR_OK, AMR_ESTAGE or the error of the request */
+    int32_t active_at_admit;  /* requests on the device right after this one was admitted */
+    int64_t bytes;            /* admitted footprint (amr_estimate_bytes) */
+    double t_submit, t_admit, t_done;  /* seconds since the server was created */
+    amr_stage_stats stage;
+} amr_request_result;
+typedef struct {
+    int64_t queued, active, peak_active, completed, active_bytes, peak_bytes;
+    double seconds;           /* since the server was created */
+} amr_server_info;
+/* Upper bound of the device bytes one model and one stage of it (mixed-precision
+ * solver) allocate. */
+int amr_estimate_bytes(const amr_model_desc *desc, int64_t *bytes);
+int amr_server_create(const amr_server_config *cfg, amr_server **out);
+/* Queues a request (copied); AMR_ENOMEM if it can never fit the budget. */
+int amr_server_submit(amr_server *s, const amr_request *req, int64_t *id);
+/* Blocks until request id has finished; U, F (ndofs, eq_id order) receive the
+ * stage's results as amr_stage_run's; err (may be null) its error message.
+ * Returns the request's status.  Each id is waited for once. */
+int amr_server_wait(amr_server *s, int64_t id, double *U, double *F, amr_request_result *res, char *err,
+                    size_t nerr);
+int amr_server_stats(amr_server *s, amr_server_info *st);
+/* Finishes the queued and running requests, then stops the slots. */
+int amr_server_destroy(amr_server *s);
+
 /* Launch shapes picked by amr_autotune (no counterpart in the reference). */
 #define AMR_MAX_TUNED_GROUPS 8
 typedef struct {
