@@ -74,6 +74,38 @@ class Block:
         self.cellshape, self.tag = cellshape, tag
 
 
+_ROW_MULT = np.array([0x9E3779B97F4A7C15, 0xC2B2AE3D27D4EB4F, 0x165667B19E3779F9, 0xD6E8FEB86659FD93,
+                      0xFF51AFD7ED558CCD, 0xC4CEB9FE1A85EC53, 0x94D049BB133111EB, 0xBF58476D1CE4E5B9,
+                      0x2545F4914F6CDD1D], dtype=np.uint64)
+
+
+def _distinct_rows(rows):
+    """For each distinct row of an int64 table: the index of its first occurrence and its count
+    (np.unique(rows, axis=0, return_index=True, return_counts=True) up to the order of the distinct
+    rows).  Rows are grouped by a 64-bit hash, and the grouping is verified row by row; a hash
+    collision falls back to the exact row sort."""
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    if len(rows) == 0 or rows.shape[1] > len(_ROW_MULT):
+        _, first, cnt = np.unique(rows, axis=0, return_index=True, return_counts=True)
+        return first, cnt
+    with np.errstate(over="ignore"):
+        h = (rows.view(np.uint64) * _ROW_MULT[:rows.shape[1]]).sum(axis=1, dtype=np.uint64)
+        h ^= h >> np.uint64(31)
+    order = np.argsort(h)
+    hs = h[order]
+    start = np.empty(len(hs), dtype=bool)
+    start[0] = True
+    start[1:] = hs[1:] != hs[:-1]
+    starts = np.nonzero(start)[0]
+    grp = np.cumsum(start) - 1
+    first = np.minimum.reduceat(order, starts)
+    if not np.array_equal(rows[order], rows[first[grp]]):
+        _, first, cnt = np.unique(rows, axis=0, return_index=True, return_counts=True)
+        return first, cnt
+    cnt = np.diff(np.append(starts, len(hs)))
+    return first, cnt
+
+
 class Mesh:
     """Mesh(blocks...): nodes (coords), elements (shape, conn), outer facets and edges."""
 
@@ -285,8 +317,7 @@ class Mesh:
             o += len(f)
         fshape = np.concatenate(fac_shape)
         fowner = np.concatenate(owner)
-        key = np.sort(allf, axis=1)
-        _, first, inv, cnt = np.unique(key, axis=0, return_index=True, return_inverse=True, return_counts=True)
+        first, cnt = _distinct_rows(np.sort(allf, axis=1))
         sel = np.sort(first[cnt == 1])
         self.face_nodes = allf[sel]
         self.face_shape = fshape[sel]
@@ -303,7 +334,7 @@ class Mesh:
                 es.append(np.full(len(e), es_shape))
             e = np.concatenate(en)
             es = np.concatenate(es)
-            _, first = np.unique(np.sort(e, axis=1), axis=0, return_index=True)
+            first, _ = _distinct_rows(np.sort(e, axis=1))
             first = np.sort(first)
             self.edge_nodes, self.edge_shape = e[first], es[first]
 

@@ -158,7 +158,7 @@ class FEModel:
         self.F = np.zeros((self.nnodes, self.ndim))  # dof.vals of the natural keys
         self.eq_id = -np.ones((self.nnodes, 3), dtype=np.int64)
         self.ndofs = self.nu = 0
-        self.active_nodes = np.unique(mesh.conn)
+        self.active_nodes = np.nonzero(np.bincount(mesh.conn, minlength=self.nnodes))[0]
         self._dof_names = ["ux", "uy", "uz"][: self.ndim]
 
     @classmethod

@@ -47,6 +47,10 @@ def parse():
     ap.add_argument("--cpu-mesh", default="20x8x8", help="bounded CPU sample of the same workload family")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-models measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--slope", default="", help="also run the TET10 slope stage at these divisions, e.g. 100x17x40")
     return ap.parse_args()
 
 
@@ -241,12 +245,206 @@ def run_ours(a):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if not a.no_batch:
+        out["batch"] = batch_leg()
+    if not a.no_serve:
+        out["serving"] = serving_leg(a.serve_requests)
+    if a.slope:
+        out["slope"] = slope_leg(a.slope)
     if rank == 0 and not a.no_cpu:
         out["cpu_baseline"] = cpu_baseline(a, steps=1, warmup=0)
     return out
 
 
 # ---------------------------------------------------------------------------
+# ---------------------------------------------------------------------------
+# Batched independent models: 512 plane-strain QUAD8 rectangles 2 x 1, n x n with
+# n uniform in [10, 60], E lognormal(ln 200e3, 0.2), nu uniform [0.2, 0.35], 3x3
+# Gauss points, left edge fixed, unit traction tx on the right edge; one linear
+# stage of all of them through the batched stage driver.
+# ---------------------------------------------------------------------------
+BATCH_SEED = 0xC4
+
+
+def _quad8_models(inst, cache, device):
+    import amaru_gpu as A
+    out = []
+    for n, E, nu in inst:
+        if n not in cache:
+            cache[n] = A.Mesh(A.Block([[0, 0], [2.0, 1.0]], nx=n, ny=n, cellshape=A.QUAD8))
+        out.append(A.FEModel(cache[n], [("all", A.LinearElastic(E=E, nu=nu))],
+                             A.MechContext(stressmodel="planestrain"), nips=9, device=device))
+    return out
+
+
+def batch_leg(count=512, steps=3):
+    import torch
+    import amaru_gpu as A
+    from amaru_gpu import _lib as L
+    rng = np.random.default_rng(BATCH_SEED)
+    ns = rng.integers(10, 61, count)
+    Es = np.exp(rng.normal(np.log(200e3), 0.2, count))
+    nus = rng.uniform(0.2, 0.35, count)
+    inst = [(int(a), float(b), float(c)) for a, b, c in zip(ns, Es, nus)]
+    bcs = [("x==0", A.SurfaceBC(ux=0, uy=0)), ("x==2", A.SurfaceBC(tx=1.0))]
+    cache = {}
+    t0 = time.perf_counter()
+    ba = A.BatchAnalysis(_quad8_models(inst, cache, False))
+    ba.addstage(bcs)
+    setup_s = time.perf_counter() - t0
+    tu = ba.autotune()
+    J = ba.joined
+    Uex, Fex = ba.configure(ba.stages[0].bcs)
+    p = L.default_stage_params(linear=L.default_solve_opts(method=L.SOLVER_MIXED, rtol=1e-8))
+    dU, dF = torch.from_numpy(Uex).cuda(), torch.from_numpy(Fex).cuda()
+    oU, oF = torch.zeros_like(dU), torch.zeros_like(dF)
+    secs, solve, launches = [], [], []
+    for r in range(steps + 1):
+        c0 = J.dev.launch_count()
+        rc, st = J.dev.stage_run_dev(dU.data_ptr(), dF.data_ptr(), p, oU.data_ptr(), oF.data_ptr())
+        if rc != 0:
+            raise RuntimeError(J.dev.last_error())
+        if r > 0:  # the first run is the warm-up
+            secs.append(st.seconds)
+            solve.append(st.solve_seconds)
+            launches.append(J.dev.launch_count() - c0)
+    ps = J.dev.part_stats()
+    kr = np.array([s.krylov_iterations for s in ps])
+    t = float(np.mean(secs))
+    # the same 32 models (every 16th) one at a time on their own handles, against the same 32 batched
+    samp = inst[::max(1, count // 32)][:32]
+    seq = 0.0
+    for m in _quad8_models(samp, cache, True):
+        setup = m.configure_dofs(bcs)
+        U0, F0 = m.get_bc_vals(setup)
+        m.dev.stage_run(U0, F0, p)
+        rc, _, _, s1 = m.dev.stage_run(U0, F0, p)
+        seq += s1.seconds
+        m.dev.close()
+    bs = A.BatchAnalysis(_quad8_models(samp, cache, False))
+    bs.addstage(bcs)
+    Us, Fs = bs.configure(bs.stages[0].bcs)
+    bs.joined.dev.stage_run(Us, Fs, p)
+    rc, _, _, s2 = bs.joined.dev.stage_run(Us, Fs, p)
+    return {"workload": "%d plane-strain QUAD8 models 2x1, n x n with n~U{10..60} (seed 0xC4), E lognormal(ln 200e3, "
+                        "0.2), nu~U[0.2,0.35], 9 IP, left edge fixed, unit tx on the right edge; one linear stage of "
+                        "every model in one batched stage (per-part PCG to 1e-8)" % count,
+            "models": count, "ndofs": int(J.ndofs), "ms_per_batch": t * 1e3, "solve_ms": float(np.mean(solve)) * 1e3,
+            "models_per_s": count / t, "dof_per_s": J.ndofs / t, "launches_per_batch": int(np.mean(launches)),
+            "krylov_iters_max": int(kr.max()), "krylov_iters_mean": float(kr.mean()),
+            "parts_converged": int(sum(s.status == 0 for s in ps)), "setup_s": setup_s,
+            "tuning": {"stiffness_epb": tu.stiffness_epb[0], "internal_epb": tu.internal_epb[0],
+                       "pcg_threads": tu.batch_threads, "pcg_ctas_per_sm": tu.batch_ctas_per_sm},
+            "sample_32": {"one_at_a_time_s": seq, "batched_s": s2.seconds, "speedup": seq / s2.seconds}}
+
+
+# ---------------------------------------------------------------------------
+# Serving: Poisson arrivals (200 requests/s, seeded) of linear-elastic HEX8
+# cantilever blocks 1 x 0.5 x 0.5 with DOFs log-uniform in [1e3, 2e6] and 1..10 increments,
+# and at 20 % elastoplastic TET10 blocks (von Mises, gravity + top surcharge,
+# automatic increments, DOFs log-uniform in [1e3, 2e5]); continuous batching
+# with admission against the free HBM.
+# ---------------------------------------------------------------------------
+SERVE_SEED = 0xC5
+
+
+def _serve_requests(count):
+    import amaru_gpu as A
+    rng = np.random.default_rng(SERVE_SEED)
+    arrivals = np.cumsum(rng.exponential(1 / 200.0, count))
+    reqs = []
+    for i in range(count):
+        tet = rng.random() < 0.2
+        incs = int(rng.integers(1, 11))
+        if tet:
+            dofs = float(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
+            k = max(1, int(round(((dofs / 3) / 16) ** (1 / 3))))  # nodes ~ (4k+1)(2k+1)^2
+            mesh = A.Mesh(A.Block([[0, 0, 0], [1.0, 0.5, 0.5]], nx=2 * k, ny=k, nz=k, cellshape=A.TET10))
+            m = A.FEModel(mesh, [("all", A.VonMises(E=50e3, nu=0.3, fy=100.0, H=1e3))], device=False)
+            bcs = [("z==0", A.SurfaceBC(ux=0, uy=0, uz=0)), ("z==0.5", A.SurfaceBC(tz=-120.0)),
+                   ("all", A.BodyC(wz=-20.0))]
+            kw = dict(nincs=incs, autoinc=True)
+        else:
+            dofs = float(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
+            k = max(1, int(round(((dofs / 3) / 2) ** (1 / 3))))  # nodes ~ (2k+1)(k+1)^2
+            mesh = A.Mesh(A.Block([[0, 0, 0], [1.0, 0.5, 0.5]], nx=2 * k, ny=k, nz=k, cellshape=A.HEX8))
+            m = A.FEModel(mesh, [("all", A.LinearElastic(E=200e3, nu=0.3))], device=False)
+            bcs = [("x==0", A.SurfaceBC(ux=0, uy=0, uz=0)), ("x==1", A.SurfaceBC(tz=-1.0))]
+            kw = dict(nincs=incs)
+        reqs.append((arrivals[i], "tet10" if tet else "hex8", m, bcs, kw))
+    return reqs
+
+
+def serving_leg(count=32, max_active=8):
+    import torch
+    from amaru_gpu import serve
+    reqs = _serve_requests(count)
+    free, _ = torch.cuda.mem_get_info()
+    budget = 0.85 * free
+    lat, out, failures = [], [], []
+    with serve.Server(hbm_budget_bytes=budget, max_active=max_active) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for at, kind, m, bcs, kw in reqs:
+            wait = at - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            tickets.append(srv.submit(m, bcs, **kw))
+        for (at, kind, m, bcs, kw), tk in zip(reqs, tickets):
+            rc, U, F, res, msg = srv.wait(tk)
+            out.append((kind, rc, res, tk.ndofs))
+            if rc != 0:
+                failures.append("%s %d DOFs: %s" % (kind, tk.ndofs, msg))
+        info = srv.info()
+    lat = np.array([r.t_done - r.t_submit for _, _, r, _ in out])
+    t_first = min(r.t_submit for _, _, r, _ in out)
+    t_last = max(r.t_done for _, _, r, _ in out)
+    span = t_last - t_first
+    dof_incs = sum(n * r.stage.increments for _, rc, r, n in out if rc == 0)
+    return {"workload": "%d requests, Poisson arrivals 200/s (seed 0xC5): HEX8 cantilever blocks 1x0.5x0.5, DOFs log-uniform "
+                        "[1e3, 2e6], 1..10 linear increments; 20%% TET10 von Mises blocks (gravity + surcharge, "
+                        "automatic increments), DOFs log-uniform [1e3, 2e5]; mixed solver to 1e-8" % count,
+            "requests": count, "completed": int(sum(rc == 0 for _, rc, _, _ in out)),
+            "tet10": int(sum(k == "tet10" for k, _, _, _ in out)),
+            "solves_per_s": count / span, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
+            "p99_ms": float(np.percentile(lat, 99)) * 1e3, "mean_ms": float(lat.mean()) * 1e3,
+            "dof_increments_per_s": dof_incs / span, "makespan_s": span, "max_active": max_active,
+            "peak_active": int(info.peak_active), "peak_admitted_gb": info.peak_bytes / 1e9,
+            "hbm_budget_gb": budget / 1e9,
+            "total_dofs": int(sum(n for _, _, _, n in out)), "failures": failures}
+
+
+# ---------------------------------------------------------------------------
+# Nonlinear geomechanics: plane-strain slope extruded along y, TET10 block mesh
+# with jittered interior vertices (seed 0xC3), von Mises E=50e3 nu=0.3 fy=100
+# H=1e3, gravity 20 + crest surcharge 200 ramped over 20 increments, Newton tol 1e-6.
+# ---------------------------------------------------------------------------
+def slope_leg(spec):
+    import amaru_gpu as A
+    from amaru_gpu import workloads as W
+    n = dims(spec)
+    g = W.SLOPE
+    t0 = time.perf_counter()
+    mesh = A.Mesh(A.Block([[0, 0, 0], [g["L"], g["W"], g["H"]]], nx=n[0], ny=n[1], nz=n[2], cellshape=A.TET10))
+    mesh.coords = W.slope_coords(mesh.coords, mesh.elem_nodes(), W.boundary_nodes(mesh), 4, *n, seed=0xC3)
+    model = A.FEModel(mesh, [("all", A.VonMises(E=50e3, nu=0.3, fy=100.0, H=1e3))])
+    ana = A.MechAnalysis(model)
+    ana.addstage(W.slope_bcs(A, 200.0), nincs=20)
+    setup_s = time.perf_counter() - t0
+    ok, msg = ana.solve(tol=1e-6)
+    st = ana.stats[0]
+    sizes = model.dev.sizes()
+    plastic = int((model.state()[:, 12] > 0).sum())
+    return {"workload": "TET10 slope %s (L=10, W=1.7, crest 4 m, toe 2 m, jittered interior, seed 0xC3), von Mises "
+                        "E=50e3 nu=0.3 fy=100 H=1e3, gravity 20 + crest surcharge 200 over 20 increments, Newton "
+                        "tol 1e-6, mixed solver to 1e-8" % spec,
+            "ok": bool(ok), "message": msg, "ndofs": int(model.ndofs), "nelems": sizes["nelems"],
+            "nnodes": sizes["nnodes"], "increments": st.increments, "newton_iterations": st.iterations,
+            "krylov_iterations": st.krylov_iterations, "stage_s": st.seconds, "solve_s": st.solve_seconds,
+            "dof_iterations_per_s": model.ndofs * st.iterations / st.seconds, "plastic_ips": plastic,
+            "setup_s": setup_s}
+
+
 def cpu_sample(nx, ny, nz, nthreads):
     """One linear increment of the same workload family on the CPU restatement: mount_K + direct solve
     (SuperLU) + update_state!.  Returns (ndofs, seconds)."""

@@ -102,3 +102,29 @@ def test_dof_numbering_matches_oracle():
     eq, ndofs, nu2, dn, dk = number_dofs(np.arange(len(mesh.coords)), presc, len(mesh.coords))
     assert nu2 == nu and ndofs == len(dofs)
     assert (eq == model.eq_id).all()
+
+
+def test_slope_mesh_keeps_boundary_planes_and_orientation():
+    """Slope mapping + interior jitter: boundary nodes stay on their planes, edge nodes at edge
+    midpoints, and every TET10 keeps the orientation it had in the block."""
+    from amaru_gpu import workloads as W
+    g = W.SLOPE
+    n = (10, 2, 4)
+    mesh = A.Mesh(A.Block([[0, 0, 0], [g["L"], g["W"], g["H"]]], nx=n[0], ny=n[1], nz=n[2], cellshape=A.TET10))
+    en = mesh.elem_nodes()
+    c0 = mesh.coords
+    c = W.slope_coords(c0, en, W.boundary_nodes(mesh), 4, *n, seed=7)
+    for k, v in ((0, 0.0), (0, g["L"]), (1, 0.0), (1, g["W"]), (2, 0.0)):
+        on = c0[:, k] == v
+        assert on.any() and (c[on, k] == v).all()
+    crest = (c0[:, 2] == g["H"]) & (c0[:, 0] <= g["x1"])
+    assert crest.any() and (c[crest, 2] == g["H"]).all()
+    for j, a, b in W.edge_pairs(c0, en, 4):
+        assert np.allclose(c[en[:, j]], 0.5 * (c[en[:, a]] + c[en[:, b]]))
+
+    def vol(x):
+        v = x[en[:, 1:4]] - x[en[:, [0]]]
+        return np.einsum("ij,ij->i", v[:, 0], np.cross(v[:, 1], v[:, 2]))
+    v0, v1 = vol(c0), vol(c)
+    assert (np.sign(v0) == np.sign(v1)).all() and (np.abs(v1) > 0.2 * np.abs(v0)).all()
+    assert not np.allclose(c, c0 * [1, 1, 1])  # jittered
