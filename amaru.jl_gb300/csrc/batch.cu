@@ -23,12 +23,18 @@
 #include <functional>
 #include <numeric>
 
+#include <cooperative_groups.h>
+
 #include "amr_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
 constexpr int kPartThreads = 512;  // fixed: the reduction order of a part depends on it
 constexpr int kWarps = kPartThreads / 32;
+constexpr int kCluster = 8;                 // CTAs that solve one large part together
+constexpr int64_t kClusterMinNodes = 2048;  // parts with this many nodes or more are large (fixed: results depend on it)
 
 struct PartStat {
     int32_t iters, refreshes, status, pad;
@@ -111,8 +117,10 @@ __device__ __forceinline__ double absnan(double x) {  // |x|, NaN as +inf (as th
     return isnan(a) ? INFINITY : a;
 }
 
-// q = K32 p on rows [n0, n1), a half-warp per row, two rows per half-warp in flight.
-// Returns this thread's part of p.q.
+// q = K32 p on rows [n0, n1), a half-warp per row, kRows rows per half-warp in flight
+// (two measured faster than four: register pressure).  Returns this thread's part of
+// p.q (its rows in increasing order).
+constexpr int kRows = 2;
 template <int B>
 __device__ float part_spmv32(int64_t n0, int64_t n1, int64_t nb, const int64_t *__restrict__ rp,
                              const int32_t *__restrict__ cj, const float *__restrict__ A, const float *__restrict__ p,
@@ -122,55 +130,52 @@ __device__ float part_spmv32(int64_t n0, int64_t n1, int64_t nb, const int64_t *
     const int hw = threadIdx.x / G, nhw = kPartThreads / G;
     const unsigned hmask = 0xffffu << (16 * (hw & 1));
     float dot = 0.0f;
-    for (int64_t base = n0 + hw; base < n1; base += 2 * nhw) {
-        const int64_t r1 = base + nhw;
-        const bool two = r1 < n1;
-        float acc0[B], acc1[B];
+    for (int64_t base = n0 + hw; base < n1; base += kRows * nhw) {
+        float acc[kRows][B];
+        int64_t a0[kRows], e0[kRows];
+        int64_t len = 0;
 #pragma unroll
-        for (int c = 0; c < B; c++) acc0[c] = acc1[c] = 0.0f;
-        const int64_t a0 = rp[base], e0 = rp[base + 1];
-        const int64_t a1 = two ? rp[r1] : 0, e1 = two ? rp[r1 + 1] : 0;
-        const int64_t len = max(e0 - a0, e1 - a1);
+        for (int r = 0; r < kRows; r++) {
+            const int64_t row = base + r * nhw;
+            a0[r] = row < n1 ? __ldg(rp + row) : 0;
+            e0[r] = row < n1 ? __ldg(rp + row + 1) : 0;
+            len = max(len, e0[r] - a0[r]);
+#pragma unroll
+            for (int c = 0; c < B; c++) acc[r][c] = 0.0f;
+        }
         for (int64_t k = lane; k < len; k += G) {
-            if (a0 + k < e0) {
-                const int64_t kk = a0 + k, j = cj[kk];
-                float xv[B];
 #pragma unroll
-                for (int d = 0; d < B; d++) xv[d] = p[j * B + d];
+            for (int r = 0; r < kRows; r++) {
+                if (a0[r] + k < e0[r]) {
+                    const int64_t kk = a0[r] + k, j = __ldg(cj + kk);
+                    float av[B * B], xv[B];
 #pragma unroll
-                for (int c = 0; c < B; c++)
+                    for (int t = 0; t < B * B; t++) av[t] = __ldcs(A + (int64_t)t * nb + kk);
 #pragma unroll
-                    for (int d = 0; d < B; d++) acc0[c] = fmaf(__ldcs(A + (int64_t)(c * B + d) * nb + kk), xv[d], acc0[c]);
-            }
-            if (a1 + k < e1) {
-                const int64_t kk = a1 + k, j = cj[kk];
-                float xv[B];
+                    for (int d = 0; d < B; d++) xv[d] = p[j * B + d];
 #pragma unroll
-                for (int d = 0; d < B; d++) xv[d] = p[j * B + d];
+                    for (int c = 0; c < B; c++)
 #pragma unroll
-                for (int c = 0; c < B; c++)
-#pragma unroll
-                    for (int d = 0; d < B; d++) acc1[c] = fmaf(__ldcs(A + (int64_t)(c * B + d) * nb + kk), xv[d], acc1[c]);
+                        for (int d = 0; d < B; d++) acc[r][c] = fmaf(av[c * B + d], xv[d], acc[r][c]);
+                }
             }
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1)
 #pragma unroll
-            for (int c = 0; c < B; c++) {
-                acc0[c] += __shfl_down_sync(hmask, acc0[c], o, G);
-                acc1[c] += __shfl_down_sync(hmask, acc1[c], o, G);
-            }
+            for (int r = 0; r < kRows; r++)
+#pragma unroll
+                for (int c = 0; c < B; c++) acc[r][c] += __shfl_down_sync(hmask, acc[r][c], o, G);
         if (lane == 0) {
 #pragma unroll
-            for (int c = 0; c < B; c++) {
-                q[base * B + c] = acc0[c];
-                dot = fmaf(p[base * B + c], acc0[c], dot);
-            }
-            if (two) {
+            for (int r = 0; r < kRows; r++) {
+                const int64_t row = base + r * nhw;
+                if (row < n1) {
 #pragma unroll
-                for (int c = 0; c < B; c++) {
-                    q[r1 * B + c] = acc1[c];
-                    dot = fmaf(p[r1 * B + c], acc1[c], dot);
+                    for (int c = 0; c < B; c++) {
+                        q[row * B + c] = acc[r][c];
+                        dot = fmaf(p[row * B + c], acc[r][c], dot);
+                    }
                 }
             }
         }
@@ -229,9 +234,9 @@ __device__ void part_residual64(int64_t n0, int64_t n1, int64_t nb, const int64_
 }
 
 struct PcgArgs {
-    int64_t nparts;
+    int64_t nlarge, nsmall;   // parts solved by a CTA cluster / by one CTA
     const int64_t *part_ptr;  // node ranges
-    const int64_t *order;     // parts, most nodes first
+    const int64_t *order;     // parts, most nodes first: the nlarge large ones, then the small ones
     const uint8_t *active;    // null: every part
     int64_t nb;
     const int64_t *rp;
@@ -245,124 +250,208 @@ struct PcgArgs {
     double *reac;
     float *x32, *r32, *z32, *p32, *q32;
     PartStat *stat;
-    unsigned long long *counter;
-    StepInfo *step;  // null: no timing
+    unsigned long long *counter;  // [0]: next large part (per cluster), [1]: next small part (per CTA)
+    StepInfo *step;               // null: no timing
     double tol2;
     int max_iters, force_every;
 };
 
-// One CTA solves one part at a time: PCG with reliable updates, as the whole-model
-// mixed solver (restart-free; refresh when the recursive residual has dropped 100x
-// since the last refresh or looks converged; convergence judged on the FP64 residual).
+struct PartSmem {
+    float sh[2 * kWarps];
+    double shd[kWarps + 1];
+    double slot[2][4];  // this CTA's partials for the cluster sums, two sets used alternately
+    long long part;
+};
+
+// Sums over the CTAs of the part: per CTA as cta_sum, then, in a cluster, the CTAs'
+// totals read from each CTA's shared memory and added in rank order (a fixed shuffle
+// tree).  Every thread of every CTA receives the same totals.
+template <int NV, bool CL>
+__device__ void part_sum(const float (&v)[NV], double (&out)[NV], PartSmem &S, int &phase) {
+    double cta[NV];
+    cta_sum<NV>(v, cta, S.sh, S.shd);
+    if (!CL) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) out[i] = cta[i];
+        return;
+    }
+    cg::cluster_group cl = cg::this_cluster();
+    double *slot = S.slot[phase & 1];
+    phase++;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < NV; i++) slot[i] = cta[i];
+    cl.sync();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        const double *rs = lane < kCluster ? cl.map_shared_rank(slot, lane) : nullptr;
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            double t = rs ? rs[i] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (lane == 0) S.shd[i] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; i++) out[i] = S.shd[i];
+    __syncthreads();
+}
+
+template <bool CL>
+__device__ double part_max(double v, PartSmem &S, int &phase) {
+    double m = cta_max(v, S.shd);
+    if (!CL) return m;
+    cg::cluster_group cl = cg::this_cluster();
+    double *slot = S.slot[phase & 1];
+    phase++;
+    if (threadIdx.x == 0) slot[0] = m;
+    cl.sync();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (unsigned r = 0; r < kCluster; r++) t = fmax(t, cl.map_shared_rank(slot, r)[0]);
+        S.shd[0] = t;
+    }
+    __syncthreads();
+    m = S.shd[0];
+    __syncthreads();
+    return m;
+}
+
+// One part's solve: PCG with reliable updates, as the whole-model mixed solver
+// (restart-free; refresh when the recursive residual has dropped 100x since the last
+// refresh or looks converged; convergence judged on the FP64 residual).  In a cluster
+// (CL) CTA `rank` owns a contiguous slice of the part's rows; p and the FP64 solution,
+// the only vectors read across slices, are published by cluster barriers.
+template <int B, bool CL>
+__device__ void solve_part(const PcgArgs &a, long long part, int rank, PartSmem &S, int &phase) {
+    constexpr int nranks = CL ? kCluster : 1;
+    const int64_t P0 = a.part_ptr[part], P1 = a.part_ptr[part + 1], len = P1 - P0;
+    const int64_t n0 = P0 + len * rank / nranks, n1 = P0 + len * (rank + 1) / nranks;
+    const int64_t i0 = n0 * B, i1 = n1 * B;
+    auto publish = [&]() {
+        if (CL) cg::this_cluster().sync();
+        else __syncthreads();
+    };
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) {
+        a.x32[i] = 0.0f;
+        a.p32[i] = 0.0f;
+    }
+    float rz = 0.0f, rr = 0.0f;
+    part_residual64<B>(n0, n1, a.nb, a.rp, a.cj, a.K64, a.fm, a.b, a.x, a.reac, a.r32, a.z32, a.Minv, rz, rr);
+    double t2[2];
+    part_sum<2, CL>({rz, rr}, t2, S, phase);
+    double gam = t2[0], rr_true = t2[1];
+    const double bnorm2 = rr_true;
+    const double stop_rr = 0.0625 * a.tol2 * bnorm2;
+    int iters = 0, refreshes = 0, status = 0, since = 0;
+    bool first = true, done = !(bnorm2 > 0.0) || rr_true <= a.tol2 * bnorm2;
+    double beta = 0.0;
+    if (isnan(rr_true)) { status = AMR_ENOCONV; done = true; }
+    while (!done) {
+        if (iters >= a.max_iters) { status = AMR_ENOCONV; break; }
+        const float bf = first ? 0.0f : (float)beta;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) a.p32[i] = fmaf(bf, a.p32[i], a.z32[i]);
+        publish();
+        const float pq = part_spmv32<B>(n0, n1, a.nb, a.rp, a.cj, a.K32, a.p32, a.q32);
+        double t1[1];
+        part_sum<1, CL>({pq}, t1, S, phase);
+        if (!(t1[0] > 0.0)) { status = AMR_ENOCONV; break; }
+        const float af = (float)(gam / t1[0]);
+        first = false;
+        float rzl = 0.0f, rrl = 0.0f;
+        for (int64_t n = n0 + threadIdx.x; n < n1; n += kPartThreads) {
+            float rv[B];
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                const int64_t i = n * B + c;
+                a.x32[i] = fmaf(af, a.p32[i], a.x32[i]);
+                rv[c] = fmaf(-af, a.q32[i], a.r32[i]);
+                a.r32[i] = rv[c];
+            }
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                float s = 0.0f;
+#pragma unroll
+                for (int d = 0; d < B; d++) s = fmaf(a.Minv[n * B * B + c * B + d], rv[d], s);
+                a.z32[n * B + c] = s;
+                rzl = fmaf(rv[c], s, rzl);
+                rrl = fmaf(rv[c], rv[c], rrl);
+            }
+        }
+        part_sum<2, CL>({rzl, rrl}, t2, S, phase);
+        beta = t2[0] / gam;
+        gam = t2[0];
+        iters++;
+        since++;
+        if (!(t2[1] > stop_rr) || t2[1] <= 1e-2 * rr_true || since >= a.force_every) {
+            for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) {
+                if (a.fm[i]) a.x[i] += (double)a.x32[i];
+                a.x32[i] = 0.0f;
+            }
+            publish();
+            rz = 0.0f;
+            rr = 0.0f;
+            part_residual64<B>(n0, n1, a.nb, a.rp, a.cj, a.K64, a.fm, a.b, a.x, a.reac, a.r32, a.z32, a.Minv, rz,
+                               rr);
+            part_sum<2, CL>({rz, rr}, t2, S, phase);
+            gam = t2[0];
+            rr_true = t2[1];
+            refreshes++;
+            since = 0;
+            if (isnan(rr_true)) { status = AMR_ENOCONV; break; }
+            if (rr_true <= a.tol2 * bnorm2) done = true;
+        }
+    }
+    double um = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads)
+        if (a.fm[i]) um = fmax(um, absnan(a.x[i]));
+    um = part_max<CL>(um, S, phase);
+    if (rank == 0 && threadIdx.x == 0) {
+        a.stat[part].iters = iters;
+        a.stat[part].refreshes = refreshes;
+        a.stat[part].status = status;
+        a.stat[part].rel_residual = bnorm2 > 0.0 ? sqrt(rr_true / bnorm2) : 0.0;
+        a.stat[part].umax = um;
+    }
+}
+
+// Persistent batched solve.  Clusters of kCluster CTAs first take the large parts
+// (at least kClusterMinNodes nodes) from counter[0], one part per cluster; then every
+// CTA takes small parts from counter[1] alone.  No CTA waits on a CTA outside its
+// cluster, and a cluster's CTAs are resident together by construction.
 template <int B>
-__global__ void __launch_bounds__(kPartThreads, 2) k_part_pcg(PcgArgs a) {
-    __shared__ float sh[2 * kWarps];
-    __shared__ double shd[kWarps + 1];
-    __shared__ long long s_part;
+__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kPartThreads, 2) k_part_pcg(PcgArgs a) {
+    __shared__ PartSmem S;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    int phase = 0;
     if (a.step && threadIdx.x == 0) atomicMin(&a.step->t0, global_ns());
     for (;;) {
-        if (threadIdx.x == 0) {
-            const unsigned long long t = atomicAdd(a.counter, 1ULL);
-            s_part = (t < (unsigned long long)a.nparts) ? (long long)a.order[t] : -1;
+        if (rank == 0 && threadIdx.x == 0) {
+            const unsigned long long t = atomicAdd(&a.counter[0], 1ULL);
+            S.part = (t < (unsigned long long)a.nlarge) ? (long long)a.order[t] : -1;
         }
-        __syncthreads();
-        const long long part = s_part;
-        __syncthreads();
-        if (part < 0) {
-            if (a.step && threadIdx.x == 0) atomicMax(&a.step->t1, global_ns());
-            return;
-        }
+        cl.sync();
+        const long long part = *cl.map_shared_rank(&S.part, 0);
+        cl.sync();
+        if (part < 0) break;
         if (a.active && !a.active[part]) continue;
-        const int64_t n0 = a.part_ptr[part], n1 = a.part_ptr[part + 1];
-        const int64_t i0 = n0 * B, i1 = n1 * B;
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) {
-            a.x32[i] = 0.0f;
-            a.p32[i] = 0.0f;
-        }
-        __syncthreads();
-        float rz = 0.0f, rr = 0.0f;
-        part_residual64<B>(n0, n1, a.nb, a.rp, a.cj, a.K64, a.fm, a.b, a.x, a.reac, a.r32, a.z32, a.Minv, rz, rr);
-        __syncthreads();
-        double t2[2];
-        cta_sum<2>({rz, rr}, t2, sh, shd);
-        double gam = t2[0], rr_true = t2[1];
-        const double bnorm2 = rr_true;
-        const double stop_rr = 0.0625 * a.tol2 * bnorm2;
-        int iters = 0, refreshes = 0, status = 0, since = 0;
-        bool first = true, done = !(bnorm2 > 0.0) || rr_true <= a.tol2 * bnorm2;
-        double beta = 0.0;
-        if (isnan(rr_true)) { status = AMR_ENOCONV; done = true; }
-        while (!done) {
-            if (iters >= a.max_iters) { status = AMR_ENOCONV; break; }
-            const float bf = first ? 0.0f : (float)beta;
-            for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) a.p32[i] = fmaf(bf, a.p32[i], a.z32[i]);
-            __syncthreads();
-            const float pq = part_spmv32<B>(n0, n1, a.nb, a.rp, a.cj, a.K32, a.p32, a.q32);
-            __syncthreads();
-            double t1[1];
-            cta_sum<1>({pq}, t1, sh, shd);
-            if (!(t1[0] > 0.0)) { status = AMR_ENOCONV; break; }
-            const float af = (float)(gam / t1[0]);
-            first = false;
-            float rzl = 0.0f, rrl = 0.0f;
-            for (int64_t n = n0 + threadIdx.x; n < n1; n += kPartThreads) {
-                float rv[B];
-#pragma unroll
-                for (int c = 0; c < B; c++) {
-                    const int64_t i = n * B + c;
-                    a.x32[i] = fmaf(af, a.p32[i], a.x32[i]);
-                    rv[c] = fmaf(-af, a.q32[i], a.r32[i]);
-                    a.r32[i] = rv[c];
-                }
-#pragma unroll
-                for (int c = 0; c < B; c++) {
-                    float s = 0.0f;
-#pragma unroll
-                    for (int d = 0; d < B; d++) s = fmaf(a.Minv[n * B * B + c * B + d], rv[d], s);
-                    a.z32[n * B + c] = s;
-                    rzl = fmaf(rv[c], s, rzl);
-                    rrl = fmaf(rv[c], rv[c], rrl);
-                }
-            }
-            __syncthreads();
-            cta_sum<2>({rzl, rrl}, t2, sh, shd);
-            beta = t2[0] / gam;
-            gam = t2[0];
-            iters++;
-            since++;
-            if (!(t2[1] > stop_rr) || t2[1] <= 1e-2 * rr_true || since >= a.force_every) {
-                for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads) {
-                    if (a.fm[i]) a.x[i] += (double)a.x32[i];
-                    a.x32[i] = 0.0f;
-                }
-                __syncthreads();
-                rz = 0.0f;
-                rr = 0.0f;
-                part_residual64<B>(n0, n1, a.nb, a.rp, a.cj, a.K64, a.fm, a.b, a.x, a.reac, a.r32, a.z32, a.Minv, rz,
-                                   rr);
-                __syncthreads();
-                cta_sum<2>({rz, rr}, t2, sh, shd);
-                gam = t2[0];
-                rr_true = t2[1];
-                refreshes++;
-                since = 0;
-                if (isnan(rr_true)) { status = AMR_ENOCONV; break; }
-                if (rr_true <= a.tol2 * bnorm2) done = true;
-            }
-        }
-        double um = 0.0;
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += kPartThreads)
-            if (a.fm[i]) um = fmax(um, absnan(a.x[i]));
-        um = cta_max(um, shd);
-        if (threadIdx.x == 0) {
-            a.stat[part].iters = iters;
-            a.stat[part].refreshes = refreshes;
-            a.stat[part].status = status;
-            a.stat[part].rel_residual = bnorm2 > 0.0 ? sqrt(rr_true / bnorm2) : 0.0;
-            a.stat[part].umax = um;
-        }
-        __syncthreads();
+        solve_part<B, true>(a, part, rank, S, phase);
     }
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long t = atomicAdd(&a.counter[1], 1ULL);
+            S.part = (t < (unsigned long long)a.nsmall) ? (long long)a.order[a.nlarge + t] : -1;
+        }
+        __syncthreads();
+        const long long part = S.part;
+        __syncthreads();
+        if (part < 0) break;
+        if (a.active && !a.active[part]) continue;
+        solve_part<B, false>(a, part, 0, S, phase);
+    }
+    if (a.step && threadIdx.x == 0) atomicMax(&a.step->t1, global_ns());
 }
 
 // ---------------------------------------------------------------------------
@@ -581,7 +670,7 @@ __global__ void k_ip_commit(int64_t nip, const int32_t *ip_part, const PartCtl *
 }  // namespace
 
 struct AmrBatch {
-    int64_t nparts = 0;
+    int64_t nparts = 0, nlarge = 0;
     std::vector<int64_t> h_ptr;
     int64_t *part_ptr = nullptr, *order = nullptr;
     int32_t *node_part = nullptr, *elem_part = nullptr, *ip_part = nullptr;
@@ -636,11 +725,14 @@ void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *ptr) {
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int64_t x, int64_t y) { return ptr[x + 1] - ptr[x] > ptr[y + 1] - ptr[y]; });
+    int64_t nlarge = 0;
+    while (nlarge < nparts && ptr[order[nlarge] + 1] - ptr[order[nlarge]] >= kClusterMinNodes) nlarge++;
     amr_batch_free(m);
     AmrBatch *b = new AmrBatch();
     m->batch = b;
     try {
         b->nparts = nparts;
+        b->nlarge = nlarge;
         b->h_ptr.assign(ptr, ptr + nparts + 1);
         const int64_t n = m->nnodes * m->B;
         amr_alloc(&b->part_ptr, nparts + 1);
@@ -653,7 +745,7 @@ void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *ptr) {
         amr_alloc(&b->active, nparts);
         amr_alloc(&b->perr, nparts);
         amr_alloc(&b->step, 1);
-        amr_alloc(&b->counter, 1);
+        amr_alloc(&b->counter, 2);
         amr_alloc(&b->x32, n); amr_alloc(&b->r32, n); amr_alloc(&b->z32, n); amr_alloc(&b->p32, n);
         amr_alloc(&b->q32, n);
         AMR_CUDA(cudaMallocHost((void **)&b->h_step, sizeof(StepInfo)));
@@ -683,7 +775,8 @@ PcgArgs pcg_args(amr_model *m, double *x, const double *b_, double *reac, const 
                  const uint8_t *active) {
     AmrBatch *b = m->batch;
     PcgArgs a;
-    a.nparts = b->nparts; a.part_ptr = b->part_ptr; a.order = b->order; a.active = active;
+    a.nlarge = b->nlarge; a.nsmall = b->nparts - b->nlarge; a.part_ptr = b->part_ptr; a.order = b->order;
+    a.active = active;
     a.nb = m->nblocks; a.rp = m->brow_ptr; a.cj = m->bcol; a.K32 = m->K32; a.K64 = m->K64; a.Minv = m->Minv32;
     a.fm = m->free_mask; a.b = b_; a.x = x; a.reac = reac;
     a.x32 = b->x32; a.r32 = b->r32; a.z32 = b->z32; a.p32 = b->p32; a.q32 = b->q32;
@@ -694,8 +787,12 @@ PcgArgs pcg_args(amr_model *m, double *x, const double *b_, double *reac, const 
 
 void launch_pcg(amr_model *m, const PcgArgs &a, int ctas_per_sm) {
     AmrBatch *b = m->batch;
-    AMR_CUDA(cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), m->stream));
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(b->nparts, (int64_t)device_sms() * ctas_per_sm));
+    AMR_CUDA(cudaMemsetAsync(b->counter, 0, 2 * sizeof(unsigned long long), m->stream));
+    // whole clusters: as many CTAs as the parts can use (a cluster per large part, a CTA per small
+    // one), at most ctas_per_sm per SM
+    const int64_t need = b->nlarge * kCluster + (b->nparts - b->nlarge);
+    const int64_t ctas = std::min<int64_t>(std::max<int64_t>(need, kCluster), (int64_t)device_sms() * ctas_per_sm);
+    const unsigned grid = (unsigned)(std::max<int64_t>(1, ctas / kCluster) * kCluster);
     if (m->B == 3) k_part_pcg<3><<<grid, kPartThreads, 0, m->stream>>>(a);
     else k_part_pcg<2><<<grid, kPartThreads, 0, m->stream>>>(a);
     AMR_COUNT(1);
