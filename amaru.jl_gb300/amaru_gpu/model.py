@@ -408,7 +408,16 @@ class BatchAnalysis:
             setup += _shift_setup(su, J.node_offsets[i], J.elem_offsets[i])
         J.eq_id, J.ndofs, J.nu, J.dof_node, J.dof_comp = number_dofs(J.active_nodes, np.concatenate(pres), J.nnodes)
         J.dev.set_dofs(J.eq_id, J.ndofs, J.nu)
-        return J.get_bc_vals(setup)
+        U, F, loads = J.bc_vals(setup)
+        # the parts' nodes are disjoint: loads that differ only in their items are one load (same sums)
+        merged = {}
+        for kind, dr, edge, fshape, items, cf in loads:
+            key = (kind, dr, edge, fshape, tuple(np.asarray(cf, dtype=np.float64).tolist()))
+            merged.setdefault(key, []).append(np.asarray(items, dtype=np.int64))
+        loads = [(k[0], k[1], k[2], k[3], np.concatenate(v), list(k[4])) for k, v in merged.items()]
+        if loads:
+            F = J.dev.assemble_loads(loads, F, 0.0)
+        return U, F
 
     def split(self, V):
         """A joined eq_id-ordered vector as one node-major (nnodes, ndim) array per part."""

@@ -149,6 +149,7 @@ void amr_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);  
 // element.cu
 void amr_stiffness(amr_model *m);                       // Kel + gather into K64/K32/Minv
 void amr_stiffness_elements(amr_model *m);              // Kel only (element kernels)
+void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2);  // K64 = a1 Ks + a2 K64, K32, Minv
 void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm);  // node-major device vectors
 void amr_apply_dofs(amr_model *m);                      // masks after amr_set_dofs
 void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double *F_nm);  // F_nm += (device)

@@ -24,6 +24,7 @@ enum VecOp {
     V_SET_AXPBY = 0,   // o = a x + b y
     V_MASK_FREE = 1,   // o = x at free slots, 0 at prescribed
     V_MASK_PRESC = 2,  // o = x at prescribed slots, 0 at free
+    V_PRESC_AX = 3,    // o = a x at prescribed slots, 0 at free
 };
 
 __global__ void k_vec(int64_t n, int op, double a, const double *x, double b, const double *y, double *o,
@@ -34,6 +35,7 @@ __global__ void k_vec(int64_t n, int op, double a, const double *x, double b, co
     case V_SET_AXPBY: o[i] = a * x[i] + (y ? b * y[i] : 0.0); break;
     case V_MASK_FREE: o[i] = fm[i] ? x[i] : 0.0; break;
     case V_MASK_PRESC: o[i] = fm[i] ? 0.0 : x[i]; break;
+    case V_PRESC_AX: o[i] = fm[i] ? 0.0 : a * x[i]; break;
     }
 }
 
@@ -661,14 +663,33 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
     if (m->batch) return amr_batch_stage(m, Uex, Fex, p, U, F, stats);  // each part its own stage
     int64_t n = m->nnodes * m->B;
     cudaStream_t s = m->stream;
-    if (p.scheme != AMR_SCHEME_FE) throw AmrError(AMR_EUNSUPPORTED, "only the FE predictor scheme is on the GPU path");
+    // predictor-corrector schemes (mech-solver.jl:280-288)
+    double p1 = 1.0, q11 = 1.0, a1 = 0.0, a2 = 0.0;
+    switch (p.scheme) {
+    case AMR_SCHEME_FE: break;
+    case AMR_SCHEME_ME: a1 = 0.5; a2 = 0.5; break;
+    case AMR_SCHEME_BE: a1 = 0.0; a2 = 1.0; break;
+    case AMR_SCHEME_RALSTON: p1 = 2.0 / 3.0; q11 = 2.0 / 3.0; a1 = 0.25; a2 = 0.75; break;
+    default: throw AmrError(AMR_EINVAL, "unknown scheme");
+    }
+    const bool corrector = p.scheme != AMR_SCHEME_FE;
     if (p.maxits < 1 || p.nincs < 1) throw AmrError(AMR_EINVAL, "bad stage parameters");
     std::vector<double *> v(10, nullptr);
     for (auto &x : v) amr_alloc(&x, n);
     double *R = v[0], *dUa = v[1], *dUi = v[2], *Rc = v[3], *dFin = v[4], *dFex = v[5], *dUitr = v[6], *Rtr = v[7],
            *reac = v[8], *dUt = v[9];
+    double *Ks = nullptr;  // the predictor's tangent, kept for the weighted corrector tangent
+    if (corrector) {
+        try {
+            amr_alloc(&Ks, (size_t)m->nblocks * m->BB);
+        } catch (...) {
+            for (auto &x : v) amr_free(x);
+            throw;
+        }
+    }
     auto release = [&]() {
         for (auto &x : v) amr_free(x);
+        amr_free(Ks);
     };
     int status = AMR_OK;
     amr_stage_stats st{};
@@ -689,7 +710,6 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
         double dTcheck = saveouts ? 1.0 / p.nouts : 1.0, Tcheck = dTcheck;
         double T = 0.0, dT = 1.0 / nincs, dTbk = 0.0;
         if (autoinc) dT = std::min({dT, p.dTmax, dTcheck, p.dT0});
-        const double p1 = 1.0, q11 = 1.0;
         // every stage mounts K at least once (the reference mounts it at every iteration;
         // a state-independent K is reused across the iterations of the stage only)
         m->K_valid = false;
@@ -715,7 +735,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 double lastres = res;
                 if (m->any_plastic || !m->K_valid) assemble(m);
                 // predictor solve: x = p1 dUi at prescribed slots, b = q11 R
-                vec(m, V_MASK_PRESC, p1, dUi, 0.0, nullptr, dUitr);
+                vec(m, V_PRESC_AX, p1, dUi, 0.0, nullptr, dUitr);
                 vec(m, V_SET_AXPBY, q11, R, 0.0, nullptr, Rtr);
                 AmrSolveResult sr = amr_solve_device(m, dUitr, Rtr, reac, p.linear);
                 st.krylov_iterations += sr.iterations;
@@ -728,7 +748,29 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 amr_update_elements(m, dUt, dFin);
                 int rc = amr_check_status(m);
                 if (rc) { syserror = true; sysmsg = rc == AMR_ERETMAP ? "return mapping failed" : "NaN values in internal forces vector"; break; }
-                AMR_CUDA(cudaMemcpyAsync(dUi, dUitr, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+                if (!corrector) {
+                    AMR_CUDA(cudaMemcpyAsync(dUi, dUitr, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+                } else {
+                    // corrector (mech-solver.jl:341-348): K = a1 K + a2 K2 with K2 the tangent of the
+                    // predictor's trial states, solve for dUi, update the states again from the committed ones
+                    AMR_CUDA(cudaMemcpyAsync(Ks, m->K64, (size_t)m->nblocks * m->BB * sizeof(double),
+                                             cudaMemcpyDeviceToDevice, s));
+                    if (m->any_plastic) assemble(m);  // a state-independent K2 equals K
+                    amr_combine_K(m, a1, Ks, a2);
+                    m->K_valid = false;  // the next iteration mounts the plain tangent again
+                    vec(m, V_MASK_PRESC, 1.0, dUi, 0.0, nullptr, dUi);
+                    vec(m, V_SET_AXPBY, 1.0, R, 0.0, nullptr, Rtr);
+                    AmrSolveResult sc = amr_solve_device(m, dUi, Rtr, reac, p.linear);
+                    st.krylov_iterations += sc.iterations;
+                    st.solve_seconds += sc.seconds;
+                    if (sc.status) { syserror = true; sysmsg = "solve_system!: Krylov solver did not converge"; break; }
+                    double um = amr_norm_inf(m, dUi, m->free_mask);
+                    if (!(um <= 1e8)) { syserror = true; sysmsg = "solve_system!: Possible syngular matrix"; break; }
+                    vec(m, V_SET_AXPBY, 1.0, dUa, 1.0, dUi, dUt);
+                    amr_update_elements(m, dUt, dFin);
+                    int rc2 = amr_check_status(m);
+                    if (rc2) { syserror = true; sysmsg = rc2 == AMR_ERETMAP ? "return mapping failed" : "NaN values in internal forces vector"; break; }
+                }
                 vec(m, V_SET_AXPBY, 1.0, dUa, 1.0, dUi, dUa);
                 vec(m, V_SET_AXPBY, 1.0, dFex, -1.0, dFin, R);
                 vec(m, V_MASK_FREE, 1.0, R, 0.0, nullptr, R);

@@ -622,6 +622,40 @@ __device__ void invert_block(const double *A, double *X) {
     }
 }
 
+// Block k (row n, column j) of K with values v: the Dirichlet-masked FP32 copy (unit diagonal at
+// prescribed DOFs) and, on the diagonal, the block-Jacobi inverses.
+template <int B>
+__device__ __forceinline__ void finish_block(int64_t n, int64_t k, int32_t j, int64_t nblocks, const double *v,
+                                             const uint8_t *fr, const uint8_t *free_mask, float *K32, float *Minv32,
+                                             double *Minv64) {
+    constexpr int BB = B * B;
+    if (!K32 && !Minv32) return;
+    uint8_t fc[B];
+#pragma unroll
+    for (int d = 0; d < B; d++) fc[d] = free_mask ? free_mask[(int64_t)j * B + d] : 1;
+    double mk[BB];
+#pragma unroll
+    for (int c = 0; c < B; c++)
+#pragma unroll
+        for (int d = 0; d < B; d++) {
+            double x = (fr[c] && fc[d]) ? v[c * B + d] : 0.0;
+            if (j == n && c == d && !fr[c]) x = 1.0;
+            mk[c * B + d] = x;
+        }
+    if (K32)
+#pragma unroll
+        for (int q = 0; q < BB; q++) K32[(int64_t)q * nblocks + k] = (float)mk[q];
+    if (j == n) {
+        double X[BB];
+        invert_block<B>(mk, X);
+#pragma unroll
+        for (int q = 0; q < BB; q++) {
+            if (Minv32) Minv32[n * BB + q] = (float)X[q];
+            if (Minv64) Minv64[n * BB + q] = X[q];
+        }
+    }
+}
+
 template <int B>
 __global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *brow_ptr, const int32_t *bcol,
                               const int64_t *contrib_ptr, const int64_t *contrib, const double *Kel,
@@ -656,32 +690,36 @@ __global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *br
         }
         if (nan) set_status(status, AMR_ENAN, -1);
         if (keep) keep[k] = (uint16_t)kb;
-        if (K32 || Minv32) {
-            uint8_t fc[B];
+        finish_block<B>(n, k, j, nblocks, v, fr, free_mask, K32, Minv32, Minv64);
+    }
+}
+
+// K = a1 Ks + a2 K (the weighted tangent of the ME / BE / Ralston schemes, mech-solver.jl:280-288,
+// K = a1*K + a2*K2 at :342-343): products and sum rounded separately, then the masked FP32 copy and
+// block-Jacobi inverses of the result.
+template <int B>
+__global__ void combine_kernel(int64_t nnodes, int64_t nblocks, const int64_t *brow_ptr, const int32_t *bcol, double a1,
+                               const double *Ks, double a2, const uint8_t *free_mask, double *K64, float *K32,
+                               float *Minv32, double *Minv64, int32_t *status) {
+    constexpr int BB = B * B;
+    int lane = threadIdx.x & 31;
+    int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= nnodes) return;
+    uint8_t fr[B];
 #pragma unroll
-            for (int d = 0; d < B; d++) fc[d] = free_mask ? free_mask[(int64_t)j * B + d] : 1;
-            double mk[BB];
+    for (int c = 0; c < B; c++) fr[c] = free_mask ? free_mask[n * B + c] : 1;
+    for (int64_t k = brow_ptr[n] + lane; k < brow_ptr[n + 1]; k += 32) {
+        double v[BB];
+        bool nan = false;
 #pragma unroll
-            for (int c = 0; c < B; c++)
-#pragma unroll
-                for (int d = 0; d < B; d++) {
-                    double x = (fr[c] && fc[d]) ? v[c * B + d] : 0.0;
-                    if (j == n && c == d && !fr[c]) x = 1.0;
-                    mk[c * B + d] = x;
-                }
-            if (K32)
-#pragma unroll
-                for (int q = 0; q < BB; q++) K32[(int64_t)q * nblocks + k] = (float)mk[q];
-            if (j == n) {
-                double X[BB];
-                invert_block<B>(mk, X);
-#pragma unroll
-                for (int q = 0; q < BB; q++) {
-                    if (Minv32) Minv32[n * BB + q] = (float)X[q];
-                    if (Minv64) Minv64[n * BB + q] = X[q];
-                }
-            }
+        for (int q = 0; q < BB; q++) {
+            const int64_t i = (int64_t)q * nblocks + k;
+            v[q] = __dadd_rn(__dmul_rn(a1, Ks[i]), __dmul_rn(a2, K64[i]));
+            K64[i] = v[q];
+            nan |= isnan(v[q]);
         }
+        if (nan) set_status(status, AMR_ENAN, -1);
+        finish_block<B>(n, k, bcol[k], nblocks, v, fr, free_mask, K32, Minv32, Minv64);
     }
 }
 
@@ -973,6 +1011,20 @@ void amr_stiffness(amr_model *m) {
                                                       m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
                                                       m->Minv32, m->Minv64, m->d_status);
     }
+    AMR_COUNT(1);
+    AMR_CUDA(cudaGetLastError());
+}
+
+void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2) {
+    unsigned grid = nblk(m->nnodes * 32, 256);
+    if (m->B == 3)
+        combine_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, a1, Ks, a2,
+                                                       m->free_mask, m->K64, m->K32, m->Minv32, m->Minv64,
+                                                       m->d_status);
+    else
+        combine_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, a1, Ks, a2,
+                                                       m->free_mask, m->K64, m->K32, m->Minv32, m->Minv64,
+                                                       m->d_status);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }

@@ -327,3 +327,22 @@ def test_config1_cantilever(n):
     Ko = O.mount_K(om, ao.ndofs)
     Kg = gm.mount_K()
     assert (Kg.indptr == Ko.indptr).all() and (Kg.indices == Ko.indices).all()
+
+
+@pytest.mark.parametrize("scheme", ["ME", "BE", "Ralston"])
+def test_predictor_corrector_schemes(scheme):
+    """mech_stage_solver! with the ME / BE / Ralston schemes (src/mech/mech-solver.jl:280-288, corrector
+    with K = a1*K + a2*K2 at :338-349) on an elastoplastic HEX8 cantilever with autoinc: the same Newton
+    iterations as the oracle and U, F within 1e-4 of max."""
+    bcs = [("x==0", "surface", dict(ux=0, uy=0, uz=0)), ("x==1", "surface", dict(tz=-30.0))]
+    om, gm, ob, gb = _models(A.HEX8, (6, 2, 2), [[0, 0, 0], [1.0, 0.2, 0.2]],
+                             ("VonMises", dict(E=200e3, nu=0.3, fy=240.0, H=2e3)), bcs)
+    ao, ag = O.MechAnalysis(om), A.MechAnalysis(gm)
+    ao.addstage(ob, nincs=6)
+    ag.addstage(gb, nincs=6)
+    assert ao.solve(scheme=scheme, autoinc=True)[0]
+    assert ag.solve(scheme=scheme, autoinc=True)[0]
+    assert gm.state()[:, 12].max() > 0
+    assert ag.stats[0].iterations == len(ao.log)  # the same Newton path, iteration for iteration
+    assert np.abs(gm.U - om.U).max() <= 1e-4 * np.abs(om.U).max()
+    assert np.abs(gm.F - om.F).max() <= 1e-4 * np.abs(om.F).max()
