@@ -63,6 +63,9 @@ struct amr_model {
     int64_t ninc = 0;
     // node-block sparsity pattern
     int64_t nblocks = 0;
+    // component stride of the SoA K64 / K32 arrays and length of bcol: nblocks rounded up to a
+    // multiple of 4, plus 4, so every component starts on 16 bytes and whole 16-byte groups stay inside
+    int64_t bstride = 0;
     int64_t *brow_ptr = nullptr;    // nnodes+1
     int32_t *bcol = nullptr;        // nblocks
     int64_t *contrib_ptr = nullptr; // nblocks+1

@@ -784,7 +784,7 @@ PcgArgs pcg_args(amr_model *m, double *x, const double *b_, double *reac, const 
     PcgArgs a;
     a.nlarge = b->nlarge; a.nsmall = b->nparts - b->nlarge; a.part_ptr = b->part_ptr; a.order = b->order;
     a.active = active;
-    a.nb = m->nblocks; a.rp = m->brow_ptr; a.cj = m->bcol; a.K32 = m->K32; a.K64 = m->K64; a.Minv = m->Minv32;
+    a.nb = m->bstride; a.rp = m->brow_ptr; a.cj = m->bcol; a.K32 = m->K32; a.K64 = m->K64; a.Minv = m->Minv32;
     a.fm = m->free_mask; a.b = b_; a.x = x; a.reac = reac;
     a.x32 = b->x32; a.r32 = b->r32; a.z32 = b->z32; a.p32 = b->p32; a.q32 = b->q32;
     a.stat = b->stat; a.counter = b->counter; a.step = nullptr; a.tol2 = o.rtol * o.rtol; a.max_iters = o.max_iters;

@@ -246,13 +246,16 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
         amr_build_pattern(m);
         // values and states
         amr_alloc(&m->Kel, (size_t)m->kel_blocks * m->BB);
-        amr_alloc(&m->K64, (size_t)m->nblocks * m->BB);
-        amr_alloc(&m->K32, (size_t)m->nblocks * m->BB);
+        amr_alloc(&m->K64, (size_t)m->bstride * m->BB);
+        amr_alloc(&m->K32, (size_t)m->bstride * m->BB);
         amr_alloc(&m->keep, m->nblocks);
         amr_alloc(&m->Minv32, (size_t)m->nnodes * m->BB);
         amr_alloc(&m->Minv64, (size_t)m->nnodes * m->BB);
         amr_alloc(&m->st, (size_t)AMR_NST * m->nip_total);
         amr_alloc(&m->stbk, (size_t)AMR_NST * m->nip_total);
+        // nodes that no element uses have no diagonal block: their block-Jacobi inverse stays 0
+        AMR_CUDA(cudaMemsetAsync(m->Minv32, 0, (size_t)m->nnodes * m->BB * sizeof(float), s));
+        AMR_CUDA(cudaMemsetAsync(m->Minv64, 0, (size_t)m->nnodes * m->BB * sizeof(double), s));
         AMR_CUDA(cudaMemsetAsync(m->st, 0, (size_t)AMR_NST * m->nip_total * sizeof(double), s));
         AMR_CUDA(cudaMemsetAsync(m->stbk, 0, (size_t)AMR_NST * m->nip_total * sizeof(double), s));
         amr_alloc(&m->Fel, fel.back());
@@ -391,7 +394,7 @@ static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t 
     AMR_CUDA(cudaMemcpy(keep.data(), m->keep, m->nblocks * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     std::vector<double> K;
     if (nzval) {
-        K.resize((size_t)m->nblocks * BB);
+        K.resize((size_t)m->bstride * BB);
         AMR_CUDA(cudaMemcpy(K.data(), m->K64, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
     }
     const std::vector<int64_t> &eq = m->h_eq_id;
@@ -425,7 +428,7 @@ static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t 
                     if (col < 0 || !(keep[k] >> (c * B + d) & 1)) continue;
                     int64_t p = pos[col]++;
                     rowval[p] = r;
-                    if (nzval) nzval[p] = K[(size_t)(c * B + d) * m->nblocks + k];
+                    if (nzval) nzval[p] = K[(size_t)(c * B + d) * m->bstride + k];
                 }
             }
         }
@@ -681,7 +684,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
     double *Ks = nullptr;  // the predictor's tangent, kept for the weighted corrector tangent
     if (corrector) {
         try {
-            amr_alloc(&Ks, (size_t)m->nblocks * m->BB);
+            amr_alloc(&Ks, (size_t)m->bstride * m->BB);
         } catch (...) {
             for (auto &x : v) amr_free(x);
             throw;
@@ -753,7 +756,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 } else {
                     // corrector (mech-solver.jl:341-348): K = a1 K + a2 K2 with K2 the tangent of the
                     // predictor's trial states, solve for dUi, update the states again from the committed ones
-                    AMR_CUDA(cudaMemcpyAsync(Ks, m->K64, (size_t)m->nblocks * m->BB * sizeof(double),
+                    AMR_CUDA(cudaMemcpyAsync(Ks, m->K64, (size_t)m->bstride * m->BB * sizeof(double),
                                              cudaMemcpyDeviceToDevice, s));
                     if (m->any_plastic) assemble(m);  // a state-independent K2 equals K
                     amr_combine_K(m, a1, Ks, a2);

@@ -1003,11 +1003,11 @@ void amr_stiffness(amr_model *m) {
     amr_stiffness_elements(m);
     unsigned grid = nblk(m->nnodes * 32, 256);
     if (m->B == 3) {
-        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
+        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
                                                       m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
                                                       m->Minv32, m->Minv64, m->d_status);
     } else {
-        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->contrib_ptr,
+        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
                                                       m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
                                                       m->Minv32, m->Minv64, m->d_status);
     }
@@ -1018,11 +1018,11 @@ void amr_stiffness(amr_model *m) {
 void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2) {
     unsigned grid = nblk(m->nnodes * 32, 256);
     if (m->B == 3)
-        combine_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, a1, Ks, a2,
+        combine_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, a1, Ks, a2,
                                                        m->free_mask, m->K64, m->K32, m->Minv32, m->Minv64,
                                                        m->d_status);
     else
-        combine_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, a1, Ks, a2,
+        combine_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, a1, Ks, a2,
                                                        m->free_mask, m->K64, m->K32, m->Minv32, m->Minv64,
                                                        m->d_status);
     AMR_COUNT(1);

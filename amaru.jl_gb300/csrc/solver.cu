@@ -587,6 +587,13 @@ void amr_solver_free(amr_model *m) {
 }
 
 template <int B>
+static void launch_spmv32(amr_model *m, AmrSolveWork *w, const float *p, float *q) {
+    k_spmv32<B><<<(unsigned)w->grid_spmv, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K32,
+                                                                     p, q, w->ctl, w->partials);
+    AMR_COUNT(1);
+}
+
+template <int B>
 static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
     AmrSolveWork *w = work(m);
     cudaStream_t s = m->stream;
@@ -604,7 +611,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     // free slots of x start at zero (the reduced system's initial guess)
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     unsigned g = (unsigned)w->grid;
-    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac, w->r32,
+    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac, w->r32,
                                        w->z32, m->Minv32, w->ctl, w->partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
@@ -625,7 +632,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
             k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
             AMR_COUNT(1);
             AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
-            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
                                                reac, w->r32, w->z32, m->Minv32, w->ctl, w->partials, 0, tol2);
             AMR_COUNT(1);
             res.refinements++;
@@ -637,9 +644,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
         for (int it = 0; it < nit; it++) {
             k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
             AMR_COUNT(1);
-            k_spmv32<B><<<(unsigned)w->grid_spmv, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->p32[0], w->q32,
-                                               w->ctl, w->partials);
-            AMR_COUNT(1);
+            launch_spmv32<B>(m, w, w->p32[0], w->q32);
             k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[0], w->q32, w->x32, w->r32, w->z32, w->ctl,
                                                  w->partials, stop_rr, delta2);
             AMR_COUNT(1);
@@ -681,7 +686,7 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
         amr_alloc(&w->ccol, w->csr_nnz);
         amr_alloc(&w->csrc, w->csr_nnz);
         amr_alloc(&w->cval, w->csr_nnz);
-        k_csr_fill<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, m->nblocks, w->crp,
+        k_csr_fill<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, m->bstride, w->crp,
                                                  w->ccol, w->csrc);
         AMR_COUNT(1);
         amr_free(cnt);
@@ -699,7 +704,7 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
     // b_red = b - K12 u2: tmp = K64 x (x holds prescribed values, zero at free slots on entry)
     int64_t nt = m->nnodes * B;
     AMR_CUDA(cudaEventRecord(m->ev0, s));
-    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, x,
+    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, x,
                                                          w->tmp);
     AMR_COUNT(1);
     // cb = b - K12 u2 on the free eq rows (b and K64 x scattered to eq order)
@@ -745,7 +750,7 @@ static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, d
     // x (node-major) free slots <- cx ; reactions and the true residual from the BSR FP64 matrix
     k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, x, w->cx, 0);
     AMR_COUNT(1);
-    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, x,
+    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, x,
                                                          w->tmp);
     AMR_COUNT(1);
     double rr = amr_masked_residual(m, b, w->tmp, reac);
@@ -873,9 +878,7 @@ static double time_spmv32(amr_model *m, int reps) {
     AMR_CUDA(cudaMemcpyAsync(w->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        k_spmv32<B><<<(unsigned)w->grid_spmv, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K32, w->z32, w->s32,
-                                           w->ctl, w->partials);
-        AMR_COUNT(1);
+        launch_spmv32<B>(m, w, w->z32, w->s32);
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));
@@ -894,7 +897,7 @@ static double time_residual64(amr_model *m, int reps) {
     AMR_CUDA(cudaMemsetAsync(b, 0, w->n * sizeof(double), s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        k_refine<B><<<g, kThreads, 0, s>>>(m->nnodes, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, u,
+        k_refine<B><<<g, kThreads, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, u,
                                            nullptr, w->r32, w->z32, m->Minv32, w->ctl, w->partials, 1, 1e-16);
         AMR_COUNT(1);
     }
@@ -1016,7 +1019,7 @@ AmrSolveResult solve_mixed_noalloc(amr_model *m, const NoAllocView &w, int grid,
     AMR_CUDA(cudaMemcpyAsync(w.ctl, &hc, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     const unsigned g = (unsigned)grid;
-    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x, w.reac,
+    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x, w.reac,
                                        w.r32, w.z32, m->Minv32, w.ctl, w.partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
@@ -1035,7 +1038,7 @@ AmrSolveResult solve_mixed_noalloc(amr_model *m, const NoAllocView &w, int grid,
             k_fold<B><<<nblk(n, 256), 256, 0, s>>>(nn, m->free_mask, w.x32, w.x);
             AMR_COUNT(1);
             AMR_CUDA(cudaMemsetAsync(&w.ctl->stop, 0, sizeof(int32_t), s));
-            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x,
+            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x,
                                                w.reac, w.r32, w.z32, m->Minv32, w.ctl, w.partials, 0, tol2);
             AMR_COUNT(1);
             res.refinements++;
@@ -1046,7 +1049,7 @@ AmrSolveResult solve_mixed_noalloc(amr_model *m, const NoAllocView &w, int grid,
         const int nit = std::min(every, o.max_iters - hc.iters);
         for (int it = 0; it < nit; it++) {
             k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w.z32, w.p32, w.ctl);
-            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->nblocks, m->brow_ptr, m->bcol, m->K32, w.p32, w.q32, w.ctl,
+            k_spmv32<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K32, w.p32, w.q32, w.ctl,
                                                w.partials);
             k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w.p32, w.q32, w.x32, w.r32, w.z32, w.ctl, w.partials,
                                                  stop_rr, delta2);
