@@ -245,6 +245,222 @@ function solve_gpu!(ana::MechAnalysis; args...)
     return Amaru.stage_iterator!(gpu_stage_solver!, ana; args...)
 end
 
-export GPUModel, solve_gpu!, gpu_stage_solver!
+# ---------------------------------------------------------------------------
+# Batches: independent models joined into one handle (amr_set_parts), each
+# running its own mech_stage_solver! with one kernel launch per step for all.
+# ---------------------------------------------------------------------------
+function model_arrays(model::FEModel)
+    elems = model.elems
+    all(e -> e isa MechSolid, elems) || error("AmaruGPU: only MechSolid elements are on the GPU path")
+    coords = zeros(3, length(model.nodes))
+    for (i, n) in enumerate(model.nodes)
+        coords[:, i] .= (n.coord.x, n.coord.y, n.coord.z)
+    end
+    nel = length(elems)
+    conn_ptr = zeros(Int64, nel + 1); conn = Int64[]
+    mat_type = zeros(Int32, nel); mat_params = zeros(8, nel)
+    for (k, e) in enumerate(elems)
+        append!(conn, [n.id - 1 for n in e.nodes])
+        conn_ptr[k+1] = length(conn)
+        mat_type[k], mat_params[:, k] = material_code(e.mat)
+    end
+    shape = Int32[SHAPES[e.shape.name] for e in elems]
+    nips = Int32[length(e.ips) for e in elems]
+    return coords, shape, nips, conn_ptr, conn, mat_type, mat_params
+end
+
+function eq_array(model::FEModel)
+    eq = fill(Int64(-1), 3, length(model.nodes))
+    for n in model.nodes, (k, key) in enumerate((:ux, :uy, :uz))
+        haskey(n.dofdict, key) && (eq[k, n.id] = n.dofdict[key].eq_id - 1)
+    end
+    return eq
+end
+
+# immutable mirror of amr_stage_stats, for arrays and for embedding in other records
+struct PartStats
+    status::Int32; increments::Int32; iterations::Int32; krylov_iterations::Int32
+    residue::Float64; T::Float64; seconds::Float64; solve_seconds::Float64
+end
+
+mutable struct GPUBatch
+    h::Ptr{Cvoid}
+    models::Vector{FEModel}
+    node_ptr::Vector{Int64}
+end
+
+"""
+    GPUBatch(models)
+
+Joins independent models (same ndim, stress model and thickness) into one device
+model, model i's nodes and elements after those of models 1..i-1, and declares
+each a part: the batched solver and stage driver then run every model as if it
+were alone.
+"""
+function GPUBatch(models::Vector{<:FEModel})
+    parts = [model_arrays(m) for m in models]
+    node_ptr = cumsum([0; [size(p[1], 2) for p in parts]])
+    coords = reduce(hcat, [p[1] for p in parts])
+    shape = reduce(vcat, [p[2] for p in parts]); nips = reduce(vcat, [p[3] for p in parts])
+    conn = reduce(vcat, [p[5] .+ node_ptr[i] for (i, p) in enumerate(parts)])
+    conn_ptr = cumsum([0; reduce(vcat, [diff(p[4]) for p in parts])])
+    mat_type = reduce(vcat, [p[6] for p in parts]); mat_params = reduce(hcat, [p[7] for p in parts])
+    ctx = models[1].ctx
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve coords shape nips conn_ptr conn mat_type mat_params begin
+        d = ModelDesc(ctx.ndim, STRESSMODELS[ctx.stressmodel], ctx.thickness, size(coords, 2), pointer(coords),
+                      length(shape), pointer(shape), pointer(nips), pointer(conn_ptr), pointer(conn),
+                      pointer(mat_type), pointer(mat_params))
+        st = check(nothing, ccall((:amr_model_create, LIB), Cint, (Ref{ModelDesc}, Ref{Ptr{Cvoid}}), d, h))
+        st === nothing || error(st.message)
+    end
+    b = GPUBatch(h[], collect(models), node_ptr)
+    finalizer(x -> ccall((:amr_model_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), b)
+    rc = ccall((:amr_set_parts, LIB), Cint, (Ptr{Cvoid}, Int64, Ptr{Int64}), b.h, length(models), node_ptr)
+    rc == 0 || error("amr_set_parts failed ($rc)")
+    return b
+end
+
+"""
+    solve_batch!(b, stages; args...)
+
+One stage per model (stages[i] for models[i]), run together: each model's DOFs are
+numbered by Amaru's configure_dofs! and its loads taken from get_bc_vals; the
+joined numbering puts every model's unknowns first.  Updates each model's dof
+values as mech_stage_solver! does and returns one status per model.
+"""
+function solve_batch!(b::GPUBatch, stages::Vector{Stage}; args...)
+    args = Amaru.checkargs(args, Amaru.mech_solver_params)
+    eqs, Us, Fs, nus, nds, dofss = [], [], [], Int[], Int[], []
+    for (m, st) in zip(b.models, stages)
+        dofs, nu = Amaru.configure_dofs!(m, st.bcs)
+        m.ndofs = length(dofs)
+        Uex, Fex = Amaru.get_bc_vals(m, st.bcs)
+        push!(eqs, eq_array(m)); push!(Us, Uex); push!(Fs, Fex); push!(nus, nu); push!(nds, length(dofs))
+        push!(dofss, dofs)
+    end
+    NU, ND = sum(nus), sum(nds)
+    offU = cumsum([0; nus[1:end-1]]); offP = cumsum([0; (nds .- nus)[1:end-1]])
+    joined(i, e) = e < 0 ? e : (e < nus[i] ? offU[i] + e : NU + offP[i] + (e - nus[i]))
+    eq = reduce(hcat, [map(e -> joined(i, e), eqs[i]) for i in eachindex(eqs)])
+    Uex = zeros(ND); Fex = zeros(ND)
+    for i in eachindex(eqs), e in 0:nds[i]-1
+        Uex[joined(i, e)+1] = Us[i][e+1]; Fex[joined(i, e)+1] = Fs[i][e+1]
+    end
+    ccall((:amr_set_dofs, LIB), Cint, (Ptr{Cvoid}, Ptr{Int64}, Int64, Int64), b.h, eq, ND, NU)
+    scheme = Dict(:FE => 0, :ME => 1, :BE => 2, :Ralston => 3)[Symbol(args.scheme)]
+    p = StageParams(args.tol, args.rtol, args.rspan, args.dT0, args.dTmin, args.dTmax, scheme, args.maxits,
+                    args.autoinc, stages[1].nincs, stages[1].nouts, SolveOpts(0, 1e-8, 20000, 32))
+    U = zeros(ND); F = zeros(ND); stats = StageStats()
+    ccall((:amr_stage_run, LIB), Cint,
+          (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ref{StageParams}, Ptr{Float64}, Ptr{Float64}, Ref{StageStats}),
+          b.h, Uex, Fex, p, U, F, stats)
+    buf = Vector{PartStats}(undef, length(b.models))
+    ccall((:amr_get_part_stats, LIB), Cint, (Ptr{Cvoid}, Int64, Ptr{PartStats}), b.h, length(b.models), buf)
+    for i in eachindex(b.models), (e, dof) in enumerate(dofss[i])
+        j = joined(i, e - 1) + 1
+        dof.vals[dof.name] += U[j]
+        dof.vals[dof.natname] += F[j]
+    end
+    return [s.status == 0 ? Amaru.success() : Amaru.failure("Solver did not converge.") for s in buf]
+end
+
+# ---------------------------------------------------------------------------
+# Serving: stages of independent models submitted as they arrive (amr_server_*).
+# ---------------------------------------------------------------------------
+struct Request
+    model::ModelDesc
+    eq_id::Ptr{Int64}; ndofs::Int64; nu::Int64
+    Uex::Ptr{Float64}; Fex::Ptr{Float64}
+    loads::Ptr{Cvoid}; nloads::Int32; pad::Int32
+    stage::StageParams
+end
+
+mutable struct RequestResult
+    status::Int32; active_at_admit::Int32; bytes::Int64
+    t_submit::Float64; t_admit::Float64; t_done::Float64
+    stage::PartStats
+    RequestResult() = new(0, 0, 0, 0.0, 0.0, 0.0, PartStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0.0))
+end
+
+struct ServerConfig
+    hbm_budget_bytes::Float64
+    max_active::Int32
+    pad::Int32
+end
+
+mutable struct GPUServer
+    h::Ptr{Cvoid}
+    pending::Dict{Int64,Tuple{FEModel,Any}}
+end
+
+"""
+    GPUServer(hbm_budget_bytes; max_active=4)
+
+A request loop on the current GPU: up to max_active requests on the device at
+once, admitted in arrival order as slots and memory free up.
+"""
+function GPUServer(budget; max_active::Integer=4)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:amr_server_create, LIB), Cint, (Ref{ServerConfig}, Ref{Ptr{Cvoid}}),
+               ServerConfig(Float64(budget), Int32(max_active), 0), h)
+    rc == 0 || error("amr_server_create failed ($rc)")
+    s = GPUServer(h[], Dict{Int64,Tuple{FEModel,Any}}())
+    finalizer(x -> ccall((:amr_server_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), s)
+    return s
+end
+
+"""
+    submit!(srv, model, stage; args...) -> id
+
+Queues one stage of `model` (solve! keyword arguments); the server copies it.
+"""
+function submit!(srv::GPUServer, model::FEModel, stage::Stage; args...)
+    args = Amaru.checkargs(args, Amaru.mech_solver_params)
+    dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
+    model.ndofs = length(dofs)
+    Uex, Fex = Amaru.get_bc_vals(model, stage.bcs)
+    coords, shape, nips, conn_ptr, conn, mat_type, mat_params = model_arrays(model)
+    eq = eq_array(model)
+    ctx = model.ctx
+    scheme = Dict(:FE => 0, :ME => 1, :BE => 2, :Ralston => 3)[Symbol(args.scheme)]
+    p = StageParams(args.tol, args.rtol, args.rspan, args.dT0, args.dTmin, args.dTmax, scheme, args.maxits,
+                    args.autoinc, stage.nincs, stage.nouts, SolveOpts(0, 1e-8, 20000, 32))
+    id = Ref{Int64}(0)
+    GC.@preserve coords shape nips conn_ptr conn mat_type mat_params eq Uex Fex begin
+        d = ModelDesc(ctx.ndim, STRESSMODELS[ctx.stressmodel], ctx.thickness, size(coords, 2), pointer(coords),
+                      length(shape), pointer(shape), pointer(nips), pointer(conn_ptr), pointer(conn),
+                      pointer(mat_type), pointer(mat_params))
+        r = Request(d, pointer(eq), length(dofs), nu, pointer(Uex), pointer(Fex), C_NULL, 0, 0, p)
+        rc = ccall((:amr_server_submit, LIB), Cint, (Ptr{Cvoid}, Ref{Request}, Ref{Int64}), srv.h, r, id)
+        rc == 0 || error("amr_server_submit failed ($rc)")
+    end
+    srv.pending[id[]] = (model, dofs)
+    return id[]
+end
+
+"""
+    wait!(srv, id) -> (status, result)
+
+Blocks until request `id` is done and updates its model's dof values as
+mech_stage_solver! does; `result` holds the submit, admit and done times.
+"""
+function wait!(srv::GPUServer, id::Integer)
+    model, dofs = pop!(srv.pending, id)
+    U = zeros(length(dofs)); F = zeros(length(dofs)); res = RequestResult(); msg = zeros(UInt8, 512)
+    rc = ccall((:amr_server_wait, LIB), Cint,
+               (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Ref{RequestResult}, Ptr{UInt8}, Csize_t),
+               srv.h, id, U, F, res, msg, length(msg))
+    if rc == 0 || rc == -11
+        for (i, dof) in enumerate(dofs)
+            dof.vals[dof.name] += U[i]
+            dof.vals[dof.natname] += F[i]
+        end
+    end
+    st = rc == 0 ? Amaru.success() : Amaru.failure(unsafe_string(pointer(msg)))
+    return st, res
+end
+
+export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!
 
 end # module
