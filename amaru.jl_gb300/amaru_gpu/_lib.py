@@ -20,7 +20,7 @@ LIN2, LIN3, TRI3, TRI6, QUAD4, QUAD8, QUAD9, TET4, TET10, HEX8, HEX20 = range(1,
 D3, PLANESTRAIN, PLANESTRESS, AXISYMMETRIC = 0, 1, 2, 3
 LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
 LOAD_FACET, LOAD_BODY = 0, 1
-SOLVER_MIXED, SOLVER_FP64 = 0, 1
+SOLVER_MIXED, SOLVER_FP64, SOLVER_AMG = 0, 1, 2
 ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
 KERNEL_SPMV32, KERNEL_RESIDUAL64 = 0, 1
 

@@ -331,8 +331,8 @@ class MechAnalysis:
         if not (1 <= maxits <= 10):
             raise ValueError("maxits must be in 1..10")
         model = self.model
-        lin = L.default_solve_opts(method=L.SOLVER_FP64 if solver == "fp64" else L.SOLVER_MIXED, rtol=linear_rtol,
-                                   refine_every=refine_every, max_iters=max_iters)
+        method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
+        lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every, max_iters=max_iters)
         for st in self.stages:
             if st.status == "done":
                 continue

@@ -36,6 +36,7 @@ struct AmrGroup {             // elements sharing (shape, quadrature)
 
 struct AmrSolveWork;          // solver workspace (solver.cu)
 struct AmrBatch;              // independent parts solved together (batch.cu)
+struct AmrAmg;                // aggregation multigrid preconditioner (amg.cu)
 
 struct amr_model {
     int ndim = 3, B = 3, BB = 9, stressmodel = 0;
@@ -100,6 +101,8 @@ struct amr_model {
     double *vtmp[8] = {nullptr};    // node-major FP64 vectors (nnodes*B)
     AmrSolveWork *sw = nullptr;
     AmrBatch *batch = nullptr;
+    AmrAmg *amg = nullptr;
+    int64_t dofs_version = 0;       // bumped by every amr_set_dofs
     // per-part masks read by the element kernels while a batched stage runs (null otherwise)
     const int32_t *bp_elem_part = nullptr;  // sorted element -> part
     const int32_t *bp_node_part = nullptr;  // node -> part
@@ -171,6 +174,11 @@ void amr_solver_free(amr_model *m);
 double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask_or_null);
 void amr_eq_to_nm(amr_model *m, const double *d_eq, double *d_nm);  // scatter eq_id-ordered -> node-major (0 elsewhere)
 void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq);
+// amg.cu: multigrid preconditioner (structure per DOF numbering, values per assembly)
+void amr_amg_prepare(amr_model *m);
+void amr_amg_vcycle(amr_model *m, const float *r, float *z);
+void amr_amg_invalidate(amr_model *m);
+void amr_amg_free(amr_model *m);
 // batch.cu: independent parts (contiguous node ranges, no element spanning two)
 void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *node_ptr);
 void amr_batch_free(amr_model *m);

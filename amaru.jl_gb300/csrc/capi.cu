@@ -285,6 +285,7 @@ int amr_model_destroy(amr_model *m) {
     if (m->stream) cudaStreamSynchronize(m->stream);
     amr_solver_free(m);
     amr_batch_free(m);
+    amr_amg_free(m);
     for (AmrGroup &g : m->groups) amr_free(g.tab);
     amr_free(m->coords); amr_free(m->conn); amr_free(m->conn_ptr); amr_free(m->mat_type); amr_free(m->mat_par);
     amr_free(m->ip_ptr); amr_free(m->kel_ptr); amr_free(m->inc_ptr); amr_free(m->inc); amr_free(m->brow_ptr);
@@ -348,6 +349,7 @@ int amr_set_dofs(amr_model *m, const int64_t *eq_id, int64_t ndofs, int64_t nu) 
         AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
         AMR_CUDA(cudaStreamSynchronize(m->stream));
+        m->dofs_version++;
         m->dofs_set = true;
         m->K_valid = false;
         if (m->sw) amr_solver_free(m);  // the comparator CSR depends on the numbering

@@ -1013,6 +1013,7 @@ void amr_stiffness(amr_model *m) {
     }
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
+    amr_amg_invalidate(m);
 }
 
 void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2) {
@@ -1027,6 +1028,7 @@ void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2) {
                                                        m->d_status);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
+    amr_amg_invalidate(m);
 }
 
 void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm) {

@@ -270,6 +270,45 @@ __global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *
     }
 }
 
+// Multigrid-preconditioned variant of the update: x += alpha p ; r -= alpha q (z = M r comes after)
+template <int B>
+__global__ void k_update32a(int64_t nn, const float *__restrict__ p, const float *__restrict__ q,
+                            float *__restrict__ x, float *__restrict__ r, const Ctl *ctl) {
+    if (ctl->stop) return;
+    const float alpha = (float)ctl->alpha;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn * B; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = fmaf(alpha, p[i], x[i]);
+        r[i] = fmaf(-alpha, q[i], r[i]);
+    }
+}
+
+// gamma = r.z and |r|^2 once z = M r.  mode 0, an iteration: beta, the counters and the refresh
+// criteria of k_update32; mode 1, after a refresh: gamma only.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_rz32(int64_t nn, const float *__restrict__ r,
+                                                   const float *__restrict__ z, Ctl *ctl, double *partials,
+                                                   double stop_rr, double delta2, int mode) {
+    if (mode == 0 && ctl->stop) return;
+    float rz = 0.0f, rr = 0.0f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn * B; i += (int64_t)gridDim.x * blockDim.x) {
+        rz = fmaf(r[i], z[i], rz);
+        rr = fmaf(r[i], r[i], rr);
+    }
+    float v[2] = {rz, rr};
+    double tot[2];
+    if (grid_sumf<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
+        if (mode == 0) {
+            ctl->beta = tot[0] / ctl->rz;
+            ctl->rz = tot[0];
+            ctl->rr = tot[1];
+            ctl->iters += 1;
+            if (!(tot[1] > stop_rr) || tot[1] <= delta2 * ctl->rr_true) ctl->stop = 1;
+        } else {
+            ctl->rz = tot[0];
+        }
+    }
+}
+
 // FP64 true residual: u64 += x32 (free slots), x32 = 0; r64 = mask(b - K64 u64);
 // reac = (K64 u64) at prescribed slots; r32 = r64; z = Minv r32 ; rz, |r64|^2
 template <int B>
@@ -664,6 +703,78 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     return res;
 }
 
+// solve_system! with the multigrid preconditioner: the mixed solver's PCG (FP32 Krylov vectors,
+// FP64 true-residual refreshes decide convergence) with z = V-cycle(r) in place of block-Jacobi.
+template <int B>
+static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
+    amr_amg_prepare(m);
+    AmrSolveWork *w = work(m);
+    cudaStream_t s = m->stream;
+    int64_t nn = m->nnodes;
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    double tol2 = o.rtol * o.rtol;
+    AMR_CUDA(cudaMemsetAsync(w->x32, 0, w->n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, w->n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w->q32, 0, w->n * sizeof(float), s));
+    {
+        Ctl c0{};
+        c0.first = 1;
+        AMR_CUDA(cudaMemcpyAsync(w->ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    }
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    const unsigned g = (unsigned)w->grid;
+    auto refresh = [&](int first) {
+        k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac,
+                                           w->r32, w->z32, m->Minv32, w->ctl, w->partials, first, tol2);
+        amr_amg_vcycle(m, w->r32, w->z32);
+        k_rz32<B><<<g, kThreads, 0, s>>>(nn, w->r32, w->z32, w->ctl, w->partials, 0.0, 0.0, 1);
+        AMR_COUNT(2);
+        AMR_CUDA(cudaGetLastError());
+    };
+    refresh(1);
+    const int every = 4;  // iterations between host checks (each iteration is a whole V-cycle)
+    const double stop_rr_rel = 0.25 * 0.25 * tol2, delta2 = 1e-2;
+    int since = 0;
+    for (;;) {
+        AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        Ctl c = *w->h_ctl;
+        res.iterations = c.iters;
+        if (c.bnorm2 == 0.0 || c.converged) break;
+        if (c.breakdown) { res.status = AMR_ENOCONV; break; }
+        if (c.iters >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        if (c.stop || since >= 64) {
+            k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
+            AMR_COUNT(1);
+            AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
+            refresh(0);
+            res.refinements++;
+            since = 0;
+            continue;
+        }
+        const double stop_rr = stop_rr_rel * c.bnorm2;
+        const int nit = std::min(every, o.max_iters - c.iters);
+        for (int it = 0; it < nit; it++) {
+            k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
+            launch_spmv32<B>(m, w, w->p32[0], w->q32);
+            k_update32a<B><<<g, kThreads, 0, s>>>(nn, w->p32[0], w->q32, w->x32, w->r32, w->ctl);
+            amr_amg_vcycle(m, w->r32, w->z32);
+            k_rz32<B><<<g, kThreads, 0, s>>>(nn, w->r32, w->z32, w->ctl, w->partials, stop_rr, delta2, 0);
+            AMR_COUNT(3);
+        }
+        AMR_CUDA(cudaGetLastError());
+        since += nit;
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    res.seconds = ms * 1e-3;
+    Ctl c = *w->h_ctl;
+    res.rel_residual = c.bnorm2 > 0 ? std::sqrt(c.rr_true / c.bnorm2) : 0.0;
+    return res;
+}
+
 template <int B>
 static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
     AmrSolveWork *w = work(m);
@@ -861,6 +972,7 @@ void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq) {
 
 AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
     if (m->batch && o.method == AMR_SOLVER_MIXED) return amr_batch_solve(m, x, b, reac, o);  // one CTA per part
+    if (o.method == AMR_SOLVER_AMG) return m->B == 3 ? solve_amg<3>(m, x, b, reac, o) : solve_amg<2>(m, x, b, reac, o);
     if (o.method == AMR_SOLVER_FP64)
         return m->B == 3 ? solve_fp64_csr<3>(m, x, b, reac, o) : solve_fp64_csr<2>(m, x, b, reac, o);
     return m->B == 3 ? solve_mixed<3>(m, x, b, reac, o) : solve_mixed<2>(m, x, b, reac, o);

@@ -6,8 +6,9 @@ Workload: linear-elastic HEX20 block 10 x 4 x 4 m meshed 100 x 40 x 40
 element lognormal(ln 30e3, 0.3) from a fixed seed, nu = 0.2, base z=0 fixed,
 uniform pressure 1.0 on the top face.  A step is one linear load increment
 of the staged Newton solver (mech_stage_solver!): device assembly of K (FP64
-element integration + deterministic scatter), FP32 block-Jacobi PCG inside
-FP64 iterative refinement to a relative residual of 1e-8, the internal-force
+element integration + deterministic scatter), FP32 PCG preconditioned by
+aggregation multigrid (or block-Jacobi with --solver mixed) inside FP64
+iterative refinement to a relative residual of 1e-8, the internal-force
 update with the constitutive state and the equilibrium check.  `value` is
 DOFs per second of that step with all inputs resident in HBM; `e2e` is the
 same step through the C ABI with host buffers (H2D of the stage's essential
@@ -47,6 +48,8 @@ def parse():
     ap.add_argument("--cpu-mesh", default="20x8x8", help="bounded CPU sample of the same workload family")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--solver", default="amg", choices=["amg", "mixed"],
+                    help="preconditioner of the FP32 PCG in the step: aggregation multigrid or block-Jacobi")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-models measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-requests", type=int, default=32)
@@ -133,7 +136,8 @@ def run_ours(a):
     dev = model.dev
     sizes = dev.sizes()
     ndofs = model.ndofs
-    lin = L.default_solve_opts(method=L.SOLVER_MIXED, rtol=1e-8)
+    step_method = L.SOLVER_AMG if a.solver == "amg" else L.SOLVER_MIXED
+    lin = L.default_solve_opts(method=step_method, rtol=1e-8)
     prm = L.default_stage_params(nincs=1, linear=lin)
     d_Uex = torch.from_numpy(Uex).cuda()
     d_Fex = torch.from_numpy(Fex).cuda()
@@ -193,18 +197,26 @@ def run_ours(a):
         except Exception:
             traffic = None
 
-    # solve-only comparison: mixed-precision refined PCG vs the plain all-FP64 GPU path, same K and RHS
+    # solve-only comparison, same K and RHS: the FP32 PCG in FP64 refinement with the multigrid and with
+    # the block-Jacobi preconditioner, against the plain all-FP64 GPU path
     solve_cmp = {}
     if not a.no_fp64:
         U0 = Uex.copy()
         F0 = Fex.copy()
-        U1, F1, s_mixed = dev.solve(U0, F0, L.default_solve_opts(method=L.SOLVER_MIXED, rtol=1e-8))
+        U1, F1, s_amg = dev.solve(U0, F0, L.default_solve_opts(method=L.SOLVER_AMG, rtol=1e-8))
+        U3, F3, s_mixed = dev.solve(U0, F0, L.default_solve_opts(method=L.SOLVER_MIXED, rtol=1e-8))
         U2, F2, s_fp64 = dev.solve(U0, F0, L.default_solve_opts(method=L.SOLVER_FP64, rtol=1e-8, max_iters=200000))
-        du = float(np.abs(U1[:model.nu] - U2[:model.nu]).max() / np.abs(U2[:model.nu]).max())
-        solve_cmp = {"mixed_s": s_mixed.seconds, "mixed_iters": s_mixed.iterations,
+        nu = model.nu
+        ref = np.abs(U2[:nu]).max()
+        s_step = s_amg if step_method == L.SOLVER_AMG else s_mixed
+        solve_cmp = {"amg_s": s_amg.seconds, "amg_iters": s_amg.iterations, "amg_rel_residual": s_amg.rel_residual,
+                     "mixed_s": s_mixed.seconds, "mixed_iters": s_mixed.iterations,
                      "mixed_rel_residual": s_mixed.rel_residual, "fp64_s": s_fp64.seconds,
                      "fp64_iters": s_fp64.iterations, "fp64_rel_residual": s_fp64.rel_residual,
-                     "speedup_vs_fp64": s_fp64.seconds / s_mixed.seconds, "max_rel_dU_mixed_vs_fp64": du}
+                     "step_solver": a.solver, "speedup_vs_fp64": s_fp64.seconds / s_step.seconds,
+                     "speedup_vs_fp64_block_jacobi": s_fp64.seconds / s_mixed.seconds,
+                     "max_rel_dU_amg_vs_fp64": float(np.abs(U1[:nu] - U2[:nu]).max() / ref),
+                     "max_rel_dU_mixed_vs_fp64": float(np.abs(U3[:nu] - U2[:nu]).max() / ref)}
 
     # e2e: the same step through the C ABI with host buffers (H2D inputs, D2H results inside)
     Uh = np.ascontiguousarray(Uex)
@@ -226,8 +238,8 @@ def run_ours(a):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 assembly/residual/state, f32 Krylov", "data": "synthetic",
         "config": {"workload": "HEX20 %dx%dx%d block 10x4x4 m, 27 IP, lognormal E (seed 0xA11A), nu=0.2, base fixed, "
-                               "top pressure 1.0; one linear increment: assemble K + PCG(f32)/IR(f64) to 1e-8 + "
-                               "internal forces" % (nx, ny, nz),
+                               "top pressure 1.0; one linear increment: assemble K + PCG(f32, %s)/IR(f64) to 1e-8 + "
+                               "internal forces" % (nx, ny, nz, "multigrid" if a.solver == "amg" else "block-Jacobi"),
                    "ndofs": ndofs, "nu": model.nu, "nnodes": sizes["nnodes"], "nelems": sizes["nelems"],
                    "nnz_blocks": sizes["nblocks"], "nnz": sizes["nblocks"] * 9,
                    "l2": "inputs larger than L2 (K32 %.2f GB, K64 %.2f GB)" % (sizes["nblocks"] * 36 / 1e9,

@@ -95,10 +95,13 @@ typedef struct {
 } amr_load;
 
 /* Linear-solver options for the Newton corrector solve. */
-enum { AMR_SOLVER_MIXED = 0, AMR_SOLVER_FP64 = 1 };
+enum { AMR_SOLVER_MIXED = 0, AMR_SOLVER_FP64 = 1, AMR_SOLVER_AMG = 2 };
 typedef struct {
     int32_t method;          /* AMR_SOLVER_MIXED: FP32 block-Jacobi PCG in FP64 iterative refinement
-                                AMR_SOLVER_FP64:  plain all-FP64 CSR Jacobi PCG */
+                                AMR_SOLVER_FP64:  plain all-FP64 CSR Jacobi PCG
+                                AMR_SOLVER_AMG:   as MIXED with an aggregation-multigrid V-cycle
+                                                  (rigid-body coarse spaces, Chebyshev/block-Jacobi
+                                                  smoothing) in place of block-Jacobi */
     double rtol;             /* relative residual ||b - K u|| / ||b|| to reach (default 1e-8) */
     int32_t max_iters;       /* cap on inner Krylov iterations (default 20000) */
     int32_t refine_every;    /* FP64 true-residual refresh interval in inner iterations (default 32) */
