@@ -33,6 +33,7 @@ namespace {
 
 constexpr int kDenseMax = 2048;  // DOFs of the coarsest (dense) level at most
 constexpr int kMaxLevels = 8;
+constexpr int kNormCtas = 512;  // CTAs of the power-iteration norm
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -156,7 +157,8 @@ struct AmrAmg {
     int64_t nc = 0;             // DOFs of the dense coarsest level
     double *Cd = nullptr;       // nc x nc FP64 work (Gauss-Jordan)
     float *Cinv = nullptr;      // nc x nc FP32 inverse
-    double *scratch = nullptr;  // norms
+    double *scratch = nullptr;  // norms: [0] result, [8..] per-CTA partials
+    unsigned int *ticket = nullptr;
     int64_t dofs_version = -1;
     bool numeric_valid = false;
 };
@@ -173,7 +175,7 @@ void amr_amg_free(amr_model *m) {
         amr_free(v.cptr); amr_free(v.ck); amr_free(v.ci); amr_free(v.null_dof);
         amr_free(v.x); amr_free(v.bv); amr_free(v.r); amr_free(v.d);
     }
-    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->scratch);
+    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->scratch); amr_free(g->ticket);
     delete g;
     m->amg = nullptr;
 }
@@ -363,7 +365,9 @@ static void amg_build_structure(amr_model *m) {
     }
     amr_alloc(&g->Cd, (size_t)g->nc * 2 * g->nc);  // [A | I] for Gauss-Jordan
     amr_alloc(&g->Cinv, (size_t)g->nc * g->nc);
-    amr_alloc(&g->scratch, 64);
+    amr_alloc(&g->scratch, 8 + kNormCtas);
+    amr_alloc(&g->ticket, 1);
+    AMR_CUDA(cudaMemset(g->ticket, 0, sizeof(unsigned int)));
     g->numeric_valid = false;
 }
 
@@ -618,18 +622,34 @@ __global__ void k_dense_mv(int64_t nc, const float *Cinv, const float *b, float 
     if (lane == 0) x[r] = s;
 }
 
-// sum of squares (one CTA, fixed order) for the power iteration
-__global__ void k_norm2(int64_t n, const float *v, double *out) {
+// sum of squares for the power iteration: per-CTA partials (fixed element assignment), the last CTA
+// adds them in CTA order
+__global__ void k_norm2(int64_t n, const float *v, double *partials, unsigned int *ticket, double *out) {
     __shared__ double sh[256];
+    __shared__ bool last;
     double s = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)v[i] * v[i];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = v[i];
+        s += x * x;
+    }
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = sh[0];
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = sh[0];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double t = 0.0;
+    for (unsigned b = 0; b < gridDim.x; b++) t += ((volatile double *)partials)[b];
+    *out = t;
+    *ticket = 0;
 }
 __global__ void k_fill(int64_t n, float v, float *x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -708,27 +728,27 @@ struct Cycle {
         AMR_COUNT(7);
         AMR_CUDA(cudaGetLastError());
     }
-    // largest eigenvalue of Dinv A by power iteration (12 steps, host-read norms)
+    // largest eigenvalue of Dinv A by power iteration (10 steps from a unit-norm start; |x| = 1 each step)
     template <int NB>
     static double lambda(amr_model *m, AmrAmg *g, AmgLevel &L, const float *A, int64_t nbs) {
         cudaStream_t s = m->stream;
         const int64_t nv = L.n * NB;
-        k_fill<<<nblk(nv, 256), 256, 0, s>>>(nv, 1.0f, L.x);
-        double lam = 1.0, n2 = 0.0;
-        for (int it = 0; it < 12; it++) {
+        const unsigned gnorm = (unsigned)std::min<int64_t>(kNormCtas, std::max<int64_t>(1, nblk(nv, 256)));
+        k_fill<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(1.0 / std::sqrt((double)nv)), L.x);
+        AMR_COUNT(1);
+        double lam = 1.0;
+        for (int it = 0; it < 10; it++) {
             bsr_res<NB>(s, L, A, nbs, L.x, nullptr, L.r);
             k_cheb<NB><<<nblk(L.n, 256), 256, 0, s>>>(L.n, 0, 0.0f, 1.0f, L.Dinv, L.r, L.d, L.bv);  // bv = Dinv A x
-            k_norm2<<<1, 256, 0, s>>>(nv, L.x, g->scratch);
-            k_norm2<<<1, 256, 0, s>>>(nv, L.bv, g->scratch + 1);
-            AMR_COUNT(3);
-            double h[2];
-            AMR_CUDA(cudaMemcpyAsync(h, g->scratch, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            k_norm2<<<gnorm, 256, 0, s>>>(nv, L.bv, g->scratch + 8, g->ticket, g->scratch);
+            AMR_COUNT(2);
+            double n2 = 0.0;
+            AMR_CUDA(cudaMemcpyAsync(&n2, g->scratch, sizeof(double), cudaMemcpyDeviceToHost, s));
             AMR_CUDA(cudaStreamSynchronize(s));
-            if (!(h[0] > 0.0) || !(h[1] > 0.0)) break;
-            lam = std::sqrt(h[1] / h[0]);
-            n2 = h[1];
+            if (!(n2 > 0.0)) break;
+            lam = std::sqrt(n2);
             AMR_CUDA(cudaMemcpyAsync(L.x, L.bv, nv * sizeof(float), cudaMemcpyDeviceToDevice, s));
-            k_scale<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(1.0 / std::sqrt(n2)), L.x);
+            k_scale<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(1.0 / lam), L.x);
             AMR_COUNT(1);
         }
         return lam;

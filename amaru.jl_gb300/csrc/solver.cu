@@ -732,8 +732,23 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
         AMR_CUDA(cudaGetLastError());
     };
     refresh(1);
+    // one iteration as a CUDA graph, captured once its arguments are fixed (after the first
+    // refresh: stop_rr depends on |b|), then replayed; its kernels are counted per replay
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long long per_iter = 0;
+    struct GraphFree {
+        cudaGraph_t &g;
+        cudaGraphExec_t &x;
+        ~GraphFree() {
+            if (x) cudaGraphExecDestroy(x);
+            if (g) cudaGraphDestroy(g);
+        }
+    } graph_free{graph, gexec};
     const int every = 4;  // iterations between host checks (each iteration is a whole V-cycle)
-    const double stop_rr_rel = 0.25 * 0.25 * tol2, delta2 = 1e-2;
+    // refresh after a 100x drop of the residual norm: the few, fast-converging iterations between
+    // refreshes keep the FP32 recursion accurate, and convergence is judged on the FP64 residual
+    const double stop_rr_rel = 0.25 * 0.25 * tol2, delta2 = 1e-4;
     int since = 0;
     for (;;) {
         AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
@@ -754,15 +769,25 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
         }
         const double stop_rr = stop_rr_rel * c.bnorm2;
         const int nit = std::min(every, o.max_iters - c.iters);
-        for (int it = 0; it < nit; it++) {
+        if (!gexec) {
+            const long long before = amr_g_launches.load();
+            AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
             k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
             launch_spmv32<B>(m, w, w->p32[0], w->q32);
             k_update32a<B><<<g, kThreads, 0, s>>>(nn, w->p32[0], w->q32, w->x32, w->r32, w->ctl);
             amr_amg_vcycle(m, w->r32, w->z32);
             k_rz32<B><<<g, kThreads, 0, s>>>(nn, w->r32, w->z32, w->ctl, w->partials, stop_rr, delta2, 0);
             AMR_COUNT(3);
+            const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+            per_iter = amr_g_launches.load() - before;
+            AMR_COUNT(-per_iter);
+            AMR_CUDA(ce);
+            AMR_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
         }
-        AMR_CUDA(cudaGetLastError());
+        for (int it = 0; it < nit; it++) {
+            AMR_CUDA(cudaGraphLaunch(gexec, s));
+            AMR_COUNT(per_iter);
+        }
         since += nit;
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
