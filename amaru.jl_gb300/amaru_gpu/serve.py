@@ -21,8 +21,8 @@ _SCHEMES = {"FE": 0, "ME": 1, "BE": 2, "Ralston": 3}
 def stage_params(nincs=1, nouts=0, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE",
                  maxits=5, autoinc=False, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000):
     """amr_stage_params with the keyword defaults of solve!(ana; ...) (src/mech/mech-solver.jl:155-168)."""
-    lin = L.default_solve_opts(method=L.SOLVER_FP64 if solver == "fp64" else L.SOLVER_MIXED, rtol=linear_rtol,
-                               refine_every=refine_every, max_iters=max_iters)
+    method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
+    lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every, max_iters=max_iters)
     return L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,
                                   scheme=_SCHEMES[scheme], maxits=maxits, autoinc=int(autoinc), nincs=nincs,
                                   nouts=nouts, linear=lin)

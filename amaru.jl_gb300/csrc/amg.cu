@@ -284,7 +284,7 @@ static void amg_build_structure(amr_model *m) {
             for (int k = 0; k < NM; k++) wmax = std::max(wmax, w[k]);
             double sc[6];
             for (int k = 0; k < NM; k++) {
-                const bool keep = wmax > 0.0 && w[k] > 1e-10 * wmax;
+                const bool keep = wmax > 0.0 && w[k] > 1e-8 * wmax;
                 sc[k] = keep ? 1.0 / std::sqrt(w[k]) : 0.0;
                 if (!keep) nulld[a * NM + k] = 1;
             }
@@ -651,9 +651,13 @@ __global__ void k_norm2(int64_t n, const float *v, double *partials, unsigned in
     *out = t;
     *ticket = 0;
 }
-__global__ void k_fill(int64_t n, float v, float *x) {
+// deterministic pseudo-random start vector in [-1, 1) (integer hash of the index), scaled by s
+__global__ void k_fill_random(int64_t n, float s, float *x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] = v;
+    if (i >= n) return;
+    uint32_t h = (uint32_t)i * 2654435761u + 0x9E3779B9u;
+    h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
+    x[i] = s * ((float)(h >> 8) * (1.0f / 8388608.0f) - 1.0f);
 }
 __global__ void k_scale(int64_t n, float s, float *x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -686,7 +690,9 @@ struct Cheb {
     float s1, s2a, s2b;  // d = s2a Dinv r (first), d = s1 d + s2b Dinv r (second)
 };
 Cheb cheb_coef(double lam) {
-    const double lo = lam / 30.0, hi = 1.1 * lam, th = 0.5 * (hi + lo), de = 0.5 * (hi - lo);
+    // a power-iteration estimate approaches lambda_max from below: the interval's top has a margin,
+    // as a smoother that sees eigenvalues above it amplifies them
+    const double lo = lam / 30.0, hi = 1.25 * lam, th = 0.5 * (hi + lo), de = 0.5 * (hi - lo);
     const double sig = th / de, rho0 = 1.0 / sig, rho1 = 1.0 / (2.0 * sig - rho0);
     return Cheb{(float)(rho1 * rho0), (float)(1.0 / th), (float)(2.0 * rho1 / de)};
 }
@@ -728,16 +734,17 @@ struct Cycle {
         AMR_COUNT(7);
         AMR_CUDA(cudaGetLastError());
     }
-    // largest eigenvalue of Dinv A by power iteration (10 steps from a unit-norm start; |x| = 1 each step)
+    // largest eigenvalue of Dinv A by power iteration (15 steps from a pseudo-random start, which excites
+    // the localized high-frequency modes of distorted elements; |x| = 1 after each step)
     template <int NB>
     static double lambda(amr_model *m, AmrAmg *g, AmgLevel &L, const float *A, int64_t nbs) {
         cudaStream_t s = m->stream;
         const int64_t nv = L.n * NB;
         const unsigned gnorm = (unsigned)std::min<int64_t>(kNormCtas, std::max<int64_t>(1, nblk(nv, 256)));
-        k_fill<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(1.0 / std::sqrt((double)nv)), L.x);
+        k_fill_random<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(std::sqrt(3.0 / (double)nv)), L.x);
         AMR_COUNT(1);
         double lam = 1.0;
-        for (int it = 0; it < 10; it++) {
+        for (int it = 0; it < 15; it++) {
             bsr_res<NB>(s, L, A, nbs, L.x, nullptr, L.r);
             k_cheb<NB><<<nblk(L.n, 256), 256, 0, s>>>(L.n, 0, 0.0f, 1.0f, L.Dinv, L.r, L.d, L.bv);  // bv = Dinv A x
             k_norm2<<<gnorm, 256, 0, s>>>(nv, L.bv, g->scratch + 8, g->ticket, g->scratch);

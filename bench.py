@@ -375,14 +375,14 @@ def _serve_requests(count):
             m = A.FEModel(mesh, [("all", A.VonMises(E=50e3, nu=0.3, fy=100.0, H=1e3))], device=False)
             bcs = [("z==0", A.SurfaceBC(ux=0, uy=0, uz=0)), ("z==0.5", A.SurfaceBC(tz=-120.0)),
                    ("all", A.BodyC(wz=-20.0))]
-            kw = dict(nincs=incs, autoinc=True)
+            kw = dict(nincs=incs, autoinc=True, solver="amg")
         else:
             dofs = float(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
             k = max(1, int(round(((dofs / 3) / 2) ** (1 / 3))))  # nodes ~ (2k+1)(k+1)^2
             mesh = A.Mesh(A.Block([[0, 0, 0], [1.0, 0.5, 0.5]], nx=2 * k, ny=k, nz=k, cellshape=A.HEX8))
             m = A.FEModel(mesh, [("all", A.LinearElastic(E=200e3, nu=0.3))], device=False)
             bcs = [("x==0", A.SurfaceBC(ux=0, uy=0, uz=0)), ("x==1", A.SurfaceBC(tz=-1.0))]
-            kw = dict(nincs=incs)
+            kw = dict(nincs=incs, solver="amg")
         reqs.append((arrivals[i], "tet10" if tet else "hex8", m, bcs, kw))
     return reqs
 
@@ -415,7 +415,7 @@ def serving_leg(count=32, max_active=8):
     dof_incs = sum(n * r.stage.increments for _, rc, r, n in out if rc == 0)
     return {"workload": "%d requests, Poisson arrivals 200/s (seed 0xC5): HEX8 cantilever blocks 1x0.5x0.5, DOFs log-uniform "
                         "[1e3, 2e6], 1..10 linear increments; 20%% TET10 von Mises blocks (gravity + surcharge, "
-                        "automatic increments), DOFs log-uniform [1e3, 2e5]; mixed solver to 1e-8" % count,
+                        "automatic increments), DOFs log-uniform [1e3, 2e5]; multigrid-preconditioned solver to 1e-8" % count,
             "requests": count, "completed": int(sum(rc == 0 for _, rc, _, _ in out)),
             "tet10": int(sum(k == "tet10" for k, _, _, _ in out)),
             "solves_per_s": count / span, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
@@ -443,13 +443,13 @@ def slope_leg(spec):
     ana = A.MechAnalysis(model)
     ana.addstage(W.slope_bcs(A, 200.0), nincs=20)
     setup_s = time.perf_counter() - t0
-    ok, msg = ana.solve(tol=1e-6)
+    ok, msg = ana.solve(tol=1e-6, solver="amg")
     st = ana.stats[0]
     sizes = model.dev.sizes()
     plastic = int((model.state()[:, 12] > 0).sum())
     return {"workload": "TET10 slope %s (L=10, W=1.7, crest 4 m, toe 2 m, jittered interior, seed 0xC3), von Mises "
                         "E=50e3 nu=0.3 fy=100 H=1e3, gravity 20 + crest surcharge 200 over 20 increments, Newton "
-                        "tol 1e-6, mixed solver to 1e-8" % spec,
+                        "tol 1e-6, multigrid-preconditioned solver to 1e-8" % spec,
             "ok": bool(ok), "message": msg, "ndofs": int(model.ndofs), "nelems": sizes["nelems"],
             "nnodes": sizes["nnodes"], "increments": st.increments, "newton_iterations": st.iterations,
             "krylov_iterations": st.krylov_iterations, "stage_s": st.seconds, "solve_s": st.solve_seconds,

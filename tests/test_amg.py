@@ -83,3 +83,23 @@ def test_amg_in_the_elastoplastic_newton_loop():
     assert gm.state()[:, 12].max() > 0
     assert ag.stats[0].iterations == len(ao.log)
     assert np.abs(gm.U - om.U).max() <= 1e-6 * np.abs(om.U).max()
+
+
+def test_amg_on_the_jittered_tet10_slope():
+    """The slope workload (distorted TET10, rollers, gravity + surcharge): the multigrid stage equals the
+    block-Jacobi stage to the solver tolerance."""
+    from amaru_gpu import workloads as W
+    g = W.SLOPE
+    n = (20, 3, 8)
+    out = []
+    for solver in ("mixed", "amg"):
+        mesh = A.Mesh(A.Block([[0, 0, 0], [g["L"], g["W"], g["H"]]], nx=n[0], ny=n[1], nz=n[2], cellshape=A.TET10))
+        mesh.coords = W.slope_coords(mesh.coords, mesh.elem_nodes(), W.boundary_nodes(mesh), 4, *n, seed=0xC3)
+        model = A.FEModel(mesh, [("all", A.VonMises(E=50e3, nu=0.3, fy=100.0, H=1e3))])
+        ana = A.MechAnalysis(model)
+        ana.addstage(W.slope_bcs(A, 200.0), nincs=5)
+        assert ana.solve(tol=1e-6, solver=solver)[0]
+        out.append((model.U.copy(), ana.stats[0]))
+    (Um, sm), (Ua, sa) = out
+    assert sa.iterations == sm.iterations and sa.krylov_iterations * 5 < sm.krylov_iterations
+    assert np.abs(Ua - Um).max() <= 1e-6 * np.abs(Um).max()
