@@ -823,6 +823,24 @@ void amr_amg_vcycle(amr_model *m, const float *r, float *z) {
     else Cycle<2, 3>::level(m, m->amg, 0, r, z);
 }
 
+// average device time of the cycle's fine-level residual r = b - K32 x (CUDA events on the handle's stream)
+double amr_amg_time_residual(amr_model *m, int reps) {
+    AmrAmg *g = m->amg;
+    if (!g || !g->numeric_valid) throw AmrError(AMR_EINVAL, "run a multigrid solve on the current K first");
+    AmgLevel &L = g->L[0];
+    cudaStream_t s = m->stream;
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    for (int i = 0; i < reps; i++) {
+        if (m->B == 3) bsr_res<3>(s, L, m->K32, m->bstride, L.x, L.bv, L.r);
+        else bsr_res<2>(s, L, m->K32, m->bstride, L.x, L.bv, L.r);
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    return ms * 1e-3 / reps;
+}
+
 void amr_amg_invalidate(amr_model *m) {
     if (m->amg) m->amg->numeric_valid = false;
 }

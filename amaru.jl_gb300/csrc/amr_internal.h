@@ -178,6 +178,7 @@ void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq);
 void amr_amg_prepare(amr_model *m);
 void amr_amg_vcycle(amr_model *m, const float *r, float *z);
 void amr_amg_invalidate(amr_model *m);
+double amr_amg_time_residual(amr_model *m, int reps);
 void amr_amg_free(amr_model *m);
 // batch.cu: independent parts (contiguous node ranges, no element spanning two)
 void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *node_ptr);

@@ -649,6 +649,10 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
             t = amr_time_solver_kernel(m, AMR_KERNEL_RESIDUAL64, reps);
             bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 + 8.0 + 4.0 + 4.0 + 1.0) + nn * BB * 4.0;
             break;
+        case AMR_KERNEL_AMG_RESIDUAL:  // as SPMV32, plus b read (x gathered, r written)
+            t = amr_amg_time_residual(m, reps);
+            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 3.0;
+            break;
         default:
             throw AmrError(AMR_EINVAL, "kernel not timed by this entry point");
         }

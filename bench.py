@@ -187,15 +187,31 @@ def run_ours(a):
     hbm = peaks.get("hbm_gbs")
     peak_kind = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
-    achieved = spmv_b / spmv_t / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "spmv32_traffic.json")
-    if os.path.exists(tp):
+    def measured_traffic(name):
+        # DRAM bytes per launch from an ncu capture of the kernel, scaled per block and per node
+        tp = os.path.join(ROOT, "profiles", name)
+        if not os.path.exists(tp):
+            return None
         try:
             tj = json.load(open(tp))
-            traffic = tj["bytes_per_block"] * sizes["nblocks"] + tj["bytes_per_node"] * sizes["nnodes"]
+            return tj["bytes_per_block"] * sizes["nblocks"] + tj["bytes_per_node"] * sizes["nnodes"]
         except Exception:
-            traffic = None
+            return None
+
+    # the dominant kernel of the step: with the multigrid, the cycle's fine residual r = b - K32 x
+    # (four launches per PCG iteration); with block-Jacobi, the PCG's SpMV
+    spmv = {"kernel": "k_spmv32 (FP32 BSR SpMV q = K p with fused p.q)", "bytes_per_launch": spmv_b,
+            "avg_launch_s": spmv_t, "achieved": spmv_b / spmv_t / 1e9,
+            "traffic": measured_traffic("spmv32_traffic.json")}
+    if step_method == L.SOLVER_AMG:
+        amg_t, amg_b = dev.time_kernel(L.KERNEL_AMG_RESIDUAL, 50)
+        dom = {"kernel": "k_bsr_res<3> (multigrid cycle's fine residual r = b - K32 x)", "bytes_per_launch": amg_b,
+               "avg_launch_s": amg_t, "achieved": amg_b / amg_t / 1e9,
+               "traffic": measured_traffic("bsr_res_traffic.json")}
+    else:
+        dom = spmv
+    achieved = dom["achieved"]
+    traffic = dom["traffic"]
 
     # solve-only comparison, same K and RHS: the FP32 PCG in FP64 refinement with the multigrid and with
     # the block-Jacobi preconditioner, against the plain all-FP64 GPU path
@@ -246,10 +262,11 @@ def run_ours(a):
                                                                              sizes["nblocks"] * 72 / 1e9),
                    "parallelism": "replicas (one model per GPU)", "setup_s": setup_s},
         "solve": dict(solve_cmp, step_solve_s=float(np.mean(solve_s)), step_krylov_iters=int(np.mean(kry))),
-        "roofline": {"bound": "hbm", "kernel": "k_spmv32 (FP32 BSR SpMV q = K p with fused p.q)",
+        "roofline": {"bound": "hbm", "kernel": dom["kernel"],
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": peak_kind, "traffic": traffic, "bytes_per_launch": spmv_b,
-                     "avg_launch_s": spmv_t,
+                     "peak_source": peak_kind, "traffic": traffic, "bytes_per_launch": dom["bytes_per_launch"],
+                     "avg_launch_s": dom["avg_launch_s"],
+                     "spmv32": dict(spmv, frac=spmv["achieved"] / hbm),
                      "residual64": {"achieved": res_b / res_t / 1e9, "frac": res_b / res_t / 1e9 / hbm,
                                     "avg_launch_s": res_t}},
         "e2e": {"value": e2e_v, "unit": "DOF/s", "h2d_bytes_per_step": 2 * ndofs * 8, "d2h_bytes_per_step": 2 * ndofs * 8,
