@@ -214,7 +214,7 @@ function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
     set_dofs!(g, model, dofs, nu)
     Uex, Fex = Amaru.get_bc_vals(model, stage.bcs)
     scheme = Dict(:FE => 0, :ME => 1, :BE => 2, :Ralston => 3)[Symbol(args.scheme)]
-    lin = SolveOpts(0, 1e-8, 20000, 32)
+    lin = SolveOpts(LINEAR_METHOD[], 1e-8, 20000, 32)
     p = StageParams(args.tol, args.rtol, args.rspan, args.dT0, args.dTmin, args.dTmax, scheme, args.maxits,
                     args.autoinc, stage.nincs, stage.nouts, lin)
     U = zeros(length(dofs))
@@ -235,12 +235,17 @@ end
 
 const GPU_MODELS = Dict{UInt,GPUModel}()
 
-"""
-    solve_gpu!(ana::MechAnalysis; args...)
+# linear method of the stage solver: 0 block-Jacobi, 2 aggregation multigrid (amr_solve_opts.method)
+const LINEAR_METHOD = Ref{Int32}(2)
 
-solve! with the stage solver replaced by gpu_stage_solver!.
 """
-function solve_gpu!(ana::MechAnalysis; args...)
+    solve_gpu!(ana::MechAnalysis; linear=:amg, args...)
+
+solve! with the stage solver replaced by gpu_stage_solver!; `linear` picks the
+preconditioner of the FP32 PCG (:amg multigrid or :jacobi block-Jacobi).
+"""
+function solve_gpu!(ana::MechAnalysis; linear::Symbol=:amg, args...)
+    LINEAR_METHOD[] = linear === :jacobi ? Int32(0) : Int32(2)
     args = Amaru.checkargs(args, Amaru.mech_solver_params)
     return Amaru.stage_iterator!(gpu_stage_solver!, ana; args...)
 end
