@@ -94,6 +94,11 @@ class ServerInfo(C.Structure):
                 ("active_bytes", C.c_int64), ("peak_bytes", C.c_int64), ("seconds", C.c_double)]
 
 
+# recovered field codes (AMR_FIELD_*) and the reference's ip_state_vals keys
+FIELD_NAMES = ["σxx", "σyy", "σzz", "σyz", "σxz", "σxy", "σvm", "σ1", "σ2", "σ3", "εxx", "εyy", "εzz", "εyz", "εxz",
+               "εxy", "ep", "epa", "j1", "srj2d"]
+NFIELD_CODES = len(FIELD_NAMES)
+
 # Every exported entry point of include/amaru_gpu.h with its ctypes signature.
 P = C.c_void_p
 SIGNATURES = {
@@ -111,6 +116,7 @@ SIGNATURES = {
     "amr_state_commit": (C.c_int, [P]),
     "amr_state_restore": (C.c_int, [P]),
     "amr_get_state": (C.c_int, [P, P]),
+    "amr_set_state": (C.c_int, [P, P]),
     "amr_get_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64)]),
     "amr_assemble_loads": (C.c_int, [P, C.POINTER(Load), C.c_int32, C.c_double, P]),
@@ -129,6 +135,11 @@ SIGNATURES = {
     "amr_server_destroy": (C.c_int, [P]),
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "amr_recovery_fields": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
+    "amr_recover_nodal": (C.c_int, [P, P]),
+    "amr_recover_nodal_dev": (C.c_int, [P, P]),
+    "amr_time_recovery": (C.c_int, [P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_int64)]),
     "amr_default_solve_opts": (None, [C.POINTER(SolveOpts)]),
     "amr_default_stage_params": (None, [C.POINTER(StageParams)]),
 }
@@ -293,6 +304,12 @@ class DeviceModel:
         check(self.h, lib().amr_get_state(self.h, ptr(s)))
         return s
 
+    def set_state(self, state):
+        s = np.ascontiguousarray(state, dtype=np.float64)
+        if s.shape != (self.sizes()["nip_total"], 16):
+            raise ValueError("state must be nip_total x 16")
+        check(self.h, lib().amr_set_state(self.h, ptr(s)))
+
     def assemble_loads(self, loads, F, t=0.0):
         arr, keep = load_array(loads)
         F = np.ascontiguousarray(F, dtype=np.float64)
@@ -343,6 +360,30 @@ class DeviceModel:
         t, b = C.c_double(), C.c_double()
         check(self.h, lib().amr_time_kernel(self.h, which, reps, C.byref(t), C.byref(b)))
         return t.value, b.value
+
+    def recovery_fields(self):
+        """Field names of the nodal recovery, in the reference's column order."""
+        codes = np.zeros(NFIELD_CODES, dtype=np.int32)
+        n = C.c_int32()
+        check(self.h, lib().amr_recovery_fields(self.h, ptr(codes), NFIELD_CODES, C.byref(n)))
+        return [FIELD_NAMES[c] for c in codes[:n.value]]
+
+    def recover_nodal(self):
+        """nodal_patch_recovery: (V (nnodes x nfields), field names) from the current IP states."""
+        names = self.recovery_fields()
+        V = np.zeros((len(names), self.sizes()["nnodes"]))
+        if names:
+            check(self.h, lib().amr_recover_nodal(self.h, ptr(V)))
+        return V.T, names
+
+    def recover_nodal_dev(self, d_V):
+        """Device-pointer variant: d_V is the raw CUDA address of nnodes x nfields doubles (column-major)."""
+        check(self.h, lib().amr_recover_nodal_dev(self.h, C.c_void_p(d_V)))
+
+    def time_recovery(self, reps):
+        t, f, n = C.c_double(), C.c_double(), C.c_int64()
+        check(self.h, lib().amr_time_recovery(self.h, reps, C.byref(t), C.byref(f), C.byref(n)))
+        return t.value, f.value, n.value
 
     def launch_count(self):
         n = C.c_int64()

@@ -13,6 +13,9 @@ from . import _lib as L
 from .expr import affine_coefficients, evaluate
 from .mesh import NPOINTS, Mesh
 
+# VTK cell type of each shape (vtk_type in src/shape/*.jl, codes of src/shape/vtk.jl)
+VTK_TYPES = {L.TRI3: 5, L.TRI6: 22, L.QUAD4: 9, L.QUAD8: 23, L.QUAD9: 28, L.TET4: 10, L.TET10: 24, L.HEX8: 12,
+             L.HEX20: 25}
 STRESSMODELS = {"d3": L.D3, "planestrain": L.PLANESTRAIN, "planestress": L.PLANESTRESS,
                 "axisymmetric": L.AXISYMMETRIC}
 
@@ -306,6 +309,35 @@ class FEModel:
 
     def state(self):
         return self.dev.state()
+
+    def set_state(self, state):
+        self.dev.set_state(state)
+
+    # ---- output data
+    def nodal_patch_recovery(self):
+        """nodal_patch_recovery(model) (src/fe-model.jl:504-702) on the device: (V (nnodes x nfields), names)."""
+        return self.dev.recover_nodal()
+
+    def update_output_data(self):
+        """node_data / elem_data of update_output_data! (src/fe-model.jl:341-427): ids, cell types, the dof values
+        (displacements and natural values), the recovered IP fields and the vector U."""
+        nn, ne = self.nnodes, len(self.mesh.shape)
+        node = {"node-id": np.arange(1, nn + 1)}
+        nat = ["fx", "fy", "fz"]
+        has = np.zeros(nn, dtype=bool)
+        has[self.active_nodes] = True
+        for i in range(self.ndim):
+            node[self._dof_names[i]] = np.where(has, self.U[:, i], 0.0)
+            node[nat[i]] = np.where(has, self.F[:, i], 0.0)
+        V, names = self.nodal_patch_recovery()
+        for j, k in enumerate(names):
+            node[k] = V[:, j]
+        U = np.zeros((nn, 3))
+        U[:, : self.ndim] = np.stack([node[k] for k in self._dof_names], 1)
+        node["U"] = U
+        elem = {"elem-id": np.arange(1, ne + 1), "cell-type": np.array([VTK_TYPES[int(s)] for s in self.mesh.shape])}
+        self.node_data, self.elem_data = node, elem
+        return node, elem
 
 
 class Stage:

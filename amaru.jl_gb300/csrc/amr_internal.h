@@ -12,6 +12,8 @@
 #define AMR_MAXN 20     // largest element (HEX20)
 #define AMR_MAXIP 27    // largest quadrature (HEX 3x3x3)
 #define AMR_NST 14      // IP state fields: sigma[6] eps[6] epa dlambda
+#define AMR_ST_SIG 0
+#define AMR_ST_EPS 6
 #define AMR_ST_EPA 12
 #define AMR_ST_DL 13
 
@@ -37,6 +39,7 @@ struct AmrGroup {             // elements sharing (shape, quadrature)
 struct AmrSolveWork;          // solver workspace (solver.cu)
 struct AmrBatch;              // independent parts solved together (batch.cu)
 struct AmrAmg;                // aggregation multigrid preconditioner (amg.cu)
+struct AmrRecovery;           // nodal patch recovery of the IP fields (recovery.cu)
 
 struct amr_model {
     int ndim = 3, B = 3, BB = 9, stressmodel = 0;
@@ -102,6 +105,7 @@ struct amr_model {
     AmrSolveWork *sw = nullptr;
     AmrBatch *batch = nullptr;
     AmrAmg *amg = nullptr;
+    AmrRecovery *rec = nullptr;
     int64_t dofs_version = 0;       // bumped by every amr_set_dofs
     // per-part masks read by the element kernels while a batched stage runs (null otherwise)
     const int32_t *bp_elem_part = nullptr;  // sorted element -> part
@@ -180,6 +184,12 @@ void amr_amg_vcycle(amr_model *m, const float *r, float *z);
 void amr_amg_invalidate(amr_model *m);
 double amr_amg_time_residual(amr_model *m, int reps);
 void amr_amg_free(amr_model *m);
+// recovery.cu: nodal_patch_recovery (structure once per model, values per call)
+void amr_recovery_prepare(amr_model *m);
+const std::vector<int32_t> &amr_recovery_codes(amr_model *m);
+void amr_recover(amr_model *m, double *d_V);  // device, nnodes x nfields column-major
+double amr_recovery_time_fit(amr_model *m, int reps, double *flops, int64_t *n_svd);
+void amr_recovery_free(amr_model *m);
 // batch.cu: independent parts (contiguous node ranges, no element spanning two)
 void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *node_ptr);
 void amr_batch_free(amr_model *m);

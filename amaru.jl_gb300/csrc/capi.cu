@@ -286,6 +286,7 @@ int amr_model_destroy(amr_model *m) {
     amr_solver_free(m);
     amr_batch_free(m);
     amr_amg_free(m);
+    amr_recovery_free(m);
     for (AmrGroup &g : m->groups) amr_free(g.tab);
     amr_free(m->coords); amr_free(m->conn); amr_free(m->conn_ptr); amr_free(m->mat_type); amr_free(m->mat_par);
     amr_free(m->ip_ptr); amr_free(m->kel_ptr); amr_free(m->inc_ptr); amr_free(m->inc); amr_free(m->brow_ptr);
@@ -513,6 +514,22 @@ int amr_get_state(amr_model *m, double *state) {
     });
 }
 
+int amr_set_state(amr_model *m, const double *state) {
+    return guarded(m, [&] {
+        if (!state) throw AmrError(AMR_EINVAL, "null argument");
+        std::vector<double> st((size_t)AMR_NST * m->nip_total);
+        int64_t o = 0;
+        for (int64_t e = 0; e < m->nelems; e++) {
+            int64_t s = m->inv_perm[e];
+            for (int64_t g = m->h_ip_ptr[s]; g < m->h_ip_ptr[s + 1]; g++, o++)
+                for (int f = 0; f < AMR_NST; f++) st[(size_t)f * m->nip_total + g] = state[16 * o + f];
+        }
+        AMR_CUDA(cudaMemcpyAsync(m->st, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        return AMR_OK;
+    });
+}
+
 int amr_assemble_loads(amr_model *m, const amr_load *loads, int32_t nloads, double t, double *F) {
     return guarded(m, [&] {
         check_dofs(m);
@@ -623,6 +640,54 @@ int amr_get_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *stat
 int amr_autotune(amr_model *m, amr_tuning *out) {
     return guarded(m, [&] {
         amr_autotune_model(m, out);
+        return AMR_OK;
+    });
+}
+
+int amr_recovery_fields(amr_model *m, int32_t *codes, int32_t cap, int32_t *nfields) {
+    return guarded(m, [&] {
+        if (!nfields || (cap > 0 && !codes)) throw AmrError(AMR_EINVAL, "null argument");
+        const std::vector<int32_t> &c = amr_recovery_codes(m);
+        for (int32_t i = 0; i < cap && i < (int32_t)c.size(); i++) codes[i] = c[i];
+        *nfields = (int32_t)c.size();
+        return AMR_OK;
+    });
+}
+
+int amr_recover_nodal_dev(amr_model *m, double *d_V) {
+    return guarded(m, [&] {
+        if (!d_V) throw AmrError(AMR_EINVAL, "null argument");
+        amr_recover(m, d_V);
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        return AMR_OK;
+    });
+}
+
+int amr_recover_nodal(amr_model *m, double *V) {
+    return guarded(m, [&] {
+        if (!V) throw AmrError(AMR_EINVAL, "null argument");
+        const size_t n = (size_t)m->nnodes * amr_recovery_codes(m).size();
+        if (!n) return AMR_OK;
+        double *d_V;
+        amr_alloc(&d_V, n);
+        try {
+            amr_recover(m, d_V);
+            AMR_CUDA(cudaMemcpyAsync(V, d_V, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+            AMR_CUDA(cudaStreamSynchronize(m->stream));
+        } catch (...) {
+            amr_free(d_V);
+            throw;
+        }
+        amr_free(d_V);
+        return AMR_OK;
+    });
+}
+
+int amr_time_recovery(amr_model *m, int32_t reps, double *avg_seconds, double *flops_per_launch,
+                      int64_t *svd_patches) {
+    return guarded(m, [&] {
+        if (reps < 1 || !avg_seconds) throw AmrError(AMR_EINVAL, "reps >= 1 and avg_seconds required");
+        *avg_seconds = amr_recovery_time_fit(m, reps, flops_per_launch, svd_patches);
         return AMR_OK;
     });
 }

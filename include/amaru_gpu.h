@@ -186,6 +186,9 @@ int amr_state_restore(amr_model *m);
 /* IP states out (nip_total x 16: sigma[6], eps[6], epa, dlambda, 0, 0) in the
  * caller's element order and IP order; nip_total via amr_get_sizes. */
 int amr_get_state(amr_model *m, double *state);
+/* IP states in, same layout (copyto! of the IpState arrays, src/ip.jl:22-57): a
+ * checkpoint restored, or states set by the caller. */
+int amr_set_state(amr_model *m, const double *state);
 int amr_get_sizes(const amr_model *m, int64_t *nnodes, int64_t *nelems, int64_t *nip_total, int64_t *nblocks);
 
 /* Distributed loads (compute_bc_vals!, src/bc.jl:116-136,175-194):
@@ -320,6 +323,33 @@ enum { AMR_KERNEL_SPMV32 = 0, AMR_KERNEL_RESIDUAL64 = 1, AMR_KERNEL_STIFFNESS = 
 int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch);
 /* Number of kernels this handle has launched since it was created. */
 int amr_launch_count(const amr_model *m, int64_t *count);
+
+/* ---- output recovery ----
+ * Nodal values of the IP fields: replaces nodal_patch_recovery (src/fe-model.jl:504-702)
+ * as called by update_output_data! (:341-427) and get_node_and_elem_vals (:430-485).
+ * Field codes name the keys of ip_state_vals (src/tools/tensors.jl:162-215,
+ * src/mech/mat/von-mises.jl:159-168,330-341, src/mech/mat/drucker-prager.jl:152-163):
+ * σxx σyy σzz σyz σxz σxy σvm σ1 σ2 σ3 εxx εyy εzz εyz εxz εxy ep epa j1 srj2d. */
+enum {
+    AMR_FIELD_SXX = 0, AMR_FIELD_SYY = 1, AMR_FIELD_SZZ = 2, AMR_FIELD_SYZ = 3, AMR_FIELD_SXZ = 4,
+    AMR_FIELD_SXY = 5, AMR_FIELD_SVM = 6, AMR_FIELD_S1 = 7, AMR_FIELD_S2 = 8, AMR_FIELD_S3 = 9,
+    AMR_FIELD_EXX = 10, AMR_FIELD_EYY = 11, AMR_FIELD_EZZ = 12, AMR_FIELD_EYZ = 13, AMR_FIELD_EXZ = 14,
+    AMR_FIELD_EXY = 15, AMR_FIELD_EP = 16, AMR_FIELD_EPA = 17, AMR_FIELD_J1 = 18, AMR_FIELD_SRJ2D = 19,
+    AMR_NFIELD_CODES = 20
+};
+/* The recovered fields in the reference's column order (first appearance over the
+ * elements): codes[0 .. min(cap, n)) and *nfields = n.  The first call builds the
+ * patch structure (outer facets, corner patches, the boundary-patch fallback). */
+int amr_recovery_fields(amr_model *m, int32_t *codes, int32_t cap, int32_t *nfields);
+/* V (nnodes x nfields, column-major as the reference's V_rec[:, i]) from the handle's
+ * current IP states; host buffer. */
+int amr_recover_nodal(amr_model *m, double *V);
+/* The same into a device buffer, on the handle's stream (synchronised on return). */
+int amr_recover_nodal_dev(amr_model *m, double *d_V);
+/* Average device time of the patch-fit kernel over reps launches (CUDA events), its
+ * algorithmic FP64 operations per launch and the patches that took the SVD path. */
+int amr_time_recovery(amr_model *m, int32_t reps, double *avg_seconds, double *flops_per_launch,
+                      int64_t *svd_patches);
 
 /* Default parameter blocks (the reference's KwArgInfo defaults). */
 void amr_default_solve_opts(amr_solve_opts *o);

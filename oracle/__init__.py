@@ -2,13 +2,18 @@
 
 TEST INFRASTRUCTURE ONLY: a restatement of NumSoftware/Amaru.jl's Float64
 algorithms (element stiffness, constitutive updates, mount_K, update_state!,
-solve_system!, get_bc_vals, the staged Newton driver and the structured
-mesher).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
-may import it, and only as the checker.  The CUDA library never calls it.
+solve_system!, get_bc_vals, the staged Newton driver, the structured mesher
+and the nodal patch recovery of the output data).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg may import it, and
+only as the checker.  The CUDA library never calls it.
 
 Parity pin: tests/test_oracle_golden.py checks this oracle against every
 known-answer test of the reference's test suite for this path
 (test/mech/elem/elastic-hex8.jl, elastic-quad4.jl, elastic-elems.jl,
-test/mech/mat/vm-3d.jl, vm-2d.jl, dp.jl, test/mesh/structured.jl).
+test/mech/mat/vm-3d.jl, vm-2d.jl, dp.jl, test/mesh/structured.jl).  The
+reference's tests hold no nodal recovery values; the recovery restatement is
+pinned by the fields it must reproduce exactly (polynomials of the regression
+space) in tests/test_recovery.py.
 """
 from .core import *  # noqa: F401,F403
+from .recovery import nodal_patch_recovery, ip_coords, ip_state_vals, field_names  # noqa: F401
