@@ -47,6 +47,7 @@ constexpr double SR2 = 1.4142135623730951;  // src/tools/constants.jl:3
 constexpr int kFitWarps = 4;                 // warps per CTA of the fit kernels
 constexpr int kTermPad = 8;                  // doubles per regression row (<= 7 terms)
 constexpr int kRedStride = 29;               // Gram partials per lane in shared memory (28 + pad)
+constexpr int kInvDiag = 72;                 // offset of the reciprocal Cholesky pivots in the factor area
 
 // ---------------------------------------------------------------------------
 // host tables
@@ -140,9 +141,11 @@ __device__ void eig3(const double *s, double *L) {
             for (int q = p + 1; q < 3; q++) {
                 const double apq = a[p][q];
                 if (apq == 0.0) continue;
-                const double th = (a[q][q] - a[p][p]) / (2.0 * apq);
-                const double t = fabs(th) > 1e150 ? 0.5 / th : copysign(1.0, th) / (fabs(th) + sqrt(th * th + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                // tangent of the rotation angle, the smaller root of t^2 + 2 theta t - 1 = 0 with
+                // theta = d / e: t = sign(d) e / (|d| + sqrt(d^2 + e^2))
+                const double d = a[q][q] - a[p][p], e = 2.0 * apq;
+                const double t = copysign(1.0, d) * e / (fabs(d) + sqrt(d * d + e * e));
+                const double c = rsqrt(t * t + 1.0), sn = t * c;
                 a[p][p] -= t * apq;
                 a[q][q] += t * apq;
                 a[p][q] = a[q][p] = 0.0;
@@ -234,6 +237,9 @@ __device__ __forceinline__ void terms(const double *x, int nt, double *p) {
     }
 }
 
+// index of entry (a, b), a <= b, of the packed upper triangle of a 7 x 7 matrix stored row by row
+__device__ __forceinline__ int packed(int a, int b) { return a * 7 - a * (a - 1) / 2 + (b - a); }
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -285,8 +291,8 @@ __device__ __forceinline__ WarpMem warp_mem(double *smem, int warp, int m_max, i
     return w;
 }
 
-// Loads the task's IPs: global indices, scaled regression rows; returns the number of terms and the
-// centre / scale of the coordinates.
+// Loads the task's IPs: global indices, scaled regression rows; returns the number of terms, the centre c
+// of the coordinates and their reciprocal scales h (x_scaled = (x - c) * h).
 // raw: the reference's own basis (global coordinates, no centring or scaling)
 template <int DIM>
 __device__ int load_task(const FitArgs &A, int64_t t, const WarpMem &w, int lane, double *c, double *h, bool raw) {
@@ -316,16 +322,16 @@ __device__ int load_task(const FitArgs &A, int64_t t, const WarpMem &w, int lane
         w.gidx[i] = gi;
         for (int d = 0; d < DIM; d++) hm[d] = fmax(hm[d], fabs(A.ipx[3 * gi + d] - c[d]));
     }
-    for (int d = 0; d < DIM; d++) {
-        h[d] = warp_max_d(hm[d]);
-        if (!(h[d] > 0.0) || raw) h[d] = 1.0;
+    for (int d = 0; d < DIM; d++) {  // h holds the reciprocal scale from here on
+        const double hd = warp_max_d(hm[d]);
+        h[d] = (!(hd > 0.0) || raw) ? 1.0 : 1.0 / hd;
     }
     if (raw) c[0] = c[1] = c[2] = 0.0;
     __syncwarp();
     for (int i = lane; i < m; i += 32) {
         double x[3], p[kTermPad];
         const int64_t gi = w.gidx[i];
-        for (int d = 0; d < DIM; d++) x[d] = (A.ipx[3 * gi + d] - c[d]) / h[d];
+        for (int d = 0; d < DIM; d++) x[d] = (A.ipx[3 * gi + d] - c[d]) * h[d];
         terms<DIM>(x, nt, p);
         for (int k = 0; k < nt; k++) w.phi[i * kTermPad + k] = p[k];
     }
@@ -341,7 +347,7 @@ __device__ void write_nodes(const FitArgs &A, int64_t t, const WarpMem &w, int l
     for (int64_t j = lane; j < n; j += 32) {
         const int32_t node = A.t_node[s0 + j];
         double x[3], p[kTermPad];
-        for (int d = 0; d < DIM; d++) x[d] = (A.coords[3 * (int64_t)node + d] - c[d]) / h[d];
+        for (int d = 0; d < DIM; d++) x[d] = (A.coords[3 * (int64_t)node + d] - c[d]) * h[d];
         terms<DIM>(x, nt, p);
         double *o = A.vst + (s0 + j) * A.nf;
         for (int k = 0; k < nfm; k++) {
@@ -400,38 +406,43 @@ __global__ void __launch_bounds__(32 * kFitWarps) k_patch_fit(FitArgs A) {
             w.bA[lane] = s;  // packed upper triangle, row by row (bA is free until the moments)
         }
         __syncwarp();
-        // Cholesky G = R'R by lane 0, from shared memory
+        // Cholesky G = R'R: the pivots on every lane, row j's off-diagonal entries on lanes i > j.
+        // R[j][i] at R[j*kTermPad+i], the reciprocal pivots at R[kInvDiag+j]
         const double *G = w.bA;
         double *R = w.R;
         bool ok = true;
         double dmin = DBL_MAX, dmax = 0.0;
-        if (lane == 0) {
-            int k = 0;
-            double Gf[7][7];
-            for (int a = 0; a < 7; a++)
-                for (int b = a; b < 7; b++, k++) Gf[a][b] = G[k];
-            for (int j = 0; j < nt && ok; j++) {
-                double d = Gf[j][j];
-                for (int q = 0; q < j; q++) d -= R[q * kTermPad + j] * R[q * kTermPad + j];
-                if (!(d > 0.0)) { ok = false; break; }
-                const double r = sqrt(d);
+#pragma unroll
+        for (int j = 0; j < 7; j++) {
+            if (j >= nt) break;
+            double d = G[packed(j, j)];
+#pragma unroll
+            for (int q = 0; q < 7; q++)
+                if (q < j) d -= R[q * kTermPad + j] * R[q * kTermPad + j];
+            if (!(d > 0.0)) { ok = false; break; }
+            const double r = sqrt(d), ir = 1.0 / r;
+            dmin = fmin(dmin, r);
+            dmax = fmax(dmax, r);
+            if (lane > j && lane < nt) {
+                double v = G[packed(j, lane)];
+#pragma unroll
+                for (int q = 0; q < 7; q++)
+                    if (q < j) v -= R[q * kTermPad + j] * R[q * kTermPad + lane];
+                R[j * kTermPad + lane] = v * ir;
+            } else if (lane == j) {
                 R[j * kTermPad + j] = r;
-                dmin = fmin(dmin, r);
-                dmax = fmax(dmax, r);
-                for (int i = j + 1; i < nt; i++) {
-                    double v = Gf[j][i];
-                    for (int q = 0; q < j; q++) v -= R[q * kTermPad + j] * R[q * kTermPad + i];
-                    R[j * kTermPad + i] = v / r;
-                }
+                R[kInvDiag + j] = ir;
             }
-            // the normal equations square the condition number: hand patches with a conditioning
-            // worse than 1e4 to the SVD path
-            if (ok && !(dmin > 1e-4 * dmax)) ok = false;
-            A.t_flag[t] = ok ? 0 : 1;
-            w.R[kTermPad * kTermPad] = ok ? 1.0 : 0.0;
+            __syncwarp();
         }
-        __syncwarp();
-        if (w.R[kTermPad * kTermPad] == 0.0) continue;
+        // the normal equations square the condition number: patches conditioned worse than 1e4 go to
+        // the SVD path
+        if (ok && !(dmin > 1e-4 * dmax)) ok = false;
+        if (lane == 0) A.t_flag[t] = ok ? 0 : 1;
+        if (!ok) {
+            __syncwarp();
+            continue;
+        }
         const int mk = A.t_mask[t];
         const int nfm = A.mask_nf[mk];
         const int32_t *flds = A.mask_fields + mk * AMR_NFIELD_CODES;
@@ -440,16 +451,29 @@ __global__ void __launch_bounds__(32 * kFitWarps) k_patch_fit(FitArgs A) {
         if (lane < nfm) {
             double y[7];
             double *b = w.bA + lane * kTermPad;
-            for (int j = 0; j < nt; j++) {
-                double v = b[j];
-                for (int q = 0; q < j; q++) v -= R[q * kTermPad + j] * y[q];
-                y[j] = v / R[j * kTermPad + j];
+#pragma unroll
+            for (int j = 0; j < 7; j++) {
+                if (j < nt) {
+                    double v = b[j];
+#pragma unroll
+                    for (int q = 0; q < 7; q++)
+                        if (q < j) v -= R[q * kTermPad + j] * y[q];
+                    y[j] = v * R[kInvDiag + j];
+                }
             }
-            for (int j = nt - 1; j >= 0; j--) {
-                double v = y[j];
-                for (int q = j + 1; q < nt; q++) v -= R[j * kTermPad + q] * b[q];
-                b[j] = v / R[j * kTermPad + j];
+#pragma unroll
+            for (int j = 6; j >= 0; j--) {
+                if (j < nt) {
+                    double v = y[j];
+#pragma unroll
+                    for (int q = 0; q < 7; q++)
+                        if (q > j && q < nt) v -= R[j * kTermPad + q] * y[q];
+                    y[j] = v * R[kInvDiag + j];
+                }
             }
+#pragma unroll
+            for (int j = 0; j < 7; j++)
+                if (j < nt) b[j] = y[j];
         }
         __syncwarp();
         write_nodes<DIM>(A, t, w, lane, nt, nfm, flds, c, h);

@@ -251,6 +251,35 @@ function solve_gpu!(ana::MechAnalysis; linear::Symbol=:amg, args...)
 end
 
 # ---------------------------------------------------------------------------
+# Output data: nodal_patch_recovery (src/fe-model.jl:504-702) on the device.
+# ---------------------------------------------------------------------------
+const FIELD_SYMBOLS = [:σxx, :σyy, :σzz, :σyz, :σxz, :σxy, :σvm, :σ1, :σ2, :σ3,
+                       :εxx, :εyy, :εzz, :εyz, :εxz, :εxy, :ep, :epa, :j1, :srj2d]
+
+"""
+    nodal_patch_recovery_gpu(model::FEModel)
+
+The `(V_rec, fields)` pair of nodal_patch_recovery(model), from the IP states the
+model's GPU handle holds (the last gpu_stage_solver! stage).
+"""
+function nodal_patch_recovery_gpu(model::FEModel)
+    g = GPU_MODELS[objectid(model)]
+    n = Ref{Int32}(0)
+    codes = zeros(Int32, length(FIELD_SYMBOLS))
+    check(g, ccall((:amr_recovery_fields, LIB), Cint, (Ptr{Cvoid}, Ptr{Int32}, Int32, Ref{Int32}),
+                   g.h, codes, Int32(length(codes)), n))
+    V = zeros(length(model.nodes), n[])
+    n[] > 0 && check(g, ccall((:amr_recover_nodal, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, V))
+    return V, FIELD_SYMBOLS[codes[1:n[]] .+ 1]
+end
+
+# GPU-backed model?  update_output_data! picks the recovery with it (the one-line hook at
+# src/fe-model.jl:379: V_rec, fields_rec = has_gpu(model) ? nodal_patch_recovery_gpu(model) :
+# nodal_patch_recovery(model)); redefining nodal_patch_recovery(::FEModel) here would replace
+# the CPU method for every model.
+has_gpu(model::FEModel) = haskey(GPU_MODELS, objectid(model))
+
+# ---------------------------------------------------------------------------
 # Batches: independent models joined into one handle (amr_set_parts), each
 # running its own mech_stage_solver! with one kernel launch per step for all.
 # ---------------------------------------------------------------------------
@@ -466,6 +495,7 @@ function wait!(srv::GPUServer, id::Integer)
     return st, res
 end
 
-export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!
+export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
+       nodal_patch_recovery_gpu, has_gpu
 
 end # module

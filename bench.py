@@ -52,6 +52,7 @@ def parse():
                     help="preconditioner of the FP32 PCG in the step: aggregation multigrid or block-Jacobi")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-models measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-recovery", action="store_true", help="skip the nodal recovery measurement")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--slope", default="", help="also run the TET10 slope stage at these divisions, e.g. 100x17x40")
     return ap.parse_args()
@@ -274,6 +275,8 @@ def run_ours(a):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if not a.no_recovery:
+        out["recovery"] = recovery_leg(model, rank == 0 and not a.no_cpu)
     if not a.no_batch:
         out["batch"] = batch_leg()
     if not a.no_serve:
@@ -283,6 +286,66 @@ def run_ours(a):
     if rank == 0 and not a.no_cpu:
         out["cpu_baseline"] = cpu_baseline(a, steps=1, warmup=0)
     return out
+
+
+# ---------------------------------------------------------------------------
+# Nodal output recovery (nodal_patch_recovery) of the step's IP states on the same
+# model: the whole device recovery (IP fields, patch fits, averaging), the same
+# call with the result copied to the host, and the patch-fit kernel against the
+# FP64 pipe.  The CPU baseline runs the oracle's restatement on a HEX20 8x4x4
+# block of the same family with seeded states.
+# ---------------------------------------------------------------------------
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (non-tensor), nominal
+
+
+def recovery_leg(model, with_cpu, reps=5):
+    import torch
+    dev = model.dev
+    t0 = time.perf_counter()
+    names = dev.recovery_fields()
+    setup_s = time.perf_counter() - t0
+    nn = dev.sizes()["nnodes"]
+    d_V = torch.zeros(len(names) * nn, dtype=torch.float64, device="cuda")
+    dev.recover_nodal_dev(d_V.data_ptr())  # warm
+    ts = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        dev.recover_nodal_dev(d_V.data_ptr())
+        ts.append(time.perf_counter() - t1)
+    te = []
+    for _ in range(reps):
+        t1 = time.perf_counter()
+        V, _ = dev.recover_nodal()
+        te.append(time.perf_counter() - t1)
+    fit_t, flops, nsvd = dev.time_recovery(10)
+    out = {"fields": len(names), "nnodes": nn, "structure_setup_s": setup_s,
+           "device_s": float(np.mean(ts)), "value": nn / float(np.mean(ts)), "unit": "nodes/s",
+           "e2e": {"value": nn / float(np.mean(te)), "unit": "nodes/s", "s": float(np.mean(te)),
+                   "d2h_bytes": int(V.size * 8)},
+           "patch_fit": {"kernel": "k_patch_fit<3> (warp per patch: Gram/Cholesky fit, moments, nodal values)",
+                         "avg_launch_s": fit_t, "flops_per_launch": flops,
+                         "achieved": flops / fit_t / 1e12, "unit": "TFLOP/s (FP64)",
+                         "peak": FP64_NOMINAL_TFLOPS, "peak_source": "nominal FP64 (no measured figure)",
+                         "frac": flops / fit_t / 1e12 / FP64_NOMINAL_TFLOPS, "svd_patches": nsvd}}
+    if with_cpu:
+        out["cpu_baseline"] = recovery_cpu_sample()
+    return out
+
+
+def recovery_cpu_sample(n=(8, 4, 4)):
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    mo = O.Mesh(O.Block([[0, 0, 0], [10.0 * n[0] / 100, 4.0 * n[1] / 40, 4.0 * n[2] / 40]], nx=n[0], ny=n[1],
+                        nz=n[2], cellshape=O.HEX20))
+    om = O.FEModel(mo, [("all", O.LinearElastic(E=30e3, nu=0.2))], nips=27)
+    om.state[:, :12] = np.random.default_rng(SEED).normal(size=(len(om.state), 12))
+    t0 = time.perf_counter()
+    O.nodal_patch_recovery(om)
+    dt = time.perf_counter() - t0
+    return {"value": om.nnodes / dt, "unit": "nodes/s", "cores": 1, "kind": "port",
+            "sample": "oracle nodal_patch_recovery (Python/numpy restatement) on HEX20 %dx%dx%d, 27 IP, %d nodes: "
+                      "%.2f s" % (n[0], n[1], n[2], om.nnodes, dt)}
 
 
 # ---------------------------------------------------------------------------
