@@ -74,6 +74,12 @@ class Tuning(C.Structure):
                 ("stiffness_seconds", C.c_double), ("internal_seconds", C.c_double)]
 
 
+class DynParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("dTmin", C.c_double), ("dTmax", C.c_double), ("rspan", C.c_double),
+                ("alpha", C.c_double), ("beta", C.c_double), ("tspan", C.c_double), ("maxits", C.c_int32),
+                ("autoinc", C.c_int32), ("nincs", C.c_int32), ("nouts", C.c_int32), ("linear", SolveOpts)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int32), ("pad", C.c_int32)]
 
@@ -135,6 +141,11 @@ SIGNATURES = {
     "amr_server_destroy": (C.c_int, [P]),
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "amr_set_density": (C.c_int, [P, P]),
+    "amr_assemble_M": (C.c_int, [P]),
+    "amr_get_M_csc": (C.c_int, [P, C.POINTER(C.c_int64), P, P, P]),
+    "amr_dyn_stage_run": (C.c_int, [P, P, P, P, P, C.POINTER(DynParams), P, P, P, P, C.POINTER(StageStats)]),
+    "amr_default_dyn_params": (None, [C.POINTER(DynParams)]),
     "amr_recovery_fields": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
     "amr_recover_nodal": (C.c_int, [P, P]),
     "amr_recover_nodal_dev": (C.c_int, [P, P]),
@@ -197,6 +208,14 @@ def default_stage_params(**kw):
             p.linear = v
         else:
             setattr(p, k, v)
+    return p
+
+
+def default_dyn_params(**kw):
+    p = DynParams()
+    lib().amr_default_dyn_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
     return p
 
 
@@ -360,6 +379,32 @@ class DeviceModel:
         t, b = C.c_double(), C.c_double()
         check(self.h, lib().amr_time_kernel(self.h, which, reps, C.byref(t), C.byref(b)))
         return t.value, b.value
+
+    def set_density(self, rho):
+        r = np.ascontiguousarray(rho, dtype=np.float64)
+        check(self.h, lib().amr_set_density(self.h, ptr(r)))
+
+    def assemble_M(self):
+        check(self.h, lib().amr_assemble_M(self.h))
+
+    def M_csc(self):
+        import scipy.sparse as sp
+        nnz = C.c_int64()
+        check(self.h, lib().amr_get_M_csc(self.h, C.byref(nnz), None, None, None))
+        colptr = np.zeros(self.ndofs + 1, dtype=np.int64)
+        rowval = np.zeros(max(nnz.value, 1), dtype=np.int64)
+        nzval = np.zeros(max(nnz.value, 1))
+        check(self.h, lib().amr_get_M_csc(self.h, C.byref(nnz), ptr(colptr), ptr(rowval), ptr(nzval)))
+        return sp.csc_matrix((nzval[:nnz.value], rowval[:nnz.value], colptr), shape=(self.ndofs, self.ndofs))
+
+    def dyn_stage_run(self, U0, U1, F0, F1, params):
+        """dyn_stage_solver!: boundary values U0 + t U1, F0 + t F1; returns (rc, U, V, A, F, stats)."""
+        ins = [np.ascontiguousarray(a, dtype=np.float64) for a in (U0, U1, F0, F1)]
+        outs = [np.zeros(self.ndofs) for _ in range(4)]
+        st = StageStats()
+        rc = lib().amr_dyn_stage_run(self.h, *[ptr(a) for a in ins], C.byref(params), *[ptr(a) for a in outs],
+                                     C.byref(st))
+        return (rc, *outs, st)
 
     def recovery_fields(self):
         """Field names of the nodal recovery, in the reference's column order."""

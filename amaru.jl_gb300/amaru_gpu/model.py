@@ -130,6 +130,7 @@ class FEModel:
         ne = len(mesh.shape)
         self.mat_type = np.full(ne, -1, dtype=np.int32)
         self.mat_params = np.zeros((ne, 8))
+        self.rho = np.zeros(ne)  # element density (MechSolid props rho, src/mech/elem/mech-solid.jl:6-29)
         enodes = mesh.elem_nodes()
         for bind in matbinds:
             if len(bind) == 4:
@@ -143,6 +144,7 @@ class FEModel:
                 sel = mesh.select_cells(enodes, filt)
             self.mat_type[sel] = mat.kind
             self.mat_params[sel] = mat.params()
+            self.rho[sel] = mat.p.get("rho", 0.0)
         if (self.mat_type < 0).any():
             raise ValueError("FEModel: some elements have no material")
         if E is not None:
@@ -179,6 +181,7 @@ class FEModel:
         out.mat_type = np.concatenate([m.mat_type for m in models])
         out.mat_params = np.concatenate([m.mat_params for m in models])
         out.nips = np.concatenate([m.nips for m in models])
+        out.rho = np.concatenate([m.rho for m in models])
         out.dev = L.DeviceModel(out.ndim, out.stressmodel, out.thickness, mesh.coords, mesh.shape, out.nips,
                                 mesh.conn_ptr, mesh.conn, out.mat_type, out.mat_params)
         out._host_fields()
@@ -384,6 +387,54 @@ class MechAnalysis:
                 return False, model.dev.last_error()
             st.status = "done"
         return True, ""
+
+
+class DynAnalysis:
+    """DynamicAnalysis(model) (src/mech/dyn-solver.jl:34-66) with addstage! and solve! (:166-186): the
+    Newmark stage solver dyn_stage_solver! (:203-534) on the device.  Boundary values must be affine in
+    time (get_bc_vals at t = Uex(0) + t (Uex(1) - Uex(0))).  The reference defines velocities and
+    accelerations only in the first stage, so an analysis has one stage."""
+
+    def __init__(self, model):
+        self.model = model
+        self.stages = []
+        self.stats = None
+
+    def addstage(self, bcs, nincs=1, nouts=0, tspan=0.0):
+        st = Stage(bcs, nincs, nouts)
+        st.tspan = float(tspan)
+        self.stages.append(st)
+
+    def solve(self, tol=0.01, dTmin=1e-7, dTmax=0.1, rspan=0.01, maxits=5, autoinc=False, alpha=0.0, beta=0.0,
+              solver="mixed", linear_rtol=1e-8, quiet=True):
+        """Returns (ok, message); dof values land in model.U, model.V, model.A, model.F (node-major)."""
+        if len(self.stages) != 1:
+            raise ValueError("a dynamic analysis has one stage (the reference defines V and A in the first only)")
+        stage = self.stages[0]
+        model = self.model
+        setup = model.configure_dofs(stage.bcs)
+        U0, F0 = model.get_bc_vals(setup, 0.0)
+        U1, F1 = model.get_bc_vals(setup, 1.0)
+        Uh, Fh = model.get_bc_vals(setup, 0.5)
+        dU, dF = U1 - U0, F1 - F0
+        for a, b, c in ((U0, dU, Uh), (F0, dF, Fh)):
+            if np.abs(a + 0.5 * b - c).max(initial=0.0) > 1e-12 * max(np.abs(c).max(initial=0.0), 1.0):
+                raise NotImplementedError("boundary values must be affine in time on the GPU path")
+        model.dev.set_density(model.rho)
+        method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
+        p = L.default_dyn_params(tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan, alpha=alpha, beta=beta,
+                                 tspan=stage.tspan, maxits=maxits, autoinc=int(autoinc), nincs=stage.nincs,
+                                 nouts=stage.nouts, linear=L.default_solve_opts(method=method, rtol=linear_rtol))
+        rc, U, V, A, F, st = model.dev.dyn_stage_run(U0, dU, F0, dF, p)
+        self.stats = st
+        if rc not in (0, -11):
+            return False, model.dev.last_error()
+        for name, vec in (("U", U), ("V", V), ("A", A), ("F", F)):
+            out = np.zeros((model.nnodes, model.ndim))
+            out[model.dof_node, model.dof_comp] = vec
+            setattr(model, name, out)
+        stage.status = "done" if rc == 0 else "failed"
+        return rc == 0, ("" if rc == 0 else model.dev.last_error())
 
 
 def _shift_setup(setup, noff, eoff):

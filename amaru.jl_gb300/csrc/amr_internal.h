@@ -106,6 +106,10 @@ struct amr_model {
     AmrBatch *batch = nullptr;
     AmrAmg *amg = nullptr;
     AmrRecovery *rec = nullptr;
+    // dynamics: element density (sorted order), the mass matrix on K's pattern and its keep bits
+    double *rho = nullptr;
+    double *M64 = nullptr;
+    uint16_t *Mkeep = nullptr;
     int64_t dofs_version = 0;       // bumped by every amr_set_dofs
     // per-part masks read by the element kernels while a batched stage runs (null otherwise)
     const int32_t *bp_elem_part = nullptr;  // sorted element -> part
@@ -160,6 +164,9 @@ void amr_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s);  
 void amr_stiffness(amr_model *m);                       // Kel + gather into K64/K32/Minv
 void amr_stiffness_elements(amr_model *m);              // Kel only (element kernels)
 void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2);  // K64 = a1 Ks + a2 K64, K32, Minv
+void amr_mass(amr_model *m);                            // mount_M: element masses gathered into M64 / Mkeep
+// K64 = Ks + s1 M + s2 (alpha M + beta Ks) (Ks may be null: K = 0), then K32, Minv
+void amr_dyn_combine(amr_model *m, const double *Ks, double s1, double s2, double alpha, double beta);
 void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm);  // node-major device vectors
 void amr_apply_dofs(amr_model *m);                      // masks after amr_set_dofs
 void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double *F_nm);  // F_nm += (device)
@@ -198,6 +205,9 @@ int amr_batch_stage(amr_model *m, const double *Uex_nm, const double *Fex_nm, co
                     double *F_nm, amr_stage_stats *stats);
 void amr_batch_part_stats(const amr_model *m, int64_t nparts, amr_stage_stats *out);
 void amr_autotune_model(amr_model *m, amr_tuning *out);
+// dyn.cu: dyn_stage_solver! on node-major device vectors; boundary values at time t are U0 + t U1, F0 + t F1
+int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const double *F0, const double *F1,
+                         const amr_dyn_params &p, double *U, double *V, double *A, double *F, amr_stage_stats *stats);
 // stage.cpp-equivalent (capi.cu)
 int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
                      double *U_nm, double *F_nm, amr_stage_stats *stats);

@@ -293,7 +293,7 @@ int amr_model_destroy(amr_model *m) {
     amr_free(m->bcol); amr_free(m->contrib_ptr); amr_free(m->contrib); amr_free(m->Kel); amr_free(m->K64);
     amr_free(m->K32); amr_free(m->keep); amr_free(m->Minv32); amr_free(m->Minv64); amr_free(m->eq_id);
     amr_free(m->free_mask); amr_free(m->dof_node); amr_free(m->st); amr_free(m->stbk); amr_free(m->Fel);
-    amr_free(m->fel_ptr); amr_free(m->d_status);
+    amr_free(m->fel_ptr); amr_free(m->d_status); amr_free(m->rho); amr_free(m->M64); amr_free(m->Mkeep);
     for (int i = 0; i < 8; i++) amr_free(m->vtmp[i]);
     if (m->h_status) cudaFreeHost(m->h_status);
     if (m->ev0) cudaEventDestroy(m->ev0);
@@ -390,15 +390,16 @@ int amr_assemble_K(amr_model *m) {
 }
 
 // Host export of K in the reference layout (CSC over eq_id order, eps drop rule)
-static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t *rowval, double *nzval) {
-    if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+// CSC of the block matrix vals (SoA, K's pattern) with the scalar entries its keep bits mark
+static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t *rowval, double *nzval,
+                       const uint16_t *d_keep, const double *d_vals) {
     int B = m->B, BB = m->BB;
     std::vector<uint16_t> keep(m->nblocks);
-    AMR_CUDA(cudaMemcpy(keep.data(), m->keep, m->nblocks * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    AMR_CUDA(cudaMemcpy(keep.data(), d_keep, m->nblocks * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     std::vector<double> K;
     if (nzval) {
         K.resize((size_t)m->bstride * BB);
-        AMR_CUDA(cudaMemcpy(K.data(), m->K64, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        AMR_CUDA(cudaMemcpy(K.data(), d_vals, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
     }
     const std::vector<int64_t> &eq = m->h_eq_id;
     // count per column (= per row of the symmetric pattern walk)
@@ -452,7 +453,8 @@ static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t 
 
 int amr_get_K_nnz(amr_model *m, int64_t *nnz) {
     return guarded(m, [&] {
-        export_csc(m, nnz, nullptr, nullptr, nullptr);
+        if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+        export_csc(m, nnz, nullptr, nullptr, nullptr, m->keep, m->K64);
         return AMR_OK;
     });
 }
@@ -460,7 +462,43 @@ int amr_get_K_nnz(amr_model *m, int64_t *nnz) {
 int amr_get_K_csc(amr_model *m, int64_t *colptr, int64_t *rowval, double *nzval) {
     return guarded(m, [&] {
         int64_t nnz = 0;
-        export_csc(m, &nnz, colptr, rowval, nzval);
+        if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+        export_csc(m, &nnz, colptr, rowval, nzval, m->keep, m->K64);
+        return AMR_OK;
+    });
+}
+
+int amr_set_density(amr_model *m, const double *rho) {
+    return guarded(m, [&] {
+        if (!rho) throw AmrError(AMR_EINVAL, "null argument");
+        std::vector<double> r(m->nelems);
+        for (int64_t e = 0; e < m->nelems; e++) {
+            if (!(rho[e] >= 0.0)) throw AmrError(AMR_EINVAL, "element " + std::to_string(e) + ": rho >= 0 required");
+            r[m->inv_perm[e]] = rho[e];
+        }
+        if (!m->rho) amr_alloc(&m->rho, m->nelems);
+        upload(m->rho, r.data(), m->nelems * sizeof(double), m->stream);
+        AMR_CUDA(cudaStreamSynchronize(m->stream));
+        return AMR_OK;
+    });
+}
+
+int amr_assemble_M(amr_model *m) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        amr_mass(m);
+        int rc = amr_check_status(m);
+        if (rc == AMR_ENEGJAC) throw AmrError(rc, "Negative Jacobian determinant in cell " + std::to_string(m->perm[m->h_status[1]] + 1));
+        if (rc) throw AmrError(rc, "mass assembly failed");
+        return AMR_OK;
+    });
+}
+
+int amr_get_M_csc(amr_model *m, int64_t *nnz, int64_t *colptr, int64_t *rowval, double *nzval) {
+    return guarded(m, [&] {
+        if (!nnz) throw AmrError(AMR_EINVAL, "null argument");
+        if (!m->M64) throw AmrError(AMR_EINVAL, "M has not been assembled");
+        export_csc(m, nnz, colptr, rowval, nzval, m->Mkeep, m->M64);
         return AMR_OK;
     });
 }
@@ -597,6 +635,45 @@ int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_
             throw;
         }
         amr_free(uex); amr_free(fex); amr_free(u); amr_free(f);
+        return rc;
+    });
+}
+
+void amr_default_dyn_params(amr_dyn_params *p) {
+    p->tol = 0.01; p->dTmin = 1e-7; p->dTmax = 0.1; p->rspan = 0.01;
+    p->alpha = 0.0; p->beta = 0.0; p->tspan = 0.0;
+    p->maxits = 5; p->autoinc = 0; p->nincs = 1; p->nouts = 0;
+    amr_default_solve_opts(&p->linear);
+}
+
+int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, const double *Fex0, const double *Fex1,
+                      const amr_dyn_params *p, double *U, double *V, double *A, double *F, amr_stage_stats *stats) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        if (!p || !Uex0 || !Uex1 || !Fex0 || !Fex1) throw AmrError(AMR_EINVAL, "null argument");
+        const int64_t n = m->nnodes * m->B;
+        std::vector<double *> d(8, nullptr);
+        auto release = [&]() {
+            for (auto &x : d) amr_free(x);
+        };
+        int rc;
+        try {
+            for (auto &x : d) amr_alloc(&x, n);
+            eq_host_to_nm(m, Uex0, d[0]);
+            eq_host_to_nm(m, Uex1, d[1]);
+            eq_host_to_nm(m, Fex0, d[2]);
+            eq_host_to_nm(m, Fex1, d[3]);
+            rc = amr_dyn_stage_device(m, d[0], d[1], d[2], d[3], *p, d[4], d[5], d[6], d[7], stats);
+            if (rc == AMR_OK || rc == AMR_ESTAGE) {
+                double *outs[4] = {U, V, A, F};
+                for (int i = 0; i < 4; i++)
+                    if (outs[i]) nm_to_eq_host(m, d[4 + i], outs[i]);
+            }
+        } catch (...) {
+            release();
+            throw;
+        }
+        release();
         return rc;
     });
 }

@@ -723,6 +723,106 @@ __global__ void combine_kernel(int64_t nnodes, int64_t nblocks, const int64_t *b
     }
 }
 
+// Kp = K + s1 M + s2 (alpha M + beta K): the pseudo-stiffness of the dynamic Newton loop
+// (src/mech/dyn-solver.jl:366-368, s1 = 4/dt^2, s2 = 2/dt), every product and sum rounded as the
+// reference's sparse operations; K absent (Ks null) gives s1 M + s2 alpha M, the mass matrix itself with
+// s1 = 1, s2 = 0.  Then the masked FP32 copy and block-Jacobi inverses of the result.
+template <int B>
+__global__ void dyn_combine_kernel(int64_t nnodes, int64_t nblocks, const int64_t *brow_ptr, const int32_t *bcol,
+                                   const double *Ks, const double *M64, double s1, double s2, double alpha,
+                                   double beta, const uint8_t *free_mask, double *K64, float *K32, float *Minv32,
+                                   double *Minv64, int32_t *status) {
+    constexpr int BB = B * B;
+    int lane = threadIdx.x & 31;
+    int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= nnodes) return;
+    uint8_t fr[B];
+#pragma unroll
+    for (int c = 0; c < B; c++) fr[c] = free_mask ? free_mask[n * B + c] : 1;
+    for (int64_t k = brow_ptr[n] + lane; k < brow_ptr[n + 1]; k += 32) {
+        double v[BB];
+        bool nan = false;
+#pragma unroll
+        for (int q = 0; q < BB; q++) {
+            const int64_t i = (int64_t)q * nblocks + k;
+            const double kk = Ks ? Ks[i] : 0.0, mm = M64[i];
+            const double c = __dadd_rn(__dmul_rn(alpha, mm), __dmul_rn(beta, kk));
+            v[q] = __dadd_rn(__dadd_rn(kk, __dmul_rn(s1, mm)), __dmul_rn(s2, c));
+            K64[i] = v[q];
+            nan |= isnan(v[q]);
+        }
+        if (nan) set_status(status, AMR_ENAN, -1);
+        finish_block<B>(n, k, bcol[k], nblocks, v, fr, free_mask, K32, Minv32, Minv64);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Element mass: elem_mass (src/mech/elem/mech-solid.jl:169-205).  EPB elements per CTA.  Phase 1,
+// thread per (element, IP): coef = rho detJ w th.  Phase 2, thread per (element, node pair a <= b):
+// m_ab = sum over the IPs of (coef N_a) N_b, written as the blocks m_ab I at (a,b) and (b,a) of the
+// staging array (N'N has no entry between different components).
+// ---------------------------------------------------------------------------
+template <int DIM, int NEN>
+__global__ void __launch_bounds__(256) mass_kernel(ModelArgs M, GroupArgs G, int epb, const double *rho,
+                                                   double *Kel, int32_t *status) {
+    constexpr int NP = NEN * (NEN + 1) / 2;
+    constexpr int BB = DIM * DIM;
+    extern __shared__ double sm[];
+    const int nip = G.nip;
+    double *sC = sm;                    // epb x NEN*DIM
+    double *sK = sC + epb * NEN * DIM;  // epb x nip
+    const int64_t e0 = G.first + (int64_t)blockIdx.x * epb;
+    const int ne = (int)min((int64_t)epb, G.first + G.count - e0);
+    const double *dNdR = G.tab;
+    const double *wq = G.tab + nip * NEN * DIM;
+    const double *Nt = wq + nip;
+    for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
+        int el = t / (NEN * DIM), q = t % (NEN * DIM);
+        int32_t node = M.conn[M.conn_ptr[e0 + el] + q / DIM];
+        sC[t] = M.coords[3 * (int64_t)node + q % DIM];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
+        const int el = t / nip, ip = t % nip;
+        const int64_t e = e0 + el;
+        const double *C = sC + el * NEN * DIM;
+        const double *D = dNdR + ip * NEN * DIM;
+        double J[DIM * DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; i++)
+#pragma unroll
+            for (int j = 0; j < DIM; j++) {
+                double s = 0.0;
+                for (int a = 0; a < NEN; a++) s += C[a * DIM + i] * D[a * DIM + j];
+                J[i * DIM + j] = s;
+            }
+        double det;
+        if (DIM == 2) det = J[0] * J[3] - J[1] * J[2];
+        else det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                   J[2] * (J[3] * J[7] - J[4] * J[6]);
+        if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
+        sK[el * nip + ip] = rho[e] * det * wq[ip] * M.thickness;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne * NP; t += blockDim.x) {
+        const int el = t / NP, p = t % NP;
+        int a = 0, rem = p;
+        while (rem >= NEN - a) { rem -= NEN - a; a++; }
+        const int b = a + rem;
+        double mab = 0.0;
+        for (int ip = 0; ip < nip; ip++) mab = fma(sK[el * nip + ip] * Nt[ip * NEN + a], Nt[ip * NEN + b], mab);
+        const int64_t base = M.kel_ptr[e0 + el];
+        double *o1 = Kel + (base + (int64_t)a * NEN + b) * BB;
+        double *o2 = Kel + (base + (int64_t)b * NEN + a) * BB;
+#pragma unroll
+        for (int q = 0; q < BB; q++) {
+            const double v = (q / DIM == q % DIM) ? mab : 0.0;
+            o1[q] = v;
+            o2[q] = v;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Internal forces with the constitutive update: thread per (element, IP).
 // ---------------------------------------------------------------------------
@@ -1026,6 +1126,55 @@ void amr_combine_K(amr_model *m, double a1, const double *Ks, double a2) {
         combine_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, a1, Ks, a2,
                                                        m->free_mask, m->K64, m->K32, m->Minv32, m->Minv64,
                                                        m->d_status);
+    AMR_COUNT(1);
+    AMR_CUDA(cudaGetLastError());
+    amr_amg_invalidate(m);
+}
+
+void amr_mass(amr_model *m) {
+    if (!m->rho) throw AmrError(AMR_EINVAL, "no density set (amr_set_density)");
+    if (!m->M64) {
+        amr_alloc(&m->M64, (size_t)m->bstride * m->BB);
+        amr_alloc(&m->Mkeep, m->nblocks);
+    }
+    for (const AmrGroup &g : m->groups) {
+        auto launch = [&](auto dim, auto nen) {
+            constexpr int DIM = decltype(dim)::value, NEN = decltype(nen)::value;
+            GroupArgs ga{g.tab, g.nip, g.first, g.count};
+            const int epb = 4;
+            const size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + g.nip);
+            mass_kernel<DIM, NEN><<<nblk(g.count, epb), 256, smem, m->stream>>>(margs(m), ga, epb, m->rho, m->Kel,
+                                                                                m->d_status);
+            AMR_COUNT(1);
+            AMR_CUDA(cudaGetLastError());
+        };
+        dispatch(
+            m, g, [&](auto n) { launch(std::integral_constant<int, 3>(), n); },
+            [&](auto n) { launch(std::integral_constant<int, 2>(), n); });
+    }
+    unsigned grid = nblk(m->nnodes * 32, 256);
+    if (m->B == 3)
+        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
+                                                      m->contrib, m->Kel, m->free_mask, m->M64, nullptr, m->Mkeep,
+                                                      nullptr, nullptr, m->d_status);
+    else
+        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
+                                                      m->contrib, m->Kel, m->free_mask, m->M64, nullptr, m->Mkeep,
+                                                      nullptr, nullptr, m->d_status);
+    AMR_COUNT(1);
+    AMR_CUDA(cudaGetLastError());
+}
+
+void amr_dyn_combine(amr_model *m, const double *Ks, double s1, double s2, double alpha, double beta) {
+    unsigned grid = nblk(m->nnodes * 32, 256);
+    if (m->B == 3)
+        dyn_combine_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, Ks, m->M64, s1,
+                                                           s2, alpha, beta, m->free_mask, m->K64, m->K32, m->Minv32,
+                                                           m->Minv64, m->d_status);
+    else
+        dyn_combine_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, Ks, m->M64, s1,
+                                                           s2, alpha, beta, m->free_mask, m->K64, m->K32, m->Minv32,
+                                                           m->Minv64, m->d_status);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
     amr_amg_invalidate(m);

@@ -324,6 +324,35 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
 /* Number of kernels this handle has launched since it was created. */
 int amr_launch_count(const amr_model *m, int64_t *count);
 
+/* ---- dynamics ----
+ * Element density (MechSolid props rho, src/mech/elem/mech-solid.jl:6-29), nelems values in the
+ * caller's element order. */
+int amr_set_density(amr_model *m, const double *rho);
+/* mount_M (src/mech/dyn-solver.jl:71-104) over elem_mass (src/mech/elem/mech-solid.jl:169-205):
+ * |M_ij| >= eps() entries summed in element order, on K's block pattern.  Needs amr_set_dofs. */
+int amr_assemble_M(amr_model *m);
+/* M as CSC (0-based, rows sorted): *nnz always; colptr/rowval/nzval filled when colptr is non-null. */
+int amr_get_M_csc(amr_model *m, int64_t *nnz, int64_t *colptr, int64_t *rowval, double *nzval);
+
+/* dyn_solver_params (src/mech/dyn-solver.jl:166-186) and the stage's tspan. */
+typedef struct {
+    double tol, dTmin, dTmax, rspan;
+    double alpha, beta;      /* Rayleigh damping C = alpha M + beta K */
+    double tspan;            /* time span of the stage (Stage.tspan), > 0 */
+    int32_t maxits, autoinc, nincs, nouts;
+    amr_solve_opts linear;   /* the Krylov solve of each Newton iteration */
+} amr_dyn_params;
+
+/* dyn_stage_solver! (src/mech/dyn-solver.jl:203-534) of a first stage: M A0 = Fex(0), then
+ * Newmark's average-acceleration rule with the reference's Newton loop and increment control.
+ * Boundary values at time t: Uex(t) = Uex0 + t Uex1, Fex(t) = Fex0 + t Fex1 (eq_id order, ndofs each;
+ * get_bc_vals of affine time functions).  Out (eq_id order, ndofs each, may be null): U (the stage's
+ * displacements), V, A, F (TFin, dof.vals[fs]).  AMR_ESTAGE when an increment fails without autoinc
+ * or below dTmin with it. */
+int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, const double *Fex0, const double *Fex1,
+                      const amr_dyn_params *p, double *U, double *V, double *A, double *F, amr_stage_stats *stats);
+void amr_default_dyn_params(amr_dyn_params *p);
+
 /* ---- output recovery ----
  * Nodal values of the IP fields: replaces nodal_patch_recovery (src/fe-model.jl:504-702)
  * as called by update_output_data! (:341-427) and get_node_and_elem_vals (:430-485).

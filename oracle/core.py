@@ -475,6 +475,7 @@ class FEModel:
         ne = len(mesh.elems)
         self.mat_type = np.full(ne, -1, dtype=np.int32)
         self.mat_par = np.zeros((ne, 8))
+        self.rho = np.zeros(ne)  # element density (MechSolid props rho, src/mech/elem/mech-solid.jl:6-29)
         for filt, mat in matbinds:
             if isinstance(filt, str) and not any(ch in filt for ch in "=<>"):
                 sel = [c for c in mesh.elems if filt in ("all", c.tag)]
@@ -483,6 +484,7 @@ class FEModel:
             for c in sel:
                 self.mat_type[c.id] = mat.kind
                 self.mat_par[c.id] = mat.params()
+                self.rho[c.id] = mat.p.get("rho", 0.0)
         if (self.mat_type < 0).any():
             raise ValueError("elements without material")
         if elem_E is not None:
