@@ -22,7 +22,7 @@ LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
 LOAD_FACET, LOAD_BODY = 0, 1
 SOLVER_MIXED, SOLVER_FP64, SOLVER_AMG = 0, 1, 2
 ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
-KERNEL_SPMV32, KERNEL_RESIDUAL64, KERNEL_AMG_RESIDUAL = 0, 1, 5
+KERNEL_SPMV32, KERNEL_RESIDUAL64, KERNEL_AMG_RESIDUAL, KERNEL_DYN_RHS = 0, 1, 5, 6
 
 
 class AmrError(RuntimeError):

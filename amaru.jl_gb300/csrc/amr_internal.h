@@ -208,6 +208,7 @@ void amr_autotune_model(amr_model *m, amr_tuning *out);
 // dyn.cu: dyn_stage_solver! on node-major device vectors; boundary values at time t are U0 + t U1, F0 + t F1
 int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const double *F0, const double *F1,
                          const amr_dyn_params &p, double *U, double *V, double *A, double *F, amr_stage_stats *stats);
+double amr_dyn_time_rhs(amr_model *m, int reps, double *bytes);
 // stage.cpp-equivalent (capi.cu)
 int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
                      double *U_nm, double *F_nm, amr_stage_stats *stats);

@@ -795,6 +795,9 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
             t = amr_amg_time_residual(m, reps);
             bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 3.0;
             break;
+        case AMR_KERNEL_DYN_RHS:
+            t = amr_dyn_time_rhs(m, reps, &bytes);
+            break;
         default:
             throw AmrError(AMR_EINVAL, "kernel not timed by this entry point");
         }

@@ -10,7 +10,7 @@
 //
 // Device layout: node-major FP64 vectors (nnodes x B) as in the static stage; M64 on K's block
 // pattern; K kept in Ks while K64 holds Kp for the solver.  C is never stored: the SpMV forms
-// alpha M_ij + beta K_ij per entry, rounded as the reference's sparse C.  For state-independent K
+// C y = alpha (M y) + beta (K y).  For state-independent K
 // (no plastic material) K is mounted once per stage and Kp only when dt changes: the reference mounts
 // both at every iteration, with the same values.
 #include <algorithm>
@@ -24,47 +24,57 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// out = base + M x + C y with C_ij = alpha M_ij + beta K_ij (K may be null); warp per node row
+// out = base + M x + C y with C = alpha M + beta K (K may be null); warp per node row.  Every block of
+// M is m_ab I (elem_mass has no entry between components, and the three diagonal components of a block
+// sum the same contributions in the same order), so the kernel reads component (0,0) of M only and forms
+// C y as alpha (M y) + beta (K y) per row; with beta = 0 it reads no K.
+constexpr int kRowLanes = 4;  // lanes per block row; the warp's rows share the reduction steps
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_dyn_rhs(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
                                                       const int32_t *__restrict__ cj, const double *__restrict__ M,
                                                       const double *__restrict__ K, double alpha, double beta,
                                                       const double *__restrict__ base, const double *__restrict__ x,
                                                       const double *__restrict__ y, double *__restrict__ out) {
-    const int lane = threadIdx.x & 31;
+    constexpr int RPW = 32 / kRowLanes;
+    const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t n = warp; n < nn; n += nw) {
-        double acc[B];
+    const bool useK = K && beta != 0.0;
+    for (int64_t n0 = warp * RPW; n0 < nn; n0 += nw * RPW) {  // whole warps: every lane reaches the shuffles
+        const int64_t n = n0 + lane / kRowLanes;
+        const bool valid = n < nn;
+        double mx[B], my[B], ky[B];
 #pragma unroll
-        for (int c = 0; c < B; c++) acc[c] = 0.0;
-        for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
-            const int64_t j = cj[k];
-            double xj[B], yj[B];
-#pragma unroll
-            for (int d = 0; d < B; d++) { xj[d] = x[j * B + d]; yj[d] = y[j * B + d]; }
-#pragma unroll
-            for (int c = 0; c < B; c++)
+        for (int c = 0; c < B; c++) mx[c] = my[c] = ky[c] = 0.0;
+        if (valid)
+            for (int64_t k = rp[n] + sub; k < rp[n + 1]; k += kRowLanes) {
+                const int64_t j = cj[k];
+                const double m = M[k];
+                double yj[B];
 #pragma unroll
                 for (int d = 0; d < B; d++) {
-                    const int64_t i = (int64_t)(c * B + d) * nb + k;
-                    const double mm = M[i], kk = K ? K[i] : 0.0;
-                    const double cc = __dadd_rn(__dmul_rn(alpha, mm), __dmul_rn(beta, kk));
-                    acc[c] = fma(mm, xj[d], acc[c]);
-                    acc[c] = fma(cc, yj[d], acc[c]);
+                    yj[d] = y[j * B + d];
+                    mx[d] = fma(m, x[j * B + d], mx[d]);
+                    my[d] = fma(m, yj[d], my[d]);
                 }
-        }
+                if (useK)
 #pragma unroll
-        for (int c = 0; c < B; c++) acc[c] = warp_sum(acc[c]);
-        if (lane == 0)
+                    for (int c = 0; c < B; c++)
 #pragma unroll
-            for (int c = 0; c < B; c++) out[n * B + c] = base[n * B + c] + acc[c];
+                        for (int d = 0; d < B; d++) ky[c] = fma(K[(int64_t)(c * B + d) * nb + k], yj[d], ky[c]);
+            }
+#pragma unroll
+        for (int c = 0; c < B; c++)
+#pragma unroll
+            for (int o = kRowLanes / 2; o > 0; o >>= 1) {
+                mx[c] += __shfl_xor_sync(0xffffffffu, mx[c], o);
+                my[c] += __shfl_xor_sync(0xffffffffu, my[c], o);
+                if (useK) ky[c] += __shfl_xor_sync(0xffffffffu, ky[c], o);
+            }
+        if (valid && sub == 0)
+#pragma unroll
+            for (int c = 0; c < B; c++)
+                out[n * B + c] = base[n * B + c] + (mx[c] + (alpha * my[c] + beta * ky[c]));
     }
 }
 
@@ -334,4 +344,39 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
     release();
     if (stats) *stats = st;
     return status;
+}
+
+// Average device time of k_dyn_rhs with both matrices read (beta != 0, K64 as the K operand) and its
+// algorithmic bytes: per block the (0,0) component of M, the 9 (4) components of K and the column index;
+// per node the row pointer and x, y, base read and out written once.
+double amr_dyn_time_rhs(amr_model *m, int reps, double *bytes) {
+    if (!m->M64) throw AmrError(AMR_EINVAL, "assemble M first");
+    const int64_t n = m->nnodes * m->B;
+    std::vector<double *> v(4, nullptr);
+    auto release = [&]() {
+        for (auto &x : v) amr_free(x);
+    };
+    double sec = 0.0;
+    try {
+        for (auto &x : v) {
+            amr_alloc(&x, n);
+            AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), m->stream));
+        }
+        rhs(m, m->K64, 0.5, 1e-4, v[0], v[1], v[2], v[3]);
+        AMR_CUDA(cudaEventRecord(m->ev0, m->stream));
+        for (int r = 0; r < reps; r++) rhs(m, m->K64, 0.5, 1e-4, v[0], v[1], v[2], v[3]);
+        AMR_CUDA(cudaEventRecord(m->ev1, m->stream));
+        AMR_CUDA(cudaEventSynchronize(m->ev1));
+        float ms = 0.f;
+        AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        sec = ms * 1e-3 / std::max(1, reps);
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+    if (bytes)
+        *bytes = (double)m->nblocks * (8.0 + 8.0 * m->BB + 4.0) + (double)(m->nnodes + 1) * 8.0 +
+                 4.0 * 8.0 * (double)n;
+    return sec;
 }

@@ -310,7 +310,11 @@ __global__ void __launch_bounds__(kThreads) k_rz32(int64_t nn, const float *__re
 }
 
 // FP64 true residual: u64 += x32 (free slots), x32 = 0; r64 = mask(b - K64 u64);
-// reac = (K64 u64) at prescribed slots; r32 = r64; z = Minv r32 ; rz, |r64|^2
+// reac = (K64 u64) at prescribed slots; r32 = r64; z = Minv r32 ; rz, |r64|^2.
+// kRowLanes lanes per block row, 32 / kRowLanes rows per warp: the FP64 pipe, not HBM, bounds this
+// kernel on GB300, and a row's three sums reduce in log2(kRowLanes) shuffle steps shared by the
+// warp's rows.  The row loop advances whole warps so every lane reaches the shuffles.
+constexpr int kRowLanes = 4;
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_refine(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
                                                      const int32_t *__restrict__ cj, const double *__restrict__ A,
@@ -319,24 +323,30 @@ __global__ void __launch_bounds__(kThreads) k_refine(int64_t nn, int64_t nb, con
                                                      float *__restrict__ r32, float *__restrict__ z,
                                                      const float *__restrict__ Minv, Ctl *ctl, double *partials,
                                                      int first, double tol2) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    constexpr int RPW = 32 / kRowLanes;
+    const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double rz = 0.0, rr = 0.0;
-    for (int64_t n = warp; n < nn; n += nw) {
+    for (int64_t n0 = warp * RPW; n0 < nn; n0 += nw * RPW) {
+        const int64_t n = n0 + lane / kRowLanes;
+        const bool valid = n < nn;
         double acc[B];
 #pragma unroll
         for (int c = 0; c < B; c++) acc[c] = 0.0;
-        for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
-            int64_t j = cj[k];
+        if (valid)
+            for (int64_t k = rp[n] + sub; k < rp[n + 1]; k += kRowLanes) {
+                int64_t j = cj[k];
 #pragma unroll
-            for (int c = 0; c < B; c++)
+                for (int c = 0; c < B; c++)
 #pragma unroll
-                for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u64[j * B + d], acc[c]);
-        }
+                    for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u64[j * B + d], acc[c]);
+            }
 #pragma unroll
-        for (int c = 0; c < B; c++) acc[c] = warp_sum(acc[c]);
-        if (lane == 0) {
+        for (int c = 0; c < B; c++)
+#pragma unroll
+            for (int o = kRowLanes / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+        if (valid && sub == 0) {
             float rv[B];
 #pragma unroll
             for (int c = 0; c < B; c++) {

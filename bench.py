@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-models measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-recovery", action="store_true", help="skip the nodal recovery measurement")
+    ap.add_argument("--no-dyn", action="store_true", help="skip the dynamic (Newmark) stage measurement")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--slope", default="", help="also run the TET10 slope stage at these divisions, e.g. 100x17x40")
     return ap.parse_args()
@@ -277,6 +278,8 @@ def run_ours(a):
     }
     if not a.no_recovery:
         out["recovery"] = recovery_leg(model, rank == 0 and not a.no_cpu)
+    if not a.no_dyn:
+        out["dynamic"] = dyn_leg(model, rank == 0 and not a.no_cpu)
     if not a.no_batch:
         out["batch"] = batch_leg()
     if not a.no_serve:
@@ -346,6 +349,66 @@ def recovery_cpu_sample(n=(8, 4, 4)):
     return {"value": om.nnodes / dt, "unit": "nodes/s", "cores": 1, "kind": "port",
             "sample": "oracle nodal_patch_recovery (Python/numpy restatement) on HEX20 %dx%dx%d, 27 IP, %d nodes: "
                       "%.2f s" % (n[0], n[1], n[2], om.nnodes, dt)}
+
+
+# ---------------------------------------------------------------------------
+# Dynamic stage (dyn_stage_solver!) on the bench model: density 2.4e-3, base fixed, the top pressure
+# applied suddenly, Rayleigh damping alpha = 0.5, beta = 1e-4, tspan 0.01 in 5 increments, the
+# multigrid-preconditioned solve to 1e-8.  value = DOFs x increments per second of device time; e2e the
+# same through the host-buffer call.  The CPU baseline runs the oracle's restatement on a HEX20 6x3x3
+# block of the same family.
+# ---------------------------------------------------------------------------
+DYN = dict(rho=2.4e-3, alpha=0.5, beta=1e-4, tspan=0.01, nincs=5)
+
+
+def dyn_leg(model, with_cpu):
+    import amaru_gpu as A
+    from amaru_gpu import _lib as L
+    model.rho[:] = DYN["rho"]
+    bcs = [("z==0", A.SurfaceBC(ux=0, uy=0, uz=0)), ("z==4", A.SurfaceBC(tz=-1.0))]
+    runs = []
+    for _ in range(2):  # the first run includes the multigrid set-up of the new pseudo-stiffness
+        ana = A.DynAnalysis(model)
+        ana.addstage(bcs, tspan=DYN["tspan"], nincs=DYN["nincs"])
+        t0 = time.perf_counter()
+        ok, msg = ana.solve(solver="amg", linear_rtol=1e-8, alpha=DYN["alpha"], beta=DYN["beta"])
+        wall = time.perf_counter() - t0
+        if not ok:
+            raise RuntimeError("dynamic stage failed: " + msg)
+        runs.append((ana.stats, wall))
+    st, wall = runs[-1]
+    nd = model.ndofs
+    rhs_t, rhs_b = model.dev.time_kernel(L.KERNEL_DYN_RHS, 20)
+    out = {"workload": "bench HEX20 model, rho %g, Rayleigh (%g, %g), tspan %g in %d increments, multigrid PCG "
+                       "to 1e-8" % (DYN["rho"], DYN["alpha"], DYN["beta"], DYN["tspan"], DYN["nincs"]),
+           "ndofs": nd, "increments": st.increments, "newton_iterations": st.iterations,
+           "krylov_iterations": st.krylov_iterations, "device_s": st.seconds, "solve_s": st.solve_seconds,
+           "value": nd * st.increments / st.seconds, "unit": "DOF-increments/s",
+           "e2e": {"value": nd * st.increments / wall, "unit": "DOF-increments/s", "s": wall,
+                   "h2d_bytes": 4 * nd * 8, "d2h_bytes": 4 * nd * 8},
+           "rhs_kernel": {"kernel": "k_dyn_rhs<3> (base + M x + (alpha M + beta K) y)", "avg_launch_s": rhs_t,
+                          "bytes_per_launch": rhs_b, "achieved_gbs": rhs_b / rhs_t / 1e9}}
+    if with_cpu:
+        out["cpu_baseline"] = dyn_cpu_sample()
+    return out
+
+
+def dyn_cpu_sample(n=(6, 3, 3)):
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    mo = O.Mesh(O.Block([[0, 0, 0], [10.0 * n[0] / 100, 4.0 * n[1] / 40, 4.0 * n[2] / 40]], nx=n[0], ny=n[1],
+                        nz=n[2], cellshape=O.HEX20))
+    om = O.FEModel(mo, [("all", O.LinearElastic(E=30e3, nu=0.2, rho=DYN["rho"]))], nips=27)
+    top = 4.0 * n[2] / 40
+    ana = O.DynAnalysis(om)
+    ana.addstage([("z==0", O.SurfaceBC(ux=0, uy=0, uz=0)), ("z==%r" % top, O.SurfaceBC(tz=-1.0))],
+                 tspan=DYN["tspan"], nincs=DYN["nincs"])
+    t0 = time.perf_counter()
+    ok, _ = ana.solve(alpha=DYN["alpha"], beta=DYN["beta"])
+    dt = time.perf_counter() - t0
+    return {"value": ana.ndofs * ana.increments / dt, "unit": "DOF-increments/s", "cores": 1, "kind": "port",
+            "sample": "oracle dyn_stage_solver! (C element kernels, Python mount_M, SuperLU) on HEX20 %dx%dx%d, "
+                      "%d DOFs, %d increments: %.2f s" % (n[0], n[1], n[2], ana.ndofs, ana.increments, dt)}
 
 
 # ---------------------------------------------------------------------------

@@ -319,7 +319,8 @@ int amr_autotune(amr_model *m, amr_tuning *out);
  * timed with CUDA events on the handle's stream, and its algorithmic bytes
  * per launch.  Needs a preceding amr_assemble_K (and a solve for the SpMV). */
 enum { AMR_KERNEL_SPMV32 = 0, AMR_KERNEL_RESIDUAL64 = 1, AMR_KERNEL_STIFFNESS = 2, AMR_KERNEL_GATHER = 3,
-       AMR_KERNEL_INTERNAL = 4, AMR_KERNEL_AMG_RESIDUAL = 5 /* the multigrid cycle's fine residual; after an AMG solve */ };
+       AMR_KERNEL_INTERNAL = 4, AMR_KERNEL_AMG_RESIDUAL = 5 /* the multigrid cycle's fine residual; after an AMG solve */,
+       AMR_KERNEL_DYN_RHS = 6 /* base + M x + C y of the dynamic Newton loop; after amr_assemble_M */ };
 int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch);
 /* Number of kernels this handle has launched since it was created. */
 int amr_launch_count(const amr_model *m, int64_t *count);
