@@ -251,6 +251,67 @@ function solve_gpu!(ana::MechAnalysis; linear::Symbol=:amg, args...)
 end
 
 # ---------------------------------------------------------------------------
+# Dynamic analyses: dyn_stage_solver! (src/mech/dyn-solver.jl:203-534) on the device.
+# ---------------------------------------------------------------------------
+struct DynParams
+    tol::Float64; dTmin::Float64; dTmax::Float64; rspan::Float64
+    alpha::Float64; beta::Float64; tspan::Float64
+    maxits::Int32; autoinc::Int32; nincs::Int32; nouts::Int32
+    linear::SolveOpts
+end
+
+"""
+    gpu_dyn_stage_solver!(ana::DynamicAnalysis, stage::Stage; args...)
+
+dyn_stage_solver! of a first stage with K, M, the solves and the IP states on the
+device.  Boundary values come from Amaru's get_bc_vals at t = 0 and t = 1 (they must
+be affine in t); ux/fx/vx/ax land in dof.vals as the reference writes them
+(src/mech/dyn-solver.jl:420-425).
+"""
+function gpu_dyn_stage_solver!(ana::DynamicAnalysis, stage::Stage; args...)
+    args = NamedTuple(args)
+    model = ana.model
+    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
+    dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
+    model.ndofs = length(dofs)
+    set_dofs!(g, model, dofs, nu)
+    rho = Float64[ elem.props.ρ for elem in model.elems ]
+    check(g, ccall((:amr_set_density, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, rho))
+    U0, F0 = Amaru.get_bc_vals(model, stage.bcs, 0.0)
+    U1, F1 = Amaru.get_bc_vals(model, stage.bcs, 1.0)
+    lin = SolveOpts(LINEAR_METHOD[], 1e-8, 20000, 32)
+    p = DynParams(args.tol, args.dTmin, args.dTmax, args.rspan, args.alpha, args.beta, stage.tspan,
+                  args.maxits, args.autoinc, stage.nincs, stage.nouts, lin)
+    n = length(dofs)
+    U, V, A, F = zeros(n), zeros(n), zeros(n), zeros(n)
+    stats = StageStats()
+    rc = ccall((:amr_dyn_stage_run, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{DynParams},
+                Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{StageStats}),
+               g.h, U0, U1 .- U0, F0, F1 .- F0, p, U, V, A, F, stats)
+    if rc == 0 || rc == -11
+        keys = Dict(:ux => (:ux, :fx, :vx, :ax), :uy => (:uy, :fy, :vy, :ay), :uz => (:uz, :fz, :vz, :az))
+        for (i, dof) in enumerate(dofs)
+            us, fs, vs, as = keys[dof.name]
+            dof.vals[us] = U[i]; dof.vals[fs] = F[i]; dof.vals[vs] = V[i]; dof.vals[as] = A[i]
+        end
+    end
+    rc == 0 && return Amaru.success()
+    return check(g, rc)
+end
+
+"""
+    solve_gpu!(ana::DynamicAnalysis; linear=:amg, args...)
+
+solve! of a dynamic analysis (dyn_solver_params) with gpu_dyn_stage_solver!.
+"""
+function solve_gpu!(ana::DynamicAnalysis; linear::Symbol=:amg, args...)
+    LINEAR_METHOD[] = linear === :jacobi ? Int32(0) : Int32(2)
+    args = Amaru.checkargs(args, Amaru.dyn_solver_params)
+    return Amaru.stage_iterator!(gpu_dyn_stage_solver!, ana; args...)
+end
+
+# ---------------------------------------------------------------------------
 # Output data: nodal_patch_recovery (src/fe-model.jl:504-702) on the device.
 # ---------------------------------------------------------------------------
 const FIELD_SYMBOLS = [:σxx, :σyy, :σzz, :σyz, :σxz, :σxy, :σvm, :σ1, :σ2, :σ3,
@@ -496,6 +557,6 @@ function wait!(srv::GPUServer, id::Integer)
 end
 
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
-       nodal_patch_recovery_gpu, has_gpu
+       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!
 
 end # module
