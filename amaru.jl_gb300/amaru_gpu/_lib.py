@@ -80,6 +80,15 @@ class DynParams(C.Structure):
                 ("autoinc", C.c_int32), ("nincs", C.c_int32), ("nouts", C.c_int32), ("linear", SolveOpts)]
 
 
+class ModalParams(C.Structure):
+    _fields_ = [("nmodes", C.c_int32), ("max_iters", C.c_int32), ("tol", C.c_double)]
+
+
+class ModalStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("block", C.c_int32), ("max_residual", C.c_double),
+                ("seconds", C.c_double)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int32), ("pad", C.c_int32)]
 
@@ -146,6 +155,8 @@ SIGNATURES = {
     "amr_get_M_csc": (C.c_int, [P, C.POINTER(C.c_int64), P, P, P]),
     "amr_dyn_stage_run": (C.c_int, [P, P, P, P, P, C.POINTER(DynParams), P, P, P, P, C.POINTER(StageStats)]),
     "amr_default_dyn_params": (None, [C.POINTER(DynParams)]),
+    "amr_modal_run": (C.c_int, [P, C.POINTER(ModalParams), P, P, C.POINTER(ModalStats)]),
+    "amr_default_modal_params": (None, [C.POINTER(ModalParams)]),
     "amr_recovery_fields": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
     "amr_recover_nodal": (C.c_int, [P, P]),
     "amr_recover_nodal_dev": (C.c_int, [P, P]),
@@ -405,6 +416,17 @@ class DeviceModel:
         rc = lib().amr_dyn_stage_run(self.h, *[ptr(a) for a in ins], C.byref(params), *[ptr(a) for a in outs],
                                      C.byref(st))
         return (rc, *outs, st)
+
+    def modal(self, nmodes=5, tol=1e-7, max_iters=1000):
+        """mech_modal_solver!: (omega (nmodes), modes (nu x nmodes), stats)."""
+        p = ModalParams()
+        lib().amr_default_modal_params(C.byref(p))
+        p.nmodes, p.tol, p.max_iters = nmodes, tol, max_iters
+        w = np.zeros(nmodes)
+        V = np.zeros((nmodes, self.nu))
+        st = ModalStats()
+        check(self.h, lib().amr_modal_run(self.h, C.byref(p), ptr(w), ptr(V), C.byref(st)))
+        return w, V.T.copy(), st
 
     def recovery_fields(self):
         """Field names of the nodal recovery, in the reference's column order."""

@@ -437,6 +437,30 @@ class DynAnalysis:
         return rc == 0, ("" if rc == 0 else model.dev.last_error())
 
 
+class ModalAnalysis:
+    """MechModalAnalysis(model) (src/mech/mech-modal-solver.jl:12-55) with addstage! and solve!(; nmodes):
+    the frequencies (freqs, rad/s) and modes (nu x nmodes) of mech_modal_solver! on the device."""
+
+    def __init__(self, model):
+        self.model = model
+        self.stages = []
+        self.freqs = np.zeros(0)
+        self.modes = np.zeros((0, 0))
+        self.stats = None
+
+    def addstage(self, bcs, nincs=1, nouts=0):
+        self.stages.append(Stage(bcs, nincs, nouts))
+
+    def solve(self, nmodes=5, tol=1e-7, max_iters=1000, quiet=True):
+        model = self.model
+        for stage in self.stages:
+            model.configure_dofs(stage.bcs)
+            model.dev.set_density(model.rho)
+            self.freqs, self.modes, self.stats = model.dev.modal(nmodes, tol, max_iters)
+            stage.status = "done"
+        return True, ""
+
+
 def _shift_setup(setup, noff, eoff):
     """A part's BC selections in the joined model's node and element numbering."""
     def sh(a):

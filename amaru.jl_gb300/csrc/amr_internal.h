@@ -209,6 +209,8 @@ void amr_autotune_model(amr_model *m, amr_tuning *out);
 int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const double *F0, const double *F1,
                          const amr_dyn_params &p, double *U, double *V, double *A, double *F, amr_stage_stats *stats);
 double amr_dyn_time_rhs(amr_model *m, int reps, double *bytes);
+// modal.cu: omega (host, nmodes) and P's eigenvectors (device, node-major columns, not normalised)
+int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, double *d_modes_nm, amr_modal_stats *stats);
 // stage.cpp-equivalent (capi.cu)
 int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
                      double *U_nm, double *F_nm, amr_stage_stats *stats);

@@ -678,6 +678,45 @@ int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, cons
     });
 }
 
+void amr_default_modal_params(amr_modal_params *p) {
+    p->nmodes = 5;
+    p->max_iters = 1000;
+    p->tol = 1e-7;
+}
+
+int amr_modal_run(amr_model *m, const amr_modal_params *p, double *omega, double *modes, amr_modal_stats *stats) {
+    return guarded(m, [&] {
+        check_dofs(m);
+        if (!p || !omega) throw AmrError(AMR_EINVAL, "null argument");
+        const int nm = p->nmodes;
+        const int64_t n = m->nnodes * m->B;
+        double *d = nullptr;
+        amr_alloc(&d, (size_t)n * std::max(1, nm));
+        int rc;
+        try {
+            rc = amr_modal_device(m, *p, omega, d, stats);
+            if (modes) {
+                std::vector<double> eq(m->ndofs);
+                for (int c = 0; c < nm; c++) {
+                    nm_to_eq_host(m, d + (size_t)c * n, eq.data());
+                    double nrm = 0.0, big = 0.0;
+                    for (int64_t i = 0; i < m->nu; i++) {
+                        nrm += eq[i] * eq[i];
+                        if (std::fabs(eq[i]) > std::fabs(big)) big = eq[i];
+                    }
+                    const double sc = (big < 0 ? -1.0 : 1.0) / std::sqrt(nrm);
+                    for (int64_t i = 0; i < m->nu; i++) modes[(size_t)c * m->nu + i] = eq[i] * sc;
+                }
+            }
+        } catch (...) {
+            amr_free(d);
+            throw;
+        }
+        amr_free(d);
+        return rc;
+    });
+}
+
 int amr_stage_run_dev(amr_model *m, const double *d_Uex, const double *d_Fex, const amr_stage_params *p,
                       double *d_U, double *d_F, amr_stage_stats *stats) {
     return guarded(m, [&] {

@@ -354,6 +354,26 @@ int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, cons
                       const amr_dyn_params *p, double *U, double *V, double *A, double *F, amr_stage_stats *stats);
 void amr_default_dyn_params(amr_dyn_params *p);
 
+/* ---- modal analysis ----
+ * mech_modal_solver! (src/mech/mech-modal-solver.jl:72-235): the nmodes eigenpairs of smallest
+ * magnitude of P = K11 ./ sum(M11, dims=1) (K11, M11 on the unknown DOFs), as Arpack's
+ * eigs(P, which=:SM) returns them after the reference's filter: omega = sqrt(lambda) ascending and P's
+ * eigenvectors, unit 2-norm, the largest entry positive.  Solved as the symmetric-definite pencil
+ * diag(L) phi = (1/lambda) K11 phi by LOBPCG with the multigrid V-cycle as preconditioner.
+ * Needs amr_set_dofs and amr_set_density (every element rho > 0). */
+typedef struct {
+    int32_t nmodes;          /* default 5, at most 10 */
+    int32_t max_iters;       /* LOBPCG iterations (default 1000) */
+    double tol;              /* relative residual of every wanted pair (default 1e-7) */
+} amr_modal_params;
+typedef struct {
+    int32_t iterations, block;
+    double max_residual, seconds;
+} amr_modal_stats;
+/* omega: nmodes values; modes: nu x nmodes, column-major, in eq_id order (may be null). */
+int amr_modal_run(amr_model *m, const amr_modal_params *p, double *omega, double *modes, amr_modal_stats *stats);
+void amr_default_modal_params(amr_modal_params *p);
+
 /* ---- output recovery ----
  * Nodal values of the IP fields: replaces nodal_patch_recovery (src/fe-model.jl:504-702)
  * as called by update_output_data! (:341-427) and get_node_and_elem_vals (:430-485).

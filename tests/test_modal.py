@@ -1,0 +1,101 @@
+"""Modal analysis: mech_modal_solver! (src/mech/mech-modal-solver.jl:72-235).
+
+The reference takes the nmodes eigenpairs of smallest magnitude of P = K11 ./ L (L the row-sum lumped
+masses of M11) with Arpack and keeps the real positive ones; its modal test (test/dynamic/modal.jl)
+has no assertion.  The oracle solves the equivalent symmetric-definite pencil diag(L) phi = mu K11 phi
+and is pinned against the reference's own formulation, the dense non-symmetric P and numpy's eig, on
+linear and serendipity cells (whose corner masses are negative).  The CUDA path (amr_modal_run,
+LOBPCG with the multigrid preconditioner) is compared with the oracle: frequencies, and modes up to the
+span of degenerate groups; at larger size through the eigen-residual of P.
+"""
+import numpy as np
+import pytest
+
+import amaru_gpu as A
+import oracle as O
+
+CASES = [(A.QUAD4, (4, 40), 0), (A.QUAD8, (3, 20), 0), (A.HEX8, (2, 12, 2), 0), (A.HEX20, (2, 8, 2), 27),
+         (A.TET10, (1, 5, 1), 0)]
+
+
+def _mesh(M, shape, n):
+    if len(n) == 2:
+        return M.Mesh(M.Block([[0, 0], [1.0, 10.0]], nx=n[0], ny=n[1], cellshape=shape))
+    return M.Mesh(M.Block([[0, 0, 0], [1.0, 10.0, 1.0]], nx=n[0], ny=n[1], nz=n[2], cellshape=shape))
+
+
+def _bcs(M, ndim):
+    return [("y==0", M.NodeBC(ux=0, uy=0) if ndim == 2 else M.NodeBC(ux=0, uy=0, uz=0))]
+
+
+MAT = dict(E=2e6, nu=0.2, rho=15.0)  # test/dynamic/modal.jl
+
+
+def _same_modes(Va, Vb, w, tol):
+    """Modes agree up to the span of each group of equal frequencies."""
+    i = 0
+    while i < len(w):
+        j = i + 1
+        while j < len(w) and abs(w[j] - w[i]) <= 1e-6 * w[i]:
+            j += 1
+        Q, _ = np.linalg.qr(Va[:, i:j])
+        res = Vb[:, i:j] - Q @ (Q.T @ Vb[:, i:j])
+        if np.abs(res).max() > tol:
+            return False
+        i = j
+    return True
+
+
+@pytest.mark.parametrize("shape, n, nips", CASES)
+def test_oracle_pencil_matches_the_dense_P_formulation(shape, n, nips):
+    om = O.FEModel(_mesh(O, shape, n), [("all", O.LinearElastic(**MAT))],
+                   stressmodel="planestrain" if len(n) == 2 else "d3", nips=nips)
+    w, V, _ = O.modal(om, _bcs(O, len(n)), 6)
+    wd, Vd, _ = O.modal_dense(om, _bcs(O, len(n)), 6)
+    assert np.abs(w - wd).max() <= 1e-9 * w.max()
+    assert _same_modes(V, Vd, w, 1e-7)
+
+
+def test_oracle_refuses_zero_density():
+    om = O.FEModel(_mesh(O, O.QUAD4, (2, 4)), [("all", O.LinearElastic(E=1.0, nu=0.2))], stressmodel="planestrain")
+    with pytest.raises(ValueError):
+        O.modal(om, _bcs(O, 2), 2)
+
+
+# ---------------------------------------------------------------------------------------------- GPU
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape, n, nips", CASES)
+def test_gpu_modes_match_the_oracle(shape, n, nips):
+    sm = "planestrain" if len(n) == 2 else "d3"
+    mo, mg = _mesh(O, shape, n), _mesh(A, shape, n)
+    mg.coords = np.ascontiguousarray(mo.coords)
+    om = O.FEModel(mo, [("all", O.LinearElastic(**MAT))], stressmodel=sm, nips=nips)
+    gm = A.FEModel(mg, [("all", A.LinearElastic(**MAT))], A.MechContext(stressmodel=sm), nips=nips)
+    w, V, nu = O.modal(om, _bcs(O, len(n)), 6)
+    ana = A.ModalAnalysis(gm)
+    ana.addstage(_bcs(A, len(n)))
+    assert ana.solve(nmodes=6, tol=1e-8)[0]
+    assert gm.nu == nu and ana.modes.shape == (nu, 6)
+    assert np.abs(ana.freqs - w).max() <= 1e-8 * w.max(), (ana.freqs, w)
+    assert _same_modes(V, ana.modes, w, 1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_modal_residual_at_size():
+    """HEX20 40x8x8 cantilever (about 73 k DOFs, 27 IPs): P v = lambda v for the returned pairs."""
+    mesh = A.Mesh(A.Block([[0, 0, 0], [4.0, 0.8, 0.8]], nx=40, ny=8, nz=8, cellshape=A.HEX20))
+    gm = A.FEModel(mesh, [("all", A.LinearElastic(E=30e3, nu=0.2, rho=2.4e-3))], nips=27)
+    ana = A.ModalAnalysis(gm)
+    ana.addstage([("x==0", A.SurfaceBC(ux=0, uy=0, uz=0))])
+    assert ana.solve(nmodes=8, tol=1e-8)[0]
+    w, V = ana.freqs, ana.modes
+    assert (np.diff(w) >= 0).all() and w[0] > 0
+    nu = gm.nu
+    K11 = gm.mount_K()[:nu, :nu]
+    gm.dev.assemble_M()
+    L = np.asarray(gm.dev.M_csc()[:nu, :nu].sum(axis=0)).ravel()
+    for i in range(len(w)):
+        Pv = K11 @ (V[:, i] / L)
+        assert np.linalg.norm(Pv - w[i] ** 2 * V[:, i]) <= 1e-6 * np.linalg.norm(Pv)
