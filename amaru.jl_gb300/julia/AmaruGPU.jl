@@ -312,6 +312,41 @@ function solve_gpu!(ana::DynamicAnalysis; linear::Symbol=:amg, args...)
 end
 
 # ---------------------------------------------------------------------------
+# Modal analyses: mech_modal_solver! (src/mech/mech-modal-solver.jl:72-235) on the device.
+# ---------------------------------------------------------------------------
+struct ModalParams
+    nmodes::Int32; max_iters::Int32; tol::Float64
+end
+mutable struct ModalStats
+    iterations::Int32; block::Int32; max_residual::Float64; seconds::Float64
+    ModalStats() = new(0, 0, 0.0, 0.0)
+end
+
+"""
+    gpu_modal_solver!(ana::MechModalAnalysis, stage::Stage; nmodes=5, args...)
+
+ana.freqs (omega, ascending) and ana.modes (P's unit eigenvectors on the unknown DOFs) of
+mech_modal_solver!, computed on the device.
+"""
+function gpu_modal_solver!(ana::MechModalAnalysis, stage::Stage; nmodes::Integer=5, args...)
+    model = ana.model
+    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
+    dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
+    model.ndofs = length(dofs)
+    set_dofs!(g, model, dofs, nu)
+    rho = Float64[ elem.props.ρ for elem in model.elems ]
+    check(g, ccall((:amr_set_density, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, rho))
+    w = zeros(nmodes)
+    V = zeros(nu, nmodes)
+    st = ModalStats()
+    check(g, ccall((:amr_modal_run, LIB), Cint, (Ptr{Cvoid}, Ref{ModalParams}, Ptr{Float64}, Ptr{Float64},
+                   Ref{ModalStats}), g.h, ModalParams(nmodes, 1000, 1e-7), w, V, st))
+    ana.freqs = w
+    ana.modes = V
+    return Amaru.success()
+end
+
+# ---------------------------------------------------------------------------
 # Output data: nodal_patch_recovery (src/fe-model.jl:504-702) on the device.
 # ---------------------------------------------------------------------------
 const FIELD_SYMBOLS = [:σxx, :σyy, :σzz, :σyz, :σxz, :σxy, :σvm, :σ1, :σ2, :σ3,
@@ -557,6 +592,6 @@ function wait!(srv::GPUServer, id::Integer)
 end
 
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
-       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!
+       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!
 
 end # module

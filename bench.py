@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-recovery", action="store_true", help="skip the nodal recovery measurement")
     ap.add_argument("--no-dyn", action="store_true", help="skip the dynamic (Newmark) stage measurement")
+    ap.add_argument("--no-modal", action="store_true", help="skip the modal analysis measurement")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--slope", default="", help="also run the TET10 slope stage at these divisions, e.g. 100x17x40")
     return ap.parse_args()
@@ -280,6 +281,8 @@ def run_ours(a):
         out["recovery"] = recovery_leg(model, rank == 0 and not a.no_cpu)
     if not a.no_dyn:
         out["dynamic"] = dyn_leg(model, rank == 0 and not a.no_cpu)
+    if not a.no_modal:
+        out["modal"] = modal_leg(model, rank == 0 and not a.no_cpu)
     if not a.no_batch:
         out["batch"] = batch_leg()
     if not a.no_serve:
@@ -409,6 +412,45 @@ def dyn_cpu_sample(n=(6, 3, 3)):
     return {"value": ana.ndofs * ana.increments / dt, "unit": "DOF-increments/s", "cores": 1, "kind": "port",
             "sample": "oracle dyn_stage_solver! (C element kernels, Python mount_M, SuperLU) on HEX20 %dx%dx%d, "
                       "%d DOFs, %d increments: %.2f s" % (n[0], n[1], n[2], ana.ndofs, ana.increments, dt)}
+
+
+# ---------------------------------------------------------------------------
+# Modal analysis (mech_modal_solver!) of the bench model, base fixed, density 2.4e-3: the 5 lowest
+# modes to a relative residual of 1e-8.  value = unknown DOFs per second of device time.  The CPU
+# baseline runs the oracle's restatement (scipy eigsh with SuperLU) on a HEX20 6x3x3 block.
+# ---------------------------------------------------------------------------
+def modal_leg(model, with_cpu, nmodes=5):
+    import amaru_gpu as A
+    model.rho[:] = DYN["rho"]
+    ana = A.ModalAnalysis(model)
+    ana.addstage([("z==0", A.SurfaceBC(ux=0, uy=0, uz=0))])
+    t0 = time.perf_counter()
+    ana.solve(nmodes=nmodes, tol=1e-8)
+    wall = time.perf_counter() - t0
+    st = ana.stats
+    out = {"workload": "bench HEX20 model, base fixed, rho %g, %d lowest modes, LOBPCG (block %d) with the "
+                       "multigrid preconditioner to 1e-8" % (DYN["rho"], nmodes, st.block),
+           "nu": model.nu, "omega": [float(w) for w in ana.freqs], "iterations": st.iterations,
+           "max_residual": st.max_residual, "device_s": st.seconds, "value": model.nu / st.seconds,
+           "unit": "DOF/s", "e2e": {"value": model.nu / wall, "unit": "DOF/s", "s": wall,
+                                   "d2h_bytes": int(model.nu * nmodes * 8)}}
+    if with_cpu:
+        out["cpu_baseline"] = modal_cpu_sample(nmodes)
+    return out
+
+
+def modal_cpu_sample(nmodes, n=(6, 3, 3)):
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    mo = O.Mesh(O.Block([[0, 0, 0], [10.0 * n[0] / 100, 4.0 * n[1] / 40, 4.0 * n[2] / 40]], nx=n[0], ny=n[1],
+                        nz=n[2], cellshape=O.HEX20))
+    om = O.FEModel(mo, [("all", O.LinearElastic(E=30e3, nu=0.2, rho=DYN["rho"]))], nips=27)
+    t0 = time.perf_counter()
+    _, _, nu = O.modal(om, [("z==0", O.SurfaceBC(ux=0, uy=0, uz=0))], nmodes)
+    dt = time.perf_counter() - t0
+    return {"value": nu / dt, "unit": "DOF/s", "cores": 1, "kind": "port",
+            "sample": "oracle mech_modal_solver! (C mount_K, Python mount_M, scipy eigsh + SuperLU) on HEX20 "
+                      "%dx%dx%d, %d unknown DOFs, %d modes: %.2f s" % (n[0], n[1], n[2], nu, nmodes, dt)}
 
 
 # ---------------------------------------------------------------------------
