@@ -89,6 +89,31 @@ class ModalStats(C.Structure):
                 ("seconds", C.c_double)]
 
 
+class VtuArray(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("type", C.c_int32), ("ncomp", C.c_int32), ("on_device", C.c_int32),
+                ("pad", C.c_int32), ("data", C.c_void_p)]
+
+
+VTU_TYPES = {np.dtype(np.float64): 0, np.dtype(np.int32): 1, np.dtype(np.int64): 2, np.dtype(np.uint64): 3}
+
+
+def vtu_arrays(items):
+    """(name, numpy array) pairs -> (ctypes array of VtuArray, kept buffers); arrays are nrows x ncomp."""
+    keep = []
+    arr = (VtuArray * max(1, len(items)))()
+    for i, (name, a) in enumerate(items):
+        a = np.asarray(a)
+        if a.dtype not in VTU_TYPES:
+            a = a.astype(np.float64)
+        a = np.asfortranarray(a)
+        nm = name.encode("utf-8")
+        keep += [a, nm]
+        arr[i].name, arr[i].type = nm, VTU_TYPES[a.dtype]
+        arr[i].ncomp = 1 if a.ndim == 1 else a.shape[1]
+        arr[i].on_device, arr[i].data = 0, a.ctypes.data
+    return arr, keep
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int32), ("pad", C.c_int32)]
 
@@ -157,6 +182,7 @@ SIGNATURES = {
     "amr_default_dyn_params": (None, [C.POINTER(DynParams)]),
     "amr_modal_run": (C.c_int, [P, C.POINTER(ModalParams), P, P, C.POINTER(ModalStats)]),
     "amr_default_modal_params": (None, [C.POINTER(ModalParams)]),
+    "amr_write_vtu": (C.c_int, [P, C.c_char_p, P, C.c_int32, P, C.c_int32, C.c_int32]),
     "amr_recovery_fields": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
     "amr_recover_nodal": (C.c_int, [P, P]),
     "amr_recover_nodal_dev": (C.c_int, [P, P]),
@@ -427,6 +453,12 @@ class DeviceModel:
         st = ModalStats()
         check(self.h, lib().amr_modal_run(self.h, C.byref(p), ptr(w), ptr(V), C.byref(st)))
         return w, V.T.copy(), st
+
+    def write_vtu(self, path, point_items, cell_items, nthreads=0):
+        pa, k1 = vtu_arrays(point_items)
+        ca, k2 = vtu_arrays(cell_items)
+        check(self.h, lib().amr_write_vtu(self.h, str(path).encode("utf-8"), C.cast(pa, C.c_void_p), len(point_items),
+                                          C.cast(ca, C.c_void_p), len(cell_items), nthreads))
 
     def recovery_fields(self):
         """Field names of the nodal recovery, in the reference's column order."""

@@ -342,6 +342,12 @@ class FEModel:
         self.node_data, self.elem_data = node, elem
         return node, elem
 
+    def save(self, path, nthreads=0):
+        """save(model, "file.vtu") (src/mesh/io.jl:167-274, 323-342): update_output_data! and the ascii VTU file
+        written by the library, byte for byte as the reference writes it."""
+        node, elem = self.update_output_data()
+        self.dev.write_vtu(path, list(node.items()), list(elem.items()), nthreads)
+
 
 class Stage:
     def __init__(self, bcs, nincs=1, nouts=0):

@@ -211,6 +211,9 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
 double amr_dyn_time_rhs(amr_model *m, int reps, double *bytes);
 // modal.cu: omega (host, nmodes) and P's eigenvectors (device, node-major columns, not normalised)
 int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, double *d_modes_nm, amr_modal_stats *stats);
+// vtu.cpp: save_vtu of the model with the caller's arrays
+void amr_vtu_write(amr_model *m, const char *path, const amr_vtu_array *pd, int npd, const amr_vtu_array *cd,
+                   int ncd, int nthreads);
 // stage.cpp-equivalent (capi.cu)
 int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
                      double *U_nm, double *F_nm, amr_stage_stats *stats);

@@ -678,6 +678,16 @@ int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, cons
     });
 }
 
+int amr_write_vtu(amr_model *m, const char *path, const amr_vtu_array *point_data, int32_t npoint,
+                  const amr_vtu_array *cell_data, int32_t ncell, int32_t nthreads) {
+    return guarded(m, [&] {
+        if (npoint < 0 || ncell < 0 || (npoint && !point_data) || (ncell && !cell_data))
+            throw AmrError(AMR_EINVAL, "bad array lists");
+        amr_vtu_write(m, path, point_data, npoint, cell_data, ncell, nthreads);
+        return AMR_OK;
+    });
+}
+
 void amr_default_modal_params(amr_modal_params *p) {
     p->nmodes = 5;
     p->max_iters = 1000;

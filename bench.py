@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-recovery", action="store_true", help="skip the nodal recovery measurement")
     ap.add_argument("--no-dyn", action="store_true", help="skip the dynamic (Newmark) stage measurement")
     ap.add_argument("--no-modal", action="store_true", help="skip the modal analysis measurement")
+    ap.add_argument("--no-vtu", action="store_true", help="skip the VTU output measurement")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--slope", default="", help="also run the TET10 slope stage at these divisions, e.g. 100x17x40")
     return ap.parse_args()
@@ -279,6 +280,8 @@ def run_ours(a):
     }
     if not a.no_recovery:
         out["recovery"] = recovery_leg(model, rank == 0 and not a.no_cpu)
+    if not a.no_vtu:
+        out["vtu"] = vtu_leg(model, rank == 0 and not a.no_cpu)
     if not a.no_dyn:
         out["dynamic"] = dyn_leg(model, rank == 0 and not a.no_cpu)
     if not a.no_modal:
@@ -352,6 +355,57 @@ def recovery_cpu_sample(n=(8, 4, 4)):
     return {"value": om.nnodes / dt, "unit": "nodes/s", "cores": 1, "kind": "port",
             "sample": "oracle nodal_patch_recovery (Python/numpy restatement) on HEX20 %dx%dx%d, 27 IP, %d nodes: "
                       "%.2f s" % (n[0], n[1], n[2], om.nnodes, dt)}
+
+
+# ---------------------------------------------------------------------------
+# VTU output (save(model, "file.vtu")) of the step's model: update_output_data! (dof values and the 16
+# recovered fields on the device) and the ascii file, to a scratch file removed afterwards; the writer's
+# host threads all, then one.  The CPU baseline is the oracle's Python writer on HEX20 8x4x4.
+# ---------------------------------------------------------------------------
+def vtu_leg(model, with_cpu):
+    d = tempfile.mkdtemp()
+    path = os.path.join(d, "out.vtu")
+    try:
+        t0 = time.perf_counter()
+        node, elem = model.update_output_data()
+        t_data = time.perf_counter() - t0
+        items = (list(node.items()), list(elem.items()))
+        res = {}
+        for nt in (0, 1):
+            t0 = time.perf_counter()
+            model.dev.write_vtu(path, *items, nthreads=nt)
+            res[nt] = time.perf_counter() - t0
+        size = os.path.getsize(path)
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+        os.rmdir(d)
+    out = {"bytes": size, "output_data_s": t_data, "write_s": res[0], "write_1thread_s": res[1],
+           "threads": os.cpu_count(), "value": size / res[0] / 1e6, "unit": "MB/s",
+           "value_1thread": size / res[1] / 1e6}
+    if with_cpu:
+        out["cpu_baseline"] = vtu_cpu_sample()
+    return out
+
+
+def vtu_cpu_sample(n=(8, 4, 4)):
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    mo = O.Mesh(O.Block([[0, 0, 0], [0.8, 0.4, 0.4]], nx=n[0], ny=n[1], nz=n[2], cellshape=O.HEX20))
+    rng = np.random.default_rng(SEED)
+    nn = len(mo.coords)
+    node = [("node-id", np.arange(1, nn + 1))] + [("f%d" % i, rng.normal(size=nn)) for i in range(22)] + \
+           [("U", rng.normal(size=(nn, 3)))]
+    ne = len(mo.elems)
+    shapes = np.array([c.shape for c in mo.elems])
+    conn_ptr = np.concatenate([[0], np.cumsum([len(c.nodes) for c in mo.elems])])
+    conn = np.array([v for c in mo.elems for v in c.nodes])
+    t0 = time.perf_counter()
+    txt = O.vtu.save_vtu(mo.coords, conn_ptr, conn, shapes, node, [("elem-id", np.arange(1, ne + 1))])
+    dt = time.perf_counter() - t0
+    return {"value": len(txt) / dt / 1e6, "unit": "MB/s", "cores": 1, "kind": "port",
+            "sample": "oracle save_vtu (Python) of HEX20 %dx%dx%d with 22 fields + U: %d bytes in %.2f s"
+                      % (n[0], n[1], n[2], len(txt), dt)}
 
 
 # ---------------------------------------------------------------------------

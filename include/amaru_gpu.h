@@ -374,6 +374,24 @@ typedef struct {
 int amr_modal_run(amr_model *m, const amr_modal_params *p, double *omega, double *modes, amr_modal_stats *stats);
 void amr_default_modal_params(amr_modal_params *p);
 
+/* ---- VTU output ----
+ * save(model, "file.vtu") -> save_vtu (src/mesh/io.jl:167-274, ascii) with the XML writer of
+ * src/tools/xml.jl:250-318, byte for byte: the model's points and cells, then the point and cell
+ * arrays in the caller's order (update_output_data!'s node_data / elem_data). */
+enum { AMR_VTU_FLOAT64 = 0, AMR_VTU_INT32 = 1, AMR_VTU_INT64 = 2, AMR_VTU_UINT64 = 3 };
+typedef struct {
+    const char *name;        /* DataArray Name */
+    int32_t type;            /* AMR_VTU_*: element type of data and the DataArray type */
+    int32_t ncomp;           /* NumberOfComponents */
+    int32_t on_device;       /* data is a device pointer */
+    int32_t pad;
+    const void *data;        /* nrows x ncomp, column-major (component c of row i at c * nrows + i);
+                                nrows = nnodes for point arrays, nelems (caller order) for cell arrays */
+} amr_vtu_array;
+/* nthreads host threads format the arrays (0: all cores). */
+int amr_write_vtu(amr_model *m, const char *path, const amr_vtu_array *point_data, int32_t npoint,
+                  const amr_vtu_array *cell_data, int32_t ncell, int32_t nthreads);
+
 /* ---- output recovery ----
  * Nodal values of the IP fields: replaces nodal_patch_recovery (src/fe-model.jl:504-702)
  * as called by update_output_data! (:341-427) and get_node_and_elem_vals (:430-485).

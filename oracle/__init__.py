@@ -4,7 +4,7 @@ TEST INFRASTRUCTURE ONLY: a restatement of NumSoftware/Amaru.jl's Float64
 algorithms (element stiffness, constitutive updates, mount_K, update_state!,
 solve_system!, get_bc_vals, the staged Newton driver, the structured mesher
 and the nodal patch recovery of the output data, mount_M, the dynamic
-Newmark solver and the modal solver).  Only tests/,
+Newmark solver, the modal solver and the VTU writer).  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg may import it, and
 only as the checker.  The CUDA library never calls it.
 
@@ -20,3 +20,4 @@ from .core import *  # noqa: F401,F403
 from .recovery import nodal_patch_recovery, ip_coords, ip_state_vals, field_names  # noqa: F401
 from .dynamic import DynAnalysis, mount_M, elem_mass  # noqa: F401
 from .modal import modal, modal_dense  # noqa: F401
+from . import vtu  # noqa: F401
