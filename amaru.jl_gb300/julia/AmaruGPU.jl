@@ -312,6 +312,43 @@ function solve_gpu!(ana::DynamicAnalysis; linear::Symbol=:amg, args...)
 end
 
 # ---------------------------------------------------------------------------
+# VTU output: save_vtu (src/mesh/io.jl:167-274, ascii) written by the library.
+# ---------------------------------------------------------------------------
+struct VtuArray
+    name::Cstring; type::Int32; ncomp::Int32; on_device::Int32; pad::Int32; data::Ptr{Cvoid}
+end
+const VTU_TYPES = Dict(Float64 => Int32(0), Int32 => Int32(1), Int64 => Int32(2), UInt64 => Int32(3))
+
+"""
+    save_gpu(model::FEModel, filename::String)
+
+save(model, filename) for .vtu files: update_output_data!(model), then the file written by
+amr_write_vtu from model.node_data and model.elem_data, byte for byte as save_vtu writes it.
+"""
+function save_gpu(model::FEModel, filename::String)
+    g = GPU_MODELS[objectid(model)]
+    Amaru.update_output_data!(model)
+    keep = Any[]
+    function arrays(d)
+        out = VtuArray[]
+        for (name, a) in d
+            isempty(a) && continue
+            a = haskey(VTU_TYPES, eltype(a)) ? a : Float64.(a)
+            push!(keep, a, name)
+            push!(out, VtuArray(Base.unsafe_convert(Cstring, name), VTU_TYPES[eltype(a)], Int32(size(a, 2)),
+                                Int32(0), Int32(0), pointer(a)))
+        end
+        return out
+    end
+    pd, cd = arrays(model.node_data), arrays(model.elem_data)
+    GC.@preserve keep begin
+        check(g, ccall((:amr_write_vtu, LIB), Cint, (Ptr{Cvoid}, Cstring, Ptr{VtuArray}, Int32, Ptr{VtuArray},
+                       Int32, Int32), g.h, filename, pd, length(pd), cd, length(cd), Int32(0)))
+    end
+    return nothing
+end
+
+# ---------------------------------------------------------------------------
 # Modal analyses: mech_modal_solver! (src/mech/mech-modal-solver.jl:72-235) on the device.
 # ---------------------------------------------------------------------------
 struct ModalParams
@@ -592,6 +629,6 @@ function wait!(srv::GPUServer, id::Integer)
 end
 
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
-       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!
+       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!, save_gpu
 
 end # module
