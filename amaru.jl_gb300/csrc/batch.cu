@@ -1097,8 +1097,8 @@ void amr_autotune_model(amr_model *m, amr_tuning *out) {
             int best_epb = g.epb;
             for (int e : {1, 2, 3, 4, 6, 8}) {
                 if (e > 1 && e * np > 512) continue;
-                const size_t smem = sizeof(double) * (size_t)e * (g.nen * ndim + 2 * g.nip * g.nen * ndim + 2 * g.nip);
-                if (smem > 200 * 1024) continue;
+                const size_t smem = sizeof(double) * (size_t)e * (g.nen * ndim + 3 * g.nip * g.nen * ndim + 2 * g.nip);
+                if (smem > 200 * 1024) continue;  // the stiffness kernel's shared memory (launch_stiff)
                 g.epb = e;
                 m->groups.assign(1, g);
                 const double ms = time_ms(m, [&] { amr_stiffness_elements(m); }, 3);

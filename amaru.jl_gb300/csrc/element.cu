@@ -345,7 +345,9 @@ __global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G
     double *sV = sG + epb * nip * NEN * DIM;      // epb x nip x NEN*DIM (plastic vectors)
     double *sW = sV + epb * nip * NEN * DIM;      // epb x nip
     double *sGam = sW + epb * nip;                // epb x nip
+    double *sWG = sGam + epb * nip;               // epb x nip x NEN*DIM: w * g, the rounded products of phase 2
     __shared__ int sPl[8];                        // per element: any plastic IP
+    __shared__ double sLam[8], sMu[8];            // per element: Lame constants
 
     const int64_t e0 = G.first + (int64_t)blockIdx.x * epb;
     const int ne = (int)min((int64_t)epb, G.first + G.count - e0);
@@ -370,12 +372,17 @@ __global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G
         double th = M.thickness;
         double w = det * wq[ip] * th;
         sW[el * nip + ip] = w;
+        {
+            double *wg = sWG + (el * nip + ip) * NEN * DIM;
+            for (int q = 0; q < NEN * DIM; q++) wg[q] = w * g[q];
+        }
         const double *par = M.mat_par + 8 * e;
         int64_t gi = M.ip_ptr[e] + ip;
         double sig[6];
         for (int i = 0; i < 6; i++) sig[i] = st[i * M.nip_total + gi];
         double lam, mu, m[6];
         lame(par[0], par[1], ps, lam, mu);
+        if (ip == 0) { sLam[el] = lam; sMu[el] = mu; }
         double gam = plastic_tangent(M.mat_type[e], par, ps, sig, st[AMR_ST_EPA * M.nip_total + gi],
                                      st[AMR_ST_DL * M.nip_total + gi], lam, mu, m);
         sGam[el * nip + ip] = gam * w;
@@ -397,13 +404,10 @@ __global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G
 #pragma unroll
         for (int q = 0; q < BB; q++) { T[q] = 0.0; P[q] = 0.0; }
         const double *gbase = sG + el * nip * NEN * DIM;
+        const double *wgbase = sWG + el * nip * NEN * DIM;
         for (int ip = 0; ip < nip; ip++) {
-            const double *ga = gbase + ip * NEN * DIM + a * DIM;
+            const double *wa = wgbase + ip * NEN * DIM + a * DIM;
             const double *gb = gbase + ip * NEN * DIM + b * DIM;
-            double w = sW[el * nip + ip];
-            double wa[DIM];
-#pragma unroll
-            for (int i = 0; i < DIM; i++) wa[i] = w * ga[i];
 #pragma unroll
             for (int i = 0; i < DIM; i++)
 #pragma unroll
@@ -424,9 +428,7 @@ __global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G
                 }
             }
         }
-        const double *par = M.mat_par + 8 * e;
-        double lam, mu;
-        lame(par[0], par[1], ps, lam, mu);
+        const double lam = sLam[el], mu = sMu[el];
         double tr = 0.0;
 #pragma unroll
         for (int i = 0; i < DIM; i++) tr += T[i * DIM + i];
@@ -1019,7 +1021,7 @@ template <int DIM, int NEN>
 void launch_stiff(amr_model *m, const AmrGroup &g) {
     GroupArgs ga{g.tab, g.nip, g.first, g.count};
     int epb = g.epb;
-    size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + 2 * g.nip * NEN * DIM + 2 * g.nip);
+    size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + 3 * g.nip * NEN * DIM + 2 * g.nip);
     constexpr int NP = NEN * (NEN + 1) / 2;
     int threads = epb * NP;
     threads = ((threads + 31) / 32) * 32;
