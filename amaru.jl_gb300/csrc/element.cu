@@ -333,8 +333,14 @@ __device__ __forceinline__ void sym_apply(const double *m, const double *g, doub
 // (element, node pair a<=b) accumulates T_ab / P_ab over the IPs and writes
 // the two element blocks (a,b), (b,a) to the staging array.
 // ---------------------------------------------------------------------------
+// CTAs per SM the stiffness kernel's registers allow: two, so one CTA's geometry phase (a thread per IP)
+// overlaps another's pair phase; three for HEX20, measured faster on the 100x40x40 block despite a
+// few spilled registers
 template <int DIM, int NEN>
-__global__ void __launch_bounds__(256) stiffness_kernel(ModelArgs M, GroupArgs G, int epb, double *Kel,
+constexpr int stiff_min_blocks() { return (DIM == 3 && NEN == 20) ? 3 : 2; }
+
+template <int DIM, int NEN>
+__global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_kernel(ModelArgs M, GroupArgs G, int epb, double *Kel,
                                                         const double *st, int32_t *status) {
     constexpr int NP = NEN * (NEN + 1) / 2;
     constexpr int BB = DIM * DIM;
@@ -829,7 +835,7 @@ __global__ void __launch_bounds__(256) mass_kernel(ModelArgs M, GroupArgs G, int
 // Internal forces with the constitutive update: thread per (element, IP).
 // ---------------------------------------------------------------------------
 template <int DIM, int NEN>
-__global__ void __launch_bounds__(256) internal_kernel(ModelArgs M, GroupArgs G, int epb, const double *dU,
+__global__ void __launch_bounds__(256, 2) internal_kernel(ModelArgs M, GroupArgs G, int epb, const double *dU,
                                                        const double *stbk, double *st, double *Fel, int32_t *status) {
     extern __shared__ double sm[];
     const int nip = G.nip;
