@@ -664,6 +664,15 @@ __device__ __forceinline__ void finish_block(int64_t n, int64_t k, int32_t j, in
     }
 }
 
+// |x| < eps() and isnan(x) on the integer pipe, from the bit pattern (the FP64 pipe is the gather's
+// bound on this GPU): the sign-cleared pattern of a double orders as its magnitude, NaNs above infinity
+__device__ __forceinline__ bool below_eps(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) < 0x3cb0000000000000LL;  // 2^-52
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
 template <int B>
 __global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *brow_ptr, const int32_t *bcol,
                               const int64_t *contrib_ptr, const int64_t *contrib, const double *Kel,
@@ -686,7 +695,7 @@ __global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *br
 #pragma unroll
             for (int q = 0; q < BB; q++) {
                 double x = src[q];
-                if (!(fabs(x) < DBL_EPSILON)) { v[q] += x; kb |= 1u << q; }  // NaN is pushed, as in mount_K
+                if (!below_eps(x)) { v[q] += x; kb |= 1u << q; }  // NaN is pushed, as in mount_K
             }
         }
         int32_t j = bcol[k];
@@ -694,7 +703,7 @@ __global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *br
 #pragma unroll
         for (int q = 0; q < BB; q++) {
             K64[(int64_t)q * nblocks + k] = v[q];
-            nan |= isnan(v[q]);
+            nan |= is_nan_bits(v[q]);
         }
         if (nan) set_status(status, AMR_ENAN, -1);
         if (keep) keep[k] = (uint16_t)kb;
