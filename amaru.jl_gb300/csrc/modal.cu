@@ -127,18 +127,17 @@ __global__ void __launch_bounds__(kThreads) k_gram(int64_t n, Cols S, Cols T, co
     double *sD = sT + kGramTile * m;       // kGramTile
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
-    // this thread's items and their (a, b, kind)
-    int ia[kGramItems], ib[kGramItems], kind[kGramItems], nmine = 0;
-    for (int w = threadIdx.x; w < nitems && nmine < kGramItems; w += blockDim.x) {
-        int v = w, k = 0;
-        if (v >= npairs) { v -= npairs; k = 1; }
-        int a = 0;
-        while (v >= m - a) { v -= m - a; a++; }
-        ia[nmine] = a; ib[nmine] = a + v; kind[nmine] = k; nmine++;
-    }
+    // this thread's items and their (a, b, kind); fixed-size loops keep them in registers
+    int ia[kGramItems], ib[kGramItems], kind[kGramItems];
     double acc[kGramItems];
 #pragma unroll
-    for (int q = 0; q < kGramItems; q++) acc[q] = 0.0;
+    for (int q = 0; q < kGramItems; q++) {
+        int v = threadIdx.x + q * blockDim.x, k = 0, a = 0;
+        if (v >= npairs) { v -= npairs; k = 1; }
+        if (v < npairs)
+            while (v >= m - a) { v -= m - a; a++; }
+        ia[q] = a; ib[q] = a + v; kind[q] = k; acc[q] = 0.0;
+    }
     for (int64_t t0 = r0; t0 < r1; t0 += kGramTile) {
         const int rows = (int)min((int64_t)kGramTile, r1 - t0);
         for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
@@ -148,19 +147,25 @@ __global__ void __launch_bounds__(kThreads) k_gram(int64_t n, Cols S, Cols T, co
         }
         for (int r = threadIdx.x; r < rows; r += blockDim.x) sD[r] = D ? D[t0 + r] : 1.0;
         __syncthreads();
-        for (int q = 0; q < nmine; q++) {
+#pragma unroll
+        for (int q = 0; q < kGramItems; q++) {
+            if (threadIdx.x + q * blockDim.x >= nitems) break;
             double s = acc[q];
+            const double *pa = sS + ia[q];
+            const double *pb = (kind[q] ? sT : sS) + ib[q];
             if (kind[q] == 0)
-                for (int r = 0; r < rows; r++) s = fma(sS[r * m + ia[q]] * sD[r], sS[r * m + ib[q]], s);
+                for (int r = 0; r < rows; r++) s = fma(pa[r * m] * sD[r], pb[r * m], s);
             else
-                for (int r = 0; r < rows; r++) s = fma(sS[r * m + ia[q]], sT[r * m + ib[q]], s);
+                for (int r = 0; r < rows; r++) s = fma(pa[r * m], pb[r * m], s);
             acc[q] = s;
         }
         __syncthreads();
     }
-    int q = 0;
-    for (int w = threadIdx.x; w < nitems && q < kGramItems; w += blockDim.x, q++)
-        partials[(int64_t)blockIdx.x * nitems + w] = acc[q];
+#pragma unroll
+    for (int q = 0; q < kGramItems; q++) {
+        const int w = threadIdx.x + q * blockDim.x;
+        if (w < nitems) partials[(int64_t)blockIdx.x * nitems + w] = acc[q];
+    }
 }
 
 // sum of the per-CTA partials, CTA order
