@@ -117,3 +117,21 @@ def test_gpu_model_save_matches_the_oracle(tmp_path):
     got = path.read_bytes()
     assert got == want.encode("utf-8")
     assert b'Name="\xcf\x83vm"' in got and os.path.getsize(path) > 10000
+
+
+@pytest.mark.gpu
+def test_gpu_model_save_2d_matches_the_oracle(tmp_path):
+    """A plane-strain QUAD8 model: points with z = 0, two dof components, the 2-D field list."""
+    mesh = A.Mesh(A.Block([[0, 0], [2.0, 0.5]], nx=8, ny=2, cellshape=A.QUAD8))
+    gm = A.FEModel(mesh, [("all", A.VonMises(E=200e3, nu=0.3, fy=240.0, H=2e3))],
+                   A.MechContext(stressmodel="planestrain"))
+    ana = A.MechAnalysis(gm)
+    ana.addstage([("x==0", A.SurfaceBC(ux=0, uy=0)), ("x==2", A.SurfaceBC(ty=-20.0))], nincs=3)
+    assert ana.solve(autoinc=True)[0]
+    path = tmp_path / "model2d.vtu"
+    gm.save(path)
+    V, names = gm.nodal_patch_recovery()
+    assert "ep" in names and "σ2" not in names
+    node, elem = O.vtu.output_data(gm.ndim, gm.nnodes, gm.mesh.shape, gm.eq_id, gm.U, gm.F, V, names)
+    want = O.vtu.save_vtu(gm.mesh.coords, gm.mesh.conn_ptr, gm.mesh.conn, gm.mesh.shape, node, elem)
+    assert path.read_bytes() == want.encode("utf-8")
