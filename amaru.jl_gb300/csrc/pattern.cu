@@ -122,7 +122,7 @@ __device__ int warp_unique_sorted(int32_t *buf, int cnt, int lane) {
         int pos = total + __popc(mask & ((1u << lane) - 1u));
         int32_t v = (i < cnt) ? buf[i] : 0;
         __syncwarp();
-        if (keep) buf[pos] = v;  // pos <= i: never overwrites an unread later entry of this round
+        if (keep) buf[pos] = v;  // pos <= i: never overwrites an unread later entry of this pass
         total += __popc(mask);
         __syncwarp();
     }
