@@ -278,20 +278,21 @@ def run_ours(a):
         "gpu_launches": launches,
         "clocks": clocks,
     }
-    if not a.no_recovery:
-        out["recovery"] = recovery_leg(model, rank == 0 and not a.no_cpu)
-    if not a.no_vtu:
-        out["vtu"] = vtu_leg(model, rank == 0 and not a.no_cpu)
-    if not a.no_dyn:
-        out["dynamic"] = dyn_leg(model, rank == 0 and not a.no_cpu)
-    if not a.no_modal:
-        out["modal"] = modal_leg(model, rank == 0 and not a.no_cpu)
-    if not a.no_batch:
-        out["batch"] = batch_leg()
-    if not a.no_serve:
-        out["serving"] = serving_leg(a.serve_requests)
-    if a.slope:
-        out["slope"] = slope_leg(a.slope)
+    # the secondary legs: a failure in one is recorded on the line and does not take the headline with it
+    legs = [("recovery", not a.no_recovery, lambda: recovery_leg(model, rank == 0 and not a.no_cpu)),
+            ("vtu", not a.no_vtu, lambda: vtu_leg(model, rank == 0 and not a.no_cpu)),
+            ("dynamic", not a.no_dyn, lambda: dyn_leg(model, rank == 0 and not a.no_cpu)),
+            ("modal", not a.no_modal, lambda: modal_leg(model, rank == 0 and not a.no_cpu)),
+            ("batch", not a.no_batch, batch_leg),
+            ("serving", not a.no_serve, lambda: serving_leg(a.serve_requests)),
+            ("slope", bool(a.slope), lambda: slope_leg(a.slope))]
+    for name, on, fn in legs:
+        if not on:
+            continue
+        try:
+            out[name] = fn()
+        except Exception as e:  # noqa: BLE001
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0 and not a.no_cpu:
         out["cpu_baseline"] = cpu_baseline(a, steps=1, warmup=0)
     return out
