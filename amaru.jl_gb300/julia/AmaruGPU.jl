@@ -8,7 +8,10 @@
 #   solve_system!(K, U, F, nu)     src/solver.jl:5
 # The element/material/stage API (FEModel, MechSolid, LinearElastic / VonMises /
 # DruckerPrager, addstage!, solve!) is unchanged.  Elements or materials the
-# library does not support raise an error: there is no CPU fallback.
+# library does not support raise an error: there is no CPU fallback.  Beside the
+# static stage it runs the dynamic stage (dyn_stage_solver!), the modal solver
+# (mech_modal_solver!), the nodal output recovery (nodal_patch_recovery) and the
+# ascii VTU writer (save_vtu) on the library.
 #
 # Index convention: the C ABI is 0-based; this file converts (eq_id - 1).
 module AmaruGPU
@@ -261,14 +264,14 @@ struct DynParams
 end
 
 """
-    gpu_dyn_stage_solver!(ana::DynamicAnalysis, stage::Stage; args...)
+    gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
 
 dyn_stage_solver! of a first stage with K, M, the solves and the IP states on the
 device.  Boundary values come from Amaru's get_bc_vals at t = 0 and t = 1 (they must
 be affine in t); ux/fx/vx/ax land in dof.vals as the reference writes them
 (src/mech/dyn-solver.jl:420-425).
 """
-function gpu_dyn_stage_solver!(ana::DynamicAnalysis, stage::Stage; args...)
+function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
     model = ana.model
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
@@ -301,11 +304,11 @@ function gpu_dyn_stage_solver!(ana::DynamicAnalysis, stage::Stage; args...)
 end
 
 """
-    solve_gpu!(ana::DynamicAnalysis; linear=:amg, args...)
+    solve_gpu!(ana::Amaru.DynamicAnalysis; linear=:amg, args...)
 
 solve! of a dynamic analysis (dyn_solver_params) with gpu_dyn_stage_solver!.
 """
-function solve_gpu!(ana::DynamicAnalysis; linear::Symbol=:amg, args...)
+function solve_gpu!(ana::Amaru.DynamicAnalysis; linear::Symbol=:amg, args...)
     LINEAR_METHOD[] = linear === :jacobi ? Int32(0) : Int32(2)
     args = Amaru.checkargs(args, Amaru.dyn_solver_params)
     return Amaru.stage_iterator!(gpu_dyn_stage_solver!, ana; args...)
