@@ -929,7 +929,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
             AMR_CUDA(cudaMemsetAsync(dUa, 0, n * sizeof(double), s));
             vec(m, V_SET_AXPBY, dT, Uex, 0.0, nullptr, dUi);
             double res = 0.0, res1 = 0.0, err = 0.0;
-            bool converged = false, syserror = false, still_linear = true;
+            bool converged = false, syserror = false;
             std::string sysmsg;
             int nits = 0;
             for (int it = 1; it <= p.maxits; it++) {
@@ -982,13 +982,11 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 err = nui / nua;
                 st.iterations++;
                 if (it == 1) res1 = res;
-                if (it > 1) still_linear = false;
                 if (res < tol) { converged = true; break; }
                 if (err < rtol) { converged = true; break; }
                 if (std::isnan(res)) break;
                 if (it > 1 && res > lastres) break;
             }
-            (void)still_linear;
             if (syserror) converged = false;
             st.residue = res;
             if (converged) {

@@ -1018,7 +1018,6 @@ template <int B>
 static double time_spmv32(amr_model *m, int reps) {
     AmrSolveWork *w = work(m);
     cudaStream_t s = m->stream;
-    unsigned g = (unsigned)w->grid;
     Ctl c{};
     c.rz = 1.0;
     c.first = 1;
