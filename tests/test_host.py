@@ -128,3 +128,28 @@ def test_slope_mesh_keeps_boundary_planes_and_orientation():
     v0, v1 = vol(c0), vol(c)
     assert (np.sign(v0) == np.sign(v1)).all() and (np.abs(v1) > 0.2 * np.abs(v0)).all()
     assert not np.allclose(c, c0 * [1, 1, 1])  # jittered
+
+
+def test_dynamic_and_modal_defaults_mirror_the_reference():
+    """dyn_solver_params (src/mech/dyn-solver.jl:166-180) and mech_modal_solver_params
+    (src/mech/mech-modal-solver.jl:49-56) defaults, as the C ABI fills them."""
+    from amaru_gpu import _lib as L
+    p = L.default_dyn_params()
+    assert (p.tol, p.dTmin, p.dTmax, p.rspan, p.maxits, p.autoinc) == (0.01, 1e-7, 0.1, 0.01, 5, 0)
+    assert (p.alpha, p.beta, p.nincs, p.nouts) == (0.0, 0.0, 1, 0)
+    q = L.ModalParams()
+    L.lib().amr_default_modal_params(L.C.byref(q))
+    assert q.nmodes == 5 and q.max_iters > 0 and 0 < q.tol < 1e-4
+
+
+def test_vtu_arrays_are_column_major_with_their_types():
+    import numpy as np
+    from amaru_gpu import _lib as L
+    U = np.arange(12, dtype=np.float64).reshape(4, 3)  # C order in, column-major out
+    ids = np.arange(1, 5, dtype=np.int64)
+    arr, keep = L.vtu_arrays([("U", U), ("node-id", ids), ("f", np.arange(4, dtype=np.int16))])
+    assert arr[0].name == b"U" and arr[0].type == 0 and arr[0].ncomp == 3
+    buf = np.ctypeslib.as_array((L.C.c_double * 12).from_address(arr[0].data))
+    assert np.array_equal(buf, U.T.reshape(-1))
+    assert arr[1].type == 2 and arr[1].ncomp == 1
+    assert arr[2].type == 0  # other dtypes are converted to Float64: the writer takes four element types
