@@ -827,7 +827,8 @@ int amr_launch_count(const amr_model *m, int64_t *count) {
 
 int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch) {
     return guarded(m, [&] {
-        if (!m->K_valid) throw AmrError(AMR_EINVAL, "assemble K first");
+        // the dynamic right-hand side reads M and a K-shaped operand only
+        if (!m->K_valid && kernel != AMR_KERNEL_DYN_RHS) throw AmrError(AMR_EINVAL, "assemble K first");
         if (reps < 1) throw AmrError(AMR_EINVAL, "reps must be >= 1");
         const double nb = (double)m->nblocks, nn = (double)m->nnodes, B = m->B, BB = m->BB;
         double t = 0.0, bytes = 0.0;

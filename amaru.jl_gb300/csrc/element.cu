@@ -1183,6 +1183,7 @@ void amr_mass(amr_model *m) {
 }
 
 void amr_dyn_combine(amr_model *m, const double *Ks, double s1, double s2, double alpha, double beta) {
+    m->K_valid = false;  // K64 holds a combination from here on: K is mounted again before it is read as K
     unsigned grid = nblk(m->nnodes * 32, 256);
     if (m->B == 3)
         dyn_combine_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, Ks, m->M64, s1,

@@ -352,6 +352,8 @@ typedef struct {
  * or below dTmin with it. */
 int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, const double *Fex0, const double *Fex1,
                       const amr_dyn_params *p, double *U, double *V, double *A, double *F, amr_stage_stats *stats);
+/* (The stage leaves the pseudo-stiffness in the handle's K storage: amr_assemble_K is needed again
+ * before amr_get_K_csc or amr_solve.) */
 void amr_default_dyn_params(amr_dyn_params *p);
 
 /* ---- modal analysis ----

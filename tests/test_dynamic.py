@@ -160,6 +160,12 @@ def test_gpu_dyn_stage_2d_with_a_time_dependent_load():
     assert ag.stats.increments == ao.increments == 10
     for k in ("U", "V", "A", "F"):
         assert _close(getattr(gm, k), getattr(om, k), 1e-7), k
+    # the stage leaves the pseudo-stiffness in K's storage: K must be mounted again before it is read
+    from amaru_gpu import _lib as L
+    with pytest.raises(L.AmrError):
+        gm.dev.K_csc()
+    gm.dev.assemble_K()
+    assert gm.dev.K_csc().nnz > 0
     # boundary values that are not affine in time are refused on the host
     ag2 = A.DynAnalysis(gm)
     ag2.addstage([("x==0", A.SurfaceBC(ux=0, uy=0)), ("x==3", A.SurfaceBC(ty="-2.0*t*t"))], tspan=0.05)
