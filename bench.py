@@ -71,6 +71,19 @@ def rank_info():
     return r, w
 
 
+def max_over_ranks(vals, device="cpu"):
+    """Element-wise maximum of a list of floats over all ranks (a barrier first, so that every rank has
+    left its timed region); the values themselves on one process."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in vals]
+    import torch
+    dist.barrier()
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu().tolist()]
+
+
 # ---------------------------------------------------------------------------
 # clocks sampled during the timed region
 class Clocks:
@@ -172,13 +185,8 @@ def run_ours(a):
         kry.append(st.krylov_iterations)
     clocks = clk.stop()
     launches = dev.launch_count() - launches0
-    t_step = max(times)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
-    mean_step = float(np.mean(times))
+    # replicas: every rank solves its own copy of the model; the slowest rank sets the job's time
+    mean_step, t_step = max_over_ranks([float(np.mean(times)), max(times)], device="cuda")
     value = world * ndofs / mean_step
 
     # roofline of the dominant kernel (FP32 BSR SpMV), timed on the library's stream
@@ -250,7 +258,7 @@ def run_ours(a):
         e2e_t.append(time.perf_counter() - t1)
         if rc != 0:
             raise RuntimeError(dev.last_error())
-    e2e_v = world * ndofs / float(np.mean(e2e_t))
+    e2e_v = world * ndofs / max_over_ranks([float(np.mean(e2e_t))], device="cuda")[0]
 
     out = {
         "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -279,10 +287,11 @@ def run_ours(a):
         "clocks": clocks,
     }
     # the secondary legs: a failure in one is recorded on the line and does not take the headline with it
-    legs = [("recovery", not a.no_recovery, lambda: recovery_leg(model, rank == 0 and not a.no_cpu)),
-            ("vtu", not a.no_vtu, lambda: vtu_leg(model, rank == 0 and not a.no_cpu)),
-            ("dynamic", not a.no_dyn, lambda: dyn_leg(model, rank == 0 and not a.no_cpu)),
-            ("modal", not a.no_modal, lambda: modal_leg(model, rank == 0 and not a.no_cpu)),
+    cpu_here = rank == 0 and world == 1 and not a.no_cpu  # the CPU samples: rank 0 of a 1-GPU run
+    legs = [("recovery", not a.no_recovery, lambda: recovery_leg(model, cpu_here)),
+            ("vtu", not a.no_vtu, lambda: vtu_leg(model, cpu_here)),
+            ("dynamic", not a.no_dyn, lambda: dyn_leg(model, cpu_here)),
+            ("modal", not a.no_modal, lambda: modal_leg(model, cpu_here)),
             ("batch", not a.no_batch, batch_leg),
             ("serving", not a.no_serve, lambda: serving_leg(a.serve_requests)),
             ("slope", bool(a.slope), lambda: slope_leg(a.slope))]
@@ -293,7 +302,7 @@ def run_ours(a):
             out[name] = fn()
         except Exception as e:  # noqa: BLE001
             out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
-    if rank == 0 and not a.no_cpu:
+    if cpu_here:
         out["cpu_baseline"] = cpu_baseline(a, steps=1, warmup=0)
     return out
 
