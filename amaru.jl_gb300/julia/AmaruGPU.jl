@@ -631,7 +631,130 @@ function wait!(srv::GPUServer, id::Integer)
     return st, res
 end
 
+# ---------------------------------------------------------------------------
+# Handle queries, IP-state checkpoints (src/ip.jl:22-57), per-element E, the
+# HBM estimate, server counters and the launch-shape autotuner.
+# ---------------------------------------------------------------------------
+function checked(g::GPUModel, rc::Integer)
+    st = check(g, rc)
+    st === nothing || error(st.message)
+    return nothing
+end
+
+"""
+    sizes(g) -> (nnodes, nelems, nip_total, nblocks)
+
+Sizes of the device model (amr_get_sizes); nblocks counts the node blocks of K's pattern.
+"""
+function sizes(g::GPUModel)
+    nn, ne, ni, nb = Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0)
+    checked(g, ccall((:amr_get_sizes, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ref{Int64}, Ref{Int64}),
+                     g.h, nn, ne, ni, nb))
+    return (nnodes=nn[], nelems=ne[], nip_total=ni[], nblocks=nb[])
+end
+
+"""
+    get_state(g) -> Matrix{Float64} (16 x nip_total)
+
+The IP states, one column per IP in element and IP order: σ (6), ε (6), εpa, Δλ and two
+zeros, as in the IpState objects of the three materials.
+"""
+function get_state(g::GPUModel)
+    S = zeros(16, sizes(g).nip_total)
+    checked(g, ccall((:amr_get_state, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, S))
+    return S
+end
+
+"""
+    set_state!(g, S)
+
+Writes IP states in the layout of get_state: a checkpoint restored, or states set by the caller.
+"""
+function set_state!(g::GPUModel, S::Matrix{Float64})
+    size(S) == (16, sizes(g).nip_total) || error("AmaruGPU: state must be 16 x nip_total")
+    checked(g, ccall((:amr_set_state, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, S))
+    return g
+end
+
+"State ← trial state (copyto!.(StateBk, State), src/mech/mech-solver.jl:333)."
+commit_state!(g::GPUModel) = (checked(g, ccall((:amr_state_commit, LIB), Cint, (Ptr{Cvoid},), g.h)); g)
+"Trial state ← committed state (copyto!.(State, StateBk), src/mech/mech-solver.jl:391,461)."
+restore_state!(g::GPUModel) = (checked(g, ccall((:amr_state_restore, LIB), Cint, (Ptr{Cvoid},), g.h)); g)
+
+"""
+    set_youngs!(g, E)
+
+Young's modulus per element (in element order), replacing the materials' E.
+"""
+function set_youngs!(g::GPUModel, E::Vector{Float64})
+    length(E) == sizes(g).nelems || error("AmaruGPU: one E per element")
+    checked(g, ccall((:amr_set_youngs, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, E))
+    return g
+end
+
+"""
+    estimate_bytes(model::FEModel) -> Int
+
+Upper bound of the device bytes one model and one stage of it take (amr_estimate_bytes),
+the figure a GPUServer admits requests by.
+"""
+function estimate_bytes(model::FEModel)
+    coords, shape, nips, conn_ptr, conn, mat_type, mat_params = model_arrays(model)
+    ctx = model.ctx
+    b = Ref{Int64}(0)
+    GC.@preserve coords shape nips conn_ptr conn mat_type mat_params begin
+        d = ModelDesc(ctx.ndim, STRESSMODELS[ctx.stressmodel], ctx.thickness, size(coords, 2), pointer(coords),
+                      length(shape), pointer(shape), pointer(nips), pointer(conn_ptr), pointer(conn),
+                      pointer(mat_type), pointer(mat_params))
+        rc = ccall((:amr_estimate_bytes, LIB), Cint, (Ref{ModelDesc}, Ref{Int64}), d, b)
+        rc == 0 || error("amr_estimate_bytes failed ($rc)")
+    end
+    return Int(b[])
+end
+
+struct ServerInfo
+    queued::Int64; active::Int64; peak_active::Int64; completed::Int64; active_bytes::Int64; peak_bytes::Int64
+    seconds::Float64
+end
+
+"""
+    stats(srv::GPUServer) -> ServerInfo
+
+Queue length, requests on the device (now and at peak), completed requests and the
+admitted bytes (now and at peak).
+"""
+function stats(srv::GPUServer)
+    st = Ref{ServerInfo}()
+    rc = ccall((:amr_server_stats, LIB), Cint, (Ptr{Cvoid}, Ref{ServerInfo}), srv.h, st)
+    rc == 0 || error("amr_server_stats failed ($rc)")
+    return st[]
+end
+
+struct Tuning
+    ngroups::Int32
+    shape::NTuple{8,Int32}
+    stiffness_epb::NTuple{8,Int32}
+    internal_epb::NTuple{8,Int32}
+    batch_threads::Int32
+    batch_ctas_per_sm::Int32
+    stiffness_seconds::Float64
+    internal_seconds::Float64
+end
+
+"""
+    autotune!(g) -> Tuning
+
+Times the candidate launch shapes of the element kernels on this model (and of the batched
+solve) and keeps the fastest; needs the DOFs set and changes no result.
+"""
+function autotune!(g::GPUModel)
+    t = Ref{Tuning}()
+    checked(g, ccall((:amr_autotune, LIB), Cint, (Ptr{Cvoid}, Ref{Tuning}), g.h, t))
+    return t[]
+end
+
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
-       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!, save_gpu
+       nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!, save_gpu,
+       sizes, get_state, set_state!, commit_state!, restore_state!, set_youngs!, estimate_bytes, stats, autotune!
 
 end # module
