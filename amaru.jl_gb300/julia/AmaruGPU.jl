@@ -676,9 +676,9 @@ function set_state!(g::GPUModel, S::Matrix{Float64})
     return g
 end
 
-"State ← trial state (copyto!.(StateBk, State), src/mech/mech-solver.jl:333)."
+"Backup states ← current states (copyto!.(StateBk, State), src/mech/mech-solver.jl:333)."
 commit_state!(g::GPUModel) = (checked(g, ccall((:amr_state_commit, LIB), Cint, (Ptr{Cvoid},), g.h)); g)
-"Trial state ← committed state (copyto!.(State, StateBk), src/mech/mech-solver.jl:391,461)."
+"Current states ← backup states (copyto!.(State, StateBk), src/mech/mech-solver.jl:391,461)."
 restore_state!(g::GPUModel) = (checked(g, ccall((:amr_state_restore, LIB), Cint, (Ptr{Cvoid},), g.h)); g)
 
 """
