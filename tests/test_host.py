@@ -32,6 +32,58 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_lib.SIGNATURES) == names
 
 
+def test_julia_binding_calls_only_declared_symbols():
+    """Julia is not installed, so the ccall binding cannot run here: every entry point it names must at
+    least be one the header declares and the library exports."""
+    src = open(os.path.join(ROOT, "amaru.jl_gb300", "julia", "AmaruGPU.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(amr_[A-Za-z0-9_]+)\s*,", src))
+    assert len(called) >= 30
+    assert called <= set(_header_functions()), sorted(called - set(_header_functions()))
+
+
+def _julia_structs():
+    """A builder of ctypes layouts for the Julia binding's structs, from their field declarations."""
+    src = open(os.path.join(ROOT, "amaru.jl_gb300", "julia", "AmaruGPU.jl")).read()
+    blocks = re.findall(r"^(?:mutable )?struct (\w+)\n(.*?)^end", src, flags=re.S | re.M)
+    decls = {name: re.findall(r"(\w+)::([\w{}, ]+?)\s*(?=;|\n|$)", body) for name, body in blocks}
+    prim = {"Int32": ctypes.c_int32, "Int64": ctypes.c_int64, "Float64": ctypes.c_double, "Cstring": ctypes.c_char_p,
+            "Int": ctypes.c_int64}
+    built = {}
+
+    def ctype(t):
+        t = t.strip()
+        if t in prim:
+            return prim[t]
+        if t.startswith("Ptr{"):
+            return ctypes.c_void_p
+        m = re.match(r"NTuple\{(\d+),\s*(\w+)\}", t)
+        if m:
+            return ctype(m.group(2)) * int(m.group(1))
+        return build(t)
+
+    def build(name):
+        if name not in built:
+            built[name] = type(name, (ctypes.Structure,), {"_fields_": [(f, ctype(t)) for f, t in decls[name]]})
+        return built[name]
+
+    return build
+
+
+def _layout(cls):
+    return ctypes.sizeof(cls), [(getattr(cls, f).offset, getattr(cls, f).size) for f, _ in cls._fields_]
+
+
+@pytest.mark.parametrize("name", ["ModelDesc", "SolveOpts", "SolveStats", "StageParams", "StageStats", "DynParams",
+                                  "VtuArray", "ModalParams", "ModalStats", "Request", "RequestResult",
+                                  "ServerConfig", "ServerInfo", "Tuning"])
+def test_julia_struct_layouts_match_the_c_abi(name):
+    """Each struct the Julia binding passes by reference has the byte layout of the ctypes mirror of the
+    same C struct (offsets and sizes field by field)."""
+    jl = _julia_structs()(name)
+    py = getattr(_lib, name)
+    assert _layout(jl) == _layout(py)
+
+
 @pytest.mark.parametrize("shape,n", [(A.HEX8, (3, 2, 2)), (A.HEX20, (3, 2, 2)), (A.TET10, (2, 2, 2)),
                                      (A.TET4, (2, 2, 1)), (A.QUAD8, (3, 2)), (A.QUAD4, (3, 2)), (A.QUAD9, (2, 2)),
                                      (A.TRI3, (2, 2)), (A.TRI6, (2, 2))])
