@@ -146,13 +146,16 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
         if (d->ndim == 3 && d->stressmodel != AMR_D3) throw AmrError(AMR_EINVAL, "3-D analyses use the d3 stress model");
         if (d->nnodes <= 0 || d->nelems <= 0) throw AmrError(AMR_EINVAL, "empty model");
         if (d->nnodes >= INT32_MAX) throw AmrError(AMR_EUNSUPPORTED, "more than 2^31 nodes");
+        if (!d->coords || !d->shape || !d->nips || !d->conn_ptr || !d->conn || !d->mat_type || !d->mat_params)
+            throw AmrError(AMR_EINVAL, "null array in the model description");
+        // 2-D analyses need thickness > 0: the condition the reference's analysis argument tables state
+        // (src/hydromech/hydromech-solver.jl:8; the mechanical one is commented out, src/mech/dyn-solver.jl:8)
+        if (d->ndim == 2 && !(d->thickness > 0.0)) throw AmrError(AMR_EINVAL, "thickness must be > 0");
         m->ndim = d->ndim; m->B = d->ndim; m->BB = d->ndim * d->ndim;
         m->stressmodel = d->stressmodel; m->thickness = d->thickness;
         m->nnodes = d->nnodes; m->nelems = d->nelems;
-        AMR_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
-        AMR_CUDA(cudaEventCreate(&m->ev0));
-        AMR_CUDA(cudaEventCreate(&m->ev1));
-        // validate elements and group them by (shape, quadrature), stable
+        // validate elements and group them by (shape, quadrature), stable; no device call before the
+        // description is known to be valid, so that a refused description touches no GPU
         std::vector<int> nq(d->nelems);
         for (int64_t e = 0; e < d->nelems; e++) {
             int sh = d->shape[e];
@@ -210,6 +213,9 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
         }
         m->nip_total = m->h_ip_ptr.back();
         m->kel_blocks = m->h_kel_ptr.back();
+        AMR_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+        AMR_CUDA(cudaEventCreate(&m->ev0));
+        AMR_CUDA(cudaEventCreate(&m->ev1));
         cudaStream_t s = m->stream;
         m->h_coords.assign(d->coords, d->coords + 3 * d->nnodes);
         amr_alloc(&m->coords, 3 * d->nnodes);

@@ -205,3 +205,52 @@ def test_vtu_arrays_are_column_major_with_their_types():
     assert np.array_equal(buf, U.T.reshape(-1))
     assert arr[1].type == 2 and arr[1].ncomp == 1
     assert arr[2].type == 0  # other dtypes are converted to Float64: the writer takes four element types
+
+
+def _desc(ndim=3, stressmodel=_lib.D3, thickness=1.0, **over):
+    """A one-element model description (HEX8 or QUAD4) with fields replaced by `over`."""
+    shape = A.HEX8 if ndim == 3 else A.QUAD4
+    box = [[0, 0, 0], [1, 1, 1]] if ndim == 3 else [[0, 0], [1, 1]]
+    mesh = A.Mesh(A.Block(box, nx=1, ny=1, nz=1 if ndim == 3 else 0, cellshape=shape))
+    arrays = dict(coords=mesh.coords, shape=np.array([over.pop("shape", shape)]), nips=np.zeros(1),
+                  conn_ptr=np.array([0, len(mesh.conn)]), conn=mesh.conn, mat_type=np.zeros(1),
+                  mat_params=np.array([200e3, 0.3, 0, 0, 0, 0, 0, 0]))
+    arrays.update(over)
+    return _lib.model_desc(ndim, stressmodel, thickness, **arrays)
+
+
+@pytest.mark.parametrize("kw,code,words", [
+    (dict(ndim=4), -1, "ndim must be 2 or 3"),
+    (dict(ndim=2, stressmodel=_lib.AXISYMMETRIC), -10, "axisymmetric"),
+    (dict(stressmodel=_lib.PLANESTRAIN), -1, "d3 stress model"),
+    (dict(ndim=2, stressmodel=_lib.PLANESTRESS, thickness=0.0), -1, "thickness must be > 0"),
+    (dict(ndim=2, stressmodel=_lib.PLANESTRAIN, thickness=float("nan")), -1, "thickness must be > 0"),
+    (dict(shape=A.QUAD4), -10, "shape not a bulk cell"),
+    (dict(conn_ptr=np.array([0, 7])), -1, "wrong node count"),
+    (dict(conn=np.array([0, 1, 2, 3, 4, 5, 6, 99])), -1, "node index out of range"),
+    (dict(nips=np.array([5])), -1, "integration points"),
+    (dict(mat_type=np.array([7])), -10, "unsupported material"),
+    (dict(mat_params=np.array([0.0, 0.3, 0, 0, 0, 0, 0, 0])), -1, "E > 0"),
+    (dict(mat_params=np.array([1.0, 0.5, 0, 0, 0, 0, 0, 0])), -1, "nu < 0.5"),
+])
+def test_model_description_refusals(kw, code, words):
+    """amr_model_create refuses a bad description with its status code and message before any device
+    call (so on a host without a GPU as well), and hands out no handle."""
+    d, keep = _desc(**kw)
+    h = ctypes.c_void_p(0)
+    rc = _lib.lib().amr_model_create(ctypes.byref(d), ctypes.byref(h))
+    assert rc == code and not h.value
+    assert words in _lib.lib().amr_create_error().decode()
+
+
+def test_model_description_refuses_null_and_empty():
+    L = _lib.lib()
+    h = ctypes.c_void_p(0)
+    assert L.amr_model_create(None, ctypes.byref(h)) == -1 and "null argument" in L.amr_create_error().decode()
+    d, keep = _desc()
+    d.coords = None
+    assert L.amr_model_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    assert "null array" in L.amr_create_error().decode()
+    d, keep = _desc()
+    d.nelems = 0
+    assert L.amr_model_create(ctypes.byref(d), ctypes.byref(h)) == -1 and "empty model" in L.amr_create_error().decode()
