@@ -10,6 +10,7 @@ evaluates essential values and nodal loads, and moves arrays across the ABI.
 import numpy as np
 
 from . import _lib as L
+from .args import DYN_SOLVER_PARAMS, MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, checkargs
 from .expr import affine_coefficients, evaluate
 from .mesh import NPOINTS, Mesh
 
@@ -369,8 +370,8 @@ class MechAnalysis:
     def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
               autoinc=False, quiet=True, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000):
         """solve!(ana; args...) (src/mech/mech-solver.jl:155-181): returns (success, message)."""
-        if not (1 <= maxits <= 10):
-            raise ValueError("maxits must be in 1..10")
+        checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, rspan=rspan, rtol=rtol, dT0=dT0,
+                  dTmin=dTmin, dTmax=dTmax, maxits=maxits, scheme=scheme)
         model = self.model
         method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
         lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every, max_iters=max_iters)
@@ -414,6 +415,7 @@ class DynAnalysis:
     def solve(self, tol=0.01, dTmin=1e-7, dTmax=0.1, rspan=0.01, maxits=5, autoinc=False, alpha=0.0, beta=0.0,
               solver="mixed", linear_rtol=1e-8, quiet=True):
         """Returns (ok, message); dof values land in model.U, model.V, model.A, model.F (node-major)."""
+        checkargs("solve!", DYN_SOLVER_PARAMS, tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan, maxits=maxits)
         if len(self.stages) != 1:
             raise ValueError("a dynamic analysis has one stage (the reference defines V and A in the first only)")
         stage = self.stages[0]
@@ -551,8 +553,8 @@ class BatchAnalysis:
     def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
               autoinc=False, quiet=True, linear_rtol=1e-8, refine_every=32, max_iters=20000):
         """solve!(ana; args...) for every part; returns a list of (success, message), one per part."""
-        if not (1 <= maxits <= 10):
-            raise ValueError("maxits must be in 1..10")
+        checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, rspan=rspan, rtol=rtol, dT0=dT0,
+                  dTmin=dTmin, dTmax=dTmax, maxits=maxits, scheme=scheme)
         J = self.joined
         lin = L.default_solve_opts(method=L.SOLVER_MIXED, rtol=linear_rtol, refine_every=refine_every,
                                    max_iters=max_iters)

@@ -13,6 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
+from .args import MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, checkargs
 from .model import number_dofs
 
 _SCHEMES = {"FE": 0, "ME": 1, "BE": 2, "Ralston": 3}
@@ -20,7 +21,10 @@ _SCHEMES = {"FE": 0, "ME": 1, "BE": 2, "Ralston": 3}
 
 def stage_params(nincs=1, nouts=0, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE",
                  maxits=5, autoinc=False, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000):
-    """amr_stage_params with the keyword defaults of solve!(ana; ...) (src/mech/mech-solver.jl:155-168)."""
+    """amr_stage_params with the keyword defaults of solve!(ana; ...) (src/mech/mech-solver.jl:155-168),
+    checked against the conditions of that table."""
+    checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, rspan=rspan, rtol=rtol, dT0=dT0,
+              dTmin=dTmin, dTmax=dTmax, maxits=maxits, scheme=scheme)
     method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
     lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every, max_iters=max_iters)
     return L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,

@@ -254,3 +254,37 @@ def test_model_description_refuses_null_and_empty():
     d, keep = _desc()
     d.nelems = 0
     assert L.amr_model_create(ctypes.byref(d), ctypes.byref(h)) == -1 and "empty model" in L.amr_create_error().decode()
+
+
+@pytest.mark.parametrize("kw,words", [
+    (dict(tol=0.0), "tol which must satisfy tol > 0"),
+    (dict(rspan=1.0), "rspan which must satisfy 0 < rspan < 1"),
+    (dict(rtol=-1e-3), "rtol which must satisfy rtol > 0"),
+    (dict(dT0=1.5), "dT0 which must satisfy 0 < dT0 <= 1"),
+    (dict(dTmin=0.0), "dTmin which must satisfy 0 < dTmin < 1"),
+    (dict(dTmax=1.0), "dTmax which must satisfy 0 < dTmax < 1"),
+    (dict(maxits=11), "maxits which must satisfy 1 <= maxits <= 10"),
+    (dict(scheme="RK4"), "scheme which must be one of"),
+])
+def test_solver_keywords_are_checked_as_the_reference_does(kw, words):
+    """solve!'s keyword conditions (mech_solver_params, src/mech/mech-solver.jl:155-167), checked on the host
+    before anything reaches the device: no model is needed to see the refusal."""
+    from amaru_gpu import serve
+    with pytest.raises(A.ArgumentError, match=words.replace("(", r"\(")):
+        A.MechAnalysis(None).solve(**kw)
+    with pytest.raises(A.ArgumentError):
+        serve.stage_params(**kw)
+
+
+@pytest.mark.parametrize("kw", [dict(tol=-1.0), dict(dTmin=2.0), dict(dTmax=0.0), dict(rspan=0.0), dict(maxits=0)])
+def test_dynamic_solver_keywords_are_checked(kw):
+    """dyn_solver_params (src/mech/dyn-solver.jl:166-186)."""
+    with pytest.raises(A.ArgumentError, match="solve!: Invalid value for argument"):
+        A.DynAnalysis(None).solve(**kw)
+
+
+def test_solver_keyword_defaults_pass_the_checks():
+    from amaru_gpu.args import MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, checkargs
+    checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=0.01, rspan=0.01, rtol=0.01, dT0=0.01,
+              dTmin=1e-7, dTmax=0.1, maxits=5, scheme="FE")
+    checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, dT0=1.0, maxits=10, scheme="Ralston")
