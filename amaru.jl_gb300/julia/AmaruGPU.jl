@@ -90,6 +90,23 @@ material_code(m::DruckerPrager) = (Int32(2), [m.E, m.ν, m.α, m.κ, m.H, 0, 0, 
 material_code(m) = error("AmaruGPU: material $(typeof(m)) is not on the GPU path")
 
 """
+    activate!(model, stage)
+
+Applies `stage.toactivate` as mech_stage_solver! does (src/mech/mech-solver.jl:216-220).  The device
+model holds every element of the FEModel, while the reference assembles only the active ones and numbers
+only their nodes (configure_dofs!, src/bc.jl:200-202); so a model that still has inactive elements is
+refused instead of being solved with a different K.
+"""
+function activate!(model::FEModel, stage::Stage)
+    for elem in stage.toactivate
+        elem.active = true
+    end
+    all(e -> e.active, model.elems) ||
+        error("AmaruGPU: inactive elements are not on the GPU path; activate every element before a GPU stage")
+    return nothing
+end
+
+"""
     GPUModel(model::FEModel)
 
 Creates the device model: nodes, MechSolid elements with their material
@@ -211,6 +228,7 @@ does (src/mech/mech-solver.jl:394-397).
 function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
     model = ana.model
+    activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
@@ -274,6 +292,7 @@ be affine in t); ux/fx/vx/ax land in dof.vals as the reference writes them
 function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
     model = ana.model
+    activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
@@ -370,6 +389,7 @@ mech_modal_solver!, computed on the device.
 """
 function gpu_modal_solver!(ana::MechModalAnalysis, stage::Stage; nmodes::Integer=5, args...)
     model = ana.model
+    activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
@@ -503,6 +523,7 @@ function solve_batch!(b::GPUBatch, stages::Vector{Stage}; args...)
     args = Amaru.checkargs(args, Amaru.mech_solver_params)
     eqs, Us, Fs, nus, nds, dofss = [], [], [], Int[], Int[], []
     for (m, st) in zip(b.models, stages)
+        activate!(m, st)
         dofs, nu = Amaru.configure_dofs!(m, st.bcs)
         m.ndofs = length(dofs)
         Uex, Fex = Amaru.get_bc_vals(m, st.bcs)
@@ -587,6 +608,7 @@ Queues one stage of `model` (solve! keyword arguments); the server copies it.
 """
 function submit!(srv::GPUServer, model::FEModel, stage::Stage; args...)
     args = Amaru.checkargs(args, Amaru.mech_solver_params)
+    activate!(model, stage)
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
     Uex, Fex = Amaru.get_bc_vals(model, stage.bcs)
