@@ -223,16 +223,30 @@ end
 mech_stage_solver! with the Newton loop, K, the solves and the IP states on
 the device.  The essential values and loads come from Amaru's own
 configure_dofs! and get_bc_vals; the dof values are updated as the reference
-does (src/mech/mech-solver.jl:394-397).
+does (src/mech/mech-solver.jl:394-397).  Afterwards the IP states are copied
+into the elements' IpState objects and the stage's records are written as the
+reference writes them: the initial record of stage 1 (:234-242), the record of
+the checkpoint at the end of the stage, numbered as the reference numbers it
+(:412-420), and the record of a failed stage (:488).  The records of
+intermediate checkpoints (nouts > 1) are not written: the increments run on the
+device without returning to Julia.
 """
 function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
     model = ana.model
+    sctx = ana.sctx
     activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
     set_dofs!(g, model, dofs, nu)
+    if stage.id == 1
+        for dof in dofs
+            dof.vals[dof.name] = 0.0
+            dof.vals[dof.natname] = 0.0
+        end
+        Amaru.update_records!(ana, force=true)
+    end
     Uex, Fex = Amaru.get_bc_vals(model, stage.bcs)
     scheme = Dict(:FE => 0, :ME => 1, :BE => 2, :Ralston => 3)[Symbol(args.scheme)]
     lin = SolveOpts(LINEAR_METHOD[], 1e-8, 20000, 32)
@@ -249,9 +263,45 @@ function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
             dof.vals[dof.name] += U[i]
             dof.vals[dof.natname] += F[i]
         end
+        sync_states!(g, model)
+        sctx.inc = stats.increments
+        sctx.T = stats.T
     end
-    rc == 0 && return Amaru.success()
-    return check(g, rc)
+    if rc == 0
+        sctx.out += max(stage.nouts, 1)  # the checkpoints of the stage; the last one is at T = 1
+        Amaru.update_records!(ana, checkpoint=true)
+        return Amaru.success()
+    end
+    st = check(g, rc)
+    rc == -11 && Amaru.update_records!(ana, force=true)
+    return st
+end
+
+"""
+    sync_states!(g, model)
+
+Copies the device IP states into the IpState objects of the model's elements, in
+element and IP order: σ and ε, and for the plastic materials εpa and Δλ (Δγ of
+DruckerPragerState).  Julia code that reads ip.state after a GPU stage, such as
+update_output_data!'s element values and the loggers, then sees the stage's
+result.
+"""
+sync_states!(g::GPUModel, model::FEModel) = (copy_states!(get_state(g), (model,)); model)
+
+# S (16 x nip, element and IP order of the models one after the other) into the IpState objects
+function copy_states!(S::Matrix{Float64}, models)
+    k = 0
+    for model in models, elem in model.elems, ip in elem.ips
+        k += 1
+        st = ip.state
+        st.σ = typeof(st.σ)(view(S, 1:6, k))
+        st.ε = typeof(st.ε)(view(S, 7:12, k))
+        hasfield(typeof(st), :εpa) && (st.εpa = S[13, k])
+        hasfield(typeof(st), :Δλ) && (st.Δλ = S[14, k])
+        hasfield(typeof(st), :Δγ) && (st.Δγ = S[14, k])
+    end
+    k == size(S, 2) || error("AmaruGPU: IP count differs from the device model's")
+    return nothing
 end
 
 const GPU_MODELS = Dict{UInt,GPUModel}()
@@ -287,7 +337,10 @@ end
 dyn_stage_solver! of a first stage with K, M, the solves and the IP states on the
 device.  Boundary values come from Amaru's get_bc_vals at t = 0 and t = 1 (they must
 be affine in t); ux/fx/vx/ax land in dof.vals as the reference writes them
-(src/mech/dyn-solver.jl:420-425).
+(src/mech/dyn-solver.jl:420-425).  The IP states are copied into the IpState
+objects and the record of the stage's last checkpoint (or of its failure) is
+written; the initial record (:299-300) and those of intermediate checkpoints are
+not, as the increments run on the device.
 """
 function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
@@ -317,9 +370,20 @@ function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...
             us, fs, vs, as = keys[dof.name]
             dof.vals[us] = U[i]; dof.vals[fs] = F[i]; dof.vals[vs] = V[i]; dof.vals[as] = A[i]
         end
+        # IP states into the IpState objects; the record of the last checkpoint (dyn-solver.jl:447-480)
+        # or of the failure (:532), with the stage's time as the reference keeps it
+        sync_states!(g, model)
+        ana.sctx.T = stats.T
+        ana.sctx.t = stats.T * stage.tspan
     end
-    rc == 0 && return Amaru.success()
-    return check(g, rc)
+    if rc == 0
+        ana.sctx.out += max(stage.nouts, 1)
+        Amaru.update_records!(ana, checkpoint=true)
+        return Amaru.success()
+    end
+    st = check(g, rc)
+    rc == -11 && Amaru.update_records!(ana, force=true)
+    return st
 end
 
 """
@@ -553,6 +617,11 @@ function solve_batch!(b::GPUBatch, stages::Vector{Stage}; args...)
         dof.vals[dof.name] += U[j]
         dof.vals[dof.natname] += F[j]
     end
+    # every part's IP states into its IpState objects (the parts' elements follow one another)
+    S = zeros(16, sum(length(e.ips) for m in b.models for e in m.elems))
+    rc = ccall((:amr_get_state, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), b.h, S)
+    rc == 0 || error("amr_get_state failed ($rc)")
+    copy_states!(S, b.models)
     return [s.status == 0 ? Amaru.success() : Amaru.failure("Solver did not converge.") for s in buf]
 end
 
