@@ -141,6 +141,27 @@ struct AmrError {
     AmrError(int c, std::string m) : code(c), msg(std::move(m)) {}
 };
 
+// Two timing events owned for one scope: destroyed on every exit, an exception included.
+struct AmrEventPair {
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    AmrEventPair() {
+        const cudaError_t e0 = cudaEventCreate(&t0);
+        const cudaError_t e1 = e0 == cudaSuccess ? cudaEventCreate(&t1) : e0;
+        if (e1 != cudaSuccess) {
+            release();
+            throw AmrError(AMR_ECUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e1));
+        }
+    }
+    ~AmrEventPair() { release(); }
+    AmrEventPair(const AmrEventPair &) = delete;
+    AmrEventPair &operator=(const AmrEventPair &) = delete;
+    void release() {
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
+        t0 = t1 = nullptr;
+    }
+};
+
 template <class T>
 inline void amr_alloc(T **p, size_t n) {
     if (n == 0) n = 1;

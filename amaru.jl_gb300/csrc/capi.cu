@@ -903,9 +903,8 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
     };
     int status = AMR_OK;
     amr_stage_stats st{};
-    cudaEvent_t t0, t1;
-    AMR_CUDA(cudaEventCreate(&t0));
-    AMR_CUDA(cudaEventCreate(&t1));
+    AmrEventPair ev;  // destroyed on every exit
+    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
     AMR_CUDA(cudaEventRecord(t0, s));
     try {
         for (double *x : {U, F, R, dUa, dUi, Rc, dFin}) AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
@@ -1048,13 +1047,9 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
         AMR_CUDA(cudaEventElapsedTime(&ms, t0, t1));
         st.seconds = ms * 1e-3;
     } catch (...) {
-        cudaEventDestroy(t0);
-        cudaEventDestroy(t1);
         release();
         throw;
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     release();
     if (stats) *stats = st;
     return status;

@@ -200,9 +200,8 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
            *reac = v[15];
     int status = AMR_OK;
     amr_stage_stats st{};
-    cudaEvent_t t0, t1;
-    AMR_CUDA(cudaEventCreate(&t0));
-    AMR_CUDA(cudaEventCreate(&t1));
+    AmrEventPair ev;  // destroyed on every exit
+    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
     try {
         AMR_CUDA(cudaEventRecord(t0, s));
         for (double *x : {U, V, A, F, Fin, Fina, dUa, dUi, Va, Aa})
@@ -334,13 +333,9 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
         AMR_CUDA(cudaEventElapsedTime(&ms, t0, t1));
         st.seconds = ms * 1e-3;
     } catch (...) {
-        cudaEventDestroy(t0);
-        cudaEventDestroy(t1);
         release();
         throw;
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     release();
     if (stats) *stats = st;
     return status;

@@ -422,9 +422,8 @@ int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, dou
     }
     cudaStream_t s = m->stream;
     const int64_t n = m->nnodes * m->B;
-    cudaEvent_t t0, t1;
-    AMR_CUDA(cudaEventCreate(&t0));
-    AMR_CUDA(cudaEventCreate(&t1));
+    AmrEventPair ev;  // destroyed on every exit
+    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
     AMR_CUDA(cudaEventRecord(t0, s));
     // K11 (masked K64, its FP32 copy and the multigrid hierarchy) and D
     amr_stiffness(m);
@@ -559,13 +558,9 @@ int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, dou
         AMR_CUDA(cudaEventElapsedTime(&ms, t0, t1));
         st.seconds = ms * 1e-3;
     } catch (...) {
-        cudaEventDestroy(t0);
-        cudaEventDestroy(t1);
         release();
         throw;
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     release();
     if (stats) *stats = st;
     return AMR_OK;
