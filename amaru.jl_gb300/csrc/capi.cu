@@ -884,29 +884,27 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
     }
     const bool corrector = p.scheme != AMR_SCHEME_FE;
     if (p.maxits < 1 || p.nincs < 1) throw AmrError(AMR_EINVAL, "bad stage parameters");
+    AmrEventPair ev;  // destroyed on every exit
+    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
     std::vector<double *> v(10, nullptr);
-    for (auto &x : v) amr_alloc(&x, n);
-    double *R = v[0], *dUa = v[1], *dUi = v[2], *Rc = v[3], *dFin = v[4], *dFex = v[5], *dUitr = v[6], *Rtr = v[7],
-           *reac = v[8], *dUt = v[9];
     double *Ks = nullptr;  // the predictor's tangent, kept for the weighted corrector tangent
-    if (corrector) {
-        try {
-            amr_alloc(&Ks, (size_t)m->bstride * m->BB);
-        } catch (...) {
-            for (auto &x : v) amr_free(x);
-            throw;
-        }
-    }
     auto release = [&]() {
         for (auto &x : v) amr_free(x);
         amr_free(Ks);
     };
+    try {
+        for (auto &x : v) amr_alloc(&x, n);
+        if (corrector) amr_alloc(&Ks, (size_t)m->bstride * m->BB);
+    } catch (...) {
+        release();
+        throw;
+    }
+    double *R = v[0], *dUa = v[1], *dUi = v[2], *Rc = v[3], *dFin = v[4], *dFex = v[5], *dUitr = v[6], *Rtr = v[7],
+           *reac = v[8], *dUt = v[9];
     int status = AMR_OK;
     amr_stage_stats st{};
-    AmrEventPair ev;  // destroyed on every exit
-    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
-    AMR_CUDA(cudaEventRecord(t0, s));
     try {
+        AMR_CUDA(cudaEventRecord(t0, s));
         for (double *x : {U, F, R, dUa, dUi, Rc, dFin}) AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
         double tol = p.tol, rtol = p.rtol, dTmin = p.dTmin;
         bool autoinc = p.autoinc != 0;

@@ -182,6 +182,8 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
     cudaStream_t s = m->stream;
     const size_t nK = (size_t)m->bstride * m->BB;
     const size_t nst = (size_t)AMR_NST * m->nip_total * sizeof(double);
+    AmrEventPair ev;  // destroyed on every exit
+    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
     std::vector<double *> v(16, nullptr);
     double *Ks = nullptr;
     auto release = [&]() {
@@ -200,8 +202,6 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
            *reac = v[15];
     int status = AMR_OK;
     amr_stage_stats st{};
-    AmrEventPair ev;  // destroyed on every exit
-    cudaEvent_t t0 = ev.t0, t1 = ev.t1;
     try {
         AMR_CUDA(cudaEventRecord(t0, s));
         for (double *x : {U, V, A, F, Fin, Fina, dUa, dUi, Va, Aa})
