@@ -168,6 +168,7 @@ inline void amr_alloc(T **p, size_t n) {
     cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
     if (e != cudaSuccess) {
         cudaGetLastError();
+        *p = nullptr;  // a failed allocation leaves nothing for the caller's cleanup to free
         throw AmrError(AMR_ENOMEM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes: " +
                                        cudaGetErrorString(e));
     }

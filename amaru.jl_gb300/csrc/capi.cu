@@ -625,10 +625,10 @@ int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_
         amr_default_stage_params(&prm);
         if (p) prm = *p;
         int64_t n = m->nnodes * m->B;
-        double *uex, *fex, *u, *f;
-        amr_alloc(&uex, n); amr_alloc(&fex, n); amr_alloc(&u, n); amr_alloc(&f, n);
+        double *uex = nullptr, *fex = nullptr, *u = nullptr, *f = nullptr;
         int rc;
         try {
+            amr_alloc(&uex, n); amr_alloc(&fex, n); amr_alloc(&u, n); amr_alloc(&f, n);
             eq_host_to_nm(m, Uex, uex);
             eq_host_to_nm(m, Fex, fex);
             rc = amr_stage_device(m, uex, fex, prm, u, f, stats);
