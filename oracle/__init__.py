@@ -14,7 +14,12 @@ known-answer test of the reference's test suite for this path
 test/mech/mat/vm-3d.jl, vm-2d.jl, dp.jl, test/mesh/structured.jl).  The
 reference's tests hold no nodal recovery values; the recovery restatement is
 pinned by the fields it must reproduce exactly (polynomials of the regression
-space) in tests/test_recovery.py.
+space) in tests/test_recovery.py.  The dynamic and modal restatements are pinned
+by properties of their methods (tests/test_dynamic.py: the consistent mass, the
+conserved discrete energy, the closed Newmark recursion; tests/test_modal.py: the
+dense eigenproblem), and the VTU writer by a snippet written from the
+reference's writer (tests/test_vtu.py).  tests/golden/ stores outputs of this
+oracle, and tests/test_golden.py checks that it still reproduces them.
 """
 from .core import *  # noqa: F401,F403
 from .recovery import nodal_patch_recovery, ip_coords, ip_state_vals, field_names  # noqa: F401
