@@ -17,8 +17,7 @@ import numpy as np
 import pytest
 
 import amaru_gpu as A
-
-pytestmark = pytest.mark.gpu
+import oracle as O
 
 SEED = 0xA11A
 
@@ -34,6 +33,20 @@ def _stage():
     return mesh, model, ana
 
 
+def test_oracle_stage_equilibrium_on_the_same_workload_family():
+    """The property itself, on the oracle's direct solve at HEX20 5x2x2: reactions (40, 0, 0 up to round-off)."""
+    mesh = O.Mesh(O.Block([[0, 0, 0], [10.0, 4.0, 4.0]], nx=5, ny=2, nz=2, cellshape=O.HEX20))
+    E = np.exp(np.random.default_rng(SEED).normal(np.log(30e3), 0.3, len(mesh.elems)))
+    om = O.FEModel(mesh, [("all", O.LinearElastic(E=30e3, nu=0.2))], nips=27, elem_E=E)
+    ana = O.MechAnalysis(om)
+    ana.addstage([("z==0", O.SurfaceBC(ux=0, uy=0, uz=0)), ("z==4", O.SurfaceBC(tz=-1.0))])
+    assert ana.solve()[0]
+    R = om.F[mesh.select_nodes("z==0")].sum(axis=0)
+    assert abs(R[2] - 40.0) <= 1e-12 * 40.0 and np.abs(R[:2]).max() <= 1e-12 * 40.0
+    assert om.U[mesh.select_nodes("z==4"), 2].max() < 0.0
+
+
+@pytest.mark.gpu
 def test_full_size_stage_equilibrium_and_repeatability():
     mesh, model, ana = _stage()
     assert model.ndofs == 2007483
