@@ -1,5 +1,10 @@
-"""Host-side logic (no GPU): the C-ABI library's exports, the structured mesher,
-expression evaluation and DOF numbering, each checked against the oracle."""
+"""Host-side logic (no GPU).
+
+  * the C-ABI library's exports, and the Julia binding's entry points and struct layouts against them;
+  * the structured mesher, expression evaluation and DOF numbering, each checked against the oracle;
+  * the boundary's refusals of bad model descriptions and solver keywords, before any device call;
+  * no CPU fallback: the GPU path raises without its library.
+"""
 import ctypes
 import os
 import re
@@ -288,3 +293,14 @@ def test_solver_keyword_defaults_pass_the_checks():
     checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=0.01, rspan=0.01, rtol=0.01, dT0=0.01,
               dTmin=1e-7, dTmax=0.1, maxits=5, scheme="FE")
     checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, dT0=1.0, maxits=10, scheme="Ralston")
+
+
+def test_the_gpu_path_fails_loudly_without_its_library(monkeypatch, tmp_path):
+    """No CPU fallback: with the CUDA library absent, loading it and building a model raise."""
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libamaru_gpu.so"))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.lib()
+    mesh = A.Mesh(A.Block([[0, 0, 0], [1, 1, 1]], nx=1, ny=1, nz=1, cellshape=A.HEX8))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        A.FEModel(mesh, [("all", A.LinearElastic(E=1.0, nu=0.2))])
