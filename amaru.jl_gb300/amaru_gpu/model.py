@@ -455,18 +455,42 @@ class ModalAnalysis:
         self.freqs = np.zeros(0)
         self.modes = np.zeros((0, 0))
         self.stats = None
+        self.alpha = self.beta = None
 
     def addstage(self, bcs, nincs=1, nouts=0):
         self.stages.append(Stage(bcs, nincs, nouts))
 
-    def solve(self, nmodes=5, tol=1e-7, max_iters=1000, quiet=True):
+    def solve(self, nmodes=5, tol=1e-7, max_iters=1000, quiet=True, rayleigh=None):
+        """rayleigh=(xi1, xi2, i1, i2) also sets self.alpha, self.beta (see set_rayleigh)."""
         model = self.model
         for stage in self.stages:
             model.configure_dofs(stage.bcs)
             model.dev.set_density(model.rho)
             self.freqs, self.modes, self.stats = model.dev.modal(nmodes, tol, max_iters)
             stage.status = "done"
+        if rayleigh is not None:
+            self.set_rayleigh(*rayleigh)
         return True, ""
+
+    def set_rayleigh(self, xi1, xi2, i1=1, i2=2):
+        """The rayleigh option of mech_modal_solver! (src/mech/mech-modal-solver.jl:204-226): Rayleigh damping
+        C = alpha M + beta K whose damping ratio alpha/(2w) + beta w/2 is xi1 at mode i1 and xi2 at mode i2
+        (1-based, as the reference reads them).  The reference asks for the four values on standard input;
+        here they are arguments.  Returns and keeps (alpha, beta)."""
+        if not (1 <= i1 <= len(self.freqs) and 1 <= i2 <= len(self.freqs)) or i1 == i2:
+            raise ValueError("two different modes among the %d computed are needed" % len(self.freqs))
+        self.alpha, self.beta = rayleigh_coefficients(self.freqs[i1 - 1], self.freqs[i2 - 1], xi1, xi2)
+        return self.alpha, self.beta
+
+
+
+def rayleigh_coefficients(w1, w2, xi1, xi2):
+    """(alpha, beta) of Rayleigh damping with damping ratio xi1 at circular frequency w1 and xi2 at w2: the
+    solution of alpha/(2 w) + beta w/2 = xi at both (src/mech/mech-modal-solver.jl:221-222)."""
+    d = w1 * w1 - w2 * w2
+    if d == 0.0:
+        raise ValueError("the two frequencies must differ")
+    return 2.0 * (w1 * w1 * w2 * xi2 - w1 * w2 * w2 * xi1) / d, 2.0 * (w1 * xi1 - w2 * xi2) / d
 
 
 def _shift_setup(setup, noff, eoff):

@@ -467,7 +467,30 @@ function gpu_modal_solver!(ana::MechModalAnalysis, stage::Stage; nmodes::Integer
                    Ref{ModalStats}), g.h, ModalParams(nmodes, 1000, 1e-7), w, V, st))
     ana.freqs = w
     ana.modes = V
+    if get(args, :rayleigh, false)
+        # the rayleigh option (src/mech/mech-modal-solver.jl:204-226): two damping ratios and two of the
+        # computed modes, read from standard input in the reference's order
+        ask(q) = (println(q); chomp(readline()))
+        ξ1 = parse(Float64, ask("Damping ratio 1 (xi1 = c/c_c)?"))
+        ξ2 = parse(Float64, ask("Damping ratio 2 (xi2 = c/c_c)?"))
+        i1 = parse(Int, ask("Mode of the first frequency?"))
+        i2 = parse(Int, ask("Mode of the second frequency?"))
+        α, β = rayleigh_coefficients(w[i1], w[i2], ξ1, ξ2)
+        Amaru.info("Rayleigh alpha: ", α)
+        Amaru.info("Rayleigh beta:", β)
+    end
     return Amaru.success()
+end
+
+"""
+    rayleigh_coefficients(w1, w2, ξ1, ξ2) -> (α, β)
+
+Rayleigh damping C = αM + βK whose damping ratio α/(2ω) + βω/2 is ξ1 at ω = w1 and ξ2 at ω = w2
+(src/mech/mech-modal-solver.jl:221-222).
+"""
+function rayleigh_coefficients(w1, w2, ξ1, ξ2)
+    d = w1^2 - w2^2
+    return 2 * (w1^2 * w2 * ξ2 - w1 * w2^2 * ξ1) / d, 2 * (w1 * ξ1 - w2 * ξ2) / d
 end
 
 # ---------------------------------------------------------------------------
@@ -846,6 +869,7 @@ end
 
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
        nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!, save_gpu,
-       sizes, get_state, set_state!, commit_state!, restore_state!, set_youngs!, estimate_bytes, stats, autotune!
+       sizes, get_state, set_state!, commit_state!, restore_state!, set_youngs!, estimate_bytes, stats, autotune!,
+       rayleigh_coefficients
 
 end # module

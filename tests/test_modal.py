@@ -99,3 +99,21 @@ def test_gpu_modal_residual_at_size():
     for i in range(len(w)):
         Pv = K11 @ (V[:, i] / L)
         assert np.linalg.norm(Pv - w[i] ** 2 * V[:, i]) <= 1e-6 * np.linalg.norm(Pv)
+
+
+def test_rayleigh_coefficients_give_the_requested_damping_ratios():
+    """mech_modal_solver!'s rayleigh option (src/mech/mech-modal-solver.jl:204-226): alpha/(2w) + beta w/2
+    equals xi1 at w1 and xi2 at w2."""
+    from amaru_gpu.model import rayleigh_coefficients
+    for w1, w2, xi1, xi2 in [(3.81, 22.9, 0.02, 0.05), (598.2, 709.0, 0.05, 0.05), (10.0, 1.0, 0.1, 0.01)]:
+        a, b = rayleigh_coefficients(w1, w2, xi1, xi2)
+        for w, xi in ((w1, xi1), (w2, xi2)):
+            assert abs(a / (2 * w) + b * w / 2 - xi) <= 1e-14 * max(1.0, xi)
+    ana = A.ModalAnalysis(None)
+    ana.freqs = np.array([3.81, 22.9, 58.6])
+    a, b = ana.set_rayleigh(0.02, 0.05, 1, 3)
+    assert (a, b) == (ana.alpha, ana.beta) == rayleigh_coefficients(3.81, 58.6, 0.02, 0.05)
+    with pytest.raises(ValueError):
+        ana.set_rayleigh(0.02, 0.05, 2, 2)
+    with pytest.raises(ValueError):
+        ana.set_rayleigh(0.02, 0.05, 1, 4)
