@@ -344,6 +344,8 @@ not, as the increments run on the device.
 """
 function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
+    get(args, :sism, false) &&
+        error("AmaruGPU: seismic input (sism=true, src/mech/dyn-solver.jl:271-287) is not on the GPU path")
     model = ana.model
     activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
