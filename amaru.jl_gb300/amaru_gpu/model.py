@@ -413,9 +413,11 @@ class DynAnalysis:
         self.stages.append(st)
 
     def solve(self, tol=0.01, dTmin=1e-7, dTmax=0.1, rspan=0.01, maxits=5, autoinc=False, alpha=0.0, beta=0.0,
-              solver="mixed", linear_rtol=1e-8, quiet=True):
-        """Returns (ok, message); dof values land in model.U, model.V, model.A, model.F (node-major)."""
-        checkargs("solve!", DYN_SOLVER_PARAMS, tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan, maxits=maxits)
+              solver="mixed", linear_rtol=1e-8, quiet=True, scheme="FE"):
+        """Returns (ok, message); dof values land in model.U, model.V, model.A, model.F (node-major).  `scheme`
+        is checked as dyn_solver_params checks it and, as in dyn_stage_solver!, not used."""
+        checkargs("solve!", DYN_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan,
+                  maxits=maxits, scheme=scheme)
         if len(self.stages) != 1:
             raise ValueError("a dynamic analysis has one stage (the reference defines V and A in the first only)")
         stage = self.stages[0]

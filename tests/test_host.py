@@ -281,7 +281,8 @@ def test_solver_keywords_are_checked_as_the_reference_does(kw, words):
         serve.stage_params(**kw)
 
 
-@pytest.mark.parametrize("kw", [dict(tol=-1.0), dict(dTmin=2.0), dict(dTmax=0.0), dict(rspan=0.0), dict(maxits=0)])
+@pytest.mark.parametrize("kw", [dict(tol=-1.0), dict(dTmin=2.0), dict(dTmax=0.0), dict(rspan=0.0), dict(maxits=0),
+                                dict(scheme="RK4")])
 def test_dynamic_solver_keywords_are_checked(kw):
     """dyn_solver_params (src/mech/dyn-solver.jl:166-186)."""
     with pytest.raises(A.ArgumentError, match="solve!: Invalid value for argument"):
