@@ -11,7 +11,7 @@ only as the checker.  The CUDA library never calls it.
 Parity pin: tests/test_oracle_golden.py checks this oracle against every
 known-answer test of the reference's test suite for this path
 (test/mech/elem/elastic-hex8.jl, elastic-quad4.jl, elastic-elems.jl,
-test/mech/mat/vm-3d.jl, vm-2d.jl, dp.jl, test/mesh/structured.jl).  The
+test/mech/mat/vm-3d.jl, vm-2d.jl, dp.jl, test/mesh/structured.jl, test/mech/elem/axisymmetric.jl).  The
 reference's tests hold no nodal recovery values; the recovery restatement is
 pinned by the fields it must reproduce exactly (polynomials of the regression
 space) in tests/test_recovery.py.  The dynamic and modal restatements are pinned

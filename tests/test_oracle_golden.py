@@ -138,3 +138,18 @@ def test_shape_functions(shape):
             rp[k] += h; rm[k] -= h
             fd = (O.shape_func(shape, rp) - O.shape_func(shape, rm)) / (2 * h)
             np.testing.assert_allclose(D[:, k], fd, atol=1e-6)
+
+
+@pytest.mark.parametrize("shape", [O.TRI3, O.TRI6, O.QUAD4, O.QUAD8])
+def test_axisymmetric(shape):
+    """test/mech/elem/axisymmetric.jl: the axisymmetric block [0,1]^2 (4x4 cells, E=100, nu=0.2, axis x=0 with
+    ux=0, base uy=0, ty=-10 on top) equals its 3-D revolution at node (1, 1) to 1e-3.  Uniaxial compression is
+    homogeneous, so both equal the exact u_r = nu*10/E = 0.02, u_y = -10/E = -0.1, which the restatement must
+    give.  (The GPU path refuses axisymmetric analyses.)"""
+    mesh = O.Mesh(O.Block([[0, 0], [1, 1]], nx=4, ny=4, cellshape=shape))
+    om = O.FEModel(mesh, [("all", O.LinearElastic(E=100.0, nu=0.2))], stressmodel="axisymmetric")
+    ana = O.MechAnalysis(om)
+    ana.addstage([("x==0", O.SurfaceBC(ux=0)), ("y==0", O.SurfaceBC(uy=0)), ("y==1", O.SurfaceBC(ty=-10))])
+    assert ana.solve()[0]
+    n = mesh.select_nodes("x==1 && y==1")[0]
+    np.testing.assert_allclose(om.U[n, :2], [0.02, -0.1], atol=1e-3)
