@@ -20,9 +20,11 @@ LIN2, LIN3, TRI3, TRI6, QUAD4, QUAD8, QUAD9, TET4, TET10, HEX8, HEX20 = range(1,
 D3, PLANESTRAIN, PLANESTRESS, AXISYMMETRIC = 0, 1, 2, 3
 LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
 LOAD_FACET, LOAD_BODY = 0, 1
-SOLVER_MIXED, SOLVER_FP64, SOLVER_AMG = 0, 1, 2
+SOLVER_MIXED, SOLVER_FP64, SOLVER_AMG, SOLVER_AMG_FP64 = 0, 1, 2, 3
 ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
 KERNEL_SPMV32, KERNEL_RESIDUAL64, KERNEL_AMG_RESIDUAL, KERNEL_DYN_RHS = 0, 1, 5, 6
+KERNEL_SPMV64, KERNEL_AMG_RESIDUAL64 = 7, 8
+PEAK_FP64_FMA, PEAK_FP32_FMA = 0, 1
 
 
 class AmrError(RuntimeError):
@@ -62,6 +64,19 @@ class StageStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("increments", C.c_int32), ("iterations", C.c_int32),
                 ("krylov_iterations", C.c_int32), ("residue", C.c_double), ("T", C.c_double),
                 ("seconds", C.c_double), ("solve_seconds", C.c_double)]
+
+
+class IterationRecord(C.Structure):
+    _fields_ = [("increment", C.c_int32), ("iteration", C.c_int32), ("krylov_iterations", C.c_int32),
+                ("converged", C.c_int32), ("T", C.c_double), ("dT", C.c_double), ("residue", C.c_double)]
+
+
+class IncrementInfo(C.Structure):
+    _fields_ = [("T", C.c_double), ("increment", C.c_int32), ("checkpoint", C.c_int32), ("ndofs", C.c_int64),
+                ("U", C.POINTER(C.c_double)), ("F", C.POINTER(C.c_double))]
+
+
+INCREMENT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(IncrementInfo))
 
 
 MAX_TUNED_GROUPS = 8
@@ -175,6 +190,10 @@ SIGNATURES = {
     "amr_server_destroy": (C.c_int, [P]),
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "amr_alloc_count": (C.c_int, [C.POINTER(C.c_int64)]),
+    "amr_get_stage_log": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
+    "amr_set_increment_callback": (C.c_int, [P, INCREMENT_FN, C.c_void_p]),
+    "amr_measure_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "amr_set_density": (C.c_int, [P, P]),
     "amr_assemble_M": (C.c_int, [P]),
     "amr_get_M_csc": (C.c_int, [P, C.POINTER(C.c_int64), P, P, P]),
@@ -227,6 +246,13 @@ def check(h, rc):
             msg = (lib().amr_create_error() or b"").decode("utf-8", "replace")
         raise AmrError(rc, msg)
     return rc
+
+
+def measure_peak(which):
+    """TFLOP/s of fused multiply-adds on the current GPU (amr_measure_peak): PEAK_FP64_FMA or PEAK_FP32_FMA."""
+    t = C.c_double()
+    check(None, lib().amr_measure_peak(which, C.byref(t)))
+    return t.value
 
 
 def default_solve_opts(**kw):
@@ -389,6 +415,33 @@ class DeviceModel:
         rc = lib().amr_stage_run(self.h, ptr(Uex), ptr(Fex), C.byref(params), ptr(U), ptr(F), C.byref(st))
         return rc, U, F, st
 
+    def stage_log(self):
+        """The last whole-model stage's Newton iterations (amr_get_stage_log)."""
+        n = C.c_int32()
+        check(self.h, lib().amr_get_stage_log(self.h, None, 0, C.byref(n)))
+        rec = (IterationRecord * max(n.value, 1))()
+        check(self.h, lib().amr_get_stage_log(self.h, rec, n.value, C.byref(n)))
+        return list(rec[:n.value])
+
+    def set_increment_callback(self, fn):
+        """fn(T, increment, checkpoint, U, F) -> truthy to stop, after every converged increment of a stage
+        (amr_set_increment_callback); U and F are copies.  None clears it."""
+        if fn is None:
+            self._inc_cb = None
+            check(self.h, lib().amr_set_increment_callback(self.h, INCREMENT_FN(), None))
+            return
+
+        def tramp(_user, info):
+            i = info.contents
+            U = np.ctypeslib.as_array(i.U, shape=(i.ndofs,)).copy() if i.ndofs else np.zeros(0)
+            F = np.ctypeslib.as_array(i.F, shape=(i.ndofs,)).copy() if i.ndofs else np.zeros(0)
+            try:
+                return 1 if fn(i.T, i.increment, bool(i.checkpoint), U, F) else 0
+            except Exception:  # noqa: BLE001 -- an exception must not cross the C ABI: stop the stage
+                return 1
+        self._inc_cb = INCREMENT_FN(tramp)  # kept alive while the library holds it
+        check(self.h, lib().amr_set_increment_callback(self.h, self._inc_cb, None))
+
     def stage_run_dev(self, d_Uex, d_Fex, params, d_U, d_F):
         """Device-pointer variant: arguments are raw CUDA device addresses (ints) of ndofs doubles."""
         st = StageStats()
@@ -487,6 +540,13 @@ class DeviceModel:
     def launch_count(self):
         n = C.c_int64()
         check(self.h, lib().amr_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    @staticmethod
+    def alloc_count():
+        """Device allocations and frees the library has made in this process (all handles)."""
+        n = C.c_int64()
+        check(None, lib().amr_alloc_count(C.byref(n)))
         return n.value
 
     def last_error(self):

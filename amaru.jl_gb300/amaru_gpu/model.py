@@ -362,18 +362,22 @@ class MechAnalysis:
         self.model = model
         self.stages = []
         self.stats = []
+        self.log = []  # (stage, inc, it, residue) per Newton iteration, as the reference's log lines
 
     def addstage(self, bcs, nincs=1, nouts=0):
         """addstage!(ana, bcs; nincs, nouts): src/analysis.jl:27-32"""
         self.stages.append(Stage(bcs, nincs, nouts))
 
     def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
-              autoinc=False, quiet=True, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000):
-        """solve!(ana; args...) (src/mech/mech-solver.jl:155-181): returns (success, message)."""
+              autoinc=False, quiet=True, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000,
+              record=None):
+        """solve!(ana; args...) (src/mech/mech-solver.jl:155-181): returns (success, message).
+        record(ana, T, checkpoint), if given, runs after every converged increment, where the reference calls
+        update_records! (:410-424), with model.U and model.F holding the dof values so far."""
         checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, rspan=rspan, rtol=rtol, dT0=dT0,
                   dTmin=dTmin, dTmax=dTmax, maxits=maxits, scheme=scheme)
         model = self.model
-        method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
+        method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG, "amg_fp64": L.SOLVER_AMG_FP64}[solver]
         lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every, max_iters=max_iters)
         for st in self.stages:
             if st.status == "done":
@@ -383,8 +387,23 @@ class MechAnalysis:
             p = L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,
                                        scheme={"FE": 0, "ME": 1, "BE": 2, "Ralston": 3}[scheme], maxits=maxits,
                                        autoinc=int(autoinc), nincs=st.nincs, nouts=st.nouts, linear=lin)
-            rc, U, F, stats = model.dev.stage_run(Uex, Fex, p)
+            if record is not None:
+                U0, F0 = model.U.copy(), model.F.copy()
+
+                def hook(T, inc, checkpoint, Us, Fs):
+                    model.U[:], model.F[:] = U0, F0
+                    model.U[model.dof_node, model.dof_comp] += Us
+                    model.F[model.dof_node, model.dof_comp] += Fs
+                    return record(self, T, checkpoint)
+                model.dev.set_increment_callback(hook)
+            try:
+                rc, U, F, stats = model.dev.stage_run(Uex, Fex, p)
+            finally:
+                if record is not None:
+                    model.dev.set_increment_callback(None)
+                    model.U[:], model.F[:] = U0, F0
             self.stats.append(stats)
+            self.log += [(st, r.increment, r.iteration, r.residue) for r in model.dev.stage_log()]
             if rc not in (0, -11):
                 raise L.AmrError(rc, model.dev.last_error())
             model.U[model.dof_node, model.dof_comp] += U
@@ -431,7 +450,7 @@ class DynAnalysis:
             if np.abs(a + 0.5 * b - c).max(initial=0.0) > 1e-12 * max(np.abs(c).max(initial=0.0), 1.0):
                 raise NotImplementedError("boundary values must be affine in time on the GPU path")
         model.dev.set_density(model.rho)
-        method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
+        method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG, "amg_fp64": L.SOLVER_AMG_FP64}[solver]
         p = L.default_dyn_params(tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan, alpha=alpha, beta=beta,
                                  tspan=stage.tspan, maxits=maxits, autoinc=int(autoinc), nincs=stage.nincs,
                                  nouts=stage.nouts, linear=L.default_solve_opts(method=method, rtol=linear_rtol))

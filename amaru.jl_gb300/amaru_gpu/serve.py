@@ -25,7 +25,7 @@ def stage_params(nincs=1, nouts=0, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dT
     checked against the conditions of that table."""
     checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, rspan=rspan, rtol=rtol, dT0=dT0,
               dTmin=dTmin, dTmax=dTmax, maxits=maxits, scheme=scheme)
-    method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG}[solver]
+    method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG, "amg_fp64": L.SOLVER_AMG_FP64}[solver]
     lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every, max_iters=max_iters)
     return L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,
                                   scheme=_SCHEMES[scheme], maxits=maxits, autoinc=int(autoinc), nincs=nincs,

@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 
 #include "amr_internal.h"
 
@@ -127,41 +128,68 @@ void parallel_for(int64_t n, F f) {
 
 }  // namespace
 
+// Values of one level in one precision: the FP32 cycle preconditions the mixed solver; the FP64 cycle,
+// built on the same structure, preconditions the all-FP64 comparator.
+template <class V>
+struct AmgVals {
+    V *A = nullptr;     // this level's matrix (levels >= 1): BSR, b x b blocks, SoA values [b*b][nbs]
+    V *Dinv = nullptr;  // n x b*b block-Jacobi inverses (level 0: the solver's own)
+    V *T = nullptr;     // n x b x NM prolongator blocks to the next level
+    V *x = nullptr, *bv = nullptr, *r = nullptr, *d = nullptr;  // vectors of this level (n*b)
+    double lam = 1.0;
+};
+
 struct AmgLevel {
     int b = 0;
     int64_t n = 0;
-    // matrix of this level (levels >= 1): BSR, b x b blocks, SoA values [b*b][nbs]
     int64_t nblocks = 0, nbs = 0;
     int64_t *rp = nullptr;
     int32_t *cj = nullptr;
     int64_t *diag = nullptr;
-    float *A = nullptr;
-    float *Dinv = nullptr;  // n x b*b block-Jacobi inverses (level 0: the solver's Minv32)
-    double lam = 1.0;
     // to the next coarser level
     int64_t naggs = 0;
     int32_t *agg = nullptr;   // node -> aggregate
-    float *T = nullptr;       // n x b x NM prolongator blocks
     int64_t *aptr = nullptr;  // aggregate -> its nodes
     int32_t *anodes = nullptr;
     int64_t *cptr = nullptr;  // coarse block -> contributions (fine block k, fine row i)
     int32_t *ck = nullptr, *ci = nullptr;
     uint8_t *null_dof = nullptr;  // coarse DOFs with no mode (aggregate of prescribed DOFs): identity
-    // vectors of this level: x, b, r, d (n*b)
-    float *x = nullptr, *bv = nullptr, *r = nullptr, *d = nullptr;
+    std::vector<double> hT;       // the prolongator blocks on the host (uploaded in FP64 on first use)
+    AmgVals<float> f32;
+    AmgVals<double> f64;
 };
 
 struct AmrAmg {
     int NM = 6;
     std::vector<AmgLevel> L;
     int64_t nc = 0;             // DOFs of the dense coarsest level
-    double *Cd = nullptr;       // nc x nc FP64 work (Gauss-Jordan)
-    float *Cinv = nullptr;      // nc x nc FP32 inverse
+    double *Cd = nullptr;       // nc x 2nc FP64 work (Gauss-Jordan)
+    float *Cinv = nullptr;      // nc x nc inverse, FP32 cycle
+    double *Cinv64 = nullptr;   // nc x nc inverse, FP64 cycle
     double *scratch = nullptr;  // norms: [0] result, [8..] per-CTA partials
     unsigned int *ticket = nullptr;
     int64_t dofs_version = -1;
-    bool numeric_valid = false;
+    bool numeric_valid = false, numeric64_valid = false;
 };
+
+namespace {
+template <class V>
+AmgVals<V> &vals(AmgLevel &L);
+template <>
+AmgVals<float> &vals<float>(AmgLevel &L) { return L.f32; }
+template <>
+AmgVals<double> &vals<double>(AmgLevel &L) { return L.f64; }
+
+template <class V>
+void free_vals(AmgVals<V> &v, bool owns_matrix) {
+    if (owns_matrix) {
+        amr_free(v.A);
+        amr_free(v.Dinv);
+    }
+    amr_free(v.T);
+    amr_free(v.x); amr_free(v.bv); amr_free(v.r); amr_free(v.d);
+}
+}  // namespace
 
 void amr_amg_free(amr_model *m) {
     AmrAmg *g = m->amg;
@@ -169,13 +197,14 @@ void amr_amg_free(amr_model *m) {
     for (size_t l = 0; l < g->L.size(); l++) {
         AmgLevel &v = g->L[l];
         if (l > 0) {
-            amr_free(v.rp); amr_free(v.cj); amr_free(v.A); amr_free(v.Dinv);
+            amr_free(v.rp); amr_free(v.cj);
         }
-        amr_free(v.diag); amr_free(v.agg); amr_free(v.T); amr_free(v.aptr); amr_free(v.anodes);
+        free_vals(v.f32, l > 0);
+        free_vals(v.f64, l > 0);
+        amr_free(v.diag); amr_free(v.agg); amr_free(v.aptr); amr_free(v.anodes);
         amr_free(v.cptr); amr_free(v.ck); amr_free(v.ci); amr_free(v.null_dof);
-        amr_free(v.x); amr_free(v.bv); amr_free(v.r); amr_free(v.d);
     }
-    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->scratch); amr_free(g->ticket);
+    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
     delete g;
     m->amg = nullptr;
 }
@@ -227,19 +256,19 @@ static void amg_build_structure(amr_model *m) {
         if (l > 0) {
             amr_alloc(&lv.rp, h.n + 1);
             amr_alloc(&lv.cj, std::max<int64_t>(lv.nblocks, 1));
-            AMR_CUDA(cudaMemcpy(lv.rp, h.rp.data(), (h.n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-            AMR_CUDA(cudaMemcpy(lv.cj, h.cj.data(), lv.nblocks * sizeof(int32_t), cudaMemcpyHostToDevice));
-            amr_alloc(&lv.A, (size_t)lv.nbs * h.b * h.b);
-            amr_alloc(&lv.Dinv, (size_t)h.n * h.b * h.b);
+            amr_h2d(m, lv.rp, h.rp.data(), (h.n + 1) * sizeof(int64_t));
+            amr_h2d(m, lv.cj, h.cj.data(), lv.nblocks * sizeof(int32_t));
+            amr_alloc(&lv.f32.A, (size_t)lv.nbs * h.b * h.b);
+            amr_alloc(&lv.f32.Dinv, (size_t)h.n * h.b * h.b);
         } else {
             lv.rp = m->brow_ptr;
             lv.cj = m->bcol;
             lv.nbs = m->bstride;
         }
         amr_alloc(&lv.diag, h.n);
-        AMR_CUDA(cudaMemcpy(lv.diag, h.diag.data(), h.n * sizeof(int64_t), cudaMemcpyHostToDevice));
+        amr_h2d(m, lv.diag, h.diag.data(), h.n * sizeof(int64_t));
         const int64_t nv = h.n * h.b;
-        amr_alloc(&lv.x, nv); amr_alloc(&lv.bv, nv); amr_alloc(&lv.r, nv); amr_alloc(&lv.d, nv);
+        amr_alloc(&lv.f32.x, nv); amr_alloc(&lv.f32.bv, nv); amr_alloc(&lv.f32.r, nv); amr_alloc(&lv.f32.d, nv);
         if (last) {
             g->nc = nv;
             g->L.push_back(lv);
@@ -257,7 +286,7 @@ static void amg_build_structure(amr_model *m) {
             for (int64_t i = 0; i < h.n; i++) anodes[fill[agg[i]]++] = (int32_t)i;
         }
         // per aggregate: orthonormal basis of the near-null space (T) and its coordinates (next level's modes)
-        std::vector<float> T((size_t)h.n * h.b * NM, 0.0f);
+        std::vector<double> T((size_t)h.n * h.b * NM, 0.0);
         HostLevel hc;
         hc.b = NM;
         hc.n = na;
@@ -295,7 +324,7 @@ static void amg_build_structure(amr_model *m) {
                     for (int k = 0; k < NM; k++) {
                         double s = 0.0;
                         for (int p = 0; p < NM; p++) s += Bm[(q * h.b + c) * NM + p] * V[p * NM + k];
-                        T[((size_t)i * h.b + c) * NM + k] = (float)(s * sc[k]);
+                        T[((size_t)i * h.b + c) * NM + k] = s * sc[k];
                     }
             }
             for (int k = 0; k < NM; k++)
@@ -345,21 +374,25 @@ static void amg_build_structure(amr_model *m) {
         }
         lv.naggs = na;
         amr_alloc(&lv.agg, h.n);
-        amr_alloc(&lv.T, T.size());
+        amr_alloc(&lv.f32.T, T.size());
         amr_alloc(&lv.aptr, na + 1);
         amr_alloc(&lv.anodes, h.n);
         amr_alloc(&lv.cptr, cptr.size());
         amr_alloc(&lv.ck, cks.size());
         amr_alloc(&lv.ci, cis.size());
         amr_alloc(&lv.null_dof, nulld.size());
-        AMR_CUDA(cudaMemcpy(lv.agg, agg.data(), h.n * sizeof(int32_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.T, T.data(), T.size() * sizeof(float), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.aptr, aptr.data(), aptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.anodes, anodes.data(), h.n * sizeof(int32_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.cptr, cptr.data(), cptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.ck, cks.data(), cks.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.ci, cis.data(), cis.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(lv.null_dof, nulld.data(), nulld.size(), cudaMemcpyHostToDevice));
+        amr_h2d(m, lv.agg, agg.data(), h.n * sizeof(int32_t));
+        {
+            const std::vector<float> T32(T.begin(), T.end());
+            amr_h2d(m, lv.f32.T, T32.data(), T32.size() * sizeof(float));
+        }
+        lv.hT = std::move(T);
+        amr_h2d(m, lv.aptr, aptr.data(), aptr.size() * sizeof(int64_t));
+        amr_h2d(m, lv.anodes, anodes.data(), h.n * sizeof(int32_t));
+        amr_h2d(m, lv.cptr, cptr.data(), cptr.size() * sizeof(int64_t));
+        amr_h2d(m, lv.ck, cks.data(), cks.size() * sizeof(int32_t));
+        amr_h2d(m, lv.ci, cis.data(), cis.size() * sizeof(int32_t));
+        amr_h2d(m, lv.null_dof, nulld.data(), nulld.size());
         g->L.push_back(lv);
         H.push_back(std::move(hc));
     }
@@ -367,52 +400,55 @@ static void amg_build_structure(amr_model *m) {
     amr_alloc(&g->Cinv, (size_t)g->nc * g->nc);
     amr_alloc(&g->scratch, 8 + kNormCtas);
     amr_alloc(&g->ticket, 1);
-    AMR_CUDA(cudaMemset(g->ticket, 0, sizeof(unsigned int)));
+    AMR_CUDA(cudaMemsetAsync(g->ticket, 0, sizeof(unsigned int), m->stream));
     g->numeric_valid = false;
 }
 
 // ---------------------------------------------------------------------------
-// device kernels
+// device kernels, templated on the value type V of the level's matrix and vectors (float for the
+// mixed solver's cycle, double for the all-FP64 comparator's)
 // ---------------------------------------------------------------------------
 namespace {
 
+__device__ __forceinline__ float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double vfma(double a, double b, double c) { return fma(a, b, c); }
+
 // coarse block (warp) = sum over its contributions (fine block k of row i, column j) of T_i' A_k T_j
-template <int BF, int NM>
+template <int BF, int NM, class V>
 __global__ void k_galerkin(int64_t ncb, const int64_t *cptr, const int32_t *ck, const int32_t *ci,
-                           const int32_t *cjf, const float *Af, int64_t nbsf, const float *T, float *Ac,
-                           int64_t nbsc) {
+                           const int32_t *cjf, const V *Af, int64_t nbsf, const V *T, V *Ac, int64_t nbsc) {
     const int lane = threadIdx.x & 31;
     const int64_t cb = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (cb >= ncb) return;
-    float acc[NM * NM];
+    V acc[NM * NM];
 #pragma unroll
-    for (int q = 0; q < NM * NM; q++) acc[q] = 0.0f;
+    for (int q = 0; q < NM * NM; q++) acc[q] = V(0);
     for (int64_t e = cptr[cb] + lane; e < cptr[cb + 1]; e += 32) {
         const int64_t k = ck[e];
         const int32_t i = ci[e], j = cjf[k];
-        float M[BF * NM];  // A_k T_j
+        V M[BF * NM];  // A_k T_j
 #pragma unroll
         for (int c = 0; c < BF; c++)
 #pragma unroll
             for (int m = 0; m < NM; m++) {
-                float s = 0.0f;
+                V s = V(0);
 #pragma unroll
-                for (int d = 0; d < BF; d++) s = fmaf(Af[(int64_t)(c * BF + d) * nbsf + k], T[((int64_t)j * BF + d) * NM + m], s);
+                for (int d = 0; d < BF; d++) s = vfma(Af[(int64_t)(c * BF + d) * nbsf + k], T[((int64_t)j * BF + d) * NM + m], s);
                 M[c * NM + m] = s;
             }
 #pragma unroll
         for (int p = 0; p < NM; p++)
 #pragma unroll
             for (int m = 0; m < NM; m++) {
-                float s = acc[p * NM + m];
+                V s = acc[p * NM + m];
 #pragma unroll
-                for (int c = 0; c < BF; c++) s = fmaf(T[((int64_t)i * BF + c) * NM + p], M[c * NM + m], s);
+                for (int c = 0; c < BF; c++) s = vfma(T[((int64_t)i * BF + c) * NM + p], M[c * NM + m], s);
                 acc[p * NM + m] = s;
             }
     }
 #pragma unroll
     for (int q = 0; q < NM * NM; q++) {
-        float v = acc[q];
+        V v = acc[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) Ac[(int64_t)q * nbsc + cb] = v;
@@ -420,16 +456,16 @@ __global__ void k_galerkin(int64_t ncb, const int64_t *cptr, const int32_t *ck, 
 }
 
 // coarse DOFs without a mode get an identity equation
-template <int NM>
-__global__ void k_null_identity(int64_t n, const uint8_t *nulld, const int64_t *diag, float *A, int64_t nbs) {
+template <int NM, class V>
+__global__ void k_null_identity(int64_t n, const uint8_t *nulld, const int64_t *diag, V *A, int64_t nbs) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n * NM) return;
-    if (nulld[t]) A[(int64_t)((t % NM) * NM + t % NM) * nbs + diag[t / NM]] = 1.0f;
+    if (nulld[t]) A[(int64_t)((t % NM) * NM + t % NM) * nbs + diag[t / NM]] = V(1);
 }
 
 // block-Jacobi inverses of the diagonal blocks (Gauss-Jordan with partial pivoting in FP64)
-template <int NB>
-__global__ void k_block_inverse(int64_t n, const int64_t *diag, const float *A, int64_t nbs, float *Dinv) {
+template <int NB, class V>
+__global__ void k_block_inverse(int64_t n, const int64_t *diag, const V *A, int64_t nbs, V *Dinv) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double M[NB][2 * NB];
@@ -454,7 +490,7 @@ __global__ void k_block_inverse(int64_t n, const int64_t *diag, const float *A, 
         }
     }
     for (int r = 0; r < NB; r++)
-        for (int c = 0; c < NB; c++) Dinv[i * NB * NB + r * NB + c] = (float)M[r][NB + c];
+        for (int c = 0; c < NB; c++) Dinv[i * NB * NB + r * NB + c] = (V)M[r][NB + c];
 }
 
 // r = b - A x  (or y = A x with b == nullptr): a half-warp per node row, two blocks per lane in
@@ -506,51 +542,94 @@ __global__ void __launch_bounds__(256) k_bsr_res(int64_t n, const int64_t *__res
     }
 }
 
+// The FP64 residual of the comparator's cycle: 4 lanes per block row (the FP64 pipe, not HBM, bounds it
+// on GB300; two shuffle steps per row).  With a row mask (the fine level, whose matrix is K64 itself and
+// not a masked copy) a masked row is that of the identity: out = b - x (or x).
+template <int NB>
+__global__ void __launch_bounds__(256) k_bsr_res64(int64_t n, const int64_t *__restrict__ rp,
+                                                   const int32_t *__restrict__ cj, const double *__restrict__ A,
+                                                   int64_t nbs, const uint8_t *__restrict__ mask,
+                                                   const double *__restrict__ x, const double *__restrict__ b,
+                                                   double *__restrict__ out) {
+    constexpr int RL = 4, RPW = 32 / RL;
+    const int lane = threadIdx.x & 31, sub = lane & (RL - 1);
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r0 = warp * RPW; r0 < n; r0 += nw * RPW) {
+        const int64_t row = r0 + lane / RL;
+        const bool valid = row < n;
+        double acc[NB];
+#pragma unroll
+        for (int c = 0; c < NB; c++) acc[c] = 0.0;
+        if (valid)
+            for (int64_t k = rp[row] + sub; k < rp[row + 1]; k += RL) {
+                const int64_t j = __ldcs(cj + k);
+                double xv[NB];
+#pragma unroll
+                for (int d = 0; d < NB; d++) xv[d] = __ldg(x + (int64_t)NB * j + d);
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+#pragma unroll
+                    for (int d = 0; d < NB; d++) acc[c] = fma(__ldcs(A + (int64_t)(c * NB + d) * nbs + k), xv[d], acc[c]);
+            }
+#pragma unroll
+        for (int c = 0; c < NB; c++)
+#pragma unroll
+            for (int o = RL / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+        if (valid && sub == 0)
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+                const int64_t i = row * NB + c;
+                const double ax = (!mask || mask[i]) ? acc[c] : x[i];
+                out[i] = b ? b[i] - ax : ax;
+            }
+    }
+}
+
 // Chebyshev steps on D^-1 A (node-block D^-1):
 //   mode 0: d = s2 Dinv r; x = d           (first step from x = 0; r is the right-hand side)
 //   mode 1: d = s2 Dinv r; x += d          (first step from a given x; r = b - A x)
 //   mode 2: d = s1 d + s2 Dinv r; x += d   (second step)
-template <int NB>
-__global__ void k_cheb(int64_t n, int mode, float s1, float s2, const float *__restrict__ Dinv,
-                       const float *__restrict__ r, float *__restrict__ d, float *__restrict__ x) {
+template <int NB, class V>
+__global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Dinv, const V *__restrict__ r,
+                       V *__restrict__ d, V *__restrict__ x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float rv[NB];
+    V rv[NB];
 #pragma unroll
     for (int c = 0; c < NB; c++) rv[c] = r[i * NB + c];
 #pragma unroll
     for (int c = 0; c < NB; c++) {
-        float s = 0.0f;
+        V s = V(0);
 #pragma unroll
-        for (int e = 0; e < NB; e++) s = fmaf(Dinv[i * NB * NB + c * NB + e], rv[e], s);
-        const float dv = mode == 2 ? fmaf(s1, d[i * NB + c], s2 * s) : s2 * s;
+        for (int e = 0; e < NB; e++) s = vfma(Dinv[i * NB * NB + c * NB + e], rv[e], s);
+        const V dv = mode == 2 ? vfma(s1, d[i * NB + c], s2 * s) : s2 * s;
         d[i * NB + c] = dv;
         x[i * NB + c] = mode == 0 ? dv : x[i * NB + c] + dv;
     }
 }
 
 // bc[a] = sum over the aggregate's nodes (in order) of T_i' r_i; warp per aggregate
-template <int NB, int NM>
-__global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anodes, const float *T,
-                           const float *r, float *bc) {
+template <int NB, int NM, class V>
+__global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anodes, const V *T, const V *r, V *bc) {
     const int lane = threadIdx.x & 31;
     const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (a >= na) return;
-    float acc[NM];
+    V acc[NM];
 #pragma unroll
-    for (int m = 0; m < NM; m++) acc[m] = 0.0f;
+    for (int m = 0; m < NM; m++) acc[m] = V(0);
     for (int64_t q = aptr[a] + lane; q < aptr[a + 1]; q += 32) {
         const int64_t i = anodes[q];
 #pragma unroll
         for (int c = 0; c < NB; c++) {
-            const float rv = r[i * NB + c];
+            const V rv = r[i * NB + c];
 #pragma unroll
-            for (int m = 0; m < NM; m++) acc[m] = fmaf(T[(i * NB + c) * NM + m], rv, acc[m]);
+            for (int m = 0; m < NM; m++) acc[m] = vfma(T[(i * NB + c) * NM + m], rv, acc[m]);
         }
     }
 #pragma unroll
     for (int m = 0; m < NM; m++) {
-        float v = acc[m];
+        V v = acc[m];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) bc[a * NM + m] = v;
@@ -558,24 +637,24 @@ __global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anode
 }
 
 // x_i += T_i xc[agg(i)]
-template <int NB, int NM>
-__global__ void k_prolong(int64_t n, const int32_t *agg, const float *T, const float *xc, float *x) {
+template <int NB, int NM, class V>
+__global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc, V *x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int64_t a = agg[i];
 #pragma unroll
     for (int c = 0; c < NB; c++) {
-        float s = x[i * NB + c];
+        V s = x[i * NB + c];
 #pragma unroll
-        for (int m = 0; m < NM; m++) s = fmaf(T[(i * NB + c) * NM + m], xc[a * NM + m], s);
+        for (int m = 0; m < NM; m++) s = vfma(T[(i * NB + c) * NM + m], xc[a * NM + m], s);
         x[i * NB + c] = s;
     }
 }
 
 // dense coarsest level: expand the BSR matrix, invert it (Gauss-Jordan, FP64), multiply
-template <int NM>
-__global__ void k_dense_expand(int64_t n, const int64_t *rp, const int32_t *cj, const float *A, int64_t nbs,
-                               double *C, int64_t nc) {
+template <int NM, class V>
+__global__ void k_dense_expand(int64_t n, const int64_t *rp, const int32_t *cj, const V *A, int64_t nbs, double *C,
+                               int64_t nc) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     for (int64_t k = rp[i]; k < rp[i + 1]; k++)
@@ -604,19 +683,21 @@ __global__ void k_gj_column(int64_t nc, int64_t p, double *C) {  // clear column
     if (r >= nc || r == p) return;
     C[r * 2 * nc + p] = 0.0;
 }
-__global__ void k_dense_extract(int64_t nc, const double *C, float *Cinv) {
+template <class V>
+__global__ void k_dense_extract(int64_t nc, const double *C, V *Cinv) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nc * nc) return;
     const int64_t r = t / nc, c = t % nc;
-    Cinv[t] = (float)(C[r * 2 * nc + nc + c] / C[r * 2 * nc + r]);
+    Cinv[t] = (V)(C[r * 2 * nc + nc + c] / C[r * 2 * nc + r]);
 }
 // x = Cinv b, warp per row
-__global__ void k_dense_mv(int64_t nc, const float *Cinv, const float *b, float *x) {
+template <class V>
+__global__ void k_dense_mv(int64_t nc, const V *Cinv, const V *b, V *x) {
     const int lane = threadIdx.x & 31;
     const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (r >= nc) return;
-    float s = 0.0f;
-    for (int64_t c = lane; c < nc; c += 32) s = fmaf(Cinv[r * nc + c], b[c], s);
+    V s = V(0);
+    for (int64_t c = lane; c < nc; c += 32) s = vfma(Cinv[r * nc + c], b[c], s);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) x[r] = s;
@@ -624,7 +705,8 @@ __global__ void k_dense_mv(int64_t nc, const float *Cinv, const float *b, float 
 
 // sum of squares for the power iteration: per-CTA partials (fixed element assignment), the last CTA
 // adds them in CTA order
-__global__ void k_norm2(int64_t n, const float *v, double *partials, unsigned int *ticket, double *out) {
+template <class V>
+__global__ void k_norm2(int64_t n, const V *v, double *partials, unsigned int *ticket, double *out) {
     __shared__ double sh[256];
     __shared__ bool last;
     double s = 0.0;
@@ -651,15 +733,19 @@ __global__ void k_norm2(int64_t n, const float *v, double *partials, unsigned in
     *out = t;
     *ticket = 0;
 }
-// deterministic pseudo-random start vector in [-1, 1) (integer hash of the index), scaled by s
-__global__ void k_fill_random(int64_t n, float s, float *x) {
+// deterministic pseudo-random start vector in [-1, 1) (integer hash of the index), scaled by s; zero
+// where a mask is given and clear
+template <class V>
+__global__ void k_fill_random(int64_t n, double s, const uint8_t *mask, V *x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t h = (uint32_t)i * 2654435761u + 0x9E3779B9u;
     h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
-    x[i] = s * ((float)(h >> 8) * (1.0f / 8388608.0f) - 1.0f);
+    const V v = (V)s * ((V)(h >> 8) * (V)(1.0f / 8388608.0f) - V(1));
+    x[i] = (mask && !mask[i]) ? V(0) : v;
 }
-__global__ void k_scale(int64_t n, float s, float *x) {
+template <class V>
+__global__ void k_scale(int64_t n, V s, V *x) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] *= s;
 }
@@ -678,84 +764,112 @@ int sm_count() {
     return sms;
 }
 
-template <int NB>
-void bsr_res(cudaStream_t s, const AmgLevel &L, const float *A, int64_t nbs, const float *x, const float *b,
-             float *out) {
-    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256), (int64_t)sm_count() * 8);
-    k_bsr_res<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, x, b, out);
+// r = b - A x on a level (mask: rows of the identity, FP64 fine level only)
+template <int NB, class V>
+void bsr_res(cudaStream_t s, const AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask, const V *x, const V *b,
+             V *out) {
+    if constexpr (std::is_same<V, float>::value) {
+        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256), (int64_t)sm_count() * 8);
+        k_bsr_res<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, x, b, out);
+    } else {
+        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
+        k_bsr_res64<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, mask, x, b, out);
+    }
     AMR_COUNT(1);
 }
 
 struct Cheb {
-    float s1, s2a, s2b;  // d = s2a Dinv r (first), d = s1 d + s2b Dinv r (second)
+    double s1, s2a, s2b;  // d = s2a Dinv r (first), d = s1 d + s2b Dinv r (second)
 };
 Cheb cheb_coef(double lam) {
     // a power-iteration estimate approaches lambda_max from below: the interval's top has a margin,
     // as a smoother that sees eigenvalues above it amplifies them
     const double lo = lam / 30.0, hi = 1.25 * lam, th = 0.5 * (hi + lo), de = 0.5 * (hi - lo);
     const double sig = th / de, rho0 = 1.0 / sig, rho1 = 1.0 / (2.0 * sig - rho0);
-    return Cheb{(float)(rho1 * rho0), (float)(1.0 / th), (float)(2.0 * rho1 / de)};
+    return Cheb{rho1 * rho0, 1.0 / th, 2.0 * rho1 / de};
 }
 
-template <int B, int NM>
+// The V-cycle on value type V.  The fine level's matrix is the solver's: K32 (masked) for float, K64 with
+// a row mask for double; its block inverses are the solver's Minv32 / Minv64.
+template <int B, int NM, class V>
 struct Cycle {
-    static void level(amr_model *m, AmrAmg *g, size_t l, const float *b, float *x) {
+    static const V *fine_A(amr_model *m) {
+        if constexpr (std::is_same<V, float>::value) return m->K32;
+        else return m->K64;
+    }
+    static V *fine_Dinv(amr_model *m) {
+        if constexpr (std::is_same<V, float>::value) return m->Minv32;
+        else return m->Minv64;
+    }
+    static const uint8_t *fine_mask(amr_model *m) {
+        if constexpr (std::is_same<V, float>::value) return nullptr;
+        else return m->free_mask;
+    }
+    static V *coarse_inverse(AmrAmg *g) {
+        if constexpr (std::is_same<V, float>::value) return g->Cinv;
+        else return g->Cinv64;
+    }
+    static void level(amr_model *m, AmrAmg *g, size_t l, const V *b, V *x) {
         cudaStream_t s = m->stream;
         AmgLevel &L = g->L[l];
         if (l + 1 == g->L.size()) {
-            k_dense_mv<<<nblk(g->nc * 32, 256), 256, 0, s>>>(g->nc, g->Cinv, b, x);
+            k_dense_mv<V><<<nblk(g->nc * 32, 256), 256, 0, s>>>(g->nc, coarse_inverse(g), b, x);
             AMR_COUNT(1);
             return;
         }
-        if (l == 0) run<B>(m, g, l, L, m->K32, m->bstride, b, x);
-        else run<NM>(m, g, l, L, L.A, L.nbs, b, x);
+        if (l == 0) run<B>(m, g, l, L, fine_A(m), m->bstride, fine_mask(m), b, x);
+        else run<NM>(m, g, l, L, vals<V>(L).A, L.nbs, nullptr, b, x);
     }
     template <int NB>
-    static void run(amr_model *m, AmrAmg *g, size_t l, AmgLevel &L, const float *A, int64_t nbs, const float *b,
-                    float *x) {
+    static void run(amr_model *m, AmrAmg *g, size_t l, AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask,
+                    const V *b, V *x) {
         cudaStream_t s = m->stream;
-        const Cheb c = cheb_coef(L.lam);
+        AmgVals<V> &v = vals<V>(L);
+        const Cheb c = cheb_coef(v.lam);
+        const V s1 = (V)c.s1, s2a = (V)c.s2a, s2b = (V)c.s2b;
         const unsigned gn = nblk(L.n, 256);
         // pre-smoothing from x = 0
-        k_cheb<NB><<<gn, 256, 0, s>>>(L.n, 0, 0.0f, c.s2a, L.Dinv, b, L.d, x);
-        bsr_res<NB>(s, L, A, nbs, x, b, L.r);
-        k_cheb<NB><<<gn, 256, 0, s>>>(L.n, 2, c.s1, c.s2b, L.Dinv, L.r, L.d, x);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x);
+        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x);
         // coarse correction
-        bsr_res<NB>(s, L, A, nbs, x, b, L.r);
+        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
         AmgLevel &C = g->L[l + 1];
-        k_restrict<NB, NM><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, L.T, L.r, C.bv);
-        level(m, g, l + 1, C.bv, C.x);
-        k_prolong<NB, NM><<<gn, 256, 0, s>>>(L.n, L.agg, L.T, C.x, x);
+        AmgVals<V> &cv = vals<V>(C);
+        k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r, cv.bv);
+        level(m, g, l + 1, cv.bv, cv.x);
+        k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x);
         // post-smoothing
-        bsr_res<NB>(s, L, A, nbs, x, b, L.r);
-        k_cheb<NB><<<gn, 256, 0, s>>>(L.n, 1, 0.0f, c.s2a, L.Dinv, L.r, L.d, x);
-        bsr_res<NB>(s, L, A, nbs, x, b, L.r);
-        k_cheb<NB><<<gn, 256, 0, s>>>(L.n, 2, c.s1, c.s2b, L.Dinv, L.r, L.d, x);
+        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x);
+        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x);
         AMR_COUNT(7);
         AMR_CUDA(cudaGetLastError());
     }
     // largest eigenvalue of Dinv A by power iteration (15 steps from a pseudo-random start, which excites
     // the localized high-frequency modes of distorted elements; |x| = 1 after each step)
     template <int NB>
-    static double lambda(amr_model *m, AmrAmg *g, AmgLevel &L, const float *A, int64_t nbs) {
+    static double lambda(amr_model *m, AmrAmg *g, AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask) {
         cudaStream_t s = m->stream;
+        AmgVals<V> &v = vals<V>(L);
         const int64_t nv = L.n * NB;
         const unsigned gnorm = (unsigned)std::min<int64_t>(kNormCtas, std::max<int64_t>(1, nblk(nv, 256)));
-        k_fill_random<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(std::sqrt(3.0 / (double)nv)), L.x);
+        k_fill_random<V><<<nblk(nv, 256), 256, 0, s>>>(nv, std::sqrt(3.0 / (double)nv), mask, v.x);
         AMR_COUNT(1);
         double lam = 1.0;
         for (int it = 0; it < 15; it++) {
-            bsr_res<NB>(s, L, A, nbs, L.x, nullptr, L.r);
-            k_cheb<NB><<<nblk(L.n, 256), 256, 0, s>>>(L.n, 0, 0.0f, 1.0f, L.Dinv, L.r, L.d, L.bv);  // bv = Dinv A x
-            k_norm2<<<gnorm, 256, 0, s>>>(nv, L.bv, g->scratch + 8, g->ticket, g->scratch);
+            bsr_res<NB, V>(s, L, A, nbs, mask, v.x, nullptr, v.r);
+            k_cheb<NB, V><<<nblk(L.n, 256), 256, 0, s>>>(L.n, 0, V(0), V(1), v.Dinv, v.r, v.d, v.bv);  // bv = Dinv A x
+            k_norm2<V><<<gnorm, 256, 0, s>>>(nv, v.bv, g->scratch + 8, g->ticket, g->scratch);
             AMR_COUNT(2);
             double n2 = 0.0;
             AMR_CUDA(cudaMemcpyAsync(&n2, g->scratch, sizeof(double), cudaMemcpyDeviceToHost, s));
             AMR_CUDA(cudaStreamSynchronize(s));
             if (!(n2 > 0.0)) break;
             lam = std::sqrt(n2);
-            AMR_CUDA(cudaMemcpyAsync(L.x, L.bv, nv * sizeof(float), cudaMemcpyDeviceToDevice, s));
-            k_scale<<<nblk(nv, 256), 256, 0, s>>>(nv, (float)(1.0 / lam), L.x);
+            AMR_CUDA(cudaMemcpyAsync(v.x, v.bv, nv * sizeof(V), cudaMemcpyDeviceToDevice, s));
+            k_scale<V><<<nblk(nv, 256), 256, 0, s>>>(nv, (V)(1.0 / lam), v.x);
             AMR_COUNT(1);
         }
         return lam;
@@ -763,76 +877,126 @@ struct Cycle {
     static void numeric(amr_model *m, AmrAmg *g) {
         cudaStream_t s = m->stream;
         const size_t nl = g->L.size();
-        g->L[0].Dinv = m->Minv32;
+        vals<V>(g->L[0]).Dinv = fine_Dinv(m);
         for (size_t l = 0; l + 1 < nl; l++) {
             AmgLevel &F = g->L[l], &C = g->L[l + 1];
+            AmgVals<V> &fv = vals<V>(F), &cv = vals<V>(C);
             const unsigned gc = nblk(C.nblocks * 32, 256);
             if (l == 0)
-                k_galerkin<B, NM><<<gc, 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, m->K32, m->bstride, F.T,
-                                                     C.A, C.nbs);
+                k_galerkin<B, NM, V><<<gc, 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, fine_A(m), m->bstride,
+                                                        fv.T, cv.A, C.nbs);
             else
-                k_galerkin<NM, NM><<<gc, 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, F.A, F.nbs, F.T, C.A,
-                                                      C.nbs);
-            k_null_identity<NM><<<nblk(C.n * NM, 256), 256, 0, s>>>(C.n, F.null_dof, C.diag, C.A, C.nbs);
+                k_galerkin<NM, NM, V><<<gc, 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, fv.A, F.nbs, fv.T, cv.A,
+                                                         C.nbs);
+            k_null_identity<NM, V><<<nblk(C.n * NM, 256), 256, 0, s>>>(C.n, F.null_dof, C.diag, cv.A, C.nbs);
             AMR_COUNT(2);
             if (l + 2 < nl) {
-                k_block_inverse<NM><<<nblk(C.n, 128), 128, 0, s>>>(C.n, C.diag, C.A, C.nbs, C.Dinv);
+                k_block_inverse<NM, V><<<nblk(C.n, 128), 128, 0, s>>>(C.n, C.diag, cv.A, C.nbs, cv.Dinv);
                 AMR_COUNT(1);
             }
             AMR_CUDA(cudaGetLastError());
         }
         for (size_t l = 0; l + 1 < nl; l++) {
             AmgLevel &L = g->L[l];
-            L.lam = l == 0 ? lambda<B>(m, g, L, m->K32, m->bstride) : lambda<NM>(m, g, L, L.A, L.nbs);
+            vals<V>(L).lam = l == 0 ? lambda<B>(m, g, L, fine_A(m), m->bstride, fine_mask(m))
+                                    : lambda<NM>(m, g, L, vals<V>(L).A, L.nbs, nullptr);
         }
         // dense coarsest level
         AmgLevel &D = g->L[nl - 1];
         const int64_t nc = g->nc, w = 2 * nc;
         k_dense_init<<<nblk(nc * w, 256), 256, 0, s>>>(nc, g->Cd);
-        k_dense_expand<NM><<<nblk(D.n, 128), 128, 0, s>>>(D.n, D.rp, D.cj, D.A, D.nbs, g->Cd, nc);
+        k_dense_expand<NM, V><<<nblk(D.n, 128), 128, 0, s>>>(D.n, D.rp, D.cj, vals<V>(D).A, D.nbs, g->Cd, nc);
         AMR_COUNT(2);
         for (int64_t p = 0; p < nc; p++) {
             k_gj_eliminate<<<nblk(nc * w, 256), 256, 0, s>>>(nc, p, g->Cd);
             k_gj_column<<<nblk(nc, 256), 256, 0, s>>>(nc, p, g->Cd);
         }
         AMR_COUNT(2 * nc);
-        k_dense_extract<<<nblk(nc * nc, 256), 256, 0, s>>>(nc, g->Cd, g->Cinv);
+        k_dense_extract<V><<<nblk(nc * nc, 256), 256, 0, s>>>(nc, g->Cd, coarse_inverse(g));
         AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
-        g->numeric_valid = true;
     }
 };
+
+// The FP64 values of every level, allocated (and the prolongator uploaded) on first use.
+void ensure_fp64(amr_model *m, AmrAmg *g) {
+    if (g->Cinv64) return;
+    for (size_t l = 0; l < g->L.size(); l++) {
+        AmgLevel &L = g->L[l];
+        AmgVals<double> &v = L.f64;
+        const int64_t nv = L.n * L.b;
+        if (l > 0) {
+            amr_alloc(&v.A, (size_t)L.nbs * L.b * L.b);
+            amr_alloc(&v.Dinv, (size_t)L.n * L.b * L.b);
+        }
+        amr_alloc(&v.x, nv); amr_alloc(&v.bv, nv); amr_alloc(&v.r, nv); amr_alloc(&v.d, nv);
+        if (!L.hT.empty()) {
+            amr_alloc(&v.T, L.hT.size());
+            amr_h2d(m, v.T, L.hT.data(), L.hT.size() * sizeof(double));
+        }
+    }
+    amr_alloc(&g->Cinv64, (size_t)g->nc * g->nc);
+}
+
+void prepare_structure(amr_model *m) {
+    if (!m->amg || m->amg->dofs_version != m->dofs_version) {
+        amg_build_structure(m);
+        m->amg->dofs_version = m->dofs_version;
+    }
+}
 
 }  // namespace
 
 // Structure once per DOF numbering, values after each assembly of K.
 void amr_amg_prepare(amr_model *m) {
-    if (!m->amg || m->amg->dofs_version != m->dofs_version) {
-        amg_build_structure(m);
-        m->amg->dofs_version = m->dofs_version;
-    }
+    prepare_structure(m);
     if (!m->amg->numeric_valid) {
-        if (m->B == 3) Cycle<3, 6>::numeric(m, m->amg);
-        else Cycle<2, 3>::numeric(m, m->amg);
+        if (m->B == 3) Cycle<3, 6, float>::numeric(m, m->amg);
+        else Cycle<2, 3, float>::numeric(m, m->amg);
+        m->amg->numeric_valid = true;
+    }
+}
+
+// The same hierarchy in FP64 (the all-FP64 comparator's preconditioner).
+void amr_amg_prepare64(amr_model *m) {
+    prepare_structure(m);
+    ensure_fp64(m, m->amg);
+    if (!m->amg->numeric64_valid) {
+        if (m->B == 3) Cycle<3, 6, double>::numeric(m, m->amg);
+        else Cycle<2, 3, double>::numeric(m, m->amg);
+        m->amg->numeric64_valid = true;
     }
 }
 
 // z = V-cycle(r), fine-level node-major FP32 vectors, on the handle's stream
 void amr_amg_vcycle(amr_model *m, const float *r, float *z) {
-    if (m->B == 3) Cycle<3, 6>::level(m, m->amg, 0, r, z);
-    else Cycle<2, 3>::level(m, m->amg, 0, r, z);
+    if (m->B == 3) Cycle<3, 6, float>::level(m, m->amg, 0, r, z);
+    else Cycle<2, 3, float>::level(m, m->amg, 0, r, z);
 }
 
-// average device time of the cycle's fine-level residual r = b - K32 x (CUDA events on the handle's stream)
-double amr_amg_time_residual(amr_model *m, int reps) {
+// z = V-cycle(r) in FP64 (zero at prescribed slots when r is)
+void amr_amg_vcycle64(amr_model *m, const double *r, double *z) {
+    if (m->B == 3) Cycle<3, 6, double>::level(m, m->amg, 0, r, z);
+    else Cycle<2, 3, double>::level(m, m->amg, 0, r, z);
+}
+
+// average device time of the cycle's fine-level residual r = b - K x (CUDA events on the handle's stream):
+// the FP32 kernel on K32, or with fp64 the comparator's on K64
+double amr_amg_time_residual(amr_model *m, int reps, bool fp64) {
     AmrAmg *g = m->amg;
-    if (!g || !g->numeric_valid) throw AmrError(AMR_EINVAL, "run a multigrid solve on the current K first");
+    if (!g || !(fp64 ? g->numeric64_valid : g->numeric_valid))
+        throw AmrError(AMR_EINVAL, "run a multigrid solve of this precision on the current K first");
     AmgLevel &L = g->L[0];
     cudaStream_t s = m->stream;
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        if (m->B == 3) bsr_res<3>(s, L, m->K32, m->bstride, L.x, L.bv, L.r);
-        else bsr_res<2>(s, L, m->K32, m->bstride, L.x, L.bv, L.r);
+        if (fp64) {
+            if (m->B == 3) bsr_res<3, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
+            else bsr_res<2, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
+        } else {
+            if (m->B == 3) bsr_res<3, float>(s, L, m->K32, m->bstride, nullptr, L.f32.x, L.f32.bv, L.f32.r);
+            else bsr_res<2, float>(s, L, m->K32, m->bstride, nullptr, L.f32.x, L.f32.bv, L.f32.r);
+        }
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));
@@ -842,5 +1006,5 @@ double amr_amg_time_residual(amr_model *m, int reps) {
 }
 
 void amr_amg_invalidate(amr_model *m) {
-    if (m->amg) m->amg->numeric_valid = false;
+    if (m->amg) m->amg->numeric_valid = m->amg->numeric64_valid = false;
 }

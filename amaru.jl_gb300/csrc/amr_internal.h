@@ -121,11 +121,17 @@ struct amr_model {
     std::string err;
     bool any_plastic = false;
     int assembly_mode = AMR_ASSEMBLY_FAST;
+    // the last whole-model static stage's Newton iterations, and the hook after each converged increment
+    std::vector<amr_iteration_record> stage_log;
+    amr_increment_fn inc_fn = nullptr;
+    void *inc_user = nullptr;
 };
 
 // helpers
 // process-wide count of kernel launches by this library (reported by amr_launch_count)
 extern std::atomic<long long> amr_g_launches;
+// process-wide count of device allocations and frees by this library (reported by amr_alloc_count)
+extern std::atomic<long long> amr_g_allocs;
 #define AMR_COUNT(n) amr_g_launches.fetch_add((n), std::memory_order_relaxed)
 #define AMR_CUDA(call)                                                                 \
     do {                                                                               \
@@ -162,22 +168,48 @@ struct AmrEventPair {
     }
 };
 
+// Device memory of the library.  Inside a call on a handle (AmrStreamScope, set by every entry point)
+// allocations and frees are stream-ordered on that handle's stream, from a library pool per device that
+// keeps freed memory for reuse and never makes one stream wait for another's frees: a handle that
+// allocates or frees does not synchronise the device, so concurrent handles (served requests) overlap.
+// Outside a call, or while the stream is being captured into a graph, they are plain cudaMalloc /
+// cudaFree.  Copies between host and library memory are ordered on the handle's stream too (amr_h2d,
+// amr_d2h).
+extern thread_local cudaStream_t amr_tl_stream;
+struct AmrStreamScope {
+    cudaStream_t prev;
+    explicit AmrStreamScope(cudaStream_t s) : prev(amr_tl_stream) { amr_tl_stream = s; }
+    ~AmrStreamScope() { amr_tl_stream = prev; }
+    AmrStreamScope(const AmrStreamScope &) = delete;
+    AmrStreamScope &operator=(const AmrStreamScope &) = delete;
+};
+void *amr_raw_alloc(size_t bytes);  // throws AmrError(AMR_ENOMEM)
+void amr_raw_free(void *p);
+void amr_trim_pool();               // returns the pool's unused memory of the current device
+
 template <class T>
 inline void amr_alloc(T **p, size_t n) {
     if (n == 0) n = 1;
-    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        *p = nullptr;  // a failed allocation leaves nothing for the caller's cleanup to free
-        throw AmrError(AMR_ENOMEM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes: " +
-                                       cudaGetErrorString(e));
-    }
+    amr_g_allocs.fetch_add(1, std::memory_order_relaxed);
+    *p = nullptr;  // a failed allocation leaves nothing for the caller's cleanup to free
+    *p = (T *)amr_raw_alloc(n * sizeof(T));
 }
 template <class T>
 inline void amr_free(T *&p) {
-    if (p) cudaFree(p);
+    if (p) {
+        amr_g_allocs.fetch_add(1, std::memory_order_relaxed);
+        amr_raw_free((void *)p);
+    }
     p = nullptr;
 }
+// small pinned host buffers (status and control-block reads), from slabs kept for the process: freeing
+// one never synchronises the device
+void *amr_pinned_alloc(size_t bytes);
+void amr_pinned_free(void *p);
+// host <-> library device memory, ordered on the handle's stream; both return once the host side may be
+// reused (amr_d2h synchronises the stream)
+void amr_h2d(amr_model *m, void *d, const void *h, size_t bytes);
+void amr_d2h(amr_model *m, void *h, const void *d, size_t bytes);
 
 // pattern.cu
 void amr_build_pattern(amr_model *m);
@@ -210,8 +242,10 @@ void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq);
 // amg.cu: multigrid preconditioner (structure per DOF numbering, values per assembly)
 void amr_amg_prepare(amr_model *m);
 void amr_amg_vcycle(amr_model *m, const float *r, float *z);
+void amr_amg_prepare64(amr_model *m);                           // the same hierarchy in FP64
+void amr_amg_vcycle64(amr_model *m, const double *r, double *z);
 void amr_amg_invalidate(amr_model *m);
-double amr_amg_time_residual(amr_model *m, int reps);
+double amr_amg_time_residual(amr_model *m, int reps, bool fp64);
 void amr_amg_free(amr_model *m);
 // recovery.cu: nodal_patch_recovery (structure once per model, values per call)
 void amr_recovery_prepare(amr_model *m);

@@ -701,7 +701,7 @@ void amr_batch_free(amr_model *m) {
     amr_free(b->ip_part); amr_free(b->stat); amr_free(b->ctl); amr_free(b->active); amr_free(b->perr);
     amr_free(b->step); amr_free(b->counter);
     amr_free(b->x32); amr_free(b->r32); amr_free(b->z32); amr_free(b->p32); amr_free(b->q32);
-    if (b->h_step) cudaFreeHost(b->h_step);
+    amr_pinned_free(b->h_step);
     delete b;
     m->batch = nullptr;
 }
@@ -755,12 +755,12 @@ void amr_batch_set(amr_model *m, int64_t nparts, const int64_t *ptr) {
         amr_alloc(&b->counter, 2);
         amr_alloc(&b->x32, n); amr_alloc(&b->r32, n); amr_alloc(&b->z32, n); amr_alloc(&b->p32, n);
         amr_alloc(&b->q32, n);
-        AMR_CUDA(cudaMallocHost((void **)&b->h_step, sizeof(StepInfo)));
-        AMR_CUDA(cudaMemcpy(b->part_ptr, ptr, (nparts + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(b->order, order.data(), nparts * sizeof(int64_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(b->node_part, npart.data(), npart.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(b->elem_part, epart.data(), epart.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-        AMR_CUDA(cudaMemcpy(b->ip_part, ipart.data(), ipart.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        b->h_step = (StepInfo *)amr_pinned_alloc(sizeof(StepInfo));
+        amr_h2d(m, b->part_ptr, ptr, (nparts + 1) * sizeof(int64_t));
+        amr_h2d(m, b->order, order.data(), nparts * sizeof(int64_t));
+        amr_h2d(m, b->node_part, npart.data(), npart.size() * sizeof(int32_t));
+        amr_h2d(m, b->elem_part, epart.data(), epart.size() * sizeof(int32_t));
+        amr_h2d(m, b->ip_part, ipart.data(), ipart.size() * sizeof(int32_t));
         b->h_ctl.resize(nparts);
         b->h_stat.resize(nparts);
     } catch (...) {
@@ -996,7 +996,7 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
     // element kernels wrote their errors per part; leave the handle's own status clear
     {
         int32_t reset[2] = {0, INT32_MAX};
-        AMR_CUDA(cudaMemcpy(m->d_status, reset, sizeof reset, cudaMemcpyHostToDevice));
+        amr_h2d(m, m->d_status, reset, sizeof reset);
     }
     if (m->any_plastic) m->K_valid = false;  // K holds the tangent of some part's last trial state
     b->stage_seconds = ms * 1e-3;

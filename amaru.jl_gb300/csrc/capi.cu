@@ -3,14 +3,137 @@
 // driver (mech_stage_solver!, src/mech/mech-solver.jl:186-492) whose vectors
 // all stay on the device.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <unordered_set>
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <optional>
 #include <stdexcept>
 
 #include "amr_internal.h"
 
 std::atomic<long long> amr_g_launches{0};
+std::atomic<long long> amr_g_allocs{0};
+thread_local cudaStream_t amr_tl_stream = nullptr;
+
+// ---------------------------------------------------------------------------
+// device memory: stream-ordered allocation from a library pool per device
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_mem_mu;
+std::map<int, cudaMemPool_t> g_pools;          // device -> the library's pool
+std::unordered_set<void *> g_pool_ptrs;        // live allocations taken from a pool
+
+cudaMemPool_t library_pool() {
+    int dev = 0;
+    AMR_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_mem_mu);
+    auto it = g_pools.find(dev);
+    if (it != g_pools.end()) return it->second;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    AMR_CUDA(cudaMemPoolCreate(&pool, &props));
+    // keep freed memory for the next allocation; never let a stream wait on another stream's frees
+    uint64_t keep = UINT64_MAX;
+    int no = 0;
+    AMR_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    AMR_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no));
+    g_pools[dev] = pool;
+    return pool;
+}
+}  // namespace
+
+void *amr_raw_alloc(size_t bytes) {
+    void *p = nullptr;
+    cudaError_t e;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (amr_tl_stream && cudaStreamIsCapturing(amr_tl_stream, &cap) == cudaSuccess &&
+        cap == cudaStreamCaptureStatusNone) {
+        e = cudaMallocFromPoolAsync(&p, bytes, library_pool(), amr_tl_stream);
+        if (e == cudaSuccess) {
+            std::lock_guard<std::mutex> lk(g_mem_mu);
+            g_pool_ptrs.insert(p);
+        }
+    } else {
+        e = cudaMalloc(&p, bytes);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw AmrError(AMR_ENOMEM, std::string("device allocation of ") + std::to_string(bytes) + " bytes: " +
+                                       cudaGetErrorString(e));
+    }
+    return p;
+}
+
+void amr_raw_free(void *p) {
+    bool pooled;
+    {
+        std::lock_guard<std::mutex> lk(g_mem_mu);
+        pooled = g_pool_ptrs.erase(p) > 0;
+    }
+    if (!pooled) {
+        cudaFree(p);
+        return;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (amr_tl_stream && cudaStreamIsCapturing(amr_tl_stream, &cap) == cudaSuccess &&
+        cap == cudaStreamCaptureStatusNone) {
+        cudaFreeAsync(p, amr_tl_stream);
+    } else {  // no stream to order the free on: wait for the device, then free
+        cudaDeviceSynchronize();
+        cudaFreeAsync(p, 0);
+        cudaStreamSynchronize(0);
+    }
+}
+
+void amr_trim_pool() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lk(g_mem_mu);
+    auto it = g_pools.find(dev);
+    if (it != g_pools.end()) cudaMemPoolTrimTo(it->second, 0);
+}
+
+namespace {
+constexpr size_t kPinnedSlot = 256, kPinnedSlab = 256;  // slot bytes, slots per slab
+std::vector<void *> g_pinned_free;
+}  // namespace
+
+void *amr_pinned_alloc(size_t bytes) {
+    if (bytes > kPinnedSlot) throw AmrError(AMR_EINVAL, "pinned buffer larger than a slot");
+    std::lock_guard<std::mutex> lk(g_mem_mu);
+    if (g_pinned_free.empty()) {
+        void *slab = nullptr;
+        AMR_CUDA(cudaMallocHost(&slab, kPinnedSlot * kPinnedSlab));
+        for (size_t i = 0; i < kPinnedSlab; i++) g_pinned_free.push_back((char *)slab + i * kPinnedSlot);
+    }
+    void *p = g_pinned_free.back();
+    g_pinned_free.pop_back();
+    return p;
+}
+
+void amr_pinned_free(void *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_mem_mu);
+    g_pinned_free.push_back(p);
+}
+
+void amr_h2d(amr_model *m, void *d, const void *h, size_t bytes) {
+    if (!bytes) return;
+    AMR_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+}
+
+void amr_d2h(amr_model *m, void *h, const void *d, size_t bytes) {
+    if (!bytes) return;
+    AMR_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+}
 double amr_time_solver_kernel(amr_model *m, int which, int reps);
 
 namespace {
@@ -68,6 +191,7 @@ int fail(amr_model *m, const AmrError &e) {
 template <class F>
 int guarded(amr_model *m, F f) {
     if (!m) return AMR_EINVAL;
+    AmrStreamScope scope(m->stream);  // the call's allocations and frees are ordered on the handle's stream
     try {
         m->err.clear();
         return f();
@@ -139,6 +263,7 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
     if (!d || !out) { g_create_error = "null argument"; return AMR_EINVAL; }
     *out = nullptr;
     amr_model *m = new amr_model();
+    std::optional<AmrStreamScope> scope;  // set once the handle's stream exists
     try {
         if (d->ndim != 2 && d->ndim != 3) throw AmrError(AMR_EINVAL, "ndim must be 2 or 3");
         if (d->stressmodel == AMR_AXISYMMETRIC) throw AmrError(AMR_EUNSUPPORTED, "axisymmetric analyses are not on the GPU path");
@@ -217,6 +342,7 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
         AMR_CUDA(cudaEventCreate(&m->ev0));
         AMR_CUDA(cudaEventCreate(&m->ev1));
         cudaStream_t s = m->stream;
+        scope.emplace(s);
         m->h_coords.assign(d->coords, d->coords + 3 * d->nnodes);
         amr_alloc(&m->coords, 3 * d->nnodes);
         upload(m->coords, d->coords, 3 * d->nnodes * sizeof(double), s);
@@ -268,7 +394,7 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
         amr_alloc(&m->d_status, 2);
         int32_t init[2] = {0, INT32_MAX};
         upload(m->d_status, init, sizeof init, s);
-        AMR_CUDA(cudaMallocHost(&m->h_status, 2 * sizeof(int32_t)));
+        m->h_status = (int32_t *)amr_pinned_alloc(2 * sizeof(int32_t));
         for (int i = 0; i < 8; i++) amr_alloc(&m->vtmp[i], m->nnodes * m->B);
         amr_alloc(&m->eq_id, 3 * m->nnodes);
         amr_alloc(&m->free_mask, m->nnodes * m->B);
@@ -288,6 +414,7 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
 
 int amr_model_destroy(amr_model *m) {
     if (!m) return AMR_OK;
+    AmrStreamScope scope(m->stream);  // the frees are ordered on the handle's stream, destroyed last
     if (m->stream) cudaStreamSynchronize(m->stream);
     amr_solver_free(m);
     amr_batch_free(m);
@@ -301,7 +428,7 @@ int amr_model_destroy(amr_model *m) {
     amr_free(m->free_mask); amr_free(m->dof_node); amr_free(m->st); amr_free(m->stbk); amr_free(m->Fel);
     amr_free(m->fel_ptr); amr_free(m->d_status); amr_free(m->rho); amr_free(m->M64); amr_free(m->Mkeep);
     for (int i = 0; i < 8; i++) amr_free(m->vtmp[i]);
-    if (m->h_status) cudaFreeHost(m->h_status);
+    amr_pinned_free(m->h_status);
     if (m->ev0) cudaEventDestroy(m->ev0);
     if (m->ev1) cudaEventDestroy(m->ev1);
     if (m->stream) cudaStreamDestroy(m->stream);
@@ -367,13 +494,13 @@ int amr_set_dofs(amr_model *m, const int64_t *eq_id, int64_t ndofs, int64_t nu) 
 int amr_set_youngs(amr_model *m, const double *E) {
     return guarded(m, [&] {
         std::vector<double> mp(8 * m->nelems);
-        AMR_CUDA(cudaMemcpy(mp.data(), m->mat_par, mp.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        amr_d2h(m, mp.data(), m->mat_par, mp.size() * sizeof(double));
         for (int64_t s = 0; s < m->nelems; s++) {
             double v = E[m->perm[s]];
             if (!(v > 0.0)) throw AmrError(AMR_EINVAL, "E must be > 0");
             mp[8 * s] = v;
         }
-        AMR_CUDA(cudaMemcpy(m->mat_par, mp.data(), mp.size() * sizeof(double), cudaMemcpyHostToDevice));
+        amr_h2d(m, m->mat_par, mp.data(), mp.size() * sizeof(double));
         m->K_valid = false;
         return AMR_OK;
     });
@@ -401,11 +528,11 @@ static void export_csc(amr_model *m, int64_t *nnz_out, int64_t *colptr, int64_t 
                        const uint16_t *d_keep, const double *d_vals) {
     int B = m->B, BB = m->BB;
     std::vector<uint16_t> keep(m->nblocks);
-    AMR_CUDA(cudaMemcpy(keep.data(), d_keep, m->nblocks * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    amr_d2h(m, keep.data(), d_keep, m->nblocks * sizeof(uint16_t));
     std::vector<double> K;
     if (nzval) {
         K.resize((size_t)m->bstride * BB);
-        AMR_CUDA(cudaMemcpy(K.data(), d_vals, K.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        amr_d2h(m, K.data(), d_vals, K.size() * sizeof(double));
     }
     const std::vector<int64_t> &eq = m->h_eq_id;
     // count per column (= per row of the symmetric pattern walk)
@@ -546,7 +673,7 @@ int amr_state_restore(amr_model *m) {
 int amr_get_state(amr_model *m, double *state) {
     return guarded(m, [&] {
         std::vector<double> st((size_t)AMR_NST * m->nip_total);
-        AMR_CUDA(cudaMemcpy(st.data(), m->st, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        amr_d2h(m, st.data(), m->st, st.size() * sizeof(double));
         int64_t o = 0;
         for (int64_t e = 0; e < m->nelems; e++) {
             int64_t s = m->inv_perm[e];
@@ -831,6 +958,27 @@ int amr_launch_count(const amr_model *m, int64_t *count) {
     return AMR_OK;
 }
 
+int amr_get_stage_log(const amr_model *m, amr_iteration_record *rec, int32_t cap, int32_t *n) {
+    if (!m || !n || cap < 0 || (cap > 0 && !rec)) return AMR_EINVAL;
+    const size_t k = std::min(m->stage_log.size(), (size_t)cap);
+    std::copy(m->stage_log.begin(), m->stage_log.begin() + k, rec);
+    *n = (int32_t)m->stage_log.size();
+    return AMR_OK;
+}
+
+int amr_set_increment_callback(amr_model *m, amr_increment_fn fn, void *user) {
+    if (!m) return AMR_EINVAL;
+    m->inc_fn = fn;
+    m->inc_user = fn ? user : nullptr;
+    return AMR_OK;
+}
+
+int amr_alloc_count(int64_t *count) {
+    if (!count) return AMR_EINVAL;
+    *count = amr_g_allocs.load();
+    return AMR_OK;
+}
+
 int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch) {
     return guarded(m, [&] {
         // the dynamic right-hand side reads M and a K-shaped operand only
@@ -848,8 +996,16 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
             bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 + 8.0 + 4.0 + 4.0 + 1.0) + nn * BB * 4.0;
             break;
         case AMR_KERNEL_AMG_RESIDUAL:  // as SPMV32, plus b read (x gathered, r written)
-            t = amr_amg_time_residual(m, reps);
+            t = amr_amg_time_residual(m, reps, false);
             bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 3.0;
+            break;
+        case AMR_KERNEL_SPMV64:  // K64 blocks + columns + row pointers; p read once, q written, row mask
+            t = amr_time_solver_kernel(m, AMR_KERNEL_SPMV64, reps);
+            bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 * 2.0 + 1.0);
+            break;
+        case AMR_KERNEL_AMG_RESIDUAL64:  // as SPMV64, plus b read
+            t = amr_amg_time_residual(m, reps, true);
+            bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 * 3.0 + 1.0);
             break;
         case AMR_KERNEL_DYN_RHS:
             t = amr_dyn_time_rhs(m, reps, &bytes);
@@ -903,6 +1059,8 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
            *reac = v[8], *dUt = v[9];
     int status = AMR_OK;
     amr_stage_stats st{};
+    m->stage_log.clear();
+    std::vector<double> hU, hF;  // the hook's host copies
     try {
         AMR_CUDA(cudaEventRecord(t0, s));
         for (double *x : {U, F, R, dUa, dUi, Rc, dFin}) AMR_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
@@ -924,7 +1082,9 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
         AMR_CUDA(cudaMemcpyAsync(m->stbk, m->st, (size_t)AMR_NST * m->nip_total * sizeof(double),
                                  cudaMemcpyDeviceToDevice, s));
         const double eps = 2.220446049250313e-16;
+        int inc = 0;  // the reference's increment counter (a failed increment's number is reused)
         while (T < 1.0 - dTmin) {
+            inc++;
             // dUex, dFex (+ carried residue)
             double dTcr = std::min(p.rspan, 1 - T);
             double acr = std::min(dT / dTcr, 1.0);
@@ -938,6 +1098,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
             int nits = 0;
             for (int it = 1; it <= p.maxits; it++) {
                 nits++;
+                const int kry0 = st.krylov_iterations;
                 if (it > 1) AMR_CUDA(cudaMemsetAsync(dUi, 0, n * sizeof(double), s));
                 double lastres = res;
                 if (m->any_plastic || !m->K_valid) assemble(m);
@@ -985,9 +1146,10 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 double nui = amr_norm_inf(m, dUi, nullptr), nua = amr_norm_inf(m, dUa, nullptr);
                 err = nui / nua;
                 st.iterations++;
+                m->stage_log.push_back(amr_iteration_record{inc, it, st.krylov_iterations - kry0, 0, T, dT, res});
                 if (it == 1) res1 = res;
-                if (res < tol) { converged = true; break; }
-                if (err < rtol) { converged = true; break; }
+                if (res < tol) { converged = true; m->stage_log.back().converged = 1; break; }
+                if (err < rtol) { converged = true; m->stage_log.back().converged = 1; break; }
                 if (std::isnan(res)) break;
                 if (it > 1 && res > lastres) break;
             }
@@ -1003,6 +1165,18 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                 st.increments++;
                 bool checkpoint = T > Tcheck - dTmin;
                 if (checkpoint) Tcheck += dTcheck;
+                if (m->inc_fn) {  // update_records!(ana, checkpoint=checkpoint)
+                    hU.resize(m->ndofs);
+                    hF.resize(m->ndofs);
+                    nm_to_eq_host(m, U, hU.data());
+                    nm_to_eq_host(m, F, hF.data());
+                    const amr_increment_info info{T, inc, checkpoint ? 1 : 0, m->ndofs, hU.data(), hF.data()};
+                    if (m->inc_fn(m->inc_user, &info) != 0) {
+                        status = AMR_ESTAGE;
+                        m->err = "the increment callback stopped the stage";
+                        break;
+                    }
+                }
                 if (autoinc) {
                     if (dTbk > 0.0) {
                         dT = std::min(dTbk, Tcheck - T);
@@ -1021,6 +1195,7 @@ int amr_stage_device(amr_model *m, const double *Uex, const double *Fex, const a
                     }
                 }
             } else {
+                inc--;
                 AMR_CUDA(cudaMemcpyAsync(m->st, m->stbk, (size_t)AMR_NST * m->nip_total * sizeof(double),
                                          cudaMemcpyDeviceToDevice, s));
                 if (m->any_plastic) m->K_valid = false;

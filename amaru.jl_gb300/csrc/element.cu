@@ -1098,7 +1098,7 @@ int amr_check_status(amr_model *m) {
     int code = m->h_status[0];
     if (code) {
         int32_t reset[2] = {0, INT32_MAX};
-        AMR_CUDA(cudaMemcpy(m->d_status, reset, sizeof reset, cudaMemcpyHostToDevice));
+        amr_h2d(m, m->d_status, reset, sizeof reset);
     }
     return code;
 }

@@ -416,7 +416,7 @@ int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, dou
     if (m->nu < 3 * k) throw AmrError(AMR_EINVAL, "too few unknown DOFs for " + std::to_string(nm) + " modes");
     {
         std::vector<double> r(m->nelems);
-        AMR_CUDA(cudaMemcpy(r.data(), m->rho, m->nelems * sizeof(double), cudaMemcpyDeviceToHost));
+        amr_d2h(m, r.data(), m->rho, m->nelems * sizeof(double));
         for (double v : r)
             if (!(v > 0.0)) throw AmrError(AMR_EINVAL, "mech_modal_solver: density should not be zero");
     }

@@ -915,7 +915,7 @@ double amr_recovery_time_fit(amr_model *m, int reps, double *flops, int64_t *n_s
     if (n_svd) {
         std::vector<int32_t> fl(R->ntasks);
         if (R->ntasks)
-            AMR_CUDA(cudaMemcpy(fl.data(), R->t_flag, R->ntasks * sizeof(int32_t), cudaMemcpyDeviceToHost));
+            amr_d2h(m, fl.data(), R->t_flag, R->ntasks * sizeof(int32_t));
         *n_svd = std::count(fl.begin(), fl.end(), 1);
     }
     return ms * 1e-3 / std::max(1, reps);

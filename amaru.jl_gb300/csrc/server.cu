@@ -27,7 +27,7 @@ using Clock = std::chrono::steady_clock;
 // Upper bound of the device bytes amr_model_create, amr_set_dofs and one
 // amr_stage_run allocate for a model, from its description (fp64: with the
 // all-FP64 comparator's CSR copy of K11 and its vectors).
-int64_t model_bytes(const amr_model_desc *d, bool fp64) {
+int64_t model_bytes(const amr_model_desc *d, int method) {
     if (!d || d->nnodes <= 0 || d->nelems <= 0 || !d->shape || !d->nips) return -1;
     const int64_t N = d->nnodes, E = d->nelems, B = d->ndim, BB = B * B;
     int64_t S = 0, C = 0, Q = 0;
@@ -48,7 +48,8 @@ int64_t model_bytes(const amr_model_desc *d, bool fp64) {
     b += 12 * BB * N + 2 * 8 * AMR_NST * Q + 8 * C * B;          // block-Jacobi, IP states, element forces
     b += 8 * 8 * N * B + 24 * N + N * B;                         // work vectors, eq_id, masks
     b += 7 * 4 * N * B + ((int64_t)1 << 20);                     // FP32 Krylov vectors, reduction scratch
-    if (fp64) b += 20 * BB * NB + 8 * 8 * N * B + 8 * N * B;     // CSR of K11 (value, column, source), vectors
+    if (method == AMR_SOLVER_FP64 || method == AMR_SOLVER_AMG_FP64) b += 4 * 8 * N * B;  // FP64 Krylov vectors
+    if (method == AMR_SOLVER_AMG_FP64) b += 80 * N * B;          // FP64 cycle vectors and prolongator
     b += 14 * 8 * N * B;                                         // stage vectors (host-buffer stage)
     b += (int64_t)64 << 20;                                      // allocation granularity and tables
     return b;
@@ -153,7 +154,7 @@ extern "C" {
 
 int amr_estimate_bytes(const amr_model_desc *desc, int64_t *bytes) {
     if (!bytes) return AMR_EINVAL;
-    const int64_t b = model_bytes(desc, false);
+    const int64_t b = model_bytes(desc, AMR_SOLVER_MIXED);
     if (b < 0) return AMR_EINVAL;
     *bytes = b;
     return AMR_OK;
@@ -181,7 +182,7 @@ int amr_server_submit(amr_server *s, const amr_request *q, int64_t *id) {
         q->ndofs < 0 || q->nu < 0 || q->nu > q->ndofs || (q->ndofs > 0 && (!q->Uex || !q->Fex)) || q->nloads < 0 ||
         (q->nloads > 0 && !q->loads))
         return AMR_EINVAL;
-    const int64_t bytes = model_bytes(&d, q->stage.linear.method == AMR_SOLVER_FP64);
+    const int64_t bytes = model_bytes(&d, q->stage.linear.method);
     if (bytes < 0) return AMR_EINVAL;
     if (bytes > (int64_t)s->cfg.hbm_budget_bytes) return AMR_ENOMEM;  // could never be admitted
     auto r = std::make_unique<Request>();

@@ -8,8 +8,9 @@
 //   correction is folded into the FP64 solution and the recursive residual is
 //   replaced (iterative refinement by reliable updates; the search direction
 //   is kept).  Convergence is decided on the FP64 true residual only.
-// AMR_SOLVER_FP64: the plain all-FP64 comparator: scalar CSR of K11 in eq_id
-//   order, Jacobi-preconditioned CG, all vectors FP64.
+// AMR_SOLVER_FP64 / AMR_SOLVER_AMG_FP64: the all-FP64 comparators of MIXED and
+//   AMG: the same Krylov method and the same preconditioner, with the FP64 matrix
+//   K64, FP64 block inverses (and an FP64 multigrid hierarchy) and FP64 vectors.
 //
 // Scalars (alpha, beta, norms) live in a device control block; each kernel's
 // last CTA reduces the per-CTA partials in a fixed order, so results are
@@ -17,6 +18,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <mutex>
 
 #include "amr_internal.h"
 
@@ -314,14 +316,16 @@ __global__ void __launch_bounds__(kThreads) k_rz32(int64_t nn, const float *__re
 // kRowLanes lanes per block row, 32 / kRowLanes rows per warp: the FP64 pipe, not HBM, bounds this
 // kernel on GB300, and a row's three sums reduce in log2(kRowLanes) shuffle steps shared by the
 // warp's rows.  The row loop advances whole warps so every lane reaches the shuffles.
+// R is the type of the Krylov vectors r, z and of the block inverses: float for the mixed path, double for
+// the all-FP64 comparator.
 constexpr int kRowLanes = 4;
-template <int B>
+template <int B, typename R = float>
 __global__ void __launch_bounds__(kThreads) k_refine(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
                                                      const int32_t *__restrict__ cj, const double *__restrict__ A,
                                                      const uint8_t *__restrict__ fmask, const double *__restrict__ b,
                                                      const double *__restrict__ u64, double *__restrict__ reac,
-                                                     float *__restrict__ r32, float *__restrict__ z,
-                                                     const float *__restrict__ Minv, Ctl *ctl, double *partials,
+                                                     R *__restrict__ r32, R *__restrict__ z,
+                                                     const R *__restrict__ Minv, Ctl *ctl, double *partials,
                                                      int first, double tol2) {
     constexpr int RPW = 32 / kRowLanes;
     const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
@@ -347,21 +351,21 @@ __global__ void __launch_bounds__(kThreads) k_refine(int64_t nn, int64_t nb, con
 #pragma unroll
             for (int o = kRowLanes / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
         if (valid && sub == 0) {
-            float rv[B];
+            R rv[B];
 #pragma unroll
             for (int c = 0; c < B; c++) {
                 double res = 0.0;
                 if (fmask[n * B + c]) res = b[n * B + c] - acc[c];
                 else if (reac) reac[n * B + c] = acc[c];
-                rv[c] = (float)res;
+                rv[c] = (R)res;
                 r32[n * B + c] = rv[c];
                 rr += res * res;
             }
 #pragma unroll
             for (int c = 0; c < B; c++) {
-                float s = 0.0f;
+                R s = 0;
 #pragma unroll
-                for (int d = 0; d < B; d++) s = fmaf(Minv[n * B * B + c * B + d], rv[d], s);
+                for (int d = 0; d < B; d++) s = fma(Minv[n * B * B + c * B + d], rv[d], s);
                 z[n * B + c] = s;
                 rz += (double)rv[c] * (double)s;
             }
@@ -390,121 +394,144 @@ __global__ void k_fold(int64_t n, const uint8_t *fmask, float *x32, double *u64)
 }
 
 // ---------------------------------------------------------------------------
-// Plain FP64 comparator: CSR over free eq ids, Jacobi PCG
+// All-FP64 comparator: the mixed path's block-Jacobi PCG with every operand in FP64.  The matrix is
+// K64 itself, not a masked copy: p and z are zero at prescribed slots (the block inverses are those of
+// the masked diagonal blocks), so K64 p equals the masked product at free rows, and prescribed rows
+// are written as zero.  kRowLanes lanes per block row: the FP64 pipe bounds these kernels on GB300,
+// and a row's sums reduce in two shuffle steps.
 // ---------------------------------------------------------------------------
-__global__ void k_csr_count(int64_t nnodes, int B, const int64_t *rp, const int32_t *cj, const int64_t *eq_id,
-                            int64_t nu, int64_t *rowcnt) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nnodes * B) return;
-    int64_t n = t / B;
-    int c = (int)(t % B);
-    int64_t row = eq_id[n * 3 + c];
-    if (row < 0 || row >= nu) return;
-    int64_t cnt = 0;
-    for (int64_t k = rp[n]; k < rp[n + 1]; k++) {
-        int64_t m = cj[k];
-        for (int d = 0; d < B; d++) {
-            int64_t col = eq_id[m * 3 + d];
-            cnt += (col >= 0 && col < nu);
-        }
-    }
-    rowcnt[row] = cnt;
-}
-
-__global__ void k_csr_fill(int64_t nnodes, int B, const int64_t *rp, const int32_t *cj, const int64_t *eq_id,
-                           int64_t nu, int64_t nb, const int64_t *crp, int32_t *ccol, int64_t *csrc) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nnodes * B) return;
-    int64_t n = t / B;
-    int c = (int)(t % B);
-    int64_t row = eq_id[n * 3 + c];
-    if (row < 0 || row >= nu) return;
-    int64_t o = crp[row];
-    for (int64_t k = rp[n]; k < rp[n + 1]; k++) {
-        int64_t m = cj[k];
-        for (int d = 0; d < B; d++) {
-            int64_t col = eq_id[m * 3 + d];
-            if (col >= 0 && col < nu) {
-                ccol[o] = (int32_t)col;
-                csrc[o] = (int64_t)(c * B + d) * nb + k;
-                o++;
-            }
-        }
-    }
-}
-
-__global__ void k_csr_values(int64_t nnz, const int64_t *src, const double *K64, double *val) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nnz) val[i] = K64[src[i]];
-}
-
-__global__ void k_csr_diag(int64_t nu, const int64_t *crp, const int32_t *ccol, const double *val, double *dinv) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nu) return;
-    double d = 0.0;
-    for (int64_t k = crp[i]; k < crp[i + 1]; k++)
-        if (ccol[k] == i) d += val[k];
-    dinv[i] = 1.0 / d;
-}
-
-// p = z + beta p (own rows) computed on the fly, q = A p, pq
-__global__ void __launch_bounds__(kThreads) k_csr_spmv(int64_t nr, const int64_t *__restrict__ rp,
-                                                       const int32_t *__restrict__ cj, const double *__restrict__ A,
-                                                       const double *__restrict__ z, const double *__restrict__ pold,
-                                                       double *__restrict__ pnew, double *__restrict__ q, Ctl *ctl,
-                                                       double *partials) {
+template <int B>
+__global__ void k_pupdate64(int64_t n, const double *__restrict__ z, double *__restrict__ p, const Ctl *ctl) {
     if (ctl->stop) return;
-    const double beta = ctl->beta;
-    int lane = threadIdx.x & 31;
-    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const double beta = ctl->first ? 0.0 : ctl->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * B; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fma(beta, p[i], z[i]);
+}
+
+// q = mask(K64 p) ; pq = p.q ; alpha = gamma / pq
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_spmv64(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
+                                                     const int32_t *__restrict__ cj, const double *__restrict__ A,
+                                                     const uint8_t *__restrict__ fmask, const double *__restrict__ p,
+                                                     double *__restrict__ q, Ctl *ctl, double *partials) {
+    if (ctl->stop) return;
+    constexpr int RPW = 32 / kRowLanes;
+    const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double dot = 0.0;
-    for (int64_t i = warp; i < nr; i += nw) {
-        double acc = 0.0;
-        for (int64_t k = rp[i] + lane; k < rp[i + 1]; k += 32) {
-            int64_t j = cj[k];
-            acc = fma(A[k], fma(beta, pold[j], z[j]), acc);
-        }
-        acc = warp_sum(acc);
-        if (lane == 0) {
-            double pn = fma(beta, pold[i], z[i]);
-            pnew[i] = pn;
-            q[i] = acc;
-            dot += pn * acc;
-        }
+    for (int64_t n0 = warp * RPW; n0 < nn; n0 += nw * RPW) {
+        const int64_t n = n0 + lane / kRowLanes;
+        const bool valid = n < nn;
+        double acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0;
+        if (valid)
+            for (int64_t k = rp[n] + sub; k < rp[n + 1]; k += kRowLanes) {
+                const int64_t j = __ldcs(cj + k);
+                double xv[B];
+#pragma unroll
+                for (int d = 0; d < B; d++) xv[d] = __ldg(p + j * B + d);
+#pragma unroll
+                for (int c = 0; c < B; c++)
+#pragma unroll
+                    for (int d = 0; d < B; d++) acc[c] = fma(__ldcs(A + (int64_t)(c * B + d) * nb + k), xv[d], acc[c]);
+            }
+#pragma unroll
+        for (int c = 0; c < B; c++)
+#pragma unroll
+            for (int o = kRowLanes / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+        if (valid && sub == 0)
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                const double v = fmask[n * B + c] ? acc[c] : 0.0;
+                q[n * B + c] = v;
+                dot = fma(p[n * B + c], v, dot);
+            }
     }
     double v[1] = {dot}, tot[1];
     if (grid_sum<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
         ctl->pq = tot[0];
         if (!(tot[0] > 0.0)) { ctl->breakdown = 1; ctl->stop = 1; }
-        else ctl->alpha = ctl->rz / tot[0];
+        else { ctl->alpha = ctl->rz / tot[0]; ctl->first = 0; }
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_csr_update(int64_t nr, const double *__restrict__ dinv,
-                                                         const double *__restrict__ p, const double *__restrict__ q,
-                                                         double *__restrict__ x, double *__restrict__ r,
-                                                         double *__restrict__ z, Ctl *ctl, double *partials,
-                                                         double tol2) {
+// u += alpha p ; r -= alpha q ; z = Minv r ; gamma = r.z, |r|^2 ; beta.  Stops for a true-residual check
+// once the recursive residual looks converged (or is NaN).
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_update64(int64_t nn, const double *__restrict__ Minv,
+                                                       const double *__restrict__ p, const double *__restrict__ q,
+                                                       double *__restrict__ u, double *__restrict__ r,
+                                                       double *__restrict__ z, Ctl *ctl, double *partials,
+                                                       double stop_rr) {
     if (ctl->stop) return;
     const double alpha = ctl->alpha;
     double rz = 0.0, rr = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = fma(alpha, p[i], x[i]);
-        double rv = fma(-alpha, q[i], r[i]);
-        r[i] = rv;
-        double zv = dinv[i] * rv;
-        z[i] = zv;
-        rz += rv * zv;
-        rr += rv * rv;
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        double rv[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            const int64_t i = n * B + c;
+            u[i] = fma(alpha, p[i], u[i]);
+            rv[c] = fma(-alpha, q[i], r[i]);
+            r[i] = rv[c];
+        }
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            double zz = 0.0;
+#pragma unroll
+            for (int d = 0; d < B; d++) zz = fma(Minv[n * B * B + c * B + d], rv[d], zz);
+            z[n * B + c] = zz;
+            rz = fma(rv[c], zz, rz);
+            rr = fma(rv[c], rv[c], rr);
+        }
     }
     double v[2] = {rz, rr}, tot[2];
     if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
         ctl->beta = tot[0] / ctl->rz;
         ctl->rz = tot[0];
         ctl->rr = tot[1];
-        if (tot[1] <= tol2 * ctl->bnorm2) { ctl->converged = 1; ctl->stop = 1; }
-        if (isnan(tot[1])) { ctl->breakdown = 1; ctl->stop = 1; }
+        ctl->iters += 1;
+        if (!(tot[1] > stop_rr)) ctl->stop = 1;
+    }
+}
+
+// Multigrid-preconditioned FP64 update: u += alpha p ; r -= alpha q (z = M r comes after)
+template <int B>
+__global__ void k_update64a(int64_t nn, const double *__restrict__ p, const double *__restrict__ q,
+                            double *__restrict__ u, double *__restrict__ r, const Ctl *ctl) {
+    if (ctl->stop) return;
+    const double alpha = ctl->alpha;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn * B; i += (int64_t)gridDim.x * blockDim.x) {
+        u[i] = fma(alpha, p[i], u[i]);
+        r[i] = fma(-alpha, q[i], r[i]);
+    }
+}
+
+// gamma = r.z and |r|^2 once z = M r, in FP64.  mode 0, an iteration: beta, the counter and the stop
+// for a true-residual check; mode 1, after a true-residual check: gamma only.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_rz64(int64_t nn, const double *__restrict__ r,
+                                                   const double *__restrict__ z, Ctl *ctl, double *partials,
+                                                   double stop_rr, int mode) {
+    if (mode == 0 && ctl->stop) return;
+    double rz = 0.0, rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn * B; i += (int64_t)gridDim.x * blockDim.x) {
+        rz = fma(r[i], z[i], rz);
+        rr = fma(r[i], r[i], rr);
+    }
+    double v[2] = {rz, rr}, tot[2];
+    if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
+        if (mode == 0) {
+            ctl->beta = tot[0] / ctl->rz;
+            ctl->rz = tot[0];
+            ctl->rr = tot[1];
+            ctl->iters += 1;
+            if (!(tot[1] > stop_rr)) ctl->stop = 1;
+        } else {
+            ctl->rz = tot[0];
+        }
     }
 }
 
@@ -521,60 +548,10 @@ __global__ void k_scatter_eq(int64_t nnodes, int B, const int64_t *eq_id, int64_
     else nm[t] = eq[e];
 }
 
-__global__ void k_csr_init(int64_t nr, const double *b, const double *dinv, double *r, double *z, double *x,
-                           Ctl *ctl, double *partials) {
-    double rz = 0.0, rr = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += (int64_t)gridDim.x * blockDim.x) {
-        double rv = b[i];
-        r[i] = rv;
-        double zv = dinv[i] * rv;
-        z[i] = zv;
-        x[i] = 0.0;
-        rz += rv * zv;
-        rr += rv * rv;
-    }
-    double v[2] = {rz, rr}, tot[2];
-    if (grid_sum<2>(v, partials, &ctl->ticket[1], tot) && threadIdx.x == 0) {
-        ctl->rz = tot[0];
-        ctl->rr = tot[1];
-        ctl->bnorm2 = tot[1];
-        ctl->beta = 0.0;
-        ctl->stop = (tot[1] == 0.0);
-        ctl->converged = ctl->stop;
-        ctl->breakdown = 0;
-    }
-}
-
-// y = K64 u (BSR FP64): used to form b - K12 u2 and the reactions
-template <int B>
-__global__ void k_bsr64(int64_t nn, int64_t nb, const int64_t *rp, const int32_t *cj, const double *A, const double *u,
-                        double *y) {
-    int lane = threadIdx.x & 31;
-    int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (n >= nn) return;
-    double acc[B];
-#pragma unroll
-    for (int c = 0; c < B; c++) acc[c] = 0.0;
-    for (int64_t k = rp[n] + lane; k < rp[n + 1]; k += 32) {
-        int64_t j = cj[k];
-#pragma unroll
-        for (int c = 0; c < B; c++)
-#pragma unroll
-            for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u[j * B + d], acc[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < B; c++) acc[c] = warp_sum(acc[c]);
-    if (lane == 0)
-#pragma unroll
-        for (int c = 0; c < B; c++) y[n * B + c] = acc[c];
-}
-
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
 
-void amr_axpy_d(int64_t n, double a, const double *x, double *y, cudaStream_t s);
-double amr_masked_residual(amr_model *m, const double *b, const double *Kx, double *reac);
 
 struct AmrSolveWork {
     int64_t n = 0;               // nnodes * B
@@ -584,13 +561,8 @@ struct AmrSolveWork {
     Ctl *ctl = nullptr;
     Ctl *h_ctl = nullptr;        // pinned
     int grid = 0, grid_spmv = 0;
-    // plain FP64 CSR path
-    int64_t csr_nnz = -1;
-    int64_t *crp = nullptr, *csrc = nullptr;
-    int32_t *ccol = nullptr;
-    double *cval = nullptr, *dinv = nullptr, *cx = nullptr, *cr = nullptr, *cz = nullptr, *cp[2] = {nullptr, nullptr},
-           *cq = nullptr, *cb = nullptr, *tmp = nullptr;
-    int64_t csr_for_nu = -1;
+    // all-FP64 comparators: Krylov vectors (allocated on their first use)
+    double *r64 = nullptr, *z64 = nullptr, *p64 = nullptr, *q64 = nullptr;
 };
 
 static AmrSolveWork *work(amr_model *m) {
@@ -602,6 +574,7 @@ static AmrSolveWork *work(amr_model *m) {
         amr_free(w->x32); amr_free(w->r32); amr_free(w->z32); amr_free(w->p32[0]); amr_free(w->p32[1]);
         amr_free(w->q32);
         amr_free(w->s32);
+        amr_free(w->r64); amr_free(w->z64); amr_free(w->p64); amr_free(w->q64);
         amr_alloc(&w->s32, n);
         amr_alloc(&w->x32, n); amr_alloc(&w->r32, n); amr_alloc(&w->z32, n); amr_alloc(&w->p32[0], n);
         amr_alloc(&w->p32[1], n); amr_alloc(&w->q32, n);
@@ -614,8 +587,8 @@ static AmrSolveWork *work(amr_model *m) {
         amr_alloc(&w->partials, (size_t)std::max(4 * w->grid, w->grid_spmv) + 8);
         if (!w->ctl) {
             amr_alloc(&w->ctl, 1);
-            AMR_CUDA(cudaMemset(w->ctl, 0, sizeof(Ctl)));
-            AMR_CUDA(cudaMallocHost(&w->h_ctl, sizeof(Ctl)));
+            AMR_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), m->stream));
+            w->h_ctl = (Ctl *)amr_pinned_alloc(sizeof(Ctl));
         }
     }
     return w;
@@ -627,10 +600,8 @@ void amr_solver_free(amr_model *m) {
     amr_free(w->x32); amr_free(w->r32); amr_free(w->z32); amr_free(w->p32[0]); amr_free(w->p32[1]); amr_free(w->q32);
     amr_free(w->s32);
     amr_free(w->partials); amr_free(w->ctl);
-    if (w->h_ctl) cudaFreeHost(w->h_ctl);
-    amr_free(w->crp); amr_free(w->csrc); amr_free(w->ccol); amr_free(w->cval); amr_free(w->dinv); amr_free(w->cx);
-    amr_free(w->cr); amr_free(w->cz); amr_free(w->cp[0]); amr_free(w->cp[1]); amr_free(w->cq); amr_free(w->cb);
-    amr_free(w->tmp);
+    amr_pinned_free(w->h_ctl);
+    amr_free(w->r64); amr_free(w->z64); amr_free(w->p64); amr_free(w->q64);
     delete w;
     m->sw = nullptr;
 }
@@ -810,121 +781,165 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
     return res;
 }
 
+// The all-FP64 comparator of solve_mixed: the same block-Jacobi PCG, with the FP64 matrix, FP64
+// block inverses and FP64 vectors, so that the two differ in precision only.  The solution is updated in
+// place (x at free slots); convergence is decided, as in the mixed path, on the true residual
+// ||mask(b - K64 x)|| / ||mask(b - K64 x0)||, recomputed whenever the recursive residual looks converged.
 template <int B>
-static AmrSolveResult solve_fp64_csr(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
+static AmrSolveResult solve_fp64(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
     AmrSolveWork *w = work(m);
     cudaStream_t s = m->stream;
-    int64_t nu = m->nu;
-    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
-    if (w->csr_for_nu != nu || w->csr_nnz < 0) {  // build the scalar CSR of K11 once per DOF numbering
-        amr_free(w->crp); amr_free(w->csrc); amr_free(w->ccol); amr_free(w->cval); amr_free(w->dinv);
-        amr_free(w->cx); amr_free(w->cr); amr_free(w->cz); amr_free(w->cp[0]); amr_free(w->cp[1]); amr_free(w->cq);
-        amr_free(w->cb); amr_free(w->tmp);
-        int64_t *cnt;
-        amr_alloc(&cnt, nu);
-        AMR_CUDA(cudaMemsetAsync(cnt, 0, nu * sizeof(int64_t), s));
-        int64_t nt = m->nnodes * B;
-        k_csr_count<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, cnt);
-        AMR_COUNT(1);
-        amr_alloc(&w->crp, nu + 1);
-        amr_scan_i64(cnt, w->crp, nu, s);
-        AMR_CUDA(cudaMemcpy(&w->csr_nnz, w->crp + nu, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        amr_alloc(&w->ccol, w->csr_nnz);
-        amr_alloc(&w->csrc, w->csr_nnz);
-        amr_alloc(&w->cval, w->csr_nnz);
-        k_csr_fill<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->brow_ptr, m->bcol, m->eq_id, nu, m->bstride, w->crp,
-                                                 w->ccol, w->csrc);
-        AMR_COUNT(1);
-        amr_free(cnt);
-        amr_alloc(&w->dinv, nu); amr_alloc(&w->cx, nu); amr_alloc(&w->cr, nu); amr_alloc(&w->cz, nu);
-        amr_alloc(&w->cp[0], nu); amr_alloc(&w->cp[1], nu); amr_alloc(&w->cq, nu); amr_alloc(&w->cb, nu);
-        amr_alloc(&w->tmp, m->nnodes * B);
-        w->csr_for_nu = nu;
-        AMR_CUDA(cudaGetLastError());
+    const int64_t nn = m->nnodes;
+    if (!w->r64) {
+        amr_alloc(&w->r64, w->n); amr_alloc(&w->z64, w->n); amr_alloc(&w->p64, w->n); amr_alloc(&w->q64, w->n);
     }
-    // values of the last assembly (part of assembly for this path, not of the solve time)
-    k_csr_values<<<nblk(w->csr_nnz, 256), 256, 0, s>>>(w->csr_nnz, w->csrc, m->K64, w->cval);
-    AMR_COUNT(1);
-    k_csr_diag<<<nblk(nu, 256), 256, 0, s>>>(nu, w->crp, w->ccol, w->cval, w->dinv);
-    AMR_COUNT(1);
-    // b_red = b - K12 u2: tmp = K64 x (x holds prescribed values, zero at free slots on entry)
-    int64_t nt = m->nnodes * B;
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    const double tol2 = o.rtol * o.rtol;
+    AMR_CUDA(cudaMemsetAsync(w->p64, 0, w->n * sizeof(double), s));
+    {
+        Ctl c0{};
+        c0.first = 1;
+        AMR_CUDA(cudaMemcpyAsync(w->ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    }
     AMR_CUDA(cudaEventRecord(m->ev0, s));
-    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, x,
-                                                         w->tmp);
-    AMR_COUNT(1);
-    // cb = b - K12 u2 on the free eq rows (b and K64 x scattered to eq order)
-    k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, (double *)b, w->cb, 1);
-    AMR_COUNT(1);
-    k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, w->tmp, w->cq, 1);
+    const unsigned g = (unsigned)w->grid;
+    k_refine<B, double><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+                                               reac, w->r64, w->z64, m->Minv64, w->ctl, w->partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
-    double tol2 = o.rtol * o.rtol;
-    AMR_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), s));
-    AMR_CUDA(cudaMemsetAsync(w->cp[0], 0, nu * sizeof(double), s));
-    unsigned g = (unsigned)w->grid;
-    amr_axpy_d(nu, -1.0, w->cq, w->cb, s);
-    k_csr_init<<<g, kThreads, 0, s>>>(nu, w->cb, w->dinv, w->cr, w->cz, w->cx, w->ctl, w->partials);
-    AMR_COUNT(1);
-    int cur = 0;
-    int every = o.refine_every > 0 ? o.refine_every : 32;
+    const int every = o.refine_every > 0 ? o.refine_every : 32;  // iterations between host checks
     for (;;) {
         AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
         AMR_CUDA(cudaStreamSynchronize(s));
-        Ctl c = *w->h_ctl;
-        if (c.converged) break;
+        const Ctl c = *w->h_ctl;
+        res.iterations = c.iters;
+        if (c.bnorm2 == 0.0 || c.converged) break;
         if (c.breakdown) { res.status = AMR_ENOCONV; break; }
-        if (res.iterations >= o.max_iters) { res.status = AMR_ENOCONV; break; }
-        int nit = std::min(every, o.max_iters - res.iterations);
+        if (c.iters >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        if (c.stop) {  // the recursive residual looks converged: check the true one
+            AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
+            k_refine<B, double><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b,
+                                                       x, reac, w->r64, w->z64, m->Minv64, w->ctl, w->partials, 0,
+                                                       tol2);
+            AMR_COUNT(1);
+            res.refinements++;
+            continue;
+        }
+        const double stop_rr = 0.25 * 0.25 * tol2 * c.bnorm2;
+        const int nit = std::min(every, o.max_iters - c.iters);
         for (int it = 0; it < nit; it++) {
-            k_csr_spmv<<<g, kThreads, 0, s>>>(nu, w->crp, w->ccol, w->cval, w->cz, w->cp[cur], w->cp[cur ^ 1], w->cq,
-                                              w->ctl, w->partials);
-            AMR_COUNT(1);
-            k_csr_update<<<g, kThreads, 0, s>>>(nu, w->dinv, w->cp[cur ^ 1], w->cq, w->cx, w->cr, w->cz, w->ctl,
-                                                w->partials, tol2);
-            AMR_COUNT(1);
-            cur ^= 1;
+            k_pupdate64<B><<<g, kThreads, 0, s>>>(nn, w->z64, w->p64, w->ctl);
+            k_spmv64<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w->p64,
+                                               w->q64, w->ctl, w->partials);
+            k_update64<B><<<g, kThreads, 0, s>>>(nn, m->Minv64, w->p64, w->q64, x, w->r64, w->z64, w->ctl,
+                                                 w->partials, stop_rr);
+            AMR_COUNT(3);
         }
         AMR_CUDA(cudaGetLastError());
-        res.iterations += nit;
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, m->ev0, m->ev1);
     res.seconds = ms * 1e-3;
-    // x (node-major) free slots <- cx ; reactions and the true residual from the BSR FP64 matrix
-    k_scatter_eq<<<nblk(nt, 256), 256, 0, s>>>(m->nnodes, B, m->eq_id, nu, x, w->cx, 0);
-    AMR_COUNT(1);
-    k_bsr64<B><<<nblk(m->nnodes * 32, 256), 256, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, x,
-                                                         w->tmp);
-    AMR_COUNT(1);
-    double rr = amr_masked_residual(m, b, w->tmp, reac);
-    Ctl c = *w->h_ctl;
-    res.rel_residual = c.bnorm2 > 0 ? std::sqrt(rr / c.bnorm2) : 0.0;
+    const Ctl c = *w->h_ctl;
+    res.rel_residual = c.bnorm2 > 0 ? std::sqrt(c.rr_true / c.bnorm2) : 0.0;
+    return res;
+}
+
+// The all-FP64 comparator of solve_amg: the same PCG with the same multigrid hierarchy (aggregates,
+// prolongators, Chebyshev smoothing, dense coarsest level) built and applied in FP64 on K64.  The
+// iteration is one CUDA graph, as in solve_amg; convergence is decided on the true residual.
+template <int B>
+static AmrSolveResult solve_amg_fp64(amr_model *m, double *x, const double *b, double *reac,
+                                     const amr_solve_opts &o) {
+    amr_amg_prepare64(m);
+    AmrSolveWork *w = work(m);
+    cudaStream_t s = m->stream;
+    const int64_t nn = m->nnodes;
+    if (!w->r64) {
+        amr_alloc(&w->r64, w->n); amr_alloc(&w->z64, w->n); amr_alloc(&w->p64, w->n); amr_alloc(&w->q64, w->n);
+    }
+    AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    const double tol2 = o.rtol * o.rtol;
+    AMR_CUDA(cudaMemsetAsync(w->p64, 0, w->n * sizeof(double), s));
+    {
+        Ctl c0{};
+        c0.first = 1;
+        AMR_CUDA(cudaMemcpyAsync(w->ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    }
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    const unsigned g = (unsigned)w->grid;
+    auto refresh = [&](int first) {
+        k_refine<B, double><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+                                                   reac, w->r64, w->z64, m->Minv64, w->ctl, w->partials, first, tol2);
+        amr_amg_vcycle64(m, w->r64, w->z64);
+        k_rz64<B><<<g, kThreads, 0, s>>>(nn, w->r64, w->z64, w->ctl, w->partials, 0.0, 1);
+        AMR_COUNT(2);
+        AMR_CUDA(cudaGetLastError());
+    };
+    refresh(1);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long long per_iter = 0;
+    struct GraphFree {
+        cudaGraph_t &g;
+        cudaGraphExec_t &x;
+        ~GraphFree() {
+            if (x) cudaGraphExecDestroy(x);
+            if (g) cudaGraphDestroy(g);
+        }
+    } graph_free{graph, gexec};
+    const int every = 4;  // iterations between host checks (each iteration is a whole V-cycle)
+    for (;;) {
+        AMR_CUDA(cudaMemcpyAsync(w->h_ctl, w->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        const Ctl c = *w->h_ctl;
+        res.iterations = c.iters;
+        if (c.bnorm2 == 0.0 || c.converged) break;
+        if (c.breakdown) { res.status = AMR_ENOCONV; break; }
+        if (c.iters >= o.max_iters) { res.status = AMR_ENOCONV; break; }
+        if (c.stop) {
+            AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
+            refresh(0);
+            res.refinements++;
+            continue;
+        }
+        const int nit = std::min(every, o.max_iters - c.iters);
+        if (!gexec) {
+            const double stop_rr = 0.25 * 0.25 * tol2 * c.bnorm2;
+            const long long before = amr_g_launches.load();
+            AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+            k_pupdate64<B><<<g, kThreads, 0, s>>>(nn, w->z64, w->p64, w->ctl);
+            k_spmv64<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w->p64,
+                                               w->q64, w->ctl, w->partials);
+            k_update64a<B><<<g, kThreads, 0, s>>>(nn, w->p64, w->q64, x, w->r64, w->ctl);
+            amr_amg_vcycle64(m, w->r64, w->z64);
+            k_rz64<B><<<g, kThreads, 0, s>>>(nn, w->r64, w->z64, w->ctl, w->partials, stop_rr, 0);
+            AMR_COUNT(4);
+            const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+            per_iter = amr_g_launches.load() - before;
+            AMR_COUNT(-per_iter);
+            AMR_CUDA(ce);
+            AMR_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
+        }
+        for (int it = 0; it < nit; it++) {
+            AMR_CUDA(cudaGraphLaunch(gexec, s));
+            AMR_COUNT(per_iter);
+        }
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    res.seconds = ms * 1e-3;
+    const Ctl c = *w->h_ctl;
+    res.rel_residual = c.bnorm2 > 0 ? std::sqrt(c.rr_true / c.bnorm2) : 0.0;
     return res;
 }
 
 // ---- small vector helpers ----
 namespace {
-__global__ void k_axpy(int64_t n, double a, const double *x, double *y) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] += a * x[i];
-}
-__global__ void k_masked_res(int64_t n, const uint8_t *fm, const double *b, const double *Kx, double *reac,
-                             double *partials, unsigned int *ticket, double *out) {
-    double rr = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (fm[i]) {
-            double r = b[i] - Kx[i];
-            rr += r * r;
-        } else if (reac) {
-            reac[i] = Kx[i];
-        }
-    }
-    double v[1] = {rr}, tot[1];
-    if (grid_sum<1>(v, partials, ticket, tot) && threadIdx.x == 0) *out = tot[0];
-}
 __global__ void k_absmax(int64_t n, const double *v, const uint8_t *fm, double *partials, unsigned int *ticket,
                          double *out) {
     double mx = 0.0;
@@ -963,24 +978,6 @@ __global__ void k_absmax(int64_t n, const double *v, const uint8_t *fm, double *
 }
 }  // namespace
 
-void amr_axpy_d(int64_t n, double a, const double *x, double *y, cudaStream_t s) {
-    if (n <= 0) return;
-    k_axpy<<<nblk(n, 256), 256, 0, s>>>(n, a, x, y);
-    AMR_COUNT(1);
-}
-
-double amr_masked_residual(amr_model *m, const double *b, const double *Kx, double *reac) {
-    AmrSolveWork *w = work(m);
-    double *out = (double *)(w->partials + 3 * (size_t)w->grid);
-    k_masked_res<<<w->grid, kThreads, 0, m->stream>>>(w->n, m->free_mask, b, Kx, reac, w->partials, &w->ctl->ticket[3],
-                                                      out);
-    AMR_COUNT(1);
-    double h = 0.0;
-    AMR_CUDA(cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
-    AMR_CUDA(cudaStreamSynchronize(m->stream));
-    return h;
-}
-
 double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask) {
     AmrSolveWork *w = work(m);
     double *out = (double *)(w->partials + 3 * (size_t)w->grid);
@@ -1008,8 +1005,9 @@ void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq) {
 AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
     if (m->batch && o.method == AMR_SOLVER_MIXED) return amr_batch_solve(m, x, b, reac, o);  // one CTA per part
     if (o.method == AMR_SOLVER_AMG) return m->B == 3 ? solve_amg<3>(m, x, b, reac, o) : solve_amg<2>(m, x, b, reac, o);
-    if (o.method == AMR_SOLVER_FP64)
-        return m->B == 3 ? solve_fp64_csr<3>(m, x, b, reac, o) : solve_fp64_csr<2>(m, x, b, reac, o);
+    if (o.method == AMR_SOLVER_FP64) return m->B == 3 ? solve_fp64<3>(m, x, b, reac, o) : solve_fp64<2>(m, x, b, reac, o);
+    if (o.method == AMR_SOLVER_AMG_FP64)
+        return m->B == 3 ? solve_amg_fp64<3>(m, x, b, reac, o) : solve_amg_fp64<2>(m, x, b, reac, o);
     return m->B == 3 ? solve_mixed<3>(m, x, b, reac, o) : solve_mixed<2>(m, x, b, reac, o);
 }
 
@@ -1025,6 +1023,29 @@ static double time_spmv32(amr_model *m, int reps) {
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
         launch_spmv32<B>(m, w, w->z32, w->s32);
+    }
+    AMR_CUDA(cudaEventRecord(m->ev1, s));
+    AMR_CUDA(cudaEventSynchronize(m->ev1));
+    float ms = 0.f;
+    AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    return ms * 1e-3 / reps;
+}
+
+template <int B>
+static double time_spmv64(amr_model *m, int reps) {
+    AmrSolveWork *w = work(m);
+    if (!w->p64) throw AmrError(AMR_EINVAL, "run an all-FP64 solve on the current K first");
+    cudaStream_t s = m->stream;
+    Ctl c{};
+    c.rz = 1.0;
+    c.first = 1;
+    AMR_CUDA(cudaMemcpyAsync(w->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    const unsigned g = (unsigned)w->grid;
+    AMR_CUDA(cudaEventRecord(m->ev0, s));
+    for (int i = 0; i < reps; i++) {
+        k_spmv64<B><<<g, kThreads, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w->z64,
+                                           w->q64, w->ctl, w->partials);
+        AMR_COUNT(1);
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));
@@ -1056,6 +1077,7 @@ static double time_residual64(amr_model *m, int reps) {
 
 double amr_time_solver_kernel(amr_model *m, int which, int reps) {
     if (which == AMR_KERNEL_SPMV32) return m->B == 3 ? time_spmv32<3>(m, reps) : time_spmv32<2>(m, reps);
+    if (which == AMR_KERNEL_SPMV64) return m->B == 3 ? time_spmv64<3>(m, reps) : time_spmv64<2>(m, reps);
     return m->B == 3 ? time_residual64<3>(m, reps) : time_residual64<2>(m, reps);
 }
 
@@ -1087,23 +1109,25 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
 void *g_noalloc_addr[kMaxDevices] = {nullptr};
-std::atomic<int> g_noalloc_lock{0};
+std::mutex g_noalloc_mutex;
 
 // Device address of g_noalloc_scratch for the current device, looked up once per device.
-// (In host code the symbol name is only a host-side stand-in, not a device address.)
+// (In host code the symbol name is only a host-side stand-in, not a device address.)  A thread
+// that finds the lookup under way sleeps on the mutex while the first one may be loading the module.
 void *noalloc_base() {
     int dev = 0;
     AMR_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) throw AmrError(AMR_EINVAL, "device ordinal out of range");
-    while (g_noalloc_lock.exchange(1)) {
-    }
-    void *p = g_noalloc_addr[dev];
+    void *p = nullptr;
     cudaError_t e = cudaSuccess;
-    if (!p) {
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e == cudaSuccess) g_noalloc_addr[dev] = p;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        p = g_noalloc_addr[dev];
+        if (!p) {
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e == cudaSuccess) g_noalloc_addr[dev] = p;
+        }
     }
-    g_noalloc_lock.store(0);
     if (e != cudaSuccess)
         throw AmrError(AMR_ECUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
     return p;
@@ -1222,6 +1246,7 @@ extern "C" int amr_solve_noalloc(amr_model *m, double *d_U, double *d_F, const a
         m->err.clear();
         if (!m->dofs_set) throw AmrError(AMR_EINVAL, "amr_set_dofs must be called first");
         if (!m->K_valid) throw AmrError(AMR_EINVAL, "K has not been assembled");
+        if (m->batch) throw AmrError(AMR_EUNSUPPORTED, "no-allocation solves of batched parts are not supported");
         if (!d_U || !d_F) throw AmrError(AMR_EINVAL, "null device buffer");
         const int64_t n = m->nnodes * m->B;
         if (n > kNoAllocMaxSlots)

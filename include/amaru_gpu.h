@@ -95,13 +95,17 @@ typedef struct {
 } amr_load;
 
 /* Linear-solver options for the Newton corrector solve. */
-enum { AMR_SOLVER_MIXED = 0, AMR_SOLVER_FP64 = 1, AMR_SOLVER_AMG = 2 };
+enum { AMR_SOLVER_MIXED = 0, AMR_SOLVER_FP64 = 1, AMR_SOLVER_AMG = 2, AMR_SOLVER_AMG_FP64 = 3 };
 typedef struct {
     int32_t method;          /* AMR_SOLVER_MIXED: FP32 block-Jacobi PCG in FP64 iterative refinement
-                                AMR_SOLVER_FP64:  plain all-FP64 CSR Jacobi PCG
+                                AMR_SOLVER_FP64:  the same block-Jacobi PCG all in FP64 (FP64 matrix,
+                                                  block inverses and vectors): MIXED's comparator
                                 AMR_SOLVER_AMG:   as MIXED with an aggregation-multigrid V-cycle
                                                   (rigid-body coarse spaces, Chebyshev/block-Jacobi
-                                                  smoothing) in place of block-Jacobi */
+                                                  smoothing) in place of block-Jacobi
+                                AMR_SOLVER_AMG_FP64: the same multigrid PCG all in FP64 (the
+                                                  hierarchy built and applied in FP64): AMG's
+                                                  comparator */
     double rtol;             /* relative residual ||b - K u|| / ||b|| to reach (default 1e-8) */
     int32_t max_iters;       /* cap on inner Krylov iterations (default 20000) */
     int32_t refine_every;    /* FP64 true-residual refresh interval in inner iterations (default 32) */
@@ -208,20 +212,58 @@ int amr_solve(amr_model *m, double *U, double *F, const amr_solve_opts *opts, am
 int amr_stage_run(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params *p, double *U,
                   double *F, amr_stage_stats *stats);
 
+/* One record per Newton iteration of the last whole-model static stage (amr_stage_run,
+ * amr_stage_run_dev), as the reference logs them (mech_stage_solver!, "inc" at
+ * src/mech/mech-solver.jl:293-297, "it ... residue" at :352): iterations that end in a
+ * system error before their residue is computed are not logged, as there. */
+typedef struct {
+    int32_t increment;         /* the reference's inc counter: 1-based; a failed increment's number is reused */
+    int32_t iteration;         /* Newton iteration within the increment, 1-based */
+    int32_t krylov_iterations; /* inner Krylov iterations of this Newton iteration */
+    int32_t converged;         /* 1 on the iteration that ended its increment converged */
+    double T;                  /* pseudo-time at the start of the increment */
+    double dT;                 /* the increment's size */
+    double residue;            /* ||R||inf after the iteration */
+} amr_iteration_record;
+/* Copies min(cap, n) records into rec (may be null with cap 0) and sets *n to the count. */
+int amr_get_stage_log(const amr_model *m, amr_iteration_record *rec, int32_t cap, int32_t *n);
+
+/* Hook of the whole-model static stage after every converged increment, where the reference calls
+ * update_records!(ana, checkpoint=checkpoint) (src/mech/mech-solver.jl:410-424) to write its output
+ * files at checkpoints (nouts) and to update its loggers and monitors.  U and F (ndofs, eq_id order)
+ * are the stage's accumulated displacements and internal forces so far (the increments of dof.vals,
+ * :394-397), in host memory the library owns for the duration of the call; the handle's IP states
+ * are the committed ones and may be read with amr_get_state.  A nonzero return stops the stage with
+ * AMR_ESTAGE, as a failed update_records! ends the reference's loop (:421-424).  fn = null clears it.
+ * No kernels of the handle are in flight during the call. */
+typedef struct {
+    double T;                  /* the stage's pseudo-time after this increment */
+    int32_t increment;         /* the reference's inc counter */
+    int32_t checkpoint;        /* 1 if this increment reached an output time (T > Tcheck - dTmin) */
+    int64_t ndofs;
+    const double *U, *F;
+} amr_increment_info;
+typedef int (*amr_increment_fn)(void *user, const amr_increment_info *info);
+int amr_set_increment_callback(amr_model *m, amr_increment_fn fn, void *user);
+
 /* amr_solve for callers that cannot allocate GPU memory while they solve (a host
  * application that gives the library a fixed memory budget up front, a real-time
  * loop that must stay out of the CUDA allocator, a memory pool that may not grow).
  * No counterpart in the reference: Amaru allocates freely in solve_system!.
- * Same semantics as amr_solve on the last assembled K, mixed-precision solver only,
- * but d_U and d_F are caller-owned DEVICE buffers of ndofs doubles (eq_id order):
+ * Same semantics as amr_solve on the last assembled K of a single model (not a
+ * batch of parts: AMR_EUNSUPPORTED), mixed-precision solver only, but d_U and d_F
+ * are caller-owned DEVICE buffers of ndofs doubles (eq_id order):
  * in: d_U[nu:] prescribed values, d_F[:nu] natural values; out: d_U[:nu] and the
  * reactions d_F[nu:].  The call allocates nothing: all scratch lives in one static
- * device array of about 11.5 MB that every GPU loading the library holds until the
- * process exits, which limits the model to nnodes x ndim <= 262 144 (larger models
- * get AMR_EINVAL; use amr_solve).  The first call on each device looks up that
- * array's device address (cudaGetSymbolAddress), so make it before any stream
- * capture.  All calls share the one array: calls whose work overlaps on the GPU
- * (other handles, other streams, other threads) race and must be serialized. */
+ * device array of about 11.5 MB, which limits the model to nnodes x ndim <= 262 144
+ * (larger models get AMR_EINVAL; use amr_solve).  The array is reserved on a device
+ * when the library's solver module is first loaded there (with CUDA's lazy module
+ * loading that can be this call's first use) and is held until the process exits:
+ * make one warm-up call, or any solve, before entering a region that may not
+ * allocate.  The first call on each device also looks up that array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls
+ * share the one array: calls whose work overlaps on the GPU (other handles, other
+ * streams, other threads) race and must be serialized. */
 int amr_solve_noalloc(amr_model *m, double *d_U, double *d_F, const amr_solve_opts *opts, amr_solve_stats *stats);
 
 /* amr_stage_run with device-resident vectors: d_Uex, d_Fex, d_U, d_F are device
@@ -320,10 +362,20 @@ int amr_autotune(amr_model *m, amr_tuning *out);
  * per launch.  Needs a preceding amr_assemble_K (and a solve for the SpMV). */
 enum { AMR_KERNEL_SPMV32 = 0, AMR_KERNEL_RESIDUAL64 = 1, AMR_KERNEL_STIFFNESS = 2, AMR_KERNEL_GATHER = 3,
        AMR_KERNEL_INTERNAL = 4, AMR_KERNEL_AMG_RESIDUAL = 5 /* the multigrid cycle's fine residual; after an AMG solve */,
-       AMR_KERNEL_DYN_RHS = 6 /* base + M x + C y of the dynamic Newton loop; after amr_assemble_M */ };
+       AMR_KERNEL_DYN_RHS = 6 /* base + M x + C y of the dynamic Newton loop; after amr_assemble_M */,
+       AMR_KERNEL_SPMV64 = 7 /* the all-FP64 PCG's q = K64 p; after an AMR_SOLVER_FP64 solve */,
+       AMR_KERNEL_AMG_RESIDUAL64 = 8 /* the FP64 cycle's fine residual; after an AMR_SOLVER_AMG_FP64 solve */ };
 int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seconds, double *bytes_per_launch);
+/* Measured arithmetic peak of the current GPU, the denominator of FP-pipe-bound kernels' rooflines:
+ * TFLOP/s of fused multiply-adds in a register-resident kernel (8 independent chains per thread, every
+ * SM full), timed with CUDA events.  No counterpart in the reference. */
+enum { AMR_PEAK_FP64_FMA = 0, AMR_PEAK_FP32_FMA = 1 };
+int amr_measure_peak(int32_t which, double *tflops);
 /* Number of kernels this handle has launched since it was created. */
 int amr_launch_count(const amr_model *m, int64_t *count);
+/* Number of device allocations and frees (cudaMalloc / cudaFree) the library has
+ * made in this process, all handles together. */
+int amr_alloc_count(int64_t *count);
 
 /* ---- dynamics ----
  * Element density (MechSolid props rho, src/mech/elem/mech-solid.jl:6-29), nelems values in the

@@ -947,7 +947,7 @@ class MechAnalysis:
                 if checkpoint:
                     Tcheck += dTcheck
                 if record is not None:
-                    record(self, T)
+                    record(self, T, checkpoint)
                 if autoinc:
                     if dTbk > 0.0:
                         dT = min(dTbk, Tcheck - T)

@@ -151,10 +151,14 @@ def test_update_state_and_tangent(mat, shape, n, box):
     assert np.abs(d.data).max(initial=0.0) <= 1e-10 * np.abs(Ko.data).max()
 
 
-@pytest.mark.parametrize("solver", ["mixed", "fp64"])
+SOLVERS = {"mixed": A.SOLVER_MIXED, "fp64": A.SOLVER_FP64, "amg": A.SOLVER_AMG, "amg_fp64": A.SOLVER_AMG_FP64}
+
+
+@pytest.mark.parametrize("solver", ["mixed", "fp64", "amg", "amg_fp64"])
 @pytest.mark.parametrize("shape,n,box", [CASES[0], CASES[1], CASES[2], CASES[4], CASES[5]])
 def test_solve_system(solver, shape, n, box):
-    """solve_system! with prescribed nonzero values: U1 and reactions F2 vs the direct solve."""
+    """solve_system! with prescribed nonzero values: U1 and reactions F2 vs the direct solve, for the
+    mixed-precision solvers and their all-FP64 comparators (the same method in FP64)."""
     bcs = BCS_3D if len(n) == 3 else BCS_2D
     om, gm, ob, gb = _models(shape, n, box, ("LinearElastic", dict(E=200e3, nu=0.3)), bcs)
     dofs, nu, setup = O.configure_dofs(om, ob)
@@ -169,12 +173,45 @@ def test_solve_system(solver, shape, n, box):
     K = O.mount_K(om, len(dofs))
     assert O.solve_system(K, Uo, Fo, nu) is None
     gm.mount_K()
-    st = gm.solve_system(Ug, Fg, method=A.SOLVER_FP64 if solver == "fp64" else A.SOLVER_MIXED, rtol=1e-10)
+    st = gm.solve_system(Ug, Fg, method=SOLVERS[solver], rtol=1e-10)
     assert st.rel_residual <= 1e-10
     sc = np.abs(Uo[:nu]).max()
     assert np.abs(Ug[:nu] - Uo[:nu]).max() <= 1e-6 * sc
     fs = np.abs(Fo[nu:]).max()
     assert np.abs(Fg[nu:] - Fo[nu:]).max() <= 1e-6 * fs
+
+
+@pytest.mark.parametrize("solver", ["fp64", "amg_fp64"])
+def test_fp64_comparator_matches_its_mixed_method(solver):
+    """The all-FP64 comparators solve the system the mixed solvers solve: the same solution to the
+    tolerance, a bitwise repeatable result, no more iterations than the mixed method, and timed
+    kernels (the FP64 SpMV / cycle residual) that run on the current K."""
+    om, gm, ob, gb = _models(A.HEX20, (8, 3, 3), [[0, 0, 0], [4, 1, 1]], ("LinearElastic", dict(E=30e3, nu=0.2)),
+                             [("z==0", "surface", dict(ux=0, uy=0, uz=0)), ("z==1", "surface", dict(tz=-1.0))])
+    U, F = gm.get_bc_vals(gm.configure_dofs(gb))
+    gm.mount_K()
+    mixed = "mixed" if solver == "fp64" else "amg"
+    Um, Fm = U.copy(), F.copy()
+    sm = gm.solve_system(Um, Fm, method=SOLVERS[mixed], rtol=1e-10)
+    U1, F1 = U.copy(), F.copy()
+    s1 = gm.solve_system(U1, F1, method=SOLVERS[solver], rtol=1e-10)
+    U2, F2 = U.copy(), F.copy()
+    gm.solve_system(U2, F2, method=SOLVERS[solver], rtol=1e-10)
+    nu = gm.nu
+    assert s1.rel_residual <= 1e-10 and sm.rel_residual <= 1e-10
+    assert np.array_equal(U1, U2) and np.array_equal(F1, F2)
+    assert np.abs(U1[:nu] - Um[:nu]).max() <= 1e-7 * np.abs(Um[:nu]).max()
+    assert np.abs(F1[nu:] - Fm[nu:]).max() <= 1e-7 * np.abs(Fm[nu:]).max()
+    assert s1.iterations <= 1.1 * sm.iterations + 3  # FP64 vectors never need more iterations
+    kernel = A._lib.KERNEL_SPMV64 if solver == "fp64" else A._lib.KERNEL_AMG_RESIDUAL64
+    t, nbytes = gm.dev.time_kernel(kernel, 3)
+    assert t > 0 and nbytes > 0
+
+
+def test_fp64_fma_peak_is_measured():
+    t64 = A._lib.measure_peak(A._lib.PEAK_FP64_FMA)
+    t32 = A._lib.measure_peak(A._lib.PEAK_FP32_FMA)
+    assert 0.1 < t64 < t32 < 1000.0
 
 
 def test_solver_reaches_1e8_and_is_reproducible():
