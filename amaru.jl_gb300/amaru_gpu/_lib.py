@@ -141,7 +141,8 @@ class Request(C.Structure):
 
 class RequestResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("active_at_admit", C.c_int32), ("bytes", C.c_int64),
-                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double), ("stage", StageStats)]
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double), ("stage", StageStats),
+                ("t_stage", C.c_double), ("dev_start", C.c_double), ("dev_end", C.c_double)]
 
 
 class ServerInfo(C.Structure):

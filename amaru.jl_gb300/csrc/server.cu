@@ -80,6 +80,7 @@ struct amr_server {
     amr_server_config cfg{};
     int device = 0;
     Clock::time_point t0;
+    cudaEvent_t ev_ref = nullptr;  // recorded at creation: the origin of the requests' device timeline
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Request *> queue;
@@ -103,8 +104,24 @@ struct amr_server {
                 rc = amr_assemble_loads(m, r->loads.data(), (int32_t)r->loads.size(), 0.0, r->Fex.data());
             r->U.assign(r->ndofs, 0.0);
             r->F.assign(r->ndofs, 0.0);
+            r->res.t_stage = now();
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            const bool timed = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+            if (timed) cudaEventRecord(e0, m->stream);
             if (!rc) rc = amr_stage_run(m, r->Uex.data(), r->Fex.data(), &r->stage, r->U.data(), r->F.data(),
                                         &r->res.stage);
+            if (timed) {
+                cudaEventRecord(e1, m->stream);
+                float a = 0.f, b = 0.f;
+                if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&a, ev_ref, e0) == cudaSuccess &&
+                    cudaEventElapsedTime(&b, ev_ref, e1) == cudaSuccess) {
+                    r->res.dev_start = a * 1e-3;
+                    r->res.dev_end = b * 1e-3;
+                }
+            }
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            cudaGetLastError();
             if (rc) {
                 char buf[512];
                 amr_last_error(m, buf, sizeof buf);
@@ -165,8 +182,10 @@ int amr_server_create(const amr_server_config *cfg, amr_server **out) {
     amr_server *s = new amr_server();
     s->cfg = *cfg;
     s->t0 = Clock::now();
-    if (cudaGetDevice(&s->device) != cudaSuccess) {
+    if (cudaGetDevice(&s->device) != cudaSuccess || cudaEventCreate(&s->ev_ref) != cudaSuccess ||
+        cudaEventRecord(s->ev_ref, 0) != cudaSuccess || cudaEventSynchronize(s->ev_ref) != cudaSuccess) {
         cudaGetLastError();
+        if (s->ev_ref) cudaEventDestroy(s->ev_ref);
         delete s;
         return AMR_ECUDA;
     }
@@ -277,6 +296,8 @@ int amr_server_destroy(amr_server *s) {
     }
     s->cv_work.notify_all();
     for (auto &t : s->workers) t.join();
+    cudaEventDestroy(s->ev_ref);
+    amr_trim_pool();  // the finished requests' memory goes back to the device
     delete s;
     return AMR_OK;
 }

@@ -217,24 +217,60 @@ function solve_system!(g::GPUModel, U::Vector{Float64}, F::Vector{Float64}; rtol
     return st === nothing ? Amaru.success() : st
 end
 
+# After every converged increment of a device stage (amr_set_increment_callback): the dof values so far,
+# the committed IP states, sctx.T / inc / out, then update_records!(ana, checkpoint=...) as
+# mech_stage_solver! calls it (src/mech/mech-solver.jl:394-424).  A failed update_records! stops the stage.
+mutable struct IncrementContext
+    ana::MechAnalysis
+    g::GPUModel
+    dofs::Vector{Amaru.Dof}
+    base_u::Vector{Float64}
+    base_f::Vector{Float64}
+end
+
+struct IncrementInfo
+    T::Float64; increment::Int32; checkpoint::Int32; ndofs::Int64
+    U::Ptr{Float64}; F::Ptr{Float64}
+end
+
+function increment_hook(user::Ptr{Cvoid}, info::Ptr{IncrementInfo})::Cint
+    try
+        ctx = unsafe_pointer_to_objref(user)::IncrementContext
+        i = unsafe_load(info)
+        U = unsafe_wrap(Array, i.U, i.ndofs)
+        F = unsafe_wrap(Array, i.F, i.ndofs)
+        for (k, dof) in enumerate(ctx.dofs)
+            dof.vals[dof.name] = ctx.base_u[k] + U[k]
+            dof.vals[dof.natname] = ctx.base_f[k] + F[k]
+        end
+        sync_states!(ctx.g, ctx.ana.model)
+        sctx = ctx.ana.sctx
+        sctx.T = i.T
+        sctx.inc = i.increment
+        i.checkpoint != 0 && (sctx.out += 1)
+        st = Amaru.update_records!(ctx.ana, checkpoint=i.checkpoint != 0)
+        return Amaru.failed(st) ? Cint(1) : Cint(0)
+    catch
+        return Cint(1)  # no Julia exception crosses the C ABI: the stage stops
+    end
+end
+
 """
     gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
 
 mech_stage_solver! with the Newton loop, K, the solves and the IP states on
 the device.  The essential values and loads come from Amaru's own
-configure_dofs! and get_bc_vals; the dof values are updated as the reference
-does (src/mech/mech-solver.jl:394-397).  Afterwards the IP states are copied
-into the elements' IpState objects and the stage's records are written as the
-reference writes them: the initial record of stage 1 (:234-242), the record of
-the checkpoint at the end of the stage, numbered as the reference numbers it
-(:412-420), and the record of a failed stage (:488).  The records of
-intermediate checkpoints (nouts > 1) are not written: the increments run on the
-device without returning to Julia.
+configure_dofs! and get_bc_vals.  After every converged increment the library
+calls back into Julia, where the dof values are updated as the reference
+does (src/mech/mech-solver.jl:394-397), the IP states are copied into the
+elements' IpState objects, and update_records! runs with the reference's
+checkpoint flag and output numbering (:410-424): every checkpoint of nouts gets
+its record, and the loggers and monitors see every increment.  Stage 1 writes
+its initial record first (:234-242), and a failed stage its last one (:488).
 """
 function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
     model = ana.model
-    sctx = ana.sctx
     activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
@@ -255,23 +291,25 @@ function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
     U = zeros(length(dofs))
     F = zeros(length(dofs))
     stats = StageStats()
-    rc = ccall((:amr_stage_run, LIB), Cint,
-               (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ref{StageParams}, Ptr{Float64}, Ptr{Float64}, Ref{StageStats}),
-               g.h, Uex, Fex, p, U, F, stats)
+    ctx = IncrementContext(ana, g, dofs, [dof.vals[dof.name] for dof in dofs], [dof.vals[dof.natname] for dof in dofs])
+    hook = @cfunction(increment_hook, Cint, (Ptr{Cvoid}, Ptr{IncrementInfo}))
+    rc = GC.@preserve ctx begin
+        ccall((:amr_set_increment_callback, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+              g.h, hook, pointer_from_objref(ctx))
+        r = ccall((:amr_stage_run, LIB), Cint,
+                  (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ref{StageParams}, Ptr{Float64}, Ptr{Float64},
+                   Ref{StageStats}), g.h, Uex, Fex, p, U, F, stats)
+        ccall((:amr_set_increment_callback, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}), g.h, C_NULL, C_NULL)
+        r
+    end
     if rc == 0 || rc == -11
-        for (i, dof) in enumerate(dofs)
-            dof.vals[dof.name] += U[i]
-            dof.vals[dof.natname] += F[i]
+        for (i, dof) in enumerate(dofs)  # the converged increments' values (as the last callback set them)
+            dof.vals[dof.name] = ctx.base_u[i] + U[i]
+            dof.vals[dof.natname] = ctx.base_f[i] + F[i]
         end
         sync_states!(g, model)
-        sctx.inc = stats.increments
-        sctx.T = stats.T
     end
-    if rc == 0
-        sctx.out += max(stage.nouts, 1)  # the checkpoints of the stage; the last one is at T = 1
-        Amaru.update_records!(ana, checkpoint=true)
-        return Amaru.success()
-    end
+    rc == 0 && return Amaru.success()
     st = check(g, rc)
     rc == -11 && Amaru.update_records!(ana, force=true)
     return st
@@ -665,7 +703,8 @@ mutable struct RequestResult
     status::Int32; active_at_admit::Int32; bytes::Int64
     t_submit::Float64; t_admit::Float64; t_done::Float64
     stage::PartStats
-    RequestResult() = new(0, 0, 0, 0.0, 0.0, 0.0, PartStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0.0))
+    t_stage::Float64; dev_start::Float64; dev_end::Float64
+    RequestResult() = new(0, 0, 0, 0.0, 0.0, 0.0, PartStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0.0), 0.0, 0.0, 0.0)
 end
 
 struct ServerConfig

@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-dyn", action="store_true", help="skip the dynamic (Newmark) stage measurement")
     ap.add_argument("--no-modal", action="store_true", help="skip the modal analysis measurement")
     ap.add_argument("--no-vtu", action="store_true", help="skip the VTU output measurement")
-    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--slope", default="100x17x40", help="TET10 slope stage divisions (408 000 elements by default)")
     ap.add_argument("--no-slope", action="store_true", help="skip the TET10 slope stage measurement")
     return ap.parse_args()
@@ -642,9 +642,12 @@ def _serve_requests(count):
     import amaru_gpu as A
     rng = np.random.default_rng(SERVE_SEED)
     arrivals = np.cumsum(rng.exponential(1 / 200.0, count))
+    is_tet = np.zeros(count, dtype=bool)
+    is_tet[:int(round(0.2 * count))] = True  # exactly 20 % elastoplastic TET10 requests, in seeded order
+    rng.shuffle(is_tet)
     reqs = []
     for i in range(count):
-        tet = rng.random() < 0.2
+        tet = bool(is_tet[i])
         incs = int(rng.integers(1, 11))
         if tet:
             dofs = float(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
@@ -691,13 +694,32 @@ def serving_leg(count=32, max_active=8):
     t_last = max(r.t_done for _, _, r, _ in out)
     span = t_last - t_first
     dof_incs = sum(n * r.stage.increments for _, rc, r, n in out if rc == 0)
+
+    def pct(v):
+        v = np.asarray(v)
+        return {"p50_ms": float(np.percentile(v, 50)) * 1e3, "p99_ms": float(np.percentile(v, 99)) * 1e3}
+    # device concurrency: the time-weighted number of requests whose stage is on the GPU (device clock)
+    ev = sorted([(r.dev_start, 1) for _, _, r, _ in out] + [(r.dev_end, -1) for _, _, r, _ in out])
+    busy, weighted, cur, t_prev = 0.0, 0.0, 0, ev[0][0]
+    for t, d in ev:
+        if cur > 0:
+            busy += t - t_prev
+            weighted += cur * (t - t_prev)
+        cur += d
+        t_prev = t
     return {"workload": "%d requests, Poisson arrivals 200/s (seed 0xC5): HEX8 cantilever blocks 1x0.5x0.5, DOFs log-uniform "
-                        "[1e3, 2e6], 1..10 linear increments; 20%% TET10 von Mises blocks (gravity + surcharge, "
+                        "[1e3, 2e6], 1..10 linear increments; exactly 20%% TET10 von Mises blocks (gravity + surcharge, "
                         "automatic increments), DOFs log-uniform [1e3, 2e5]; multigrid-preconditioned solver to 1e-8" % count,
             "requests": count, "completed": int(sum(rc == 0 for _, rc, _, _ in out)),
             "tet10": int(sum(k == "tet10" for k, _, _, _ in out)),
             "solves_per_s": count / span, "p50_ms": float(np.percentile(lat, 50)) * 1e3,
             "p99_ms": float(np.percentile(lat, 99)) * 1e3, "mean_ms": float(lat.mean()) * 1e3,
+            "latency_parts": {"queue": pct([r.t_admit - r.t_submit for _, _, r, _ in out]),
+                              "host_setup": pct([r.t_stage - r.t_admit for _, _, r, _ in out]),
+                              "stage_device": pct([r.stage.seconds for _, _, r, _ in out]),
+                              "stage_wall": pct([r.t_done - r.t_stage for _, _, r, _ in out])},
+            "device_overlap": {"busy_s": busy, "mean_requests_on_device": weighted / busy if busy else 0.0,
+                               "stage_device_s_sum": float(sum(r.stage.seconds for _, _, r, _ in out))},
             "dof_increments_per_s": dof_incs / span, "makespan_s": span, "max_active": max_active,
             "peak_active": int(info.peak_active), "peak_admitted_gb": info.peak_bytes / 1e9,
             "hbm_budget_gb": budget / 1e9,

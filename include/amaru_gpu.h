@@ -319,6 +319,10 @@ typedef struct {
     int64_t bytes;            /* admitted footprint (amr_estimate_bytes) */
     double t_submit, t_admit, t_done;  /* seconds since the server was created */
     amr_stage_stats stage;
+    double t_stage;           /* host set-up done (model created, DOFs set, loads assembled), stage starts */
+    double dev_start, dev_end;/* the stage's span on the request's stream, seconds on the device clock
+                                 since the server was created (CUDA events): requests whose spans
+                                 intersect ran on the GPU at the same time */
 } amr_request_result;
 typedef struct {
     int64_t queued, active, peak_active, completed, active_bytes, peak_bytes;

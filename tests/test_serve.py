@@ -7,7 +7,10 @@ Checked here:
   (MechAnalysis on its own handle), and that equals the oracle within 1e-6;
 * admission never lets the admitted footprints exceed the HBM budget, and a
   request waits for memory that running requests free;
-* a request that can never fit is refused at submit.
+* a request that can never fit is refused at submit;
+* two admitted requests run on the GPU at the same time: their stages' spans on the
+  device clock (CUDA events on each request's stream) intersect, and each result is
+  bitwise the one it gets alone.
 """
 import numpy as np
 import pytest
@@ -122,3 +125,22 @@ def test_request_beyond_the_budget_is_refused():
         with pytest.raises(A.AmrError) as e:
             srv.submit(m, _bcs("hex8"))
         assert e.value.code == -9
+
+
+def test_admitted_requests_overlap_on_the_device():
+    reqs = [("hex8", (40, 8, 8), 190e3, 6), ("hex8", (40, 8, 8), 210e3, 6)]
+    models = [_model(k, n, E) for k, n, E, _ in reqs]
+    with serve.Server(hbm_budget_bytes=64e9, max_active=2) as srv:
+        tickets = [srv.submit(m, _bcs(k), nincs=inc, solver="amg") for m, (k, n, E, inc) in zip(models, reqs)]
+        out = [srv.wait(t) for t in tickets]
+    (rc0, U0, F0, r0, m0), (rc1, U1, F1, r1, m1) = out
+    assert rc0 == 0 and rc1 == 0, (m0, m1)
+    assert r0.dev_end > r0.dev_start > 0 and r1.dev_end > r1.dev_start > 0
+    assert r0.dev_start < r1.dev_end and r1.dev_start < r0.dev_end  # both stages on the GPU at once
+    assert r0.stage.seconds <= (r0.dev_end - r0.dev_start) * 1.01 + 1e-4
+    for (k, n, E, inc), (rc, U, F, res, msg) in zip(reqs, out):
+        alone = _model(k, n, E, device=True)
+        ana = A.MechAnalysis(alone)
+        ana.addstage(_bcs(k), nincs=inc)
+        assert ana.solve(solver="amg")[0]
+        assert np.array_equal(U, alone.U) and np.array_equal(F, alone.F)
