@@ -92,7 +92,9 @@ class Tuning(C.Structure):
 class DynParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("dTmin", C.c_double), ("dTmax", C.c_double), ("rspan", C.c_double),
                 ("alpha", C.c_double), ("beta", C.c_double), ("tspan", C.c_double), ("maxits", C.c_int32),
-                ("autoinc", C.c_int32), ("nincs", C.c_int32), ("nouts", C.c_int32), ("linear", SolveOpts)]
+                ("autoinc", C.c_int32), ("nincs", C.c_int32), ("nouts", C.c_int32), ("linear", SolveOpts),
+                ("sism", C.c_int32), ("sism_dir", C.c_int32), ("tss", C.c_double), ("tds", C.c_double),
+                ("sism_acc", C.c_void_p), ("sism_n", C.c_int64)]
 
 
 class ModalParams(C.Structure):

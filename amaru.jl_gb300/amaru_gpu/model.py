@@ -432,9 +432,12 @@ class DynAnalysis:
         self.stages.append(st)
 
     def solve(self, tol=0.01, dTmin=1e-7, dTmax=0.1, rspan=0.01, maxits=5, autoinc=False, alpha=0.0, beta=0.0,
-              solver="mixed", linear_rtol=1e-8, quiet=True, scheme="FE"):
+              solver="mixed", linear_rtol=1e-8, quiet=True, scheme="FE", sism=False, tss=0.0, tds=0.0,
+              sism_file="", sism_dir="fx"):
         """Returns (ok, message); dof values land in model.U, model.V, model.A, model.F (node-major).  `scheme`
-        is checked as dyn_solver_params checks it and, as in dyn_stage_solver!, not used."""
+        is checked as dyn_solver_params checks it and, as in dyn_stage_solver!, not used.  sism: seismic input,
+        the record of sism_file (read as readdlm reads it, times 9.81) spread over tds from t = 0, applied as
+        M (a(t) e_dir) while tss <= t <= tss + tds (sismic_force, src/mech/dyn-solver.jl:106-157)."""
         checkargs("solve!", DYN_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan,
                   maxits=maxits, scheme=scheme)
         if len(self.stages) != 1:
@@ -454,7 +457,16 @@ class DynAnalysis:
         p = L.default_dyn_params(tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan, alpha=alpha, beta=beta,
                                  tspan=stage.tspan, maxits=maxits, autoinc=int(autoinc), nincs=stage.nincs,
                                  nouts=stage.nouts, linear=L.default_solve_opts(method=method, rtol=linear_rtol))
+        acc = None
+        if sism:
+            dirs = {"ux": 0, "fx": 0, "uy": 1, "fy": 1, "uz": 2, "fz": 2}
+            if sism_dir not in dirs:
+                raise KeyError(sism_dir)  # node.dofdict[keysis] fails for a key no node has
+            acc = np.ascontiguousarray(9.81 * np.loadtxt(sism_file, ndmin=2).reshape(-1), dtype=np.float64)
+            p.sism, p.sism_dir, p.tss, p.tds = 1, dirs[sism_dir], float(tss), float(tds)
+            p.sism_acc, p.sism_n = acc.ctypes.data, len(acc)
         rc, U, V, A, F, st = model.dev.dyn_stage_run(U0, dU, F0, dF, p)
+        del acc
         self.stats = st
         if rc not in (0, -11):
             return False, model.dev.last_error()

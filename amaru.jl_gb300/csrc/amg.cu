@@ -22,6 +22,8 @@
 // patterns depend only on the pattern, the coordinates and the DOF numbering
 // (host, once); the coarse values, block inverses, lambdas and the dense
 // inverse depend on K (device, after each assembly).
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -170,6 +172,14 @@ struct AmrAmg {
     unsigned int *ticket = nullptr;
     int64_t dofs_version = -1;
     bool numeric_valid = false, numeric64_valid = false;
+    // The FP32 cycle's fine-level residual reads an FP16 copy of the symmetrically scaled matrix
+    // A16 = S K32 S, S = diag(s_n) per node with s_n = 1/rs_n a power of two and rs_n^2 >= the node's
+    // largest diagonal entry, so |A16| <= 1 for an SPD K and the copy is exactly symmetric.  The residual
+    // r = b - K x is then rs_i sum_j A16_ij xt_j with xt = x rs kept, one 16-byte gather per block, by the
+    // smoother and the prolongation of that level.
+    __half *A16 = nullptr;      // SoA [B*B][bstride]
+    float *rs = nullptr;        // nnodes: 1 / s_n
+    float *xt = nullptr;        // nnodes x 4 (3-D) or x 2 (2-D): x rs
 };
 
 namespace {
@@ -205,6 +215,7 @@ void amr_amg_free(amr_model *m) {
         amr_free(v.cptr); amr_free(v.ck); amr_free(v.ci); amr_free(v.null_dof);
     }
     amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
+    amr_free(g->A16); amr_free(g->rs); amr_free(g->xt);
     delete g;
     m->amg = nullptr;
 }
@@ -400,6 +411,10 @@ static void amg_build_structure(amr_model *m) {
     amr_alloc(&g->Cinv, (size_t)g->nc * g->nc);
     amr_alloc(&g->scratch, 8 + kNormCtas);
     amr_alloc(&g->ticket, 1);
+    amr_alloc(&g->A16, (size_t)m->bstride * B * B);
+    amr_alloc(&g->rs, m->nnodes);
+    amr_alloc(&g->xt, (size_t)m->nnodes * (B == 3 ? 4 : 2));
+    AMR_CUDA(cudaMemsetAsync(g->xt, 0, (size_t)m->nnodes * (B == 3 ? 4 : 2) * sizeof(float), m->stream));
     AMR_CUDA(cudaMemsetAsync(g->ticket, 0, sizeof(unsigned int), m->stream));
     g->numeric_valid = false;
 }
@@ -563,14 +578,14 @@ __global__ void __launch_bounds__(256) k_bsr_res64(int64_t n, const int64_t *__r
         for (int c = 0; c < NB; c++) acc[c] = 0.0;
         if (valid)
             for (int64_t k = rp[row] + sub; k < rp[row + 1]; k += RL) {
-                const int64_t j = __ldcs(cj + k);
+                const int64_t j = __ldg(cj + k);
                 double xv[NB];
 #pragma unroll
                 for (int d = 0; d < NB; d++) xv[d] = __ldg(x + (int64_t)NB * j + d);
 #pragma unroll
                 for (int c = 0; c < NB; c++)
 #pragma unroll
-                    for (int d = 0; d < NB; d++) acc[c] = fma(__ldcs(A + (int64_t)(c * NB + d) * nbs + k), xv[d], acc[c]);
+                    for (int d = 0; d < NB; d++) acc[c] = fma(__ldg(A + (int64_t)(c * NB + d) * nbs + k), xv[d], acc[c]);
             }
 #pragma unroll
         for (int c = 0; c < NB; c++)
@@ -586,16 +601,135 @@ __global__ void __launch_bounds__(256) k_bsr_res64(int64_t n, const int64_t *__r
     }
 }
 
+// The fine-level FP16 copy: rs_n = the smallest power of two >= sqrt(the node's largest diagonal entry)
+template <int NB>
+__global__ void k_fine_scale(int64_t n, const int64_t *diag, const float *A, int64_t nbs, float *rs) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float dmax = 0.0f;
+    if (diag[i] >= 0)
+#pragma unroll
+        for (int c = 0; c < NB; c++) dmax = fmaxf(dmax, A[(int64_t)(c * NB + c) * nbs + diag[i]]);
+    float r = 1.0f;
+    if (dmax > 0.0f && isfinite(dmax)) {
+        int e = 0;
+        frexpf(sqrtf(dmax), &e);  // sqrt(dmax) < 2^e
+        r = ldexpf(1.0f, e);
+    }
+    rs[i] = r;
+}
+
+// A16 = (A_ij / (rs_i rs_j)) in FP16 (power-of-two scaling: exact before the rounding), saturated; warp per row
+template <int NB>
+__global__ void k_fine_half(int64_t n, const int64_t *rp, const int32_t *cj, const float *A, int64_t nbs,
+                            const float *rs, __half *A16) {
+    const int lane = threadIdx.x & 31;
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    const float si = 1.0f / rs[row];
+    for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+        const float sij = si / rs[cj[k]];
+#pragma unroll
+        for (int q = 0; q < NB * NB; q++) {
+            const float v = fminf(fmaxf(A[(int64_t)q * nbs + k] * sij, -65504.0f), 65504.0f);
+            A16[(int64_t)q * nbs + k] = __float2half_rn(v);
+        }
+    }
+}
+
+// the scaled iterate xt of the fine level: one 16-byte (3-D) or 8-byte (2-D) gather per block; coarse
+// block sizes have none (their kernels get a null xt)
+template <int NB>
+struct FineX {
+    using T = float4;
+    __device__ static T make(const float *) { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+    __device__ static void get(const T &, float *) {}
+};
+template <>
+struct FineX<3> {
+    using T = float4;
+    __device__ static T make(const float *v) { return make_float4(v[0], v[1], v[2], 0.0f); }
+    __device__ static void get(const T &t, float *v) { v[0] = t.x; v[1] = t.y; v[2] = t.z; }
+};
+template <>
+struct FineX<2> {
+    using T = float2;
+    __device__ static T make(const float *v) { return make_float2(v[0], v[1]); }
+    __device__ static void get(const T &t, float *v) { v[0] = t.x; v[1] = t.y; }
+};
+
+// r = b - K x (b null: K x) from A16 and xt: G lanes per row, each lane 8 consecutive blocks per step (one
+// 16-byte load per component and two of column indices, from the row's start rounded down to 8), the
+// matrix streamed (evict-first), xt through the read-only path
+template <int NB>
+__global__ void __launch_bounds__(256) k_bsr_res16(int64_t n, const int64_t *__restrict__ rp,
+                                                   const int32_t *__restrict__ cj, const __half *__restrict__ A,
+                                                   int64_t nbs, const float *__restrict__ rs,
+                                                   const typename FineX<NB>::T *__restrict__ xt,
+                                                   const float *__restrict__ b, float *__restrict__ out) {
+    constexpr int G = 4;
+    const int lane = threadIdx.x % G;
+    const unsigned gmask = 0xfu << (G * ((threadIdx.x & 31) / G));
+    const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t row = grp; row < n; row += ng) {
+        float acc[NB];
+#pragma unroll
+        for (int c = 0; c < NB; c++) acc[c] = 0.0f;
+        const int64_t k0 = rp[row], k1 = rp[row + 1];
+        for (int64_t kc = (k0 & ~int64_t(7)) + 8 * lane; kc < k1; kc += 8 * G) {
+            const int4 j0 = __ldcs(reinterpret_cast<const int4 *>(cj + kc));
+            const int4 j1 = __ldcs(reinterpret_cast<const int4 *>(cj + kc + 4));
+            uint4 a[NB * NB];
+#pragma unroll
+            for (int q = 0; q < NB * NB; q++) a[q] = __ldcs(reinterpret_cast<const uint4 *>(A + (int64_t)q * nbs + kc));
+            const int js[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+#pragma unroll
+            for (int u2 = 0; u2 < 4; u2++) {
+                float2 av[NB * NB];
+#pragma unroll
+                for (int q = 0; q < NB * NB; q++) {
+                    const unsigned w = u2 == 0 ? a[q].x : u2 == 1 ? a[q].y : u2 == 2 ? a[q].z : a[q].w;
+                    av[q] = __half22float2(*reinterpret_cast<const __half2 *>(&w));
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int u = 2 * u2 + h;
+                    const int64_t k = kc + u;
+                    if (k < k0 || k >= k1) continue;
+                    float xv[NB];
+                    FineX<NB>::get(__ldg(xt + js[u]), xv);
+#pragma unroll
+                    for (int c = 0; c < NB; c++)
+#pragma unroll
+                        for (int d = 0; d < NB; d++) acc[c] = fmaf(h ? av[c * NB + d].y : av[c * NB + d].x, xv[d], acc[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < NB; c++) acc[c] += __shfl_down_sync(gmask, acc[c], o, G);
+        if (lane == 0) {
+            const float r = rs[row];
+#pragma unroll
+            for (int c = 0; c < NB; c++) out[row * NB + c] = b ? b[row * NB + c] - r * acc[c] : r * acc[c];
+        }
+    }
+}
+
 // Chebyshev steps on D^-1 A (node-block D^-1):
 //   mode 0: d = s2 Dinv r; x = d           (first step from x = 0; r is the right-hand side)
 //   mode 1: d = s2 Dinv r; x += d          (first step from a given x; r = b - A x)
 //   mode 2: d = s1 d + s2 Dinv r; x += d   (second step)
+//   xt (fine level of the FP32 cycle, may be null): xt_i = rs_i x_i as well
 template <int NB, class V>
 __global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Dinv, const V *__restrict__ r,
-                       V *__restrict__ d, V *__restrict__ x) {
+                       V *__restrict__ d, V *__restrict__ x, const float *__restrict__ rs = nullptr,
+                       typename FineX<NB>::T *__restrict__ xt = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    V rv[NB];
+    V rv[NB], xn[NB];
 #pragma unroll
     for (int c = 0; c < NB; c++) rv[c] = r[i * NB + c];
 #pragma unroll
@@ -605,7 +739,14 @@ __global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Di
         for (int e = 0; e < NB; e++) s = vfma(Dinv[i * NB * NB + c * NB + e], rv[e], s);
         const V dv = mode == 2 ? vfma(s1, d[i * NB + c], s2 * s) : s2 * s;
         d[i * NB + c] = dv;
-        x[i * NB + c] = mode == 0 ? dv : x[i * NB + c] + dv;
+        xn[c] = mode == 0 ? dv : x[i * NB + c] + dv;
+        x[i * NB + c] = xn[c];
+    }
+    if (xt) {
+        float v[NB];
+#pragma unroll
+        for (int c = 0; c < NB; c++) v[c] = (float)xn[c] * rs[i];
+        xt[i] = FineX<NB>::make(v);
     }
 }
 
@@ -637,17 +778,26 @@ __global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anode
 }
 
 // x_i += T_i xc[agg(i)]
+// x_i += T_i xc[agg(i)]  (and xt_i = rs_i x_i on the fine level of the FP32 cycle)
 template <int NB, int NM, class V>
-__global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc, V *x) {
+__global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc, V *x, const float *rs = nullptr,
+                          typename FineX<NB>::T *xt = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int64_t a = agg[i];
+    float v[NB];
 #pragma unroll
     for (int c = 0; c < NB; c++) {
         V s = x[i * NB + c];
 #pragma unroll
         for (int m = 0; m < NM; m++) s = vfma(T[(i * NB + c) * NM + m], xc[a * NM + m], s);
         x[i * NB + c] = s;
+        v[c] = (float)s;
+    }
+    if (xt) {
+#pragma unroll
+        for (int c = 0; c < NB; c++) v[c] *= rs[i];
+        xt[i] = FineX<NB>::make(v);
     }
 }
 
@@ -828,21 +978,38 @@ struct Cycle {
         const Cheb c = cheb_coef(v.lam);
         const V s1 = (V)c.s1, s2a = (V)c.s2a, s2b = (V)c.s2b;
         const unsigned gn = nblk(L.n, 256);
+        // the FP32 cycle's fine level: residuals from the FP16 copy and the scaled iterate xt
+        using XT = typename FineX<NB>::T;
+        constexpr bool kHalf = std::is_same<V, float>::value && NB == B && (NB == 2 || NB == 3);
+        const bool half = kHalf && l == 0;
+        XT *xt = half ? reinterpret_cast<XT *>(g->xt) : nullptr;
+        const float *rs = half ? g->rs : nullptr;
+        auto residual = [&]() {
+            if constexpr (kHalf) {
+                if (half) {
+                    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
+                    k_bsr_res16<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, g->A16, nbs, g->rs, xt, b, v.r);
+                    AMR_COUNT(1);
+                    return;
+                }
+            }
+            bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+        };
         // pre-smoothing from x = 0
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x);
-        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x, rs, xt);
+        residual();
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, rs, xt);
         // coarse correction
-        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+        residual();
         AmgLevel &C = g->L[l + 1];
         AmgVals<V> &cv = vals<V>(C);
         k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r, cv.bv);
         level(m, g, l + 1, cv.bv, cv.x);
-        k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x);
+        k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt);
         // post-smoothing
-        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x);
-        bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+        residual();
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x, rs, xt);
+        residual();
         k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x);
         AMR_COUNT(7);
         AMR_CUDA(cudaGetLastError());
@@ -894,6 +1061,13 @@ struct Cycle {
                 k_block_inverse<NM, V><<<nblk(C.n, 128), 128, 0, s>>>(C.n, C.diag, cv.A, C.nbs, cv.Dinv);
                 AMR_COUNT(1);
             }
+            AMR_CUDA(cudaGetLastError());
+        }
+        if constexpr (std::is_same<V, float>::value) {  // the fine level's FP16 copy
+            AmgLevel &F = g->L[0];
+            k_fine_scale<B><<<nblk(F.n, 256), 256, 0, s>>>(F.n, F.diag, m->K32, m->bstride, g->rs);
+            k_fine_half<B><<<nblk(F.n * 32, 256), 256, 0, s>>>(F.n, F.rp, F.cj, m->K32, m->bstride, g->rs, g->A16);
+            AMR_COUNT(2);
             AMR_CUDA(cudaGetLastError());
         }
         for (size_t l = 0; l + 1 < nl; l++) {
@@ -980,28 +1154,43 @@ void amr_amg_vcycle64(amr_model *m, const double *r, double *z) {
     else Cycle<2, 3, double>::level(m, m->amg, 0, r, z);
 }
 
-// average device time of the cycle's fine-level residual r = b - K x (CUDA events on the handle's stream):
-// the FP32 kernel on K32, or with fp64 the comparator's on K64
-double amr_amg_time_residual(amr_model *m, int reps, bool fp64) {
+// average device time of the cycle's fine-level residual r = b - K x (CUDA events on the handle's stream) and
+// its algorithmic bytes per launch: the FP32 cycle's kernel on the FP16 copy, or with fp64 the comparator's on
+// K64
+double amr_amg_time_residual(amr_model *m, int reps, bool fp64, double *bytes) {
     AmrAmg *g = m->amg;
     if (!g || !(fp64 ? g->numeric64_valid : g->numeric_valid))
         throw AmrError(AMR_EINVAL, "run a multigrid solve of this precision on the current K first");
     AmgLevel &L = g->L[0];
     cudaStream_t s = m->stream;
+    const int B = m->B;
+    const double nb = (double)m->nblocks, nn = (double)m->nnodes;
+    const unsigned grid16 = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
         if (fp64) {
-            if (m->B == 3) bsr_res<3, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
+            if (B == 3) bsr_res<3, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
             else bsr_res<2, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
+        } else if (B == 3) {
+            k_bsr_res16<3><<<grid16, 256, 0, s>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs,
+                                                 reinterpret_cast<const float4 *>(g->xt), L.f32.bv, L.f32.r);
+            AMR_COUNT(1);
         } else {
-            if (m->B == 3) bsr_res<3, float>(s, L, m->K32, m->bstride, nullptr, L.f32.x, L.f32.bv, L.f32.r);
-            else bsr_res<2, float>(s, L, m->K32, m->bstride, nullptr, L.f32.x, L.f32.bv, L.f32.r);
+            k_bsr_res16<2><<<grid16, 256, 0, s>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs,
+                                                 reinterpret_cast<const float2 *>(g->xt), L.f32.bv, L.f32.r);
+            AMR_COUNT(1);
         }
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));
     float ms = 0.f;
     AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    if (bytes) {
+        // blocks (values + column) + row pointers + per node: b read, r written, and x (FP64: read once, plus
+        // the row mask) or the FP16 path's scale and scaled iterate (one 16- or 8-byte vector per node)
+        if (fp64) *bytes = nb * (8.0 * B * B + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 * 3.0 + 1.0);
+        else *bytes = nb * (2.0 * B * B + 4.0) + (nn + 1) * 8.0 + nn * (4.0 * B * 2.0 + 4.0 + (B == 3 ? 16.0 : 8.0));
+    }
     return ms * 1e-3 / reps;
 }
 

@@ -67,8 +67,9 @@ struct amr_model {
     int64_t ninc = 0;
     // node-block sparsity pattern
     int64_t nblocks = 0;
-    // component stride of the SoA K64 / K32 arrays and length of bcol: nblocks rounded up to a
-    // multiple of 4, plus 4, so every component starts on 16 bytes and whole 16-byte groups stay inside
+    // component stride of the SoA K64 / K32 (and the cycle's FP16) arrays and length of bcol: nblocks
+    // rounded up to a multiple of 8, plus 8, so every component starts on 16 bytes and whole 16-byte
+    // groups of 8 blocks (FP16 values, column indices) stay inside
     int64_t bstride = 0;
     int64_t *brow_ptr = nullptr;    // nnodes+1
     int32_t *bcol = nullptr;        // nblocks
@@ -245,7 +246,7 @@ void amr_amg_vcycle(amr_model *m, const float *r, float *z);
 void amr_amg_prepare64(amr_model *m);                           // the same hierarchy in FP64
 void amr_amg_vcycle64(amr_model *m, const double *r, double *z);
 void amr_amg_invalidate(amr_model *m);
-double amr_amg_time_residual(amr_model *m, int reps, bool fp64);
+double amr_amg_time_residual(amr_model *m, int reps, bool fp64, double *bytes);
 void amr_amg_free(amr_model *m);
 // recovery.cu: nodal_patch_recovery (structure once per model, values per call)
 void amr_recovery_prepare(amr_model *m);

@@ -777,6 +777,7 @@ void amr_default_dyn_params(amr_dyn_params *p) {
     p->alpha = 0.0; p->beta = 0.0; p->tspan = 0.0;
     p->maxits = 5; p->autoinc = 0; p->nincs = 1; p->nouts = 0;
     amr_default_solve_opts(&p->linear);
+    p->sism = 0; p->sism_dir = 0; p->tss = 0.0; p->tds = 0.0; p->sism_acc = nullptr; p->sism_n = 0;
 }
 
 int amr_dyn_stage_run(amr_model *m, const double *Uex0, const double *Uex1, const double *Fex0, const double *Fex1,
@@ -987,25 +988,23 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
         const double nb = (double)m->nblocks, nn = (double)m->nnodes, B = m->B, BB = m->BB;
         double t = 0.0, bytes = 0.0;
         switch (kernel) {
-        case AMR_KERNEL_SPMV32:  // K32 blocks + block columns + row pointers; p read once, q written
+        case AMR_KERNEL_SPMV32:  // K32 blocks + block columns + row pointers; p (padded) read once, q written
             t = amr_time_solver_kernel(m, AMR_KERNEL_SPMV32, reps);
-            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 2.0;
+            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * ((B == 3 ? 4.0 : 2.0) + B);
             break;
         case AMR_KERNEL_RESIDUAL64:  // K64 blocks + columns + row pointers; u, b read; r32, z written; Minv read
             t = amr_time_solver_kernel(m, AMR_KERNEL_RESIDUAL64, reps);
             bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 + 8.0 + 4.0 + 4.0 + 1.0) + nn * BB * 4.0;
             break;
-        case AMR_KERNEL_AMG_RESIDUAL:  // as SPMV32, plus b read (x gathered, r written)
-            t = amr_amg_time_residual(m, reps, false);
-            bytes = nb * (4.0 * BB + 4.0) + (nn + 1) * 8.0 + 4.0 * nn * B * 3.0;
+        case AMR_KERNEL_AMG_RESIDUAL:  // the FP16 copy's blocks, row pointers, b, r, the scale and xt per node
+            t = amr_amg_time_residual(m, reps, false, &bytes);
             break;
         case AMR_KERNEL_SPMV64:  // K64 blocks + columns + row pointers; p read once, q written, row mask
             t = amr_time_solver_kernel(m, AMR_KERNEL_SPMV64, reps);
             bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 * 2.0 + 1.0);
             break;
         case AMR_KERNEL_AMG_RESIDUAL64:  // as SPMV64, plus b read
-            t = amr_amg_time_residual(m, reps, true);
-            bytes = nb * (8.0 * BB + 4.0) + (nn + 1) * 8.0 + nn * B * (8.0 * 3.0 + 1.0);
+            t = amr_amg_time_residual(m, reps, true, &bytes);
             break;
         case AMR_KERNEL_DYN_RHS:
             t = amr_dyn_time_rhs(m, reps, &bytes);

@@ -125,6 +125,15 @@ __global__ void k_dyn_axpby(int64_t n, double a, const double *x, double b, cons
     o[i] = y ? __dadd_rn(__dmul_rn(a, x[i]), __dmul_rn(b, y[i])) : __dmul_rn(a, x[i]);
 }
 
+// M e_dir: the row sums of the mass blocks' scalar (every block is m I), in component dir
+__global__ void k_mass_rowsum(int64_t nnodes, int B, int dir, const int64_t *rp, const double *M, double *me) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nnodes) return;
+    double acc = 0.0;
+    for (int64_t k = rp[i]; k < rp[i + 1]; k++) acc += M[k];  // component (0,0) of block k
+    for (int c = 0; c < B; c++) me[i * B + c] = c == dir ? acc : 0.0;
+}
+
 }  // namespace
 
 namespace {
@@ -164,6 +173,21 @@ void axpby(amr_model *m, double a, const double *x, double b, const double *y, d
     AMR_CUDA(cudaGetLastError());
 }
 
+// The acceleration of sismic_force (src/mech/dyn-solver.jl:110-146) at t: the record preceded by 0 at
+// times i tds / n, linear between samples, from the last interval that holds t (the reference's search
+// never stops early); beyond the record the reference fails, and so does this.
+double seismic_acceleration(const amr_dyn_params &p, double t) {
+    const int64_t n = p.sism_n;
+    auto at = [&](int64_t i) { return i == 0 ? 0.0 : p.sism_acc[i - 1]; };
+    auto ts = [&](int64_t i) { return (double)i * p.tds / (double)n; };
+    int64_t ini = -1;
+    for (int64_t i = 0; i < n; i++)
+        if (ts(i) <= t && t <= ts(i + 1)) ini = i;
+    if (ini < 0) throw AmrError(AMR_EINVAL, "the seismic record does not cover t = " + std::to_string(t));
+    const double m = (at(ini + 1) - at(ini)) / (ts(ini + 1) - ts(ini));
+    return at(ini) + m * (t - ts(ini));
+}
+
 double round_sig3(double x) {
     if (x == 0.0 || !std::isfinite(x)) return x;
     const double e = std::floor(std::log10(std::fabs(x)));
@@ -178,13 +202,15 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
                          amr_stage_stats *stats) {
     if (m->batch) throw AmrError(AMR_EUNSUPPORTED, "dynamic stages of batched parts are not supported");
     if (p.maxits < 1 || p.nincs < 1 || !(p.tspan > 0.0)) throw AmrError(AMR_EINVAL, "bad dynamic stage parameters");
+    if (p.sism && (!p.sism_acc || p.sism_n < 1 || !(p.tds > 0.0) || p.sism_dir < 0 || p.sism_dir >= m->ndim))
+        throw AmrError(AMR_EINVAL, "seismic input needs a record, tds > 0 and a direction of the model");
     const int64_t n = m->nnodes * m->B;
     cudaStream_t s = m->stream;
     const size_t nK = (size_t)m->bstride * m->BB;
     const size_t nst = (size_t)AMR_NST * m->nip_total * sizeof(double);
     AmrEventPair ev;  // destroyed on every exit
     cudaEvent_t t0 = ev.t0, t1 = ev.t1;
-    std::vector<double *> v(16, nullptr);
+    std::vector<double *> v(17, nullptr);
     double *Ks = nullptr;
     auto release = [&]() {
         for (auto &x : v) amr_free(x);
@@ -199,7 +225,7 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
     }
     double *Fex = v[0], *Uex = v[1], *Fin = v[2], *Fina = v[3], *FexFin = v[4], *dUa = v[5], *dUi = v[6],
            *dUt = v[7], *dFin = v[8], *Va = v[9], *Aa = v[10], *x1 = v[11], *y1 = v[12], *dFp = v[13], *R = v[14],
-           *reac = v[15];
+           *reac = v[15], *Me = v[16];
     int status = AMR_OK;
     amr_stage_stats st{};
     try {
@@ -213,6 +239,11 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
         amr_mass(m);
         if (int rc = amr_check_status(m)) throw AmrError(rc, "mass assembly failed");
         axpby(m, 1.0, F0, 0.0, F1, Fex);
+        if (p.sism) {  // M e_dir once: M does not change in the stage (the reference mounts it again)
+            k_mass_rowsum<<<blocks(m->nnodes), kThreads, 0, s>>>(m->nnodes, m->B, p.sism_dir, m->brow_ptr, m->M64, Me);
+            AMR_COUNT(1);
+            if (p.tss <= 0.0) axpby(m, 1.0, Fex, seismic_acceleration(p, 0.0), Me, Fex);
+        }
         amr_dyn_combine(m, nullptr, 1.0, 0.0, 0.0, 0.0);  // K64 = M
         AMR_CUDA(cudaMemsetAsync(reac, 0, n * sizeof(double), s));
         {
@@ -235,6 +266,8 @@ int amr_dyn_stage_device(amr_model *m, const double *U0, const double *U1, const
             const double s1 = 4.0 / (dt * dt), s2 = 2.0 / dt;
             axpby(m, 1.0, U0, t + dt, U1, Uex);
             axpby(m, 1.0, F0, t + dt, F1, Fex);
+            if (p.sism && p.tss <= t + dt && p.tds + p.tss >= t + dt)
+                axpby(m, 1.0, Fex, seismic_acceleration(p, t + dt), Me, Fex);
             axpby(m, 1.0, Fex, -1.0, Fina, FexFin);
             AMR_CUDA(cudaMemsetAsync(dUa, 0, n * sizeof(double), s));
             AMR_CUDA(cudaMemcpyAsync(dUi, Uex, n * sizeof(double), cudaMemcpyDeviceToDevice, s));

@@ -258,7 +258,7 @@ void amr_build_pattern(amr_model *m) {
     AMR_CUDA(cudaMemcpyAsync(&m->nblocks, m->brow_ptr + m->nnodes, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaStreamSynchronize(s));
     if (m->nblocks >= INT32_MAX) throw AmrError(AMR_EUNSUPPORTED, "more than 2^31 nonzero blocks");
-    m->bstride = (m->nblocks + 3) / 4 * 4 + 4;
+    m->bstride = (m->nblocks + 7) / 8 * 8 + 8;
     amr_alloc(&m->bcol, m->bstride);
     pattern_rows<<<gp, kPatWarps * 32, 0, s>>>(m->conn, m->conn_ptr, m->inc_ptr, m->inc, m->nnodes, m->brow_ptr,
                                                nullptr, m->bcol, overflow);

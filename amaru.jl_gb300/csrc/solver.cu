@@ -230,8 +230,108 @@ __global__ void __launch_bounds__(kThreads) k_spmv32(int64_t nn, int64_t nb, con
     }
 }
 
-// x += alpha p ; r -= alpha q ; z = Minv r ; gamma = r.z, |r|^2 ; beta = gamma / gamma_old
+// The PCG direction in a padded layout, one aligned vector per node (float4 in 3-D, float2 in 2-D), so
+// that the SpMV gathers it with one load per block.
 template <int B>
+struct DirVec;
+template <>
+struct DirVec<3> {
+    using T = float4;
+    static constexpr int S = 4;
+    __device__ static void get(const T &t, float *v) { v[0] = t.x; v[1] = t.y; v[2] = t.z; }
+    __device__ static T make(const float *v) { return make_float4(v[0], v[1], v[2], 0.0f); }
+};
+template <>
+struct DirVec<2> {
+    using T = float2;
+    static constexpr int S = 2;
+    __device__ static void get(const T &t, float *v) { v[0] = t.x; v[1] = t.y; }
+    __device__ static T make(const float *v) { return make_float2(v[0], v[1]); }
+};
+
+// p = z + beta p on the padded direction
+template <int B>
+__global__ void k_pupdate32v(int64_t nn, const float *__restrict__ z, typename DirVec<B>::T *__restrict__ p,
+                             const Ctl *ctl) {
+    if (ctl->stop) return;
+    const float beta = ctl->first ? 0.0f : (float)ctl->beta;
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        float v[B];
+        DirVec<B>::get(p[n], v);
+#pragma unroll
+        for (int c = 0; c < B; c++) v[c] = fmaf(beta, v[c], z[n * B + c]);
+        p[n] = DirVec<B>::make(v);
+    }
+}
+
+// q = K32 p ; pq = p.q ; alpha = gamma / pq, with the padded direction: 8 lanes per block row, each lane 4
+// consecutive blocks per step (one 16-byte load per component and one of column indices, from the row's
+// start rounded down to 4), one gather of p per block.  The matrix streams (evict-first).
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_spmv32v(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
+                                                      const int32_t *__restrict__ cj, const float *__restrict__ A,
+                                                      const typename DirVec<B>::T *__restrict__ p,
+                                                      float *__restrict__ q, Ctl *ctl, double *partials) {
+    if (ctl->stop) return;
+    constexpr int G = 8;
+    const int lane = threadIdx.x % G;
+    const unsigned gmask = 0xffu << (G * ((threadIdx.x & 31) / G));
+    const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+    float dot = 0.0f;
+    for (int64_t n = grp; n < nn; n += ng) {
+        float acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0f;
+        const int64_t k0 = rp[n], k1 = rp[n + 1];
+        for (int64_t kc = (k0 & ~int64_t(3)) + 4 * lane; kc < k1; kc += 4 * G) {
+            const int4 jj = __ldcs(reinterpret_cast<const int4 *>(cj + kc));
+            float4 a[B * B];
+#pragma unroll
+            for (int q4 = 0; q4 < B * B; q4++) a[q4] = __ldcs(reinterpret_cast<const float4 *>(A + (int64_t)q4 * nb + kc));
+            const int js[4] = {jj.x, jj.y, jj.z, jj.w};
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t k = kc + u;
+                if (k < k0 || k >= k1) continue;
+                float xv[B];
+                DirVec<B>::get(__ldg(p + js[u]), xv);
+#pragma unroll
+                for (int c = 0; c < B; c++)
+#pragma unroll
+                    for (int d = B - 1; d >= 0; d--) {
+                        const float4 &t = a[c * B + d];
+                        const float av = u == 0 ? t.x : u == 1 ? t.y : u == 2 ? t.z : t.w;
+                        acc[c] = fmaf(av, xv[d], acc[c]);
+                    }
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < B; c++) acc[c] += __shfl_down_sync(gmask, acc[c], o, G);
+        if (lane == 0) {
+            float pv[B];
+            DirVec<B>::get(p[n], pv);
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                q[n * B + c] = acc[c];
+                dot = fmaf(pv[c], acc[c], dot);
+            }
+        }
+    }
+    float v[1] = {dot};
+    double tot[1];
+    if (grid_sumf<1>(v, partials, &ctl->ticket[0], tot) && threadIdx.x == 0) {
+        ctl->pq = tot[0];
+        if (!(tot[0] > 0.0)) { ctl->breakdown = 1; ctl->stop = 1; }
+        else { ctl->alpha = ctl->rz / tot[0]; ctl->first = 0; }
+    }
+}
+
+// x += alpha p ; r -= alpha q ; z = Minv r ; gamma = r.z, |r|^2 ; beta = gamma / gamma_old
+// (PS: floats per node of p, B or the padded direction's 4)
+template <int B, int PS = B>
 __global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *__restrict__ Minv,
                                                        const float *__restrict__ p, const float *__restrict__ q,
                                                        float *__restrict__ x, float *__restrict__ r,
@@ -245,7 +345,7 @@ __global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *
 #pragma unroll
         for (int c = 0; c < B; c++) {
             const int64_t i = n * B + c;
-            x[i] = fmaf(alpha, p[i], x[i]);
+            x[i] = fmaf(alpha, p[n * PS + c], x[i]);
             rv[c] = fmaf(-alpha, q[i], r[i]);
             r[i] = rv[c];
         }
@@ -273,13 +373,13 @@ __global__ void __launch_bounds__(kThreads) k_update32(int64_t nn, const float *
 }
 
 // Multigrid-preconditioned variant of the update: x += alpha p ; r -= alpha q (z = M r comes after)
-template <int B>
+template <int B, int PS = B>
 __global__ void k_update32a(int64_t nn, const float *__restrict__ p, const float *__restrict__ q,
                             float *__restrict__ x, float *__restrict__ r, const Ctl *ctl) {
     if (ctl->stop) return;
     const float alpha = (float)ctl->alpha;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn * B; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = fmaf(alpha, p[i], x[i]);
+        x[i] = fmaf(alpha, p[(i / B) * PS + i % B], x[i]);
         r[i] = fmaf(-alpha, q[i], r[i]);
     }
 }
@@ -340,11 +440,14 @@ __global__ void __launch_bounds__(kThreads) k_refine(int64_t nn, int64_t nb, con
         for (int c = 0; c < B; c++) acc[c] = 0.0;
         if (valid)
             for (int64_t k = rp[n] + sub; k < rp[n + 1]; k += kRowLanes) {
-                int64_t j = cj[k];
+                const int64_t j = __ldg(cj + k);
+                double xv[B];
+#pragma unroll
+                for (int d = 0; d < B; d++) xv[d] = __ldg(u64 + j * B + d);
 #pragma unroll
                 for (int c = 0; c < B; c++)
 #pragma unroll
-                    for (int d = 0; d < B; d++) acc[c] = fma(A[(int64_t)(c * B + d) * nb + k], u64[j * B + d], acc[c]);
+                    for (int d = 0; d < B; d++) acc[c] = fma(__ldg(A + (int64_t)(c * B + d) * nb + k), xv[d], acc[c]);
             }
 #pragma unroll
         for (int c = 0; c < B; c++)
@@ -428,14 +531,16 @@ __global__ void __launch_bounds__(kThreads) k_spmv64(int64_t nn, int64_t nb, con
         for (int c = 0; c < B; c++) acc[c] = 0.0;
         if (valid)
             for (int64_t k = rp[n] + sub; k < rp[n + 1]; k += kRowLanes) {
-                const int64_t j = __ldcs(cj + k);
+                // the read-only path for the matrix too: measured faster than evict-first loads here, where
+                // the FP64 pipe and not HBM is the bound
+                const int64_t j = __ldg(cj + k);
                 double xv[B];
 #pragma unroll
                 for (int d = 0; d < B; d++) xv[d] = __ldg(p + j * B + d);
 #pragma unroll
                 for (int c = 0; c < B; c++)
 #pragma unroll
-                    for (int d = 0; d < B; d++) acc[c] = fma(__ldcs(A + (int64_t)(c * B + d) * nb + k), xv[d], acc[c]);
+                    for (int d = 0; d < B; d++) acc[c] = fma(__ldg(A + (int64_t)(c * B + d) * nb + k), xv[d], acc[c]);
             }
 #pragma unroll
         for (int c = 0; c < B; c++)
@@ -576,7 +681,8 @@ static AmrSolveWork *work(amr_model *m) {
         amr_free(w->s32);
         amr_free(w->r64); amr_free(w->z64); amr_free(w->p64); amr_free(w->q64);
         amr_alloc(&w->s32, n);
-        amr_alloc(&w->x32, n); amr_alloc(&w->r32, n); amr_alloc(&w->z32, n); amr_alloc(&w->p32[0], n);
+        amr_alloc(&w->x32, n); amr_alloc(&w->r32, n); amr_alloc(&w->z32, n);
+        amr_alloc(&w->p32[0], (size_t)m->nnodes * (m->B == 3 ? 4 : 2));  // the padded direction
         amr_alloc(&w->p32[1], n); amr_alloc(&w->q32, n);
         int dev = 0, sms = 148;
         cudaGetDevice(&dev);
@@ -608,8 +714,17 @@ void amr_solver_free(amr_model *m) {
 
 template <int B>
 static void launch_spmv32(amr_model *m, AmrSolveWork *w, const float *p, float *q) {
-    k_spmv32<B><<<(unsigned)w->grid_spmv, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K32,
-                                                                     p, q, w->ctl, w->partials);
+    using PT = typename DirVec<B>::T;
+    k_spmv32v<B><<<(unsigned)w->grid_spmv, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol,
+                                                                      m->K32, reinterpret_cast<const PT *>(p), q,
+                                                                      w->ctl, w->partials);
+    AMR_COUNT(1);
+}
+template <int B>
+static void launch_pupdate32(amr_model *m, AmrSolveWork *w) {
+    using PT = typename DirVec<B>::T;
+    k_pupdate32v<B><<<(unsigned)w->grid, kThreads, 0, m->stream>>>(m->nnodes, w->z32, reinterpret_cast<PT *>(w->p32[0]),
+                                                                    w->ctl);
     AMR_COUNT(1);
 }
 
@@ -621,7 +736,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
     double tol2 = o.rtol * o.rtol;
     AMR_CUDA(cudaMemsetAsync(w->x32, 0, w->n * sizeof(float), s));
-    AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, w->n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, (size_t)nn * DirVec<B>::S * sizeof(float), s));
     AMR_CUDA(cudaMemsetAsync(w->q32, 0, w->n * sizeof(float), s));
     {
         Ctl c0{};
@@ -662,11 +777,10 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
         double stop_rr = stop_rr_rel * c.bnorm2;
         int nit = std::min(every, o.max_iters - c.iters);
         for (int it = 0; it < nit; it++) {
-            k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
-            AMR_COUNT(1);
+            launch_pupdate32<B>(m, w);
             launch_spmv32<B>(m, w, w->p32[0], w->q32);
-            k_update32<B><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[0], w->q32, w->x32, w->r32, w->z32, w->ctl,
-                                                 w->partials, stop_rr, delta2);
+            k_update32<B, DirVec<B>::S><<<g, kThreads, 0, s>>>(nn, m->Minv32, w->p32[0], w->q32, w->x32, w->r32,
+                                                                w->z32, w->ctl, w->partials, stop_rr, delta2);
             AMR_COUNT(1);
         }
         AMR_CUDA(cudaGetLastError());
@@ -695,7 +809,7 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
     AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
     double tol2 = o.rtol * o.rtol;
     AMR_CUDA(cudaMemsetAsync(w->x32, 0, w->n * sizeof(float), s));
-    AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, w->n * sizeof(float), s));
+    AMR_CUDA(cudaMemsetAsync(w->p32[0], 0, (size_t)nn * DirVec<B>::S * sizeof(float), s));
     AMR_CUDA(cudaMemsetAsync(w->q32, 0, w->n * sizeof(float), s));
     {
         Ctl c0{};
@@ -753,12 +867,12 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
         if (!gexec) {
             const long long before = amr_g_launches.load();
             AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-            k_pupdate32<B><<<g, kThreads, 0, s>>>(nn, w->z32, w->p32[0], w->ctl);
+            launch_pupdate32<B>(m, w);
             launch_spmv32<B>(m, w, w->p32[0], w->q32);
-            k_update32a<B><<<g, kThreads, 0, s>>>(nn, w->p32[0], w->q32, w->x32, w->r32, w->ctl);
+            k_update32a<B, DirVec<B>::S><<<g, kThreads, 0, s>>>(nn, w->p32[0], w->q32, w->x32, w->r32, w->ctl);
             amr_amg_vcycle(m, w->r32, w->z32);
             k_rz32<B><<<g, kThreads, 0, s>>>(nn, w->r32, w->z32, w->ctl, w->partials, stop_rr, delta2, 0);
-            AMR_COUNT(3);
+            AMR_COUNT(2);
             const cudaError_t ce = cudaStreamEndCapture(s, &graph);
             per_iter = amr_g_launches.load() - before;
             AMR_COUNT(-per_iter);
@@ -1022,7 +1136,7 @@ static double time_spmv32(amr_model *m, int reps) {
     AMR_CUDA(cudaMemcpyAsync(w->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        launch_spmv32<B>(m, w, w->z32, w->s32);
+        launch_spmv32<B>(m, w, w->p32[0], w->s32);
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
     AMR_CUDA(cudaEventSynchronize(m->ev1));

@@ -17,6 +17,7 @@
 module AmaruGPU
 
 using Amaru
+using DelimitedFiles
 using SparseArrays
 
 const LIB = get(ENV, "AMARU_GPU_LIB", joinpath(@__DIR__, "..", "amaru_gpu", "libamaru_gpu.so"))
@@ -367,7 +368,13 @@ struct DynParams
     alpha::Float64; beta::Float64; tspan::Float64
     maxits::Int32; autoinc::Int32; nincs::Int32; nouts::Int32
     linear::SolveOpts
+    sism::Int32; sism_dir::Int32
+    tss::Float64; tds::Float64
+    sism_acc::Ptr{Float64}; sism_n::Int64
 end
+
+# component of a seismic direction key (node.dofdict holds both the dof name and its natural name)
+const SISM_DIRS = Dict(:ux => 0, :fx => 0, :uy => 1, :fy => 1, :uz => 2, :fz => 2)
 
 """
     gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
@@ -382,8 +389,6 @@ not, as the increments run on the device.
 """
 function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
-    get(args, :sism, false) &&
-        error("AmaruGPU: seismic input (sism=true, src/mech/dyn-solver.jl:271-287) is not on the GPU path")
     model = ana.model
     activate!(model, stage)
     g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
@@ -395,12 +400,17 @@ function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...
     U0, F0 = Amaru.get_bc_vals(model, stage.bcs, 0.0)
     U1, F1 = Amaru.get_bc_vals(model, stage.bcs, 1.0)
     lin = SolveOpts(LINEAR_METHOD[], 1e-8, 20000, 32)
+    # seismic input: the record of sism_file (readdlm, times 9.81, row by row, as sismic_force reads it)
+    sism = get(args, :sism, false)
+    acc = sism ? vec(permutedims(9.81 .* readdlm(args.sism_file))) : Float64[]
     p = DynParams(args.tol, args.dTmin, args.dTmax, args.rspan, args.alpha, args.beta, stage.tspan,
-                  args.maxits, args.autoinc, stage.nincs, stage.nouts, lin)
+                  args.maxits, args.autoinc, stage.nincs, stage.nouts, lin,
+                  Int32(sism), Int32(get(SISM_DIRS, Symbol(get(args, :sism_dir, "fx")), 0)),
+                  get(args, :tss, 0.0), get(args, :tds, 0.0), pointer(acc), Int64(length(acc)))
     n = length(dofs)
     U, V, A, F = zeros(n), zeros(n), zeros(n), zeros(n)
     stats = StageStats()
-    rc = ccall((:amr_dyn_stage_run, LIB), Cint,
+    rc = GC.@preserve acc ccall((:amr_dyn_stage_run, LIB), Cint,
                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{DynParams},
                 Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{StageStats}),
                g.h, U0, U1 .- U0, F0, F1 .- F0, p, U, V, A, F, stats)

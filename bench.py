@@ -59,6 +59,11 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--slope", default="100x17x40", help="TET10 slope stage divisions (408 000 elements by default)")
     ap.add_argument("--no-slope", action="store_true", help="skip the TET10 slope stage measurement")
+    ap.add_argument("--amg-solve-only", action="store_true",
+                    help="profile driver: assemble the --mesh workload, run --steps multigrid solves, print their "
+                         "times and exit")
+    ap.add_argument("--batch-only", type=int, default=0,
+                    help="profile driver: run the batched-models leg alone with this many models and exit")
     return ap.parse_args()
 
 
@@ -213,14 +218,16 @@ def run_ours(a):
 
     # the dominant kernel of the step: with the multigrid, the cycle's fine residual r = b - K32 x
     # (four launches per PCG iteration); with block-Jacobi, the PCG's SpMV
-    spmv = {"kernel": "k_spmv32 (FP32 BSR SpMV q = K p with fused p.q)", "bytes_per_launch": spmv_b,
+    spmv = {"kernel": "k_spmv32v<3> (FP32 BSR SpMV q = K p with fused p.q, padded direction)",
+            "bytes_per_launch": spmv_b,
             "avg_launch_s": spmv_t, "achieved": spmv_b / spmv_t / 1e9,
-            "traffic": measured_traffic("spmv32_traffic.json")}
+            "traffic": measured_traffic("spmv32v_traffic.json")}
     if step_method == L.SOLVER_AMG:
         amg_t, amg_b = dev.time_kernel(L.KERNEL_AMG_RESIDUAL, 50)
-        dom = {"kernel": "k_bsr_res<3> (multigrid cycle's fine residual r = b - K32 x)", "bytes_per_launch": amg_b,
+        dom = {"kernel": "k_bsr_res16<3> (multigrid cycle's fine residual r = b - K x from the FP16 copy of the "
+                         "scaled matrix)", "bytes_per_launch": amg_b,
                "avg_launch_s": amg_t, "achieved": amg_b / amg_t / 1e9,
-               "traffic": measured_traffic("bsr_res_traffic.json")}
+               "traffic": measured_traffic("bsr_res16_traffic.json")}
     else:
         dom = spmv
     achieved = dom["achieved"]
@@ -809,8 +816,25 @@ def run_reference(a):
             "e2e": {"value": cb["value"], "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def amg_solve_only(a):
+    """Profile driver: the bench workload at --mesh, assembled once, then --steps multigrid solves of it."""
+    from amaru_gpu import _lib as L
+    model, Uex, Fex = workload_gpu(*dims(a.mesh))
+    model.dev.assemble_K()
+    out = []
+    for _ in range(max(a.steps, 1)):
+        _, _, st = model.dev.solve(Uex, Fex, L.default_solve_opts(method=L.SOLVER_AMG, rtol=1e-8))
+        out.append({"s": st.seconds, "iterations": st.iterations, "rel_residual": st.rel_residual})
+    return {"amg_solve_only": a.mesh, "solves": out}
+
+
 def main():
     a = parse()
+    if a.amg_solve_only or a.batch_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(amg_solve_only(a) if a.amg_solve_only else batch_leg(a.batch_only)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
         import torch.distributed as dist

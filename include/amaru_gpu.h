@@ -398,6 +398,17 @@ typedef struct {
     double tspan;            /* time span of the stage (Stage.tspan), > 0 */
     int32_t maxits, autoinc, nincs, nouts;
     amr_solve_opts linear;   /* the Krylov solve of each Newton iteration */
+    /* Seismic input (the sism keywords of dyn_solver_params, src/mech/dyn-solver.jl:182-186, applied as
+     * sismic_force, :106-157, at :271-287 and :348-352): while tss <= t <= tss + tds the force M (a(t) e_dir)
+     * is added to Fex(t), a(t) linear between the record's samples, spread uniformly over tds after an
+     * initial 0.  The reference binds tss, tds, sism_file and sism_dir only as keywords, not in its stage
+     * function, which stops there with an undefined-variable error; this is the evident intent. */
+    int32_t sism;            /* 1: seismic input on */
+    int32_t sism_dir;        /* 0, 1, 2: the x, y, z component (sism_dir "fx"/"ux", "fy", "fz") */
+    double tss, tds;         /* start time and duration of the record */
+    const double *sism_acc;  /* the record's accelerations in file order, row by row, in model units
+                                (the reference multiplies the file's values by 9.81) */
+    int64_t sism_n;          /* number of samples */
 } amr_dyn_params;
 
 /* dyn_stage_solver! (src/mech/dyn-solver.jl:203-534) of a first stage: M A0 = Fex(0), then

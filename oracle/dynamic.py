@@ -56,6 +56,26 @@ def mount_M(model, ndofs):
     return sp.coo_matrix((V, (R, Cc)), shape=(ndofs, ndofs)).tocsc()
 
 
+SISM_DIRS = {"ux": 0, "fx": 0, "uy": 1, "fy": 1, "uz": 2, "fz": 2}
+
+
+def sismic_acceleration(acc, tds, tf):
+    """The acceleration of sismic_force (dyn-solver.jl:110-146): samples acc (the record, row by row)
+    preceded by 0 at times i tds / n, linear between them, from the last interval holding tf (its loop
+    never breaks early); no interval holds tf beyond tds, where the reference fails."""
+    n = len(acc)
+    AS2 = np.concatenate([[0.0], acc])
+    vts = np.array([i * tds / n for i in range(n + 1)])
+    ini = -1
+    for i in range(n):
+        if vts[i] <= tf <= vts[i + 1]:
+            ini = i
+    if ini < 0:
+        raise ValueError("the seismic record does not cover t = %g" % tf)
+    m = (AS2[ini + 1] - AS2[ini]) / (vts[ini + 1] - vts[ini])
+    return AS2[ini] + m * (tf - vts[ini])
+
+
 class DynStage:
     def __init__(self, bcs, nincs=1, nouts=0, tspan=0.0):
         self.bcs, self.nincs, self.nouts, self.tspan = list(bcs), nincs, nouts, float(tspan)
@@ -74,12 +94,28 @@ class DynAnalysis:
         self.stages.append(DynStage(bcs, nincs, nouts, tspan))
 
     def solve(self, tol=0.01, dTmin=1e-7, dTmax=0.1, rspan=0.01, scheme="FE", maxits=5, autoinc=False,
-              alpha=0.0, beta=0.0):
+              alpha=0.0, beta=0.0, sism=False, tss=0.0, tds=0.0, sism_file="", sism_dir="fx"):
+        """sism: seismic input as dyn_stage_solver! intends it (dyn-solver.jl:106-157,271-287,348-352): the
+        record of sism_file (readdlm, times 9.81) spread uniformly over tds, the force M (a(t) e_dir)
+        added to Fex while tss <= t <= tss + tds."""
         if len(self.stages) != 1:
             raise ValueError("the dynamic solver runs one stage (velocities and accelerations exist in the first)")
-        return self._stage(self.stages[0], tol, dTmin, dTmax, maxits, autoinc, alpha, beta)
+        seis = None
+        if sism:
+            AS = 9.81 * np.loadtxt(sism_file, ndmin=2)
+            seis = (AS.reshape(-1), float(tss), float(tds), SISM_DIRS[sism_dir])
+        return self._stage(self.stages[0], tol, dTmin, dTmax, maxits, autoinc, alpha, beta, seis)
 
-    def _stage(self, stage, tol, dTmin, dTmax, maxits, autoinc, alpha, beta):
+    def _seismic(self, M, ndofs, seis, tf):
+        """sismic_force (dyn-solver.jl:106-157): a(tf) interpolated in the record, M (a e_dir)."""
+        acc, _, tds, comp = seis
+        a = sismic_acceleration(acc, tds, tf)
+        VAS = np.zeros(ndofs)
+        q = self.model.eq_id[:, comp]
+        VAS[q[q >= 0]] += a
+        return M @ VAS
+
+    def _stage(self, stage, tol, dTmin, dTmax, maxits, autoinc, alpha, beta, seis=None):
         model = self.model
         dofs, nu, setup = configure_dofs(model, stage.bcs)
         ndofs = len(dofs)
@@ -94,6 +130,8 @@ class DynAnalysis:
         A = np.zeros(ndofs)
         V = np.zeros(ndofs)
         Uex, Fex = get_bc_vals(model, setup, ndofs, 0.0)
+        if seis is not None and seis[1] <= 0.0:
+            Fex = Fex + self._seismic(M, ndofs, seis, 0.0)
         msg = solve_system(M, A, Fex, nu)
         self.A0, self.F0 = A.copy(), Fex.copy()
         StateBk = model.state.copy()
@@ -120,6 +158,8 @@ class DynAnalysis:
             dt = tspan * dT
             inc += 1
             Uex, Fex = get_bc_vals(model, setup, ndofs, t + dt)
+            if seis is not None and seis[1] <= t + dt <= seis[2] + seis[1]:
+                Fex = Fex + self._seismic(M, ndofs, seis, t + dt)
             Fex_Fin = Fex - Fina
             dUa[:] = 0.0
             dUi[:] = Uex

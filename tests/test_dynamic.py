@@ -10,6 +10,11 @@ closed recursion U_{n+1} = Keff^-1 (F + M(4/dt^2 U + 4/dt V + A) + C(2/dt U + V)
 (amr_assemble_M, amr_dyn_stage_run) is then compared with the oracle: M entry by entry, and U, V, A,
 F and the increment counts of elastic and elastoplastic stages, 2-D and 3-D, with time-dependent
 loads; at larger size through the energy property.
+
+Seismic input (sism, sismic_force, src/mech/dyn-solver.jl:106-157,271-287,348-352): the acceleration
+record is interpolated as the reference does (a leading 0, samples spread over tds, linear between
+them); the oracle's stage equals the closed recursion with the load M (a(t) e_dir) at every step while
+the record runs; the CUDA path equals the oracle, with the record starting at t = 0 and later.
 """
 import numpy as np
 import pytest
@@ -90,7 +95,75 @@ def test_oracle_matches_the_closed_newmark_recursion():
     assert np.abs(ana.A[:nu] - Ac).max() <= 1e-8 * np.abs(Ac).max()
 
 
+SEIS_BCS = lambda M: [("y==0", M.SurfaceBC(ux=0, uy=0, uz=0))]  # noqa: E731
+SEIS_RECORD = "0.10 0.35 -0.20\n-0.45 0.05 0.30\n"            # readdlm's 2 x 3 matrix, read row by row
+
+
+def test_oracle_seismic_acceleration_interpolates_the_record():
+    from oracle.dynamic import sismic_acceleration
+    acc = np.array([1.0, 3.0, 2.0])
+    for t, a in ((0.0, 0.0), (0.05, 0.5), (0.1, 1.0), (0.15, 2.0), (0.25, 2.5), (0.3, 2.0)):
+        assert abs(sismic_acceleration(acc, 0.3, t) - a) < 1e-12
+    with pytest.raises(ValueError):
+        sismic_acceleration(acc, 0.3, 0.31)
+
+
+def test_oracle_seismic_stage_matches_the_closed_recursion(tmp_path):
+    f = tmp_path / "record.dat"
+    f.write_text(SEIS_RECORD)
+    alpha, beta, tspan, nincs = 2.0, 1e-4, 0.06, 6
+    _, om = _beam(O, n=(1, 6, 1))
+    ana = O.DynAnalysis(om)
+    ana.addstage(SEIS_BCS(O), tspan=tspan, nincs=nincs)
+    assert ana.solve(alpha=alpha, beta=beta, sism=True, tss=0.0, tds=tspan, sism_file=str(f), sism_dir="fx")[0]
+    from oracle.dynamic import sismic_acceleration
+    nu, nd = ana.nu, ana.ndofs
+    Kf = O.mount_K(om, nd).toarray()
+    Mf = O.mount_M(om, nd).toarray()
+    e = np.zeros(nd)
+    e[om.eq_id[:, 0][om.eq_id[:, 0] >= 0]] = 1.0  # the x component of every node, prescribed ones too
+    acc = 9.81 * np.loadtxt(str(f), ndmin=2).reshape(-1)
+    K, Mm = Kf[:nu, :nu], Mf[:nu, :nu]
+    Cm = alpha * Mm + beta * K
+    dt = tspan / nincs
+    F = lambda t: (Mf @ (sismic_acceleration(acc, tspan, t) * e))[:nu]  # noqa: E731
+    U, V = np.zeros(nu), np.zeros(nu)
+    Ac = np.linalg.solve(Mm, F(0.0))
+    Keff = K + 4 / dt ** 2 * Mm + 2 / dt * Cm
+    for i in range(1, nincs + 1):
+        Un = np.linalg.solve(Keff, F(i * dt) + Mm @ (4 / dt ** 2 * U + 4 / dt * V + Ac) + Cm @ (2 / dt * U + V))
+        Vn = 2 / dt * (Un - U) - V
+        Ac = 4 / dt ** 2 * (Un - U) - 4 / dt * V - Ac
+        U, V = Un, Vn
+    assert np.abs(U).max() > 0
+    assert np.abs(ana.U[:nu] - U).max() <= 1e-9 * np.abs(U).max()
+    assert np.abs(ana.V[:nu] - V).max() <= 1e-9 * np.abs(V).max()
+    assert np.abs(ana.A[:nu] - Ac).max() <= 1e-8 * np.abs(Ac).max()
+
+
 # ---------------------------------------------------------------------------------------------- GPU
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tss,tds", [(0.0, 0.04), (0.02, 0.06)])
+def test_gpu_seismic_stage_matches_the_oracle(tmp_path, tss, tds):
+    """The record ends inside the stage (0, 0.04), or starts late (0.02); sismic_force reads the record at
+    the absolute time t + dt, so a late start needs a record that still covers it."""
+    f = tmp_path / "record.dat"
+    f.write_text(SEIS_RECORD)
+    mat = dict(E=30e6, nu=0.2, rho=24.0)
+    om, gm = _pair(A.HEX8, (2, 8, 2), ((0, 0, 0), (0.2, 2.0, 0.2)), O.LinearElastic(**mat), A.LinearElastic(**mat))
+    ao, ag = O.DynAnalysis(om), A.DynAnalysis(gm)
+    ao.addstage(SEIS_BCS(O), tspan=0.06, nincs=6)
+    ag.addstage(SEIS_BCS(A), tspan=0.06, nincs=6)
+    kw = dict(alpha=2.0, beta=1e-4, sism=True, tss=tss, tds=tds, sism_file=str(f), sism_dir="ux")
+    assert ao.solve(**kw)[0]
+    ok, msg = ag.solve(linear_rtol=1e-10, **kw)
+    assert ok, msg
+    assert ag.stats.increments == ao.increments == 6
+    for k in ("U", "V", "A", "F"):
+        assert _close(getattr(gm, k), getattr(om, k), 1e-7), k
+    assert np.abs(gm.U[:, 0]).max() > 0
 
 
 def _pair(shape, n, box, mat_o, mat_g, ctx="d3", **kw):
