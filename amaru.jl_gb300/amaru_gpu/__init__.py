@@ -9,6 +9,7 @@ update, the loads and the staged Newton loop with its linear solver run.
 """
 from ._lib import (AmrError, HEX8, HEX20, LIN2, LIN3, QUAD4, QUAD8, QUAD9, TET4, TET10, TRI3, TRI6,  # noqa: F401
                    SOLVER_AMG, SOLVER_AMG_FP64, SOLVER_FP64, SOLVER_MIXED, lib)
+from . import coupled  # noqa: F401
 from .args import ArgumentError  # noqa: F401
 from .expr import evaluate  # noqa: F401
 from .mesh import Block, Mesh  # noqa: F401

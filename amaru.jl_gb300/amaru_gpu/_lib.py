@@ -25,6 +25,7 @@ ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
 KERNEL_SPMV32, KERNEL_RESIDUAL64, KERNEL_AMG_RESIDUAL, KERNEL_DYN_RHS = 0, 1, 5, 6
 KERNEL_SPMV64, KERNEL_AMG_RESIDUAL64 = 7, 8
 PEAK_FP64_FMA, PEAK_FP32_FMA = 0, 1
+COUPLED_HYDRO, COUPLED_THERMO = 0, 1
 
 
 class AmrError(RuntimeError):
@@ -95,6 +96,11 @@ class DynParams(C.Structure):
                 ("autoinc", C.c_int32), ("nincs", C.c_int32), ("nouts", C.c_int32), ("linear", SolveOpts),
                 ("sism", C.c_int32), ("sism_dir", C.c_int32), ("tss", C.c_double), ("tds", C.c_double),
                 ("sism_acc", C.c_void_p), ("sism_n", C.c_int64)]
+
+
+class CoupledDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pad", C.c_int32), ("gammaw", C.c_double), ("T0", C.c_double),
+                ("params", C.c_void_p)]
 
 
 class ModalParams(C.Structure):
@@ -194,6 +200,8 @@ SIGNATURES = {
     "amr_time_kernel": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "amr_launch_count": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_alloc_count": (C.c_int, [C.POINTER(C.c_int64)]),
+    "amr_coupled_mount": (C.c_int, [P, C.POINTER(CoupledDesc), P, C.c_int64, C.c_double, P, C.POINTER(C.c_int64),
+                                    P, P, P, P]),
     "amr_get_stage_log": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
     "amr_set_increment_callback": (C.c_int, [P, INCREMENT_FN, C.c_void_p]),
     "amr_measure_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),

@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "amaru_gpu", "libamaru_gpu.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-SOURCES = ["shapes.cpp", "pattern.cu", "element.cu", "solver.cu", "capi.cu", "batch.cu", "server.cu", "amg.cu", "recovery.cu", "dyn.cu", "modal.cu", "vtu.cpp", "peak.cu"]
+SOURCES = ["shapes.cpp", "pattern.cu", "element.cu", "solver.cu", "capi.cu", "batch.cu", "server.cu", "amg.cu", "recovery.cu", "dyn.cu", "modal.cu", "vtu.cpp", "peak.cu", "coupled.cu"]
 
 
 def _headers():

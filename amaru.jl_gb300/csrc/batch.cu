@@ -503,6 +503,8 @@ __global__ void k_ctl_begin(int64_t np, PartCtl *c, uint8_t *active, int32_t *pe
 struct SlotArgs {
     int64_t n;
     int B;
+    double p1, q11;  // the predictor's factors of the scheme (mech-solver.jl:280-288)
+    int corrector;   // ME / BE / Ralston: dUi comes from the corrector solve
     const int32_t *node_part;
     const PartCtl *c;
     const uint8_t *active;
@@ -526,8 +528,30 @@ __global__ void k_slot_begin(SlotArgs a) {
     } else {
         a.dUi[t] = 0.0;
     }
-    a.dUitr[t] = a.fm[t] ? 0.0 : a.dUi[t];
+    a.dUitr[t] = a.fm[t] ? 0.0 : a.p1 * a.dUi[t];
+    a.Rtr[t] = a.q11 * a.R[t] + 0.0;
+}
+
+// corrector of ME / BE / Ralston (mech-solver.jl:341-348): parts whose predictor update failed leave the
+// iteration; the others solve the weighted tangent for dUi (prescribed values kept) with the residual R
+__global__ void k_ctl_corr(int64_t np, const int32_t *perr, uint8_t *active) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < np && active[i] && perr[i]) active[i] = 0;
+}
+
+__global__ void k_slot_corr(SlotArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    if (!a.active[a.node_part[t / a.B]]) return;
+    if (a.fm[t]) a.dUi[t] = 0.0;
     a.Rtr[t] = 1.0 * a.R[t] + 0.0;
+}
+
+__global__ void k_slot_mid2(SlotArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    if (!a.active[a.node_part[t / a.B]]) return;
+    a.dUt[t] = 1.0 * a.dUa[t] + 1.0 * a.dUi[t];
 }
 
 __global__ void k_ctl_mid(int64_t np, PartCtl *c, const PartStat *st, uint8_t *active) {
@@ -554,7 +578,7 @@ __global__ void k_slot_post(SlotArgs a) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.n) return;
     if (!a.active[a.node_part[t / a.B]]) return;
-    const double di = a.dUitr[t];
+    const double di = a.corrector ? a.dUi[t] : a.dUitr[t];
     a.dUi[t] = di;
     a.dUa[t] = 1.0 * a.dUa[t] + 1.0 * di;
     const double r = 1.0 * a.dFex[t] + -1.0 * a.dFin[t];
@@ -866,19 +890,33 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
                     double *F, amr_stage_stats *stats) {
     AmrBatch *b = m->batch;
     cudaStream_t s = m->stream;
-    if (prm.scheme != AMR_SCHEME_FE) throw AmrError(AMR_EUNSUPPORTED, "only the FE predictor scheme is on the GPU path");
+    // predictor-corrector schemes (mech-solver.jl:280-288), as the whole-model driver runs them
+    double p1 = 1.0, q11 = 1.0, a1 = 0.0, a2 = 0.0;
+    switch (prm.scheme) {
+    case AMR_SCHEME_FE: break;
+    case AMR_SCHEME_ME: a1 = 0.5; a2 = 0.5; break;
+    case AMR_SCHEME_BE: a1 = 0.0; a2 = 1.0; break;
+    case AMR_SCHEME_RALSTON: p1 = 2.0 / 3.0; q11 = 2.0 / 3.0; a1 = 0.25; a2 = 0.75; break;
+    default: throw AmrError(AMR_EINVAL, "unknown scheme");
+    }
+    const bool corrector = prm.scheme != AMR_SCHEME_FE;
     if (prm.maxits < 1 || prm.nincs < 1) throw AmrError(AMR_EINVAL, "bad stage parameters");
     if (prm.linear.method != AMR_SOLVER_MIXED)
         throw AmrError(AMR_EUNSUPPORTED, "batched stages use the mixed-precision solver");
     const int64_t n = m->nnodes * m->B, np = b->nparts;
     std::vector<double *> v(10, nullptr);
+    double *Ks = nullptr;  // the predictor's tangent, kept for the weighted corrector tangent
     struct Release {
         std::vector<double *> &v;
+        double *&Ks;
         ~Release() {
             for (auto &x : v) amr_free(x);
+            amr_free(Ks);
         }
-    } release{v};
+    } release{v, Ks};
     for (auto &x : v) amr_alloc(&x, n);
+    const size_t nK = (size_t)m->bstride * m->BB;
+    if (corrector) amr_alloc(&Ks, nK);
     double *R = v[0], *dUa = v[1], *dUi = v[2], *Rc = v[3], *dFin = v[4], *dFex = v[5], *dUitr = v[6], *Rtr = v[7],
            *reac = v[8], *dUt = v[9];
     b->have_stage = false;
@@ -929,8 +967,11 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
     sa.n = n; sa.B = m->B; sa.node_part = b->node_part; sa.c = b->ctl; sa.active = b->active; sa.fm = m->free_mask;
     sa.Uex = Uex; sa.Fex = Fex; sa.U = U; sa.F = F; sa.R = R; sa.Rc = Rc; sa.dUa = dUa; sa.dUi = dUi;
     sa.dUitr = dUitr; sa.Rtr = Rtr; sa.dUt = dUt; sa.dFin = dFin; sa.dFex = dFex;
+    sa.p1 = p1; sa.q11 = q11; sa.corrector = corrector ? 1 : 0;
     PcgArgs pa = pcg_args(m, dUitr, Rtr, reac, prm.linear, b->active);
     pa.step = b->step;
+    PcgArgs pc = pcg_args(m, dUi, Rtr, reac, prm.linear, b->active);  // the corrector's solve
+    pc.step = b->step;
     const unsigned gs = nblk(n, 256), gp = nblk(np, 128), gi = nblk(m->nip_total, 256);
     const unsigned gn = (unsigned)std::min<int64_t>(np, (int64_t)device_sms() * 4);
 
@@ -943,12 +984,28 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
         k_ctl_begin<<<gp, 128, 0, s>>>(np, b->ctl, b->active, b->perr, sp);
         k_slot_begin<<<gs, 256, 0, s>>>(sa);
         AMR_COUNT(2);
-        if (m->any_plastic) amr_stiffness(m);
+        // the tangent at the current states (a corrector left the weighted one in K: mount it again)
+        if (m->any_plastic || corrector) amr_stiffness(m);
         launch_pcg(m, pa, b->ctas_per_sm);
         k_ctl_mid<<<gp, 128, 0, s>>>(np, b->ctl, b->stat, b->active);
         k_slot_mid<<<gs, 256, 0, s>>>(sa);
         AMR_COUNT(2);
         amr_update_elements(m, dUt, dFin);
+        if (corrector) {
+            // K = a1 K + a2 K2, K2 the tangent at the predictor's trial states (mech-solver.jl:341-348)
+            k_ctl_corr<<<gp, 128, 0, s>>>(np, b->perr, b->active);
+            AMR_COUNT(1);
+            AMR_CUDA(cudaMemcpyAsync(Ks, m->K64, nK * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            if (m->any_plastic) amr_stiffness(m);  // a state-independent K2 equals K
+            amr_combine_K(m, a1, Ks, a2);
+            k_slot_corr<<<gs, 256, 0, s>>>(sa);
+            AMR_COUNT(1);
+            launch_pcg(m, pc, b->ctas_per_sm);
+            k_ctl_mid<<<gp, 128, 0, s>>>(np, b->ctl, b->stat, b->active);
+            k_slot_mid2<<<gs, 256, 0, s>>>(sa);
+            AMR_COUNT(2);
+            amr_update_elements(m, dUt, dFin);
+        }
         k_slot_post<<<gs, 256, 0, s>>>(sa);
         k_part_norms<<<gn, kPartThreads, 0, s>>>(np, m->B, b->part_ptr, b->active, R, dUi, dUa, b->ctl);
         k_ctl_end<<<gp, 128, 0, s>>>(np, b->ctl, b->perr, sp, b->step);
@@ -998,7 +1055,8 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
         int32_t reset[2] = {0, INT32_MAX};
         amr_h2d(m, m->d_status, reset, sizeof reset);
     }
-    if (m->any_plastic) m->K_valid = false;  // K holds the tangent of some part's last trial state
+    // K holds the tangent of some part's last trial state, or a corrector's weighted tangent
+    if (m->any_plastic || corrector) m->K_valid = false;
     b->stage_seconds = ms * 1e-3;
     b->stage_solve_seconds = solve_s;
     b->have_stage = true;

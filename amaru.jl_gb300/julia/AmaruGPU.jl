@@ -88,6 +88,9 @@ end
 material_code(m::LinearElastic) = (Int32(0), [m.E, m.ν, 0, 0, 0, 0, 0, 0])
 material_code(m::VonMises) = (Int32(1), [m.E, m.ν, m.σy, m.H, 0, 0, 0, 0])
 material_code(m::DruckerPrager) = (Int32(2), [m.E, m.ν, m.α, m.κ, m.H, 0, 0, 0])
+# the linear elastic skeletons of the coupled elements (their fluid / thermal parameters go to the mount)
+material_code(m::LinearElasticSeep) = (Int32(0), [m.E, m.ν, 0, 0, 0, 0, 0, 0])
+material_code(m::LinearElasticThermo) = (Int32(0), [m.E, m.ν, 0, 0, 0, 0, 0, 0])
 material_code(m) = error("AmaruGPU: material $(typeof(m)) is not on the GPU path")
 
 """
@@ -115,7 +118,8 @@ parameters and quadrature, pattern and contribution map (amr_model_create).
 """
 function GPUModel(model::FEModel)
     elems = model.elems
-    all(e -> e isa MechSolid, elems) || error("AmaruGPU: only MechSolid elements are on the GPU path")
+    all(e -> e isa MechSolid || e isa HMSolid || e isa TMSolid, elems) ||
+        error("AmaruGPU: only MechSolid, HMSolid and TMSolid elements are on the GPU path")
     nnodes = length(model.nodes)
     coords = zeros(3, nnodes)
     for (i, n) in enumerate(model.nodes)
@@ -578,7 +582,8 @@ has_gpu(model::FEModel) = haskey(GPU_MODELS, objectid(model))
 # ---------------------------------------------------------------------------
 function model_arrays(model::FEModel)
     elems = model.elems
-    all(e -> e isa MechSolid, elems) || error("AmaruGPU: only MechSolid elements are on the GPU path")
+    all(e -> e isa MechSolid || e isa HMSolid || e isa TMSolid, elems) ||
+        error("AmaruGPU: only MechSolid, HMSolid and TMSolid elements are on the GPU path")
     coords = zeros(3, length(model.nodes))
     for (i, n) in enumerate(model.nodes)
         coords[:, i] .= (n.coord.x, n.coord.y, n.coord.z)
@@ -918,9 +923,73 @@ function autotune!(g::GPUModel)
     return t[]
 end
 
+# ---------------------------------------------------------------------------
+# Coupled mounts: hm_mount_global_matrices (src/hydromech/hydromech-solver.jl:31-130) and
+# tm_mount_global_matrices (src/thermomech/thermomech-solver.jl:80-170) on the device.
+# ---------------------------------------------------------------------------
+struct CoupledDesc
+    kind::Int32; pad::Int32
+    gammaw::Float64; T0::Float64
+    params::Ptr{Float64}
+end
+
+function coupled_mount(model::FEModel, ndofs::Int, Δt::Float64, kind::Int32, key::Symbol)
+    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
+    nn = length(model.nodes)
+    eq4 = fill(Int64(-1), 4, nn)     # ux, uy, uz, the scalar; 0-based
+    phi = zeros(ndofs)               # dof.vals of the scalar DOFs, as the reference reads them
+    for (i, node) in enumerate(model.nodes)
+        for (c, k) in enumerate((:ux, :uy, :uz))
+            haskey(node.dofdict, k) && (eq4[c, i] = node.dofdict[k].eq_id - 1)
+        end
+        if haskey(node.dofdict, key)
+            dof = node.dofdict[key]
+            eq4[4, i] = dof.eq_id - 1
+            phi[dof.eq_id] = dof.vals[key]
+        end
+    end
+    prm = zeros(3, length(model.elems))
+    for (k, e) in enumerate(model.elems)
+        if kind == 0  # HMSolid: Biot's alpha, permeability, storativity (LinearElasticSeep)
+            prm[:, k] .= (e.props.α, e.mat.k, e.mat.S)
+        else          # TMSolid: thermal expansion, conductivity (LinearElasticThermo), rho cv
+            prm[:, k] .= (e.props.α, e.mat.k, e.props.ρ * e.props.cv)
+        end
+    end
+    nnz = Ref{Int64}(0)
+    local colptr, rowval, nzval, rhs
+    GC.@preserve prm eq4 phi begin
+        d = CoupledDesc(kind, 0, kind == 0 ? model.ctx.γw : 0.0, kind == 1 ? model.ctx.T0 : 0.0, pointer(prm))
+        checked(g, ccall((:amr_coupled_mount, LIB), Cint, (Ptr{Cvoid}, Ref{CoupledDesc}, Ptr{Int64}, Int64, Float64,
+                         Ptr{Float64}, Ref{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}),
+                         g.h, d, eq4, ndofs, Δt, phi, nnz, C_NULL, C_NULL, C_NULL, C_NULL))
+        colptr = zeros(Int64, ndofs + 1); rowval = zeros(Int64, nnz[]); nzval = zeros(nnz[]); rhs = zeros(ndofs)
+        checked(g, ccall((:amr_coupled_mount, LIB), Cint, (Ptr{Cvoid}, Ref{CoupledDesc}, Ptr{Int64}, Int64, Float64,
+                         Ptr{Float64}, Ref{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}),
+                         g.h, d, eq4, ndofs, Δt, phi, nnz, colptr, rowval, nzval, rhs))
+    end
+    return SparseMatrixCSC(ndofs, ndofs, colptr .+ 1, rowval .+ 1, nzval), rhs
+end
+
+"""
+    gpu_hm_mount_global_matrices(model, ndofs, Δt)
+
+hm_mount_global_matrices (src/hydromech/hydromech-solver.jl:31-130) on the device for HMSolid elements with
+LinearElasticSeep: (G, RHS) with every element entry and the reference's summation order.
+"""
+gpu_hm_mount_global_matrices(model::FEModel, ndofs::Int, Δt::Float64) = coupled_mount(model, ndofs, Δt, Int32(0), :uw)
+
+"""
+    gpu_tm_mount_global_matrices(model, ndofs, Δt)
+
+tm_mount_global_matrices (src/thermomech/thermomech-solver.jl:80-170) on the device for TMSolid elements with
+LinearElasticThermo: (G, RHS).
+"""
+gpu_tm_mount_global_matrices(model::FEModel, ndofs::Int, Δt::Float64) = coupled_mount(model, ndofs, Δt, Int32(1), :ut)
+
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
        nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!, save_gpu,
        sizes, get_state, set_state!, commit_state!, restore_state!, set_youngs!, estimate_bytes, stats, autotune!,
-       rayleigh_coefficients
+       rayleigh_coefficients, gpu_hm_mount_global_matrices, gpu_tm_mount_global_matrices
 
 end # module

@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--slope", default="100x17x40", help="TET10 slope stage divisions (408 000 elements by default)")
     ap.add_argument("--no-slope", action="store_true", help="skip the TET10 slope stage measurement")
+    ap.add_argument("--no-coupled", action="store_true", help="skip the hydromechanical mount measurement")
     ap.add_argument("--amg-solve-only", action="store_true",
                     help="profile driver: assemble the --mesh workload, run --steps multigrid solves, print their "
                          "times and exit")
@@ -349,7 +350,8 @@ def run_ours(a):
             ("modal", not a.no_modal, lambda: modal_leg(model, cpu_here)),
             ("batch", not a.no_batch, batch_leg),
             ("serving", not a.no_serve, lambda: serving_leg(a.serve_requests)),
-            ("slope", bool(a.slope) and not a.no_slope, lambda: slope_leg(a.slope))]
+            ("slope", bool(a.slope) and not a.no_slope, lambda: slope_leg(a.slope)),
+            ("coupled", not a.no_coupled, lambda: coupled_leg(cpu_here))]
     for name, on, fn in legs:
         if not on:
             continue
@@ -789,6 +791,54 @@ def slope_leg(spec):
             "krylov_iterations": st.krylov_iterations, "stage_s": st.seconds, "solve_s": st.solve_seconds,
             "dof_iterations_per_s": model.ndofs * st.iterations / st.seconds, "plastic_ips": plastic,
             "setup_s": setup_s}
+
+
+# ---------------------------------------------------------------------------
+# Hydromechanical mount (hm_mount_global_matrices): HEX20 block 3 x 1.2 x 1.2 meshed 30 x 12 x 12, linear
+# elastic skeleton (E 1e4, nu 0.25), Biot alpha 0.9, permeability 2.5e-3, storativity 1e-4, gammaw 10, dt 0.05;
+# base fixed, top drained.  value = DOFs per second of the whole call (device mount, CSC export to the host).
+# The CPU baseline runs the oracle's restatement on HEX20 3 x 2 x 2.
+# ---------------------------------------------------------------------------
+def _coupled_case(M, CPm, n):
+    box = [[0, 0, 0], [0.1 * n[0], 0.1 * n[1], 0.1 * n[2]]]
+    mesh = M.Mesh(M.Block(box, nx=n[0], ny=n[1], nz=n[2], cellshape=M.HEX20))
+    model = M.FEModel(mesh, [("all", M.LinearElastic(E=1e4, nu=0.25))])
+    z = np.asarray(mesh.coords)[:, 2]
+    pres = np.zeros((len(z), 4), dtype=bool)
+    pres[np.isclose(z, 0.0), :3] = True
+    pres[np.isclose(z, z.max()), 3] = True
+    eq4, nd, nu = CPm.coupled_dofs(model, pres)
+    prm = np.tile([0.9, 2.5e-3, 1e-4], (len(model.shape) if hasattr(model, "shape") else len(mesh.shape), 1))
+    return model, eq4, nd, prm
+
+
+def coupled_leg(with_cpu, n=(30, 12, 12), reps=3):
+    import amaru_gpu as A
+    from amaru_gpu import coupled as CP
+    model, eq4, nd, prm = _coupled_case(A, CP, n)
+    phi = np.zeros(nd)
+    G, _ = CP.mount_coupled(model, CP.HYDRO, prm, eq4, nd, 0.05, phi, gammaw=10.0)  # warm
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        G, R = CP.mount_coupled(model, CP.HYDRO, prm, eq4, nd, 0.05, phi, gammaw=10.0)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    out = {"workload": "hm_mount_global_matrices: HEX20 %dx%dx%d block, linear elastic skeleton, Biot 0.9, k 2.5e-3, "
+                       "S 1e-4, gammaw 10, dt 0.05, base fixed, top drained; the whole call (device mount and CSC "
+                       "export to host)" % n, "ndofs": nd, "nnz": int(G.nnz), "s": t, "value": nd / t,
+           "unit": "DOF/s"}
+    if with_cpu:
+        import oracle as O
+        from oracle import coupled as OC
+        m2, e2, n2, p2 = _coupled_case(O, OC, (3, 2, 2))
+        t0 = time.perf_counter()
+        OC.mount_coupled(m2, OC.HYDRO, p2, e2, n2, 0.05, np.zeros(n2), gammaw=10.0)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n2 / dt, "unit": "DOF/s", "cores": 1, "kind": "port",
+                               "sample": "oracle hm_mount_global_matrices (numpy) on HEX20 3x2x2, %d DOFs: %.2f s"
+                                         % (n2, dt)}
+    return out
 
 
 def cpu_sample(nx, ny, nz, nthreads):

@@ -488,6 +488,31 @@ int amr_recover_nodal_dev(amr_model *m, double *d_V);
 int amr_time_recovery(amr_model *m, int32_t reps, double *avg_seconds, double *flops_per_launch,
                       int64_t *svd_patches);
 
+/* ---- coupled mounts ----
+ * hm_mount_global_matrices (src/hydromech/hydromech-solver.jl:31-130) for HMSolid elements with a linear
+ * elastic skeleton and constant isotropic permeability (LinearElasticSeep), and tm_mount_global_matrices
+ * (src/thermomech/thermomech-solver.jl:80-170) for TMSolid elements with a linear elastic skeleton and
+ * constant conductivity: G = [K, C; s C', dt H + Cap] with every element entry pushed (no eps() drop) and
+ * duplicates summed in the reference's order, and RHS = -dt H phi (+ dt Q for the hydraulic mount).  The
+ * handle's elements give the geometry and E, nu (LinearElastic); the scalar field lives on the basic (corner)
+ * nodes. */
+enum { AMR_COUPLED_HYDRO = 0, AMR_COUPLED_THERMO = 1 };
+typedef struct {
+    int32_t kind;            /* AMR_COUPLED_HYDRO or AMR_COUPLED_THERMO */
+    int32_t pad;
+    double gammaw;           /* HYDRO: the analysis' water unit weight (HydromechAnalysis gammaw) */
+    double T0;               /* THERMO: the reference temperature T0 in degrees C; C' is scaled by T0 + 273.15 */
+    const double *params;    /* nelems x 3, caller's element order.  HYDRO: Biot's alpha, permeability k,
+                                storativity S.  THERMO: thermal expansion alpha, conductivity k, rho cv */
+} amr_coupled_desc;
+/* eq4: nnodes x 4 DOF numbers (ux, uy, uz, and the scalar uw / ut; -1 where a node has none), as
+ * configure_dofs! numbers them; phi: ndofs current DOF values (eq order), of which the scalar ones are read
+ * (dof.vals[:uw] / dof.vals[:ut]).  *nnz always; with colptr non-null also G in CSC (colptr ndofs+1, rowval /
+ * nzval nnz, rows sorted) and rhs (ndofs). */
+int amr_coupled_mount(amr_model *m, const amr_coupled_desc *d, const int64_t *eq4, int64_t ndofs, double dt,
+                      const double *phi, int64_t *nnz, int64_t *colptr, int64_t *rowval, double *nzval,
+                      double *rhs);
+
 /* Default parameter blocks (the reference's KwArgInfo defaults). */
 void amr_default_solve_opts(amr_solve_opts *o);
 void amr_default_stage_params(amr_stage_params *p);

@@ -8,6 +8,7 @@ Checked here:
 * a part's result is bitwise the same alone (a batch of one) and in the mix;
 * elastoplastic parts over several increments, with Newton iteration counts equal
   to the model run alone;
+* the ME / BE / Ralston schemes per part, against each model alone with the scheme;
 * the batched solve_system! per part;
 * a part that fails its stage leaves the others untouched;
 * the autotuner changes launch shapes only, not results.
@@ -102,6 +103,34 @@ def test_elastoplastic_parts_over_increments():
     one.addstage(_bcs(A, 1.0), nincs=5)
     assert one.solve(tol=1e-6)[0][0]
     assert np.array_equal(one.models[0].U, ba.models[2].U)
+
+
+@pytest.mark.parametrize("scheme", ["ME", "BE", "Ralston"])
+def test_predictor_corrector_schemes_per_part(scheme):
+    """The ME / BE / Ralston schemes (src/mech/mech-solver.jl:280-288,341-350) run per part in the batched
+    stage: each part takes the Newton iterations of the same model run alone with the scheme, and its U and F
+    agree with it; a part's result is bitwise the same alone and in the mix."""
+    inst = _instances(13, 4, 2, 6)
+    kw = dict(tol=1e-6, scheme=scheme, autoinc=True)
+    mats = [A.VonMises(E=E, nu=nu, fy=0.9, H=1e3) for _, E, nu in inst]
+    ba = A.BatchAnalysis([_gpu_model(n, mat, False) for (n, _, _), mat in zip(inst, mats)])
+    ba.addstage(_bcs(A, 1.0), nincs=4)
+    res = ba.solve(**kw)
+    assert any(ok for ok, _ in res)
+    for k, ((n, E, nu), m) in enumerate(zip(inst, ba.models)):
+        alone = _gpu_model(n, A.VonMises(E=E, nu=nu, fy=0.9, H=1e3), True)
+        ana = A.MechAnalysis(alone)
+        ana.addstage(_bcs(A, 1.0), nincs=4)
+        ok = ana.solve(**kw)[0]
+        assert ok == res[k][0]  # the same outcome as the model alone
+        assert ba.part_stats[0][k].increments == ana.stats[0].increments
+        assert ba.part_stats[0][k].iterations == ana.stats[0].iterations
+        if ok:
+            assert _close(m.U, alone.U) and _close(m.F, alone.F)
+    one = A.BatchAnalysis([_gpu_model(inst[1][0], A.VonMises(E=inst[1][1], nu=inst[1][2], fy=0.9, H=1e3), False)])
+    one.addstage(_bcs(A, 1.0), nincs=4)
+    assert one.solve(**kw)[0][0] == res[1][0]
+    assert np.array_equal(one.models[0].U, ba.models[1].U)
 
 
 def test_batched_solve_system_per_part():

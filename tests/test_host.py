@@ -80,7 +80,8 @@ def _layout(cls):
 
 @pytest.mark.parametrize("name", ["ModelDesc", "SolveOpts", "SolveStats", "StageParams", "StageStats", "DynParams",
                                   "VtuArray", "ModalParams", "ModalStats", "Request", "RequestResult",
-                                  "ServerConfig", "ServerInfo", "Tuning", "IncrementInfo"])
+                                  "ServerConfig", "ServerInfo", "Tuning", "IncrementInfo",
+                                  "CoupledDesc"])
 def test_julia_struct_layouts_match_the_c_abi(name):
     """Each struct the Julia binding passes by reference has the byte layout of the ctypes mirror of the
     same C struct (offsets and sizes field by field)."""
