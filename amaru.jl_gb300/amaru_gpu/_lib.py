@@ -162,6 +162,8 @@ class ServerInfo(C.Structure):
 FIELD_NAMES = ["σxx", "σyy", "σzz", "σyz", "σxz", "σxy", "σvm", "σ1", "σ2", "σ3", "εxx", "εyy", "εzz", "εyz", "εxz",
                "εxy", "ep", "epa", "j1", "srj2d"]
 NFIELD_CODES = len(FIELD_NAMES)
+# the keys the codes carry in an axisymmetric analysis (src/tools/tensors.jl:182-193)
+AXI_FIELD_NAMES = {0: "σrr", 2: "σtt", 5: "σry", 10: "εrr", 12: "εtt", 15: "εry"}
 
 # Every exported entry point of include/amaru_gpu.h with its ctypes signature.
 P = C.c_void_p
@@ -181,6 +183,7 @@ SIGNATURES = {
     "amr_state_restore": (C.c_int, [P]),
     "amr_get_state": (C.c_int, [P, P]),
     "amr_set_state": (C.c_int, [P, P]),
+    "amr_get_elem_nips": (C.c_int, [P, P]),
     "amr_get_sizes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64)]),
     "amr_assemble_loads": (C.c_int, [P, C.POINTER(Load), C.c_int32, C.c_double, P]),
@@ -213,6 +216,7 @@ SIGNATURES = {
     "amr_modal_run": (C.c_int, [P, C.POINTER(ModalParams), P, P, C.POINTER(ModalStats)]),
     "amr_default_modal_params": (None, [C.POINTER(ModalParams)]),
     "amr_write_vtu": (C.c_int, [P, C.c_char_p, P, C.c_int32, P, C.c_int32, C.c_int32]),
+    "amr_write_vtu_compressed": (C.c_int, [P, C.c_char_p, P, C.c_int32, P, C.c_int32, C.c_int32]),
     "amr_recovery_fields": (C.c_int, [P, P, C.c_int32, C.POINTER(C.c_int32)]),
     "amr_recover_nodal": (C.c_int, [P, P]),
     "amr_recover_nodal_dev": (C.c_int, [P, P]),
@@ -334,6 +338,7 @@ class DeviceModel:
         self.h = h
         self._keep = None
         self.ndim = ndim
+        self.stressmodel = stressmodel
         self.ndofs = 0
         self.nu = 0
 
@@ -396,6 +401,12 @@ class DeviceModel:
         s = np.zeros((n, 16))
         check(self.h, lib().amr_get_state(self.h, ptr(s)))
         return s
+
+    def elem_nips(self):
+        """The IP count of each element (its rows of state()), element order."""
+        out = np.zeros(self.sizes()["nelems"], dtype=np.int32)
+        check(self.h, lib().amr_get_elem_nips(self.h, ptr(out)))
+        return out
 
     def set_state(self, state):
         s = np.ascontiguousarray(state, dtype=np.float64)
@@ -518,18 +529,20 @@ class DeviceModel:
         check(self.h, lib().amr_modal_run(self.h, C.byref(p), ptr(w), ptr(V), C.byref(st)))
         return w, V.T.copy(), st
 
-    def write_vtu(self, path, point_items, cell_items, nthreads=0):
+    def write_vtu(self, path, point_items, cell_items, nthreads=0, compress=False):
         pa, k1 = vtu_arrays(point_items)
         ca, k2 = vtu_arrays(cell_items)
-        check(self.h, lib().amr_write_vtu(self.h, str(path).encode("utf-8"), C.cast(pa, C.c_void_p), len(point_items),
-                                          C.cast(ca, C.c_void_p), len(cell_items), nthreads))
+        fn = lib().amr_write_vtu_compressed if compress else lib().amr_write_vtu
+        check(self.h, fn(self.h, str(path).encode("utf-8"), C.cast(pa, C.c_void_p), len(point_items),
+                         C.cast(ca, C.c_void_p), len(cell_items), nthreads))
 
     def recovery_fields(self):
         """Field names of the nodal recovery, in the reference's column order."""
         codes = np.zeros(NFIELD_CODES, dtype=np.int32)
         n = C.c_int32()
         check(self.h, lib().amr_recovery_fields(self.h, ptr(codes), NFIELD_CODES, C.byref(n)))
-        return [FIELD_NAMES[c] for c in codes[:n.value]]
+        names = AXI_FIELD_NAMES if self.stressmodel == AXISYMMETRIC else {}
+        return [names.get(int(c), FIELD_NAMES[c]) for c in codes[:n.value]]
 
     def recover_nodal(self):
         """nodal_patch_recovery: (V (nnodes x nfields), field names) from the current IP states."""

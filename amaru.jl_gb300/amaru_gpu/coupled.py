@@ -22,13 +22,13 @@ _BASIC_NPOINTS = {L.HEX8: 8, L.HEX20: 8, L.TET4: 4, L.TET10: 4, L.QUAD4: 4, L.QU
 
 def coupled_dofs(model, prescribed):
     """configure_dofs! (src/bc.jl:198-233) for coupled elements (elem_config_dofs, hydromech-solid.jl:51-61):
-    per used node ux, uy[, uz], and on basic nodes the scalar, numbered node by node, unknowns first and
-    prescribed last.  prescribed: boolean (nnodes, 4), column 3 the scalar.  Returns (eq4, ndofs, nu)."""
+    per node of an active element ux, uy[, uz], and on basic nodes the scalar, numbered node by node, unknowns
+    first and prescribed last.  prescribed: boolean (nnodes, 4), column 3 the scalar.  Returns (eq4, ndofs, nu)."""
     mesh = model.mesh
     nn, ndim = model.nnodes, model.ndim
     used = np.zeros(nn, dtype=bool)
     basic = np.zeros(nn, dtype=bool)
-    for e in range(len(mesh.shape)):
+    for e in np.nonzero(model.active)[0]:
         nodes = mesh.conn[mesh.conn_ptr[e]:mesh.conn_ptr[e + 1]]
         used[nodes] = True
         basic[nodes[:_BASIC_NPOINTS[int(mesh.shape[e])]]] = True
@@ -47,10 +47,16 @@ def coupled_dofs(model, prescribed):
 def mount_coupled(model, kind, params, eq4, ndofs, dt, phi, gammaw=1.0, T0=0.0):
     """(G, RHS): G as a scipy CSC matrix in the reference's layout (every element entry, duplicates summed in
     the reference's order), RHS = -dt H phi (+ dt Q for HYDRO).  params: nelems x 3 (HYDRO: Biot alpha, k, S;
-    THERMO: expansion alpha, k, rho cv); phi: the current DOF values (eq order)."""
+    THERMO: expansion alpha, k, rho cv); phi: the current DOF values (eq order).  The mounts loop over the
+    active elements (hydromech-solver.jl:211-213); the device model holds them after configure_dofs!."""
     import scipy.sparse as sp
-    prm = np.ascontiguousarray(params, dtype=np.float64).reshape(-1, 3)
-    eq = np.ascontiguousarray(eq4, dtype=np.int64)
+    model._sync_active()
+    prm = np.asarray(params, dtype=np.float64).reshape(-1, 3)
+    eq = np.asarray(eq4, dtype=np.int64)
+    if model._dev_elems is not None:
+        prm, eq = prm[model._dev_elems], eq[model._dev_nodes]
+    prm = np.ascontiguousarray(prm)
+    eq = np.ascontiguousarray(eq)
     ph = np.ascontiguousarray(phi, dtype=np.float64)
     d = L.CoupledDesc()
     d.kind, d.gammaw, d.T0, d.params = int(kind), float(gammaw), float(T0), prm.ctypes.data

@@ -151,6 +151,7 @@ class FEModel:
         if E is not None:
             self.mat_params[:, 0] = E
         self.nips = np.full(ne, nips, dtype=np.int32)
+        self.active = np.ones(ne, dtype=bool)  # elem.active (src/fe-model.jl:156)
         self.dev = None
         if device:
             self.dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, mesh.coords, mesh.shape, self.nips,
@@ -164,8 +165,14 @@ class FEModel:
         self.F = np.zeros((self.nnodes, self.ndim))  # dof.vals of the natural keys
         self.eq_id = -np.ones((self.nnodes, 3), dtype=np.int64)
         self.ndofs = self.nu = 0
-        self.active_nodes = np.nonzero(np.bincount(mesh.conn, minlength=self.nnodes))[0]
+        self.used_nodes = np.nonzero(np.bincount(mesh.conn, minlength=self.nnodes))[0]  # the nodes with dofs
+        self.active_nodes = self.used_nodes
         self._dof_names = ["ux", "uy", "uz"][: self.ndim]
+        # the device model holds the active elements (_dev_elems, None: all) and their nodes (_dev_nodes)
+        self._dev_elems = self._dev_nodes = None
+        self._g2l = self._e2l = None
+        self._state_rest = None  # IP states of every element while the device holds a subset
+        self._ip_ptr = None
 
     @classmethod
     def join(cls, models):
@@ -173,6 +180,8 @@ class FEModel:
         the batched solver and stage driver then run every part as if it were alone."""
         models = list(models)
         m0 = models[0]
+        if any(not m.active.all() for m in models):
+            raise ValueError("joined models must have every element active")
         for m in models:
             if (m.ndim, m.stressmodel, m.thickness) != (m0.ndim, m0.stressmodel, m0.thickness):
                 raise ValueError("joined models must share ndim, stress model and thickness")
@@ -183,6 +192,7 @@ class FEModel:
         out.mat_params = np.concatenate([m.mat_params for m in models])
         out.nips = np.concatenate([m.nips for m in models])
         out.rho = np.concatenate([m.rho for m in models])
+        out.active = np.ones(len(out.mat_type), dtype=bool)
         out.dev = L.DeviceModel(out.ndim, out.stressmodel, out.thickness, mesh.coords, mesh.shape, out.nips,
                                 mesh.conn_ptr, mesh.conn, out.mat_type, out.mat_params)
         out._host_fields()
@@ -194,8 +204,80 @@ class FEModel:
         """changequadrature!(elems, n) (src/element.jl:185-188): rebuilds the device model."""
         self.nips[:] = n
         self.dev.close()
-        self.dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, self.mesh.coords, self.mesh.shape,
-                                 self.nips, self.mesh.conn_ptr, self.mesh.conn, self.mat_type, self.mat_params)
+        self.dev = self._device_over(None)  # fresh IP states; the next configure_dofs! takes the active set
+        self._dev_elems = self._state_rest = self._ip_ptr = None
+        self.active_nodes = self.used_nodes
+
+    # ---- element activation: elem.active and a stage's toactivate (src/mech/mech-solver.jl:216-220)
+    def set_active(self, sel, active=True):
+        """elem.active = active for the selected elements: ids, a boolean mask, a tag or a filter expression."""
+        self.active[self._elem_sel(sel)] = bool(active)
+
+    def _elem_sel(self, sel):
+        if isinstance(sel, str):
+            if sel == "all":
+                return np.arange(len(self.active))
+            if not any(ch in sel for ch in "=<>"):
+                return np.nonzero(self.mesh.tags == sel)[0]
+            return self.mesh.select_cells(self.mesh.elem_nodes(), sel)
+        a = np.asarray(sel)
+        return np.nonzero(a)[0] if a.dtype == bool else a.astype(np.int64).reshape(-1)
+
+    def _device_over(self, elems):
+        """A device model over the elements elems (None: all) and the nodes they use, renumbered in id order."""
+        mesh = self.mesh
+        if elems is None:
+            self._dev_nodes = self._g2l = self._e2l = None
+            return L.DeviceModel(self.ndim, self.stressmodel, self.thickness, mesh.coords, mesh.shape, self.nips,
+                                 mesh.conn_ptr, mesh.conn, self.mat_type, self.mat_params)
+        cp = mesh.conn_ptr
+        cnt = cp[elems + 1] - cp[elems]
+        conn = np.concatenate([mesh.conn[cp[e]:cp[e + 1]] for e in elems]) if len(elems) else np.zeros(0, np.int64)
+        nodes = np.unique(conn)
+        g2l = np.full(self.nnodes, -1, dtype=np.int64)
+        g2l[nodes] = np.arange(len(nodes))
+        e2l = np.full(len(self.active), -1, dtype=np.int64)
+        e2l[elems] = np.arange(len(elems))
+        ptr = np.zeros(len(elems) + 1, dtype=np.int64)
+        ptr[1:] = np.cumsum(cnt)
+        self._dev_nodes, self._g2l, self._e2l = nodes, g2l, e2l
+        return L.DeviceModel(self.ndim, self.stressmodel, self.thickness, mesh.coords[nodes], mesh.shape[elems],
+                             self.nips[elems], ptr, g2l[conn], self.mat_type[elems], self.mat_params[elems])
+
+    def _ip_rows(self, elems):
+        """The rows of the given elements in the all-element state layout."""
+        if self._ip_ptr is None:
+            nips = self.dev.elem_nips()
+            if self._dev_elems is not None:
+                raise RuntimeError("IP layout unknown")
+            self._ip_ptr = np.concatenate([[0], np.cumsum(nips)]).astype(np.int64)
+        p = self._ip_ptr
+        return np.concatenate([np.arange(p[e], p[e + 1]) for e in elems]) if len(elems) else np.zeros(0, np.int64)
+
+    def _sync_active(self):
+        """Rebuilds the device model over the active elements when the set changed since the last stage; the IP
+        states move with their elements (inactive ones keep theirs on the host)."""
+        if self.dev is None:
+            return
+        want = None if self.active.all() else np.nonzero(self.active)[0].astype(np.int64)
+        have = self._dev_elems
+        if (want is None and have is None) or (want is not None and have is not None and np.array_equal(want, have)):
+            return
+        if getattr(self, "node_offsets", None) is not None:
+            raise ValueError("joined models must have every element active")
+        if self._ip_ptr is None and have is None:
+            self._ip_rows(np.zeros(0, np.int64))
+        full = self.state()
+        self.dev.close()
+        self.dev = self._device_over(want)
+        self._dev_elems = want
+        self._state_rest = None if want is None else full
+        self.dev.set_state(full if want is None else full[self._ip_rows(want)])
+        self.active_nodes = self.used_nodes if want is None else self._dev_nodes
+
+    def dev_rho(self):
+        """The densities of the elements on the device."""
+        return self.rho if self._dev_elems is None else self.rho[self._dev_elems]
 
     # ---- configure_dofs! (src/bc.jl:198-233)
     def _select(self, bc, filt):
@@ -220,6 +302,7 @@ class FEModel:
             sel = np.nonzero(mesh.tags == filt)[0]
         else:
             sel = mesh.select_cells(enodes, filt)
+        sel = sel[self.active[sel]]  # model.elems.active[bc.filter] (src/bc.jl:159)
         return sel, enodes[sel]
 
     def _prescribed(self, bcs):
@@ -236,11 +319,14 @@ class FEModel:
         return presc, setup
 
     def configure_dofs(self, bcs):
+        """configure_dofs! (src/bc.jl:198-233) over the nodes of the active elements."""
+        self._sync_active()
         presc, setup = self._prescribed(bcs)
         self.eq_id, self.ndofs, self.nu, self.dof_node, self.dof_comp = number_dofs(self.active_nodes, presc,
                                                                                    self.nnodes)
         if self.dev is not None:
-            self.dev.set_dofs(self.eq_id, self.ndofs, self.nu)
+            self.dev.set_dofs(self.eq_id if self._dev_nodes is None else self.eq_id[self._dev_nodes], self.ndofs,
+                              self.nu)
         return setup
 
     # ---- get_bc_vals (src/bc.jl:237-249)
@@ -258,6 +344,10 @@ class FEModel:
         loads = []
         c = self.mesh.coords
         for bc, sel, objs, nodes in setup:
+            if len(nodes) and (self.eq_id[nodes, 0] < 0).any():
+                # such a node keeps eq_id 0 (Dof(), src/dof.jl:15-17): the reference's U[dof.eq_id] fails there
+                bad = int(nodes[self.eq_id[nodes, 0] < 0][0])
+                raise ValueError("boundary condition on node %d, which belongs to no active element" % (bad + 1))
             for key, val in bc.conds.items():
                 if key in self._dof_names:
                     k = self._dof_names.index(key)
@@ -278,12 +368,15 @@ class FEModel:
                     cf = affine_coefficients(val, self.ndim)
                     for fs in np.unique(shapes):
                         rows = table[shapes == fs][:, :NPOINTS[int(fs)]]
+                        if self._g2l is not None:
+                            rows = self._g2l[rows]
                         loads.append((L.LOAD_FACET, _DIR[key[1:]], 1 if key[0] == "q" else 0, int(fs), rows, cf))
                 else:
                     if key not in ("wx", "wy", "wz"):
                         raise ValueError("body condition %s is not applicable" % key)
                     cf = affine_coefficients(val, self.ndim)
-                    loads.append((L.LOAD_BODY, _DIR[key[1]], 0, 0, np.asarray(sel, dtype=np.int64), cf))
+                    items = np.asarray(sel, dtype=np.int64)
+                    loads.append((L.LOAD_BODY, _DIR[key[1]], 0, 0, items if self._e2l is None else self._e2l[items], cf))
         return U, F, loads
 
     # ---- the solver-level plugin functions the library replaces
@@ -312,15 +405,41 @@ class FEModel:
         return st
 
     def state(self):
-        return self.dev.state()
+        """IP states of every element (nip_total x 16, element order); inactive elements keep theirs."""
+        if self._dev_elems is None:
+            return self.dev.state()
+        full = self._state_rest.copy()
+        full[self._ip_rows(self._dev_elems)] = self.dev.state()
+        return full
 
     def set_state(self, state):
-        self.dev.set_state(state)
+        if self._dev_elems is None:
+            self.dev.set_state(state)
+            return
+        state = np.asarray(state, dtype=np.float64)
+        if state.shape != self._state_rest.shape:
+            raise ValueError("state must be nip_total x 16")
+        self._state_rest = state.copy()
+        self.dev.set_state(state[self._ip_rows(self._dev_elems)])
+
+    def _with_all_elements(self, fn):
+        """fn(device model over every element, with the current IP states): output covers every element, as
+        update_output_data! does (src/fe-model.jl:341-427)."""
+        if self._dev_elems is None:
+            return fn(self.dev)
+        full = self.state()
+        dev = L.DeviceModel(self.ndim, self.stressmodel, self.thickness, self.mesh.coords, self.mesh.shape, self.nips,
+                            self.mesh.conn_ptr, self.mesh.conn, self.mat_type, self.mat_params)
+        try:
+            dev.set_state(full)
+            return fn(dev)
+        finally:
+            dev.close()
 
     # ---- output data
     def nodal_patch_recovery(self):
         """nodal_patch_recovery(model) (src/fe-model.jl:504-702) on the device: (V (nnodes x nfields), names)."""
-        return self.dev.recover_nodal()
+        return self._with_all_elements(lambda d: d.recover_nodal())
 
     def update_output_data(self):
         """node_data / elem_data of update_output_data! (src/fe-model.jl:341-427): ids, cell types, the dof values
@@ -329,7 +448,7 @@ class FEModel:
         node = {"node-id": np.arange(1, nn + 1)}
         nat = ["fx", "fy", "fz"]
         has = np.zeros(nn, dtype=bool)
-        has[self.active_nodes] = True
+        has[self.used_nodes] = True
         for i in range(self.ndim):
             node[self._dof_names[i]] = np.where(has, self.U[:, i], 0.0)
             node[nat[i]] = np.where(has, self.F[:, i], 0.0)
@@ -343,16 +462,59 @@ class FEModel:
         self.node_data, self.elem_data = node, elem
         return node, elem
 
-    def save(self, path, nthreads=0):
-        """save(model, "file.vtu") (src/mesh/io.jl:167-274, 323-342): update_output_data! and the ascii VTU file
-        written by the library, byte for byte as the reference writes it."""
+    def save(self, path, nthreads=0, compress=False):
+        """save(model, "file.vtu"; compress) (src/mesh/io.jl:167-274, 323-342): update_output_data! and the VTU
+        file written by the library, byte for byte as the reference writes it: ascii, or the arrays appended as
+        zlib blocks with compress=True.  Tagged elements add the tag columns save_vtu adds."""
         node, elem = self.update_output_data()
-        self.dev.write_vtu(path, list(node.items()), list(elem.items()), nthreads)
+        items = list(elem.items()) + vtu_tag_columns(self.mesh.tags)
+        self._with_all_elements(lambda d: d.write_vtu(path, list(node.items()), items, nthreads, compress))
+
+
+def vtu_tag_columns(tags):
+    """The tag fields save_vtu adds to elem_data (src/mesh/io.jl:168-192) when the elements carry tags: tag-s1
+    and tag-s2, the tag's UTF-8 bytes cut at 8 (safe_string_cut, src/tools/encode.jl:25-36) and packed
+    little-endian (encode_string_to_uint64, :3-11), and tag, the tag's index.  The reference numbers the
+    tags in the iteration order of a Julia Set, which follows Julia's string hash; here they are numbered
+    in order of first appearance, so the tag column is a permutation of the reference's while tag-s1 and
+    tag-s2 are the same."""
+    tags = ["" if t is None else str(t) for t in tags]
+    uniq = list(dict.fromkeys(tags))
+    if len(uniq) == 0 or (len(uniq) == 1 and uniq[0] == ""):
+        return []
+    idx = {t: i for i, t in enumerate(uniq)}
+
+    def cut(t):
+        # safe_string_cut(t, 8): whole when shorter than 8 bytes; else cut after byte 8, which the
+        # reference manages only when byte 8 is a one-byte character (else its s[1:8] / s[p+1:end]
+        # raise): the same cases are refused here
+        b = t.encode("utf-8")
+        if len(b) > 16:
+            raise ValueError("Mesh: tag '%s' too long. Max length is 16 UTF units." % t)
+        if 8 > len(b):
+            return b, b""
+        if b[7] >= 0x80:
+            raise ValueError("Mesh: tag '%s' cannot be cut after its 8th byte" % t)
+        return b[:8], b[8:]
+
+    def pack(b):
+        return sum(int(c) << (8 * i) for i, c in enumerate(b))
+
+    parts = {t: cut(t) for t in uniq}
+    s1 = np.array([pack(parts[t][0]) for t in tags], dtype=np.uint64)
+    s2 = np.array([pack(parts[t][1]) for t in tags], dtype=np.uint64)
+    return [("tag-s1", s1), ("tag-s2", s2), ("tag", np.array([idx[t] for t in tags], dtype=np.int64))]
 
 
 class Stage:
-    def __init__(self, bcs, nincs=1, nouts=0):
+    def __init__(self, bcs, nincs=1, nouts=0, toactivate=()):
         self.bcs, self.nincs, self.nouts, self.status = list(bcs), nincs, nouts, "pending"
+        self.toactivate = toactivate  # element ids, a mask, a tag or a filter (src/stage.jl:8,16)
+
+    def activate(self, model):
+        """elem.active = true for the stage's toactivate (src/mech/mech-solver.jl:216-219)."""
+        if self.toactivate is not None and not (isinstance(self.toactivate, (list, tuple)) and not self.toactivate):
+            model.set_active(self.toactivate, True)
 
 
 class MechAnalysis:
@@ -364,9 +526,9 @@ class MechAnalysis:
         self.stats = []
         self.log = []  # (stage, inc, it, residue) per Newton iteration, as the reference's log lines
 
-    def addstage(self, bcs, nincs=1, nouts=0):
-        """addstage!(ana, bcs; nincs, nouts): src/analysis.jl:27-32"""
-        self.stages.append(Stage(bcs, nincs, nouts))
+    def addstage(self, bcs, nincs=1, nouts=0, toactivate=()):
+        """addstage!(ana, bcs; nincs, nouts, toactivate): src/analysis.jl:27-32"""
+        self.stages.append(Stage(bcs, nincs, nouts, toactivate))
 
     def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
               autoinc=False, quiet=True, linear_rtol=1e-8, solver="mixed", refine_every=32, max_iters=20000,
@@ -382,6 +544,7 @@ class MechAnalysis:
         for st in self.stages:
             if st.status == "done":
                 continue
+            st.activate(model)
             setup = model.configure_dofs(st.bcs)
             Uex, Fex = model.get_bc_vals(setup)
             p = L.default_stage_params(tol=tol, rtol=rtol, rspan=rspan, dT0=dT0, dTmin=dTmin, dTmax=dTmax,
@@ -426,8 +589,8 @@ class DynAnalysis:
         self.stages = []
         self.stats = None
 
-    def addstage(self, bcs, nincs=1, nouts=0, tspan=0.0):
-        st = Stage(bcs, nincs, nouts)
+    def addstage(self, bcs, nincs=1, nouts=0, tspan=0.0, toactivate=()):
+        st = Stage(bcs, nincs, nouts, toactivate)
         st.tspan = float(tspan)
         self.stages.append(st)
 
@@ -444,6 +607,7 @@ class DynAnalysis:
             raise ValueError("a dynamic analysis has one stage (the reference defines V and A in the first only)")
         stage = self.stages[0]
         model = self.model
+        stage.activate(model)
         setup = model.configure_dofs(stage.bcs)
         U0, F0 = model.get_bc_vals(setup, 0.0)
         U1, F1 = model.get_bc_vals(setup, 1.0)
@@ -452,7 +616,7 @@ class DynAnalysis:
         for a, b, c in ((U0, dU, Uh), (F0, dF, Fh)):
             if np.abs(a + 0.5 * b - c).max(initial=0.0) > 1e-12 * max(np.abs(c).max(initial=0.0), 1.0):
                 raise NotImplementedError("boundary values must be affine in time on the GPU path")
-        model.dev.set_density(model.rho)
+        model.dev.set_density(model.dev_rho())
         method = {"mixed": L.SOLVER_MIXED, "fp64": L.SOLVER_FP64, "amg": L.SOLVER_AMG, "amg_fp64": L.SOLVER_AMG_FP64}[solver]
         p = L.default_dyn_params(tol=tol, dTmin=dTmin, dTmax=dTmax, rspan=rspan, alpha=alpha, beta=beta,
                                  tspan=stage.tspan, maxits=maxits, autoinc=int(autoinc), nincs=stage.nincs,
@@ -490,15 +654,16 @@ class ModalAnalysis:
         self.stats = None
         self.alpha = self.beta = None
 
-    def addstage(self, bcs, nincs=1, nouts=0):
-        self.stages.append(Stage(bcs, nincs, nouts))
+    def addstage(self, bcs, nincs=1, nouts=0, toactivate=()):
+        self.stages.append(Stage(bcs, nincs, nouts, toactivate))
 
     def solve(self, nmodes=5, tol=1e-7, max_iters=1000, quiet=True, rayleigh=None):
         """rayleigh=(xi1, xi2, i1, i2) also sets self.alpha, self.beta (see set_rayleigh)."""
         model = self.model
         for stage in self.stages:
+            stage.activate(model)
             model.configure_dofs(stage.bcs)
-            model.dev.set_density(model.rho)
+            model.dev.set_density(model.dev_rho())
             self.freqs, self.modes, self.stats = model.dev.modal(nmodes, tol, max_iters)
             stage.status = "done"
         if rayleigh is not None:

@@ -914,6 +914,15 @@ int sm_count() {
     return sms;
 }
 
+// the FP32 cycle's fine residual r = b - K x from the FP16 copy
+template <int NB>
+void launch_res16(amr_model *m, const AmrAmg *g, const AmgLevel &L, const typename FineX<NB>::T *xt, const float *b,
+                  float *r) {
+    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
+    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r);
+    AMR_COUNT(1);
+}
+
 // r = b - A x on a level (mask: rows of the identity, FP64 fine level only)
 template <int NB, class V>
 void bsr_res(cudaStream_t s, const AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask, const V *x, const V *b,
@@ -987,9 +996,7 @@ struct Cycle {
         auto residual = [&]() {
             if constexpr (kHalf) {
                 if (half) {
-                    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
-                    k_bsr_res16<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, g->A16, nbs, g->rs, xt, b, v.r);
-                    AMR_COUNT(1);
+                    launch_res16<NB>(m, g, L, xt, b, v.r);
                     return;
                 }
             }
@@ -1165,20 +1172,15 @@ double amr_amg_time_residual(amr_model *m, int reps, bool fp64, double *bytes) {
     cudaStream_t s = m->stream;
     const int B = m->B;
     const double nb = (double)m->nblocks, nn = (double)m->nnodes;
-    const unsigned grid16 = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
         if (fp64) {
             if (B == 3) bsr_res<3, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
             else bsr_res<2, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
         } else if (B == 3) {
-            k_bsr_res16<3><<<grid16, 256, 0, s>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs,
-                                                 reinterpret_cast<const float4 *>(g->xt), L.f32.bv, L.f32.r);
-            AMR_COUNT(1);
+            launch_res16<3>(m, g, L, reinterpret_cast<const float4 *>(g->xt), L.f32.bv, L.f32.r);
         } else {
-            k_bsr_res16<2><<<grid16, 256, 0, s>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs,
-                                                 reinterpret_cast<const float2 *>(g->xt), L.f32.bv, L.f32.r);
-            AMR_COUNT(1);
+            launch_res16<2>(m, g, L, reinterpret_cast<const float2 *>(g->xt), L.f32.bv, L.f32.r);
         }
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));

@@ -270,7 +270,7 @@ double amr_dyn_time_rhs(amr_model *m, int reps, double *bytes);
 int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, double *d_modes_nm, amr_modal_stats *stats);
 // vtu.cpp: save_vtu of the model with the caller's arrays
 void amr_vtu_write(amr_model *m, const char *path, const amr_vtu_array *pd, int npd, const amr_vtu_array *cd,
-                   int ncd, int nthreads);
+                   int ncd, int nthreads, bool compress);
 // stage.cpp-equivalent (capi.cu)
 int amr_stage_device(amr_model *m, const double *Uex_nm, const double *Fex_nm, const amr_stage_params &p,
                      double *U_nm, double *F_nm, amr_stage_stats *stats);

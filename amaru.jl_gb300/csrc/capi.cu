@@ -266,7 +266,6 @@ int amr_model_create(const amr_model_desc *d, amr_model **out) {
     std::optional<AmrStreamScope> scope;  // set once the handle's stream exists
     try {
         if (d->ndim != 2 && d->ndim != 3) throw AmrError(AMR_EINVAL, "ndim must be 2 or 3");
-        if (d->stressmodel == AMR_AXISYMMETRIC) throw AmrError(AMR_EUNSUPPORTED, "axisymmetric analyses are not on the GPU path");
         if (d->stressmodel < 0 || d->stressmodel > 3) throw AmrError(AMR_EINVAL, "bad stress model");
         if (d->ndim == 3 && d->stressmodel != AMR_D3) throw AmrError(AMR_EINVAL, "3-D analyses use the d3 stress model");
         if (d->nnodes <= 0 || d->nelems <= 0) throw AmrError(AMR_EINVAL, "empty model");
@@ -685,6 +684,14 @@ int amr_get_state(amr_model *m, double *state) {
     });
 }
 
+int amr_get_elem_nips(const amr_model *m, int32_t *nips) {
+    return guarded(const_cast<amr_model *>(m), [&] {
+        if (!nips) throw AmrError(AMR_EINVAL, "null argument");
+        for (int64_t e = 0; e < m->nelems; e++) nips[e] = m->h_nips[m->inv_perm[e]];
+        return AMR_OK;
+    });
+}
+
 int amr_set_state(amr_model *m, const double *state) {
     return guarded(m, [&] {
         if (!state) throw AmrError(AMR_EINVAL, "null argument");
@@ -817,7 +824,17 @@ int amr_write_vtu(amr_model *m, const char *path, const amr_vtu_array *point_dat
     return guarded(m, [&] {
         if (npoint < 0 || ncell < 0 || (npoint && !point_data) || (ncell && !cell_data))
             throw AmrError(AMR_EINVAL, "bad array lists");
-        amr_vtu_write(m, path, point_data, npoint, cell_data, ncell, nthreads);
+        amr_vtu_write(m, path, point_data, npoint, cell_data, ncell, nthreads, false);
+        return AMR_OK;
+    });
+}
+
+int amr_write_vtu_compressed(amr_model *m, const char *path, const amr_vtu_array *point_data, int32_t npoint,
+                             const amr_vtu_array *cell_data, int32_t ncell, int32_t nthreads) {
+    return guarded(m, [&] {
+        if (npoint < 0 || ncell < 0 || (npoint && !point_data) || (ncell && !cell_data))
+            throw AmrError(AMR_EINVAL, "bad array lists");
+        amr_vtu_write(m, path, point_data, npoint, cell_data, ncell, nthreads, true);
         return AMR_OK;
     });
 }

@@ -15,7 +15,11 @@
 //     K_ab = lambda T_ab + mu T_ab^T + mu tr(T_ab) I - P_ab,
 //     T_ab = sum_ip w_ip g_a g_b^T,   P_ab = sum_ip w_ip gamma_ip (S g_a)(S g_b)^T,
 // with g = dN/dX at the IP, w_ip = detJ * weight * thickness and S the symmetric
-// tensor of m.  This is B^T D B written without the zeros of B.
+// tensor of m.  This is B^T D B written without the zeros of B.  Axisymmetric
+// analyses (mech-solid.jl:94-102,143) add the hoop strain u_r / r (B row zz =
+// N_a / r on the radial component, h_a below) and take the thickness 2 pi r at
+// the IP, r = sum N_a x_a: the pair formula gains the terms of h_a h_b, h_a g_b
+// and g_a h_b, and the plastic vectors S g_a the term m_zz h_a.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -352,6 +356,7 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
     double *sW = sV + epb * nip * NEN * DIM;      // epb x nip
     double *sGam = sW + epb * nip;                // epb x nip
     double *sWG = sGam + epb * nip;               // epb x nip x NEN*DIM: w * g, the rounded products of phase 2
+    double *sH = sWG + epb * nip * NEN * DIM;     // axisymmetric: epb x nip x NEN, h = N / r
     __shared__ int sPl[8];                        // per element: any plastic IP
     __shared__ double sLam[8], sMu[8];            // per element: Lame constants
 
@@ -359,7 +364,9 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
     const int ne = (int)min((int64_t)epb, G.first + G.count - e0);
     const double *dNdR = G.tab;
     const double *wq = G.tab + nip * NEN * DIM;
+    const double *Nt = wq + nip;
     const bool ps = (M.stressmodel == AMR_PLANESTRESS);
+    const bool axi = DIM == 2 && M.stressmodel == AMR_AXISYMMETRIC;
 
     for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
         int el = t / (NEN * DIM), q = t % (NEN * DIM);
@@ -376,6 +383,14 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
         double det = ip_geometry<DIM>(NEN, dNdR + ip * NEN * DIM, sC + el * NEN * DIM, g);
         if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
         double th = M.thickness;
+        if (axi) {
+            const double *N = Nt + ip * NEN, *C = sC + el * NEN * DIM;
+            double r = 0.0;
+            for (int a = 0; a < NEN; a++) r += C[a * DIM] * N[a];
+            th = 2 * M_PI * r;
+            double *h = sH + (el * nip + ip) * NEN;
+            for (int a = 0; a < NEN; a++) h[a] = N[a] / r;
+        }
         double w = det * wq[ip] * th;
         sW[el * nip + ip] = w;
         {
@@ -396,6 +411,8 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
             sPl[el] = 1;
             double *v = sV + (el * nip + ip) * NEN * DIM;
             for (int a = 0; a < NEN; a++) sym_apply<DIM>(m, g + a * DIM, v + a * DIM);
+            if (axi)
+                for (int a = 0; a < NEN; a++) v[a * DIM] += m[2] * sH[(el * nip + ip) * NEN + a];
         }
     }
     __syncthreads();
@@ -444,6 +461,21 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
 #pragma unroll
             for (int j = 0; j < DIM; j++)
                 K[i * DIM + j] = lam * T[i * DIM + j] + mu * T[j * DIM + i] + (i == j ? mu * tr : 0.0) - P[i * DIM + j];
+        if (axi) {  // hoop terms: X1 = sum w h_a g_b, X2 = sum w g_a h_b, X3 = sum w h_a h_b
+            double X1[2] = {0.0, 0.0}, X2[2] = {0.0, 0.0}, X3 = 0.0;
+            for (int ip = 0; ip < nip; ip++) {
+                const double *hh = sH + (el * nip + ip) * NEN;
+                const double wha = sW[el * nip + ip] * hh[a], hb = hh[b];
+                const double *wa = wgbase + ip * NEN * DIM + a * DIM;
+                const double *gb = gbase + ip * NEN * DIM + b * DIM;
+                X1[0] = fma(wha, gb[0], X1[0]); X1[1] = fma(wha, gb[1], X1[1]);
+                X2[0] = fma(wa[0], hb, X2[0]); X2[1] = fma(wa[1], hb, X2[1]);
+                X3 = fma(wha, hb, X3);
+            }
+            K[0] += lam * (X1[0] + X2[0] + X3) + 2.0 * mu * X3;
+            K[1] += lam * X1[1];
+            K[DIM] += lam * X2[1];
+        }
         int64_t base = M.kel_ptr[e];
         double *o1 = Kel + (base + (int64_t)a * NEN + b) * BB;
 #pragma unroll
@@ -473,9 +505,10 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
 #define RSUB __dsub_rn
 #define RDIV __ddiv_rn
 
-// B[l][(b,d)] of setB (mech-solid.jl:82-121) from g = dN/dX of node b
+// B[l][(b,d)] of setB (mech-solid.jl:82-121) from g = dN/dX of node b; hb = N_b / r, the hoop row of an
+// axisymmetric analysis (0 otherwise)
 template <int DIM>
-__device__ __forceinline__ double ref_B(int l, int d, const double *g) {
+__device__ __forceinline__ double ref_B(int l, int d, const double *g, double hb) {
     if (DIM == 3) {
         switch (l) {
         case 0: return d == 0 ? g[0] : 0.0;
@@ -489,6 +522,7 @@ __device__ __forceinline__ double ref_B(int l, int d, const double *g) {
     switch (l) {
     case 0: return d == 0 ? g[0] : 0.0;
     case 1: return d == 1 ? g[1] : 0.0;
+    case 2: return d == 0 ? hb : 0.0;
     case 5: return d == 0 ? RDIV(g[1], SQ2) : RDIV(g[0], SQ2);
     default: return 0.0;
     }
@@ -499,10 +533,11 @@ __global__ void __launch_bounds__(256) stiffness_ref_kernel(ModelArgs M, GroupAr
                                                             int32_t *status) {
     constexpr int ND = NEN * DIM;
     constexpr int NE = (ND * ND + 255) / 256;
-    __shared__ double sC[ND], sG[ND], sD[36], sDB[6 * ND], sIJ[9], sCoef;
+    __shared__ double sC[ND], sG[ND], sD[36], sDB[6 * ND], sIJ[9], sCoef, sH[NEN];
     const int64_t e = G.first + blockIdx.x;
     const int nip = G.nip;
     const bool ps = (M.stressmodel == AMR_PLANESTRESS);
+    const bool axi = DIM == 2 && M.stressmodel == AMR_AXISYMMETRIC;
     for (int t = threadIdx.x; t < ND; t += blockDim.x) {
         int32_t node = M.conn[M.conn_ptr[e] + t / DIM];
         sC[t] = M.coords[3 * (int64_t)node + t % DIM];
@@ -542,7 +577,17 @@ __global__ void __launch_bounds__(256) stiffness_ref_kernel(ModelArgs M, GroupAr
                 sIJ[8] = RDIV(RSUB(RMUL(J[0], J[4]), RMUL(J[1], J[3])), det);
             }
             if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
-            sCoef = RMUL(RMUL(det, G.tab[nip * ND + ip]), M.thickness);
+            double th = M.thickness;
+            if (axi) {  // r = ip.coord.x, th = 2 pi r (mech-solid.jl:143), h = N / r
+                const double *N = G.tab + nip * ND + nip + ip * NEN;
+                double r = 0.0;
+                for (int i = 0; i < NEN; i++) r = RADD(r, RMUL(sC[i * DIM], N[i]));
+                th = RMUL(2 * M_PI, r);
+                for (int i = 0; i < NEN; i++) sH[i] = RDIV(N[i], r);
+            } else {
+                for (int i = 0; i < NEN; i++) sH[i] = 0.0;
+            }
+            sCoef = RMUL(RMUL(det, G.tab[nip * ND + ip]), th);
             // D: calcDe (linear-elastic.jl:98-119), plastic part as De - gamma m m^T
             double E = par[0], nu = par[1];
             for (int q = 0; q < 36; q++) sD[q] = 0.0;
@@ -580,7 +625,7 @@ __global__ void __launch_bounds__(256) stiffness_ref_kernel(ModelArgs M, GroupAr
             int k = t / ND, j = t % ND;
             const double *gb = sG + (j / DIM) * DIM;
             double s = 0.0;
-            for (int l = 0; l < 6; l++) s = RADD(s, RMUL(sD[6 * k + l], ref_B<DIM>(l, j % DIM, gb)));
+            for (int l = 0; l < 6; l++) s = RADD(s, RMUL(sD[6 * k + l], ref_B<DIM>(l, j % DIM, gb, sH[j / DIM])));
             sDB[t] = s;
         }
         __syncthreads();
@@ -592,7 +637,7 @@ __global__ void __launch_bounds__(256) stiffness_ref_kernel(ModelArgs M, GroupAr
                 int i = idx / ND, j = idx % ND;
                 const double *gi = sG + (i / DIM) * DIM;
                 double s = 0.0;
-                for (int k = 0; k < 6; k++) s = RADD(s, RMUL(ref_B<DIM>(k, i % DIM, gi), sDB[k * ND + j]));
+                for (int k = 0; k < 6; k++) s = RADD(s, RMUL(ref_B<DIM>(k, i % DIM, gi, sH[i / DIM]), sDB[k * ND + j]));
                 acc[q] = RADD(acc[q], RMUL(coef, s));
             }
         }
@@ -818,7 +863,13 @@ __global__ void __launch_bounds__(256) mass_kernel(ModelArgs M, GroupArgs G, int
         else det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
                    J[2] * (J[3] * J[7] - J[4] * J[6]);
         if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
-        sK[el * nip + ip] = rho[e] * det * wq[ip] * M.thickness;
+        double th = M.thickness;
+        if (DIM == 2 && M.stressmodel == AMR_AXISYMMETRIC) {  // th = 2 pi r (mech-solid.jl:180)
+            double r = 0.0;
+            for (int a = 0; a < NEN; a++) r += C[a * DIM] * Nt[ip * NEN + a];
+            th = 2 * M_PI * r;
+        }
+        sK[el * nip + ip] = rho[e] * det * wq[ip] * th;
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ne * NP; t += blockDim.x) {
@@ -855,7 +906,9 @@ __global__ void __launch_bounds__(256, 2) internal_kernel(ModelArgs M, GroupArgs
     const int ne = (int)min((int64_t)epb, G.first + G.count - e0);
     const double *dNdR = G.tab;
     const double *wq = G.tab + nip * NEN * DIM;
+    const double *Nt = wq + nip;
     const bool ps = (M.stressmodel == AMR_PLANESTRESS);
+    const bool axi = DIM == 2 && M.stressmodel == AMR_AXISYMMETRIC;
     for (int t = threadIdx.x; t < ne * NEN * DIM; t += blockDim.x) {
         int el = t / (NEN * DIM), q = t % (NEN * DIM);
         int64_t node = M.conn[M.conn_ptr[e0 + el] + q / DIM];
@@ -887,6 +940,15 @@ __global__ void __launch_bounds__(256, 2) internal_kernel(ModelArgs M, GroupArgs
                 de[5] += (ga[1] * ua[0] + ga[0] * ua[1]) * ISQ2;
             }
         }
+        double th = M.thickness, rr = 1.0;
+        if (axi) {  // hoop strain u_r / r and th = 2 pi r (mech-solid.jl:94-102,260)
+            const double *N = Nt + ip * NEN, *C = sC + el * NEN * DIM;
+            double r = 0.0;
+            for (int a = 0; a < NEN; a++) r += C[a * DIM] * N[a];
+            rr = r;
+            th = 2 * M_PI * r;
+            for (int a = 0; a < NEN; a++) de[2] += N[a] / r * u[a * DIM];
+        }
         int64_t gi = M.ip_ptr[e] + ip;
         double s0[AMR_NST], s1[AMR_NST], ds[6];
         for (int f = 0; f < AMR_NST; f++) s0[f] = stbk[f * M.nip_total + gi];
@@ -898,11 +960,12 @@ __global__ void __launch_bounds__(256, 2) internal_kernel(ModelArgs M, GroupArgs
             for (int i = 0; i < 6; i++) ds[i] = 0.0;
         }
         for (int f = 0; f < AMR_NST; f++) st[f * M.nip_total + gi] = s1[f];
-        double coef = det * wq[ip] * M.thickness;
+        double coef = det * wq[ip] * th;
         double *fo = sF + (el * nip + ip) * NEN * DIM;
         for (int a = 0; a < NEN; a++) {
             double v[DIM];
             sym_apply<DIM>(ds, g + a * DIM, v);
+            if (axi) v[0] += ds[2] * (Nt[ip * NEN + a] / rr);
 #pragma unroll
             for (int c = 0; c < DIM; c++) fo[a * DIM + c] = coef * v[c];
         }
@@ -1002,6 +1065,7 @@ __global__ void load_kernel(int kind, int dir, int edge_key, int np, int fd, int
             for (int k = 0; k < ndim; k++) Q[k] = val * nv[k] / ln;
         }
         double th = (kind == AMR_LOAD_FACET && edge_key) ? 1.0 : thickness;
+        if (stressmodel == AMR_AXISYMMETRIC && !(kind == AMR_LOAD_FACET && edge_key)) th = 2 * M_PI * X[0];
         double coef = jn * W[q] * th;
         for (int a = 0; a < np; a++)
             for (int k = 0; k < ndim; k++) F[a * ndim + k] += coef * N[a] * Q[k];
@@ -1036,7 +1100,8 @@ template <int DIM, int NEN>
 void launch_stiff(amr_model *m, const AmrGroup &g) {
     GroupArgs ga{g.tab, g.nip, g.first, g.count};
     int epb = g.epb;
-    size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + 3 * g.nip * NEN * DIM + 2 * g.nip);
+    size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + 3 * g.nip * NEN * DIM + 2 * g.nip +
+                                                 (m->stressmodel == AMR_AXISYMMETRIC ? g.nip * NEN : 0));
     constexpr int NP = NEN * (NEN + 1) / 2;
     int threads = epb * NP;
     threads = ((threads + 31) / 32) * 32;
@@ -1240,6 +1305,8 @@ void amr_loads(amr_model *m, const amr_load *loads, int nloads, double t, double
             }
         }
         if (L.dir < 0 || L.dir > 3 || (L.dir == 2 && m->ndim == 2)) throw AmrError(AMR_EINVAL, "bad load direction");
+        if (L.kind == AMR_LOAD_FACET && L.edge_key && m->stressmodel == AMR_AXISYMMETRIC)  // distributed.jl:89
+            throw AmrError(AMR_EINVAL, "mech_boundary_forces: edge boundary conditions are not applicable in a axisymmetric analysis");
         for (int64_t v : nodes)
             if (v < 0 || v >= m->nnodes) throw AmrError(AMR_EINVAL, "bad node id in load");
         // quadrature table of the facet / element default rule

@@ -24,11 +24,13 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kMaxCols = 16;   // block size limit of the multi-vector SpMV
+constexpr int kMaxCols = 16;   // columns per launch of the multi-vector SpMV and of the combination kernel
+constexpr int kMaxBlock = 64;  // LOBPCG block width limit (nmodes + guard vectors)
 constexpr int kRowLanes = 4;   // lanes per block row in the SpMV
-constexpr int kGramTile = 32;  // rows per shared-memory tile of the Gram kernel
+constexpr int kGramTile = 32;  // rows per shared-memory tile of the Gram kernel (fewer for wide blocks)
 constexpr int kGramCtas = 304;
-constexpr int kGramItems = 10; // Gram items per thread (2 m(m+1)/2 <= kGramItems * kThreads)
+constexpr int kGramItems = 10; // Gram items per thread and launch (wider Grams take several launches)
+constexpr size_t kGramSmem = 48 * 1024;
 
 unsigned blocks(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + kThreads - 1) / kThreads); }
 
@@ -117,14 +119,16 @@ struct Cols {
 
 // Per-CTA partial Gram sums over a contiguous row range: items [0, npairs) are S_a' diag(D) S_b (D null:
 // weight 1), items [npairs, 2 npairs) are S_a' T_b (when T is given), (a <= b), upper triangle by rows.
+// This launch computes items [item0, item0 + kGramItems * blockDim.x) of the nitems; tile rows per
+// shared-memory stage.
 __global__ void __launch_bounds__(kThreads) k_gram(int64_t n, Cols S, Cols T, const double *D, int nitems,
-                                                   double *partials) {
+                                                   int item0, int tile, double *partials) {
     extern __shared__ double sm[];
     const int m = S.ncol;
     const int npairs = m * (m + 1) / 2;
-    double *sS = sm;                       // kGramTile x m
-    double *sT = sS + kGramTile * m;       // kGramTile x m
-    double *sD = sT + kGramTile * m;       // kGramTile
+    double *sS = sm;                       // tile x m
+    double *sT = sS + tile * m;            // tile x m
+    double *sD = sT + tile * m;            // tile
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
     // this thread's items and their (a, b, kind); fixed-size loops keep them in registers
@@ -132,14 +136,14 @@ __global__ void __launch_bounds__(kThreads) k_gram(int64_t n, Cols S, Cols T, co
     double acc[kGramItems];
 #pragma unroll
     for (int q = 0; q < kGramItems; q++) {
-        int v = threadIdx.x + q * blockDim.x, k = 0, a = 0;
+        int v = item0 + threadIdx.x + q * blockDim.x, k = 0, a = 0;
         if (v >= npairs) { v -= npairs; k = 1; }
         if (v < npairs)
             while (v >= m - a) { v -= m - a; a++; }
         ia[q] = a; ib[q] = a + v; kind[q] = k; acc[q] = 0.0;
     }
-    for (int64_t t0 = r0; t0 < r1; t0 += kGramTile) {
-        const int rows = (int)min((int64_t)kGramTile, r1 - t0);
+    for (int64_t t0 = r0; t0 < r1; t0 += tile) {
+        const int rows = (int)min((int64_t)tile, r1 - t0);
         for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
             const int r = e / m, j = e % m;
             sS[r * m + j] = S.col(j, n)[t0 + r];
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(kThreads) k_gram(int64_t n, Cols S, Cols T, co
         __syncthreads();
 #pragma unroll
         for (int q = 0; q < kGramItems; q++) {
-            if (threadIdx.x + q * blockDim.x >= nitems) break;
+            if (item0 + threadIdx.x + q * blockDim.x >= nitems) break;
             double s = acc[q];
             const double *pa = sS + ia[q];
             const double *pb = (kind[q] ? sT : sS) + ib[q];
@@ -163,7 +167,7 @@ __global__ void __launch_bounds__(kThreads) k_gram(int64_t n, Cols S, Cols T, co
     }
 #pragma unroll
     for (int q = 0; q < kGramItems; q++) {
-        const int w = threadIdx.x + q * blockDim.x;
+        const int w = item0 + threadIdx.x + q * blockDim.x;
         if (w < nitems) partials[(int64_t)blockIdx.x * nitems + w] = acc[q];
     }
 }
@@ -177,11 +181,13 @@ __global__ void k_gram_reduce(int nctas, int nitems, const double *partials, dou
     out[w] = s;
 }
 
-// out (ncol_out columns) = S C with C (S.ncol x ncol_out, row-major) in shared memory; thread per row
-__global__ void __launch_bounds__(kThreads) k_combo(int64_t n, Cols S, const double *C, int nout, double *out) {
+// out (nout columns, nout <= kMaxCols) = S C with C's nout columns read at row stride ldc (C row-major,
+// S.ncol rows) into shared memory; thread per row
+__global__ void __launch_bounds__(kThreads) k_combo(int64_t n, Cols S, const double *C, int ldc, int nout,
+                                                    double *out) {
     extern __shared__ double sC[];
     const int m = S.ncol;
-    for (int e = threadIdx.x; e < m * nout; e += blockDim.x) sC[e] = C[e];
+    for (int e = threadIdx.x; e < m * nout; e += blockDim.x) sC[e] = C[(int64_t)(e / nout) * ldc + e % nout];
     __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -365,14 +371,18 @@ struct ModalWork {
         for (; i < 3; i++) { c.p[i] = nullptr; c.w[i] = 0; }
         return c;
     }
-    // Gram items of S (weights D, or 1 when null) and S'T into host[0 .. nitems)
+    // Gram items of S (weights D, or 1 when null) and S'T into host[0 .. nitems): launches of
+    // kGramItems * kThreads items each, all into the same per-CTA partials
     void gram(const Cols &S, const Cols &T, const double *D) {
         const int npairs = S.ncol * (S.ncol + 1) / 2;
         const int nitems = T.ncol ? 2 * npairs : npairs;
-        if (nitems > kGramItems * kThreads || nitems > max_items) throw AmrError(AMR_EINVAL, "modal block too large");
-        const size_t smem = sizeof(double) * (2 * (size_t)kGramTile * S.ncol + kGramTile);
-        k_gram<<<kGramCtas, kThreads, smem, m->stream>>>(n, S, T, D, nitems, partials);
-        AMR_COUNT(1);
+        if (nitems > max_items) throw AmrError(AMR_EINVAL, "modal block too large");
+        const int tile = (int)std::min<size_t>(kGramTile, kGramSmem / (sizeof(double) * (2 * (size_t)S.ncol + 1)));
+        const size_t smem = sizeof(double) * (2 * (size_t)tile * S.ncol + tile);
+        for (int i0 = 0; i0 < nitems; i0 += kGramItems * kThreads) {
+            k_gram<<<kGramCtas, kThreads, smem, m->stream>>>(n, S, T, D, nitems, i0, tile, partials);
+            AMR_COUNT(1);
+        }
         k_gram_reduce<<<(nitems + kThreads - 1) / kThreads, kThreads, 0, m->stream>>>(kGramCtas, nitems, partials, gout);
         AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
@@ -380,25 +390,35 @@ struct ModalWork {
         AMR_CUDA(cudaMemcpyAsync(host.data(), gout, nitems * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
         AMR_CUDA(cudaStreamSynchronize(m->stream));
     }
+    // out_c = mask(K x_c), c < ncol, in launches of kMaxCols columns
     void spmv(int ncol, const double *x, double *out) {
         int dev = 0, sms = 0;
         AMR_CUDA(cudaGetDevice(&dev));
         AMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const unsigned g = (unsigned)std::max<int64_t>(
             1, std::min<int64_t>((m->nnodes * kRowLanes + kThreads - 1) / kThreads, (int64_t)sms * 8));
-        if (m->B == 3)
-            k_spmv_multi<3><<<g, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64,
-                                                           m->free_mask, ncol, x, out);
-        else
-            k_spmv_multi<2><<<g, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64,
-                                                           m->free_mask, ncol, x, out);
-        AMR_COUNT(1);
+        for (int c0 = 0; c0 < ncol; c0 += kMaxCols) {
+            const int nc = std::min(kMaxCols, ncol - c0);
+            const double *xc = x + (size_t)c0 * n;
+            double *oc = out + (size_t)c0 * n;
+            if (m->B == 3)
+                k_spmv_multi<3><<<g, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64,
+                                                               m->free_mask, nc, xc, oc);
+            else
+                k_spmv_multi<2><<<g, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64,
+                                                               m->free_mask, nc, xc, oc);
+            AMR_COUNT(1);
+        }
         AMR_CUDA(cudaGetLastError());
     }
+    // out (nout columns) = S C, C row-major S.ncol x nout, in launches of kMaxCols columns
     void combo(const Cols &S, const double *d_C, int nout, double *out) {
-        const size_t smem = sizeof(double) * (size_t)S.ncol * nout;
-        k_combo<<<blocks(n), kThreads, smem, m->stream>>>(n, S, d_C, nout, out);
-        AMR_COUNT(1);
+        for (int c0 = 0; c0 < nout; c0 += kMaxCols) {
+            const int nc = std::min(kMaxCols, nout - c0);
+            const size_t smem = sizeof(double) * (size_t)S.ncol * nc;
+            k_combo<<<blocks(n), kThreads, smem, m->stream>>>(n, S, d_C + c0, nout, nc, out + (size_t)c0 * n);
+            AMR_COUNT(1);
+        }
         AMR_CUDA(cudaGetLastError());
     }
 };
@@ -410,9 +430,11 @@ int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, dou
     if (m->batch) throw AmrError(AMR_EUNSUPPORTED, "modal analyses of batched parts are not supported");
     if (!m->rho) throw AmrError(AMR_EINVAL, "no density set (amr_set_density)");
     const int nm = p.nmodes;
-    const int guard = std::max(2, (nm + 1) / 2);
-    const int k = nm + guard;
-    if (nm < 1 || k > kMaxCols) throw AmrError(AMR_EINVAL, "nmodes must be in 1.." + std::to_string(kMaxCols - 2 - (kMaxCols - 2) / 3));
+    auto block_of = [](int q) { return q + std::max(2, (q + 1) / 2); };
+    int nmax = 1;
+    while (block_of(nmax + 1) <= kMaxBlock) nmax++;
+    if (nm < 1 || nm > nmax) throw AmrError(AMR_EINVAL, "nmodes must be in 1.." + std::to_string(nmax));
+    const int k = block_of(nm);
     if (m->nu < 3 * k) throw AmrError(AMR_EINVAL, "too few unknown DOFs for " + std::to_string(nm) + " modes");
     {
         std::vector<double> r(m->nelems);
@@ -544,7 +566,11 @@ int amr_modal_device(amr_model *m, const amr_modal_params &p, double *omega, dou
         st.iterations = it;
         st.block = k;
         st.max_residual = maxres;
-        if (!converged) throw AmrError(AMR_ENOCONV, "modal: LOBPCG did not converge in " + std::to_string(p.max_iters) + " iterations");
+        if (!converged) {
+            if (stats) *stats = st;  // the caller sees how far it got
+            throw AmrError(AMR_ENOCONV, "modal: LOBPCG did not converge in " + std::to_string(p.max_iters) +
+                                            " iterations (largest relative residual " + std::to_string(maxres) + ")");
+        }
         for (int c = 0; c < nm; c++) {
             if (!(theta[c] > 0.0)) throw AmrError(AMR_ENOCONV, "modal: fewer than nmodes positive eigenvalues");
             omega[c] = std::sqrt(1.0 / theta[c]);

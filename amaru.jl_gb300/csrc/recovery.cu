@@ -96,6 +96,14 @@ int corners(int shape) {
 int field_codes(int stressmodel, int mat, int32_t *out) {
     int n = 0;
     const bool d3 = stressmodel == AMR_D3;
+    if (stressmodel == AMR_AXISYMMETRIC) {  // σrr σyy σtt σry σvm εrr εyy εtt εry (tensors.jl:182-193)
+        const int32_t ax[9] = {AMR_FIELD_SXX, AMR_FIELD_SYY, AMR_FIELD_SZZ, AMR_FIELD_SXY, AMR_FIELD_SVM,
+                               AMR_FIELD_EXX, AMR_FIELD_EYY, AMR_FIELD_EZZ, AMR_FIELD_EXY};
+        for (int k = 0; k < 9; k++) out[n++] = ax[k];
+        if (mat == AMR_VON_MISES) out[n++] = AMR_FIELD_EP;
+        else if (mat == AMR_DRUCKER_PRAGER) { out[n++] = AMR_FIELD_EPA; out[n++] = AMR_FIELD_J1; out[n++] = AMR_FIELD_SRJ2D; }
+        return n;
+    }
     for (int c = AMR_FIELD_SXX; c <= AMR_FIELD_S1; c++) out[n++] = c;
     if (d3) out[n++] = AMR_FIELD_S2;
     out[n++] = AMR_FIELD_S3;

@@ -1,5 +1,5 @@
-// VTU output: save_vtu (src/mesh/io.jl:167-274) with get_array_node! (:117-158, ascii) and the XML
-// writer of src/tools/xml.jl:250-318, byte for byte.
+// VTU output: save_vtu (src/mesh/io.jl:167-274) with get_array_node! (:117-158) and the XML writer of
+// src/tools/xml.jl:250-318, byte for byte, in ascii or, with compress=true, as appended raw zlib blocks.
 //
 // The file holds the model's points (coordinates as Float64 x 3), cells (0-based connectivity in
 // Amaru's local node order, offsets and VTK cell types as Int32) and the caller's point and cell
@@ -7,18 +7,48 @@
 // Printf output: NaN and Inf spelt as Julia does); an integer entry is the number and two spaces; a
 // row is one line whose leading blanks become the element's indentation plus three.  Arrays come from
 // host or device buffers; large arrays are formatted by host threads in row chunks, concatenated in
-// order.  Tags are not written: elements of this path carry none.
+// order.  In the compressed form every DataArray is a self-closing element with format "appended" and
+// the offset of its block; a block is the UInt64 header (1, n, n, compressed n) and the zlib stream
+// (level 4, the zlib defaults of window 15 and memory level 8: the settings of the reference's
+// ZlibCompressorStream) of the array's bytes in row order, blocks compressed by host threads in
+// parallel and appended in order after "_" in <AppendedData encoding="raw">.  zlib is the system's
+// libz.so.1, opened at the first compressed write.  Tags are columns the caller passes (tag-s1, tag-s2,
+// tag), as update_output_data! leaves them in elem_data.
+#include <dlfcn.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
 #include "amr_internal.h"
 
 namespace {
+
+// the two zlib entry points the compressed form uses (zlib.h: compress2, compressBound)
+using compress2_fn = int (*)(unsigned char *, unsigned long *, const unsigned char *, unsigned long, int);
+using bound_fn = unsigned long (*)(unsigned long);
+struct Zlib {
+    compress2_fn compress2 = nullptr;
+    bound_fn bound = nullptr;
+};
+const Zlib &zlib() {
+    static Zlib z;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *h = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!h) return;
+        z.compress2 = reinterpret_cast<compress2_fn>(dlsym(h, "compress2"));
+        z.bound = reinterpret_cast<bound_fn>(dlsym(h, "compressBound"));
+        if (!z.compress2 || !z.bound) z.compress2 = nullptr;
+    });
+    if (!z.compress2) throw AmrError(AMR_EUNSUPPORTED, "compressed VTU output needs zlib (libz.so.1)");
+    return z;
+}
 
 // VTK cell type of each shape (vtk_type in src/shape/*.jl, codes of src/shape/vtk.jl)
 int vtk_type(int shape) {
@@ -122,6 +152,24 @@ void write_array(std::string &out, const Array &a, int level, int nthreads) {
     out += ind0 + "</DataArray>\n";
 }
 
+// the array's block of the appended data: header and zlib stream of its row-major bytes
+std::string compressed_block(const Array &a) {
+    const size_t es = elem_size(a.type), n = a.host.size();
+    std::vector<unsigned char> rows(n);
+    for (int64_t i = 0; i < a.nrows; i++)
+        for (int c = 0; c < a.ncomp; c++)
+            std::memcpy(&rows[((size_t)i * a.ncomp + c) * es], &a.host[((size_t)c * a.nrows + i) * es], es);
+    const Zlib &z = zlib();
+    unsigned long zn = z.bound((unsigned long)n);
+    std::string blk(32 + zn, '\0');
+    const int rc = z.compress2(reinterpret_cast<unsigned char *>(&blk[32]), &zn, rows.data(), (unsigned long)n, 4);
+    if (rc != 0) throw AmrError(AMR_EINVAL, "zlib compress2 failed (" + std::to_string(rc) + ")");
+    const uint64_t head[4] = {1, (uint64_t)n, (uint64_t)n, (uint64_t)zn};
+    std::memcpy(&blk[0], head, 32);
+    blk.resize(32 + zn);
+    return blk;
+}
+
 Array take(const amr_vtu_array &d, int64_t nrows) {
     if (!d.name || !type_name(d.type) || d.ncomp < 1 || (!d.data && nrows > 0))
         throw AmrError(AMR_EINVAL, "bad VTU array description");
@@ -140,7 +188,7 @@ Array take(const amr_vtu_array &d, int64_t nrows) {
 }  // namespace
 
 void amr_vtu_write(amr_model *m, const char *path, const amr_vtu_array *pd, int npd, const amr_vtu_array *cd,
-                   int ncd, int nthreads) {
+                   int ncd, int nthreads, bool compress) {
     if (!path) throw AmrError(AMR_EINVAL, "null path");
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     const int64_t nn = m->nnodes, ne = m->nelems;
@@ -172,9 +220,41 @@ void amr_vtu_write(amr_model *m, const char *path, const amr_vtu_array *pd, int 
     std::vector<Array> pa, ca;
     for (int i = 0; i < npd; i++) pa.push_back(take(pd[i], nn));
     for (int i = 0; i < ncd; i++) ca.push_back(take(cd[i], ne));
+    // compressed form: every array's block, compressed in parallel, offsets in document order
+    std::vector<const Array *> order{&pts, &conn, &offs, &types};
+    for (const Array &a : pa)
+        if (a.nrows * a.ncomp > 0) order.push_back(&a);
+    for (const Array &a : ca)
+        if (a.nrows * a.ncomp > 0) order.push_back(&a);
+    std::vector<std::string> blocks;
+    std::vector<size_t> offset;
+    if (compress) {
+        zlib();
+        blocks.resize(order.size());
+        std::vector<std::thread> th;
+        const int nt = std::max(1, std::min<int>(nthreads, (int)order.size()));
+        for (int t = 0; t < nt; t++)
+            th.emplace_back([&, t]() {
+                for (size_t i = t; i < order.size(); i += nt) blocks[i] = compressed_block(*order[i]);
+            });
+        for (auto &x : th) x.join();
+        size_t o = 0;
+        for (auto &b : blocks) { offset.push_back(o); o += b.size(); }
+    }
+    size_t next = 0;  // index into order of the next array written
+    auto array = [&](std::string &out, const Array &a) {
+        if (!compress) {
+            write_array(out, a, 4, nthreads);
+            return;
+        }
+        out += std::string("            <DataArray type=\"") + type_name(a.type) + "\" Name=\"" + a.name +
+               "\" NumberOfComponents=\"" + std::to_string(a.ncomp) + "\" format=\"appended\" offset=\"" +
+               std::to_string(offset[next]) + "\"/>\n";
+        next++;
+    };
     // document (xml.jl save + writenode)
     std::string out;
-    out.reserve((size_t)nn * (3 + 16) * 22 + (size_t)conn.nrows * 14);
+    if (!compress) out.reserve((size_t)nn * (3 + 16) * 22 + (size_t)conn.nrows * 14);
     out += "<?xml version=\"1.0\" encoding=\"UTF-8\"?>\n";
     out += "<!-- File generated by Amaru Finite Element Code -->\n";
     out += "<VTKFile type=\"UnstructuredGrid\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\" "
@@ -182,12 +262,12 @@ void amr_vtu_write(amr_model *m, const char *path, const amr_vtu_array *pd, int 
     out += "   <UnstructuredGrid>\n";
     out += "      <Piece NumberOfPoints=\"" + std::to_string(nn) + "\" NumberOfCells=\"" + std::to_string(ne) + "\">\n";
     out += "         <Points>\n";
-    write_array(out, pts, 4, nthreads);
+    array(out, pts);
     out += "         </Points>\n";
     out += "         <Cells>\n";
-    write_array(out, conn, 4, nthreads);
-    write_array(out, offs, 4, nthreads);
-    write_array(out, types, 4, nthreads);
+    array(out, conn);
+    array(out, offs);
+    array(out, types);
     out += "         </Cells>\n";
     auto section = [&](const char *tag, const std::vector<Array> &arrs) {
         if (arrs.empty()) return;  // no data: no element (save_vtu's has_node_data / has_elem_data)
@@ -199,17 +279,26 @@ void amr_vtu_write(amr_model *m, const char *path, const amr_vtu_array *pd, int 
         }
         out += std::string("         <") + tag + ">\n";
         for (const Array &a : arrs)
-            if (a.nrows * a.ncomp > 0) write_array(out, a, 4, nthreads);  // empty arrays are skipped
+            if (a.nrows * a.ncomp > 0) array(out, a);  // empty arrays are skipped
         out += std::string("         </") + tag + ">\n";
     };
     section("PointData", pa);
     section("CellData", ca);
     out += "      </Piece>\n";
     out += "   </UnstructuredGrid>\n";
-    out += "</VTKFile>\n";
     FILE *f = std::fopen(path, "wb");
     if (!f) throw AmrError(AMR_EINVAL, std::string("cannot open ") + path);
-    const size_t w = std::fwrite(out.data(), 1, out.size(), f);
+    bool ok = true;
+    auto put = [&](const std::string &x) { ok = ok && std::fwrite(x.data(), 1, x.size(), f) == x.size(); };
+    if (compress) {
+        out += "   <AppendedData encoding=\"raw\">\n_";
+        put(out);
+        for (auto &b : blocks) put(b);
+        put("\n   </AppendedData>\n</VTKFile>\n");
+    } else {
+        out += "</VTKFile>\n";
+        put(out);
+    }
     const int rc = std::fclose(f);
-    if (w != out.size() || rc != 0) throw AmrError(AMR_EINVAL, std::string("write failed: ") + path);
+    if (!ok || rc != 0) throw AmrError(AMR_EINVAL, std::string("write failed: ") + path);
 }

@@ -71,6 +71,8 @@ mutable struct GPUModel
     h::Ptr{Cvoid}
     ndofs::Int
     nu::Int
+    elems::Vector{Any}   # the elements on the device, in model order (the active ones)
+    nodes::Vector{Int}   # the ids of their nodes, ascending: device node k is model node nodes[k]
 end
 
 function check(m::Union{GPUModel,Nothing}, rc::Integer)
@@ -97,33 +99,32 @@ material_code(m) = error("AmaruGPU: material $(typeof(m)) is not on the GPU path
     activate!(model, stage)
 
 Applies `stage.toactivate` as mech_stage_solver! does (src/mech/mech-solver.jl:216-220).  The device
-model holds every element of the FEModel, while the reference assembles only the active ones and numbers
-only their nodes (configure_dofs!, src/bc.jl:200-202); so a model that still has inactive elements is
-refused instead of being solved with a different K.
+model holds the active elements and their nodes (gpu_model!), so the stage assembles and updates only
+the active elements and configure_dofs! numbers only their nodes (src/bc.jl:200-203).
 """
 function activate!(model::FEModel, stage::Stage)
     for elem in stage.toactivate
         elem.active = true
     end
-    all(e -> e.active, model.elems) ||
-        error("AmaruGPU: inactive elements are not on the GPU path; activate every element before a GPU stage")
     return nothing
 end
 
 """
-    GPUModel(model::FEModel)
+    GPUModel(model::FEModel; elems=model.elems)
 
-Creates the device model: nodes, MechSolid elements with their material
-parameters and quadrature, pattern and contribution map (amr_model_create).
+Creates the device model over `elems` and the nodes they use: nodes, MechSolid elements with their
+material parameters and quadrature, pattern and contribution map (amr_model_create).
 """
-function GPUModel(model::FEModel)
-    elems = model.elems
+function GPUModel(model::FEModel; elems=model.elems)
     all(e -> e isa MechSolid || e isa HMSolid || e isa TMSolid, elems) ||
         error("AmaruGPU: only MechSolid, HMSolid and TMSolid elements are on the GPU path")
-    nnodes = length(model.nodes)
+    ids = sort(unique([n.id for e in elems for n in e.nodes]))
+    loc = Dict(id => k - 1 for (k, id) in enumerate(ids))
+    nnodes = length(ids)
     coords = zeros(3, nnodes)
-    for (i, n) in enumerate(model.nodes)
-        coords[:, i] .= (n.coord.x, n.coord.y, n.coord.z)
+    for (k, id) in enumerate(ids)
+        n = model.nodes[id]
+        coords[:, k] .= (n.coord.x, n.coord.y, n.coord.z)
     end
     nel = length(elems)
     shape = Int32[SHAPES[e.shape.name] for e in elems]
@@ -133,7 +134,7 @@ function GPUModel(model::FEModel)
     mat_type = zeros(Int32, nel)
     mat_params = zeros(8, nel)
     for (k, e) in enumerate(elems)
-        append!(conn, [n.id - 1 for n in e.nodes])
+        append!(conn, [loc[n.id] for n in e.nodes])
         conn_ptr[k+1] = length(conn)
         t, p = material_code(e.mat)
         mat_type[k] = t
@@ -149,9 +150,65 @@ function GPUModel(model::FEModel)
         st = check(nothing, rc)
         st === nothing || error(st.message)
     end
-    g = GPUModel(h[], 0, 0)
-    finalizer(x -> ccall((:amr_model_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), g)
+    g = GPUModel(h[], 0, 0, collect(Any, elems), ids)
+    finalizer(release!, g)
     return g
+end
+
+function release!(g::GPUModel)
+    g.h == C_NULL || ccall((:amr_model_destroy, LIB), Cint, (Ptr{Cvoid},), g.h)
+    g.h = C_NULL
+    return nothing
+end
+
+"""
+    gpu_model!(model) -> GPUModel
+
+The model's device handle over its active elements: kept while the active set stays, rebuilt when a
+stage's toactivate changed it.  A new handle takes the IP states of the elements' IpState objects
+(where sync_states! left the last stage's), so the states move with their elements.
+"""
+function gpu_model!(model::FEModel)
+    act = [e for e in model.elems if e.active]
+    g = get(GPU_MODELS, objectid(model), nothing)
+    if g === nothing || length(g.elems) != length(act) || any(a !== b for (a, b) in zip(g.elems, act))
+        g === nothing || release!(g)
+        g = GPUModel(model; elems=act)
+        load_states!(g)
+        GPU_MODELS[objectid(model)] = g
+    end
+    return g
+end
+
+# the IpState objects of g's elements into the device (the inverse of sync_states!)
+function load_states!(g::GPUModel)
+    S = zeros(16, sum(length(e.ips) for e in g.elems; init=0))
+    k = 0
+    for elem in g.elems, ip in elem.ips
+        k += 1
+        st = ip.state
+        S[1:6, k] .= st.σ
+        S[7:12, k] .= st.ε
+        hasfield(typeof(st), :εpa) && (S[13, k] = st.εpa)
+        hasfield(typeof(st), :Δλ) && (S[14, k] = st.Δλ)
+        hasfield(typeof(st), :Δγ) && (S[14, k] = st.Δγ)
+    end
+    set_state!(g, S)
+    return g
+end
+
+# fn(handle over every element of the model, holding the IpState objects' states): output covers every
+# element, as update_output_data! does (src/fe-model.jl:341-427)
+function with_all_elements(fn, model::FEModel)
+    g = GPU_MODELS[objectid(model)]
+    length(g.elems) == length(model.elems) && return fn(g)
+    full = GPUModel(model)
+    try
+        load_states!(full)
+        return fn(full)
+    finally
+        release!(full)
+    end
 end
 
 """
@@ -160,11 +217,12 @@ end
 Passes the numbering of configure_dofs! (src/bc.jl:198-233) to the library.
 """
 function set_dofs!(g::GPUModel, model::FEModel, dofs, nu)
-    eq = fill(Int64(-1), 3, length(model.nodes))
+    eq = fill(Int64(-1), 3, length(g.nodes))
     keys = (:ux, :uy, :uz)
-    for n in model.nodes
+    for (i, id) in enumerate(g.nodes)
+        n = model.nodes[id]
         for (k, key) in enumerate(keys)
-            haskey(n.dofdict, key) && (eq[k, n.id] = n.dofdict[key].eq_id - 1)
+            haskey(n.dofdict, key) && (eq[k, i] = n.dofdict[key].eq_id - 1)
         end
     end
     rc = ccall((:amr_set_dofs, LIB), Cint, (Ptr{Cvoid}, Ptr{Int64}, Int64, Int64), g.h, eq, length(dofs), nu)
@@ -277,7 +335,7 @@ function gpu_stage_solver!(ana::MechAnalysis, stage::Stage; args...)
     args = NamedTuple(args)
     model = ana.model
     activate!(model, stage)
-    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
+    g = gpu_model!(model)
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
     set_dofs!(g, model, dofs, nu)
@@ -329,12 +387,15 @@ DruckerPragerState).  Julia code that reads ip.state after a GPU stage, such as
 update_output_data!'s element values and the loggers, then sees the stage's
 result.
 """
-sync_states!(g::GPUModel, model::FEModel) = (copy_states!(get_state(g), (model,)); model)
+sync_states!(g::GPUModel, model::FEModel) = (copy_states!(get_state(g), g.elems); model)
 
 # S (16 x nip, element and IP order of the models one after the other) into the IpState objects
-function copy_states!(S::Matrix{Float64}, models)
+copy_states!(S::Matrix{Float64}, models::Union{Tuple,AbstractVector{<:FEModel}}) =
+    copy_states!(S, [elem for model in models for elem in model.elems])
+
+function copy_states!(S::Matrix{Float64}, elems::AbstractVector)
     k = 0
-    for model in models, elem in model.elems, ip in elem.ips
+    for elem in elems, ip in elem.ips
         k += 1
         st = ip.state
         st.σ = typeof(st.σ)(view(S, 1:6, k))
@@ -395,11 +456,11 @@ function gpu_dyn_stage_solver!(ana::Amaru.DynamicAnalysis, stage::Stage; args...
     args = NamedTuple(args)
     model = ana.model
     activate!(model, stage)
-    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
+    g = gpu_model!(model)
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
     set_dofs!(g, model, dofs, nu)
-    rho = Float64[ elem.props.ρ for elem in model.elems ]
+    rho = Float64[ elem.props.ρ for elem in g.elems ]
     check(g, ccall((:amr_set_density, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, rho))
     U0, F0 = Amaru.get_bc_vals(model, stage.bcs, 0.0)
     U1, F1 = Amaru.get_bc_vals(model, stage.bcs, 1.0)
@@ -460,14 +521,27 @@ end
 const VTU_TYPES = Dict(Float64 => Int32(0), Int32 => Int32(1), Int64 => Int32(2), UInt64 => Int32(3))
 
 """
-    save_gpu(model::FEModel, filename::String)
+    save_gpu(model::FEModel, filename::String; compress=false)
 
-save(model, filename) for .vtu files: update_output_data!(model), then the file written by
-amr_write_vtu from model.node_data and model.elem_data, byte for byte as save_vtu writes it.
+save(model, filename; compress) for .vtu files: update_output_data!(model), the tag fields save_vtu adds
+(src/mesh/io.jl:168-192, with Amaru's own encoders and the same Set order), then the file written by
+amr_write_vtu (ascii) or amr_write_vtu_compressed (zlib blocks appended) from model.node_data and
+model.elem_data, byte for byte as save_vtu writes it.
 """
-function save_gpu(model::FEModel, filename::String)
-    g = GPU_MODELS[objectid(model)]
+function save_gpu(model::FEModel, filename::String; compress::Bool=false)
     Amaru.update_output_data!(model)
+    tags = collect(Set(elem.tag for elem in model.elems))
+    if length(tags) > 1 || tags[1] != ""
+        tag_d = Dict(tag => i for (i, tag) in enumerate(tags))
+        parts = Tuple{String,String}[]
+        for tag in tags
+            length(codeunits(tag)) > 16 && error("Mesh: tag '$tag' too long. Max length is 16 UTF units.")
+            push!(parts, Amaru.safe_string_cut(tag, 8))
+        end
+        model.elem_data["tag-s1"] = UInt64[Amaru.encode_string_to_uint64(parts[tag_d[e.tag]][1]) for e in model.elems]
+        model.elem_data["tag-s2"] = UInt64[Amaru.encode_string_to_uint64(parts[tag_d[e.tag]][2]) for e in model.elems]
+        model.elem_data["tag"] = Int[tag_d[e.tag] - 1 for e in model.elems]
+    end
     keep = Any[]
     function arrays(d)
         out = VtuArray[]
@@ -481,9 +555,15 @@ function save_gpu(model::FEModel, filename::String)
         return out
     end
     pd, cd = arrays(model.node_data), arrays(model.elem_data)
-    GC.@preserve keep begin
-        check(g, ccall((:amr_write_vtu, LIB), Cint, (Ptr{Cvoid}, Cstring, Ptr{VtuArray}, Int32, Ptr{VtuArray},
-                       Int32, Int32), g.h, filename, pd, length(pd), cd, length(cd), Int32(0)))
+    with_all_elements(model) do g
+        GC.@preserve keep begin
+            rc = compress ?
+                ccall((:amr_write_vtu_compressed, LIB), Cint, (Ptr{Cvoid}, Cstring, Ptr{VtuArray}, Int32,
+                      Ptr{VtuArray}, Int32, Int32), g.h, filename, pd, length(pd), cd, length(cd), Int32(0)) :
+                ccall((:amr_write_vtu, LIB), Cint, (Ptr{Cvoid}, Cstring, Ptr{VtuArray}, Int32, Ptr{VtuArray},
+                      Int32, Int32), g.h, filename, pd, length(pd), cd, length(cd), Int32(0))
+            check(g, rc)
+        end
     end
     return nothing
 end
@@ -508,11 +588,11 @@ mech_modal_solver!, computed on the device.
 function gpu_modal_solver!(ana::MechModalAnalysis, stage::Stage; nmodes::Integer=5, args...)
     model = ana.model
     activate!(model, stage)
-    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
+    g = gpu_model!(model)
     dofs, nu = Amaru.configure_dofs!(model, stage.bcs)
     model.ndofs = length(dofs)
     set_dofs!(g, model, dofs, nu)
-    rho = Float64[ elem.props.ρ for elem in model.elems ]
+    rho = Float64[ elem.props.ρ for elem in g.elems ]
     check(g, ccall((:amr_set_density, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, rho))
     w = zeros(nmodes)
     V = zeros(nu, nmodes)
@@ -552,6 +632,9 @@ end
 # ---------------------------------------------------------------------------
 const FIELD_SYMBOLS = [:σxx, :σyy, :σzz, :σyz, :σxz, :σxy, :σvm, :σ1, :σ2, :σ3,
                        :εxx, :εyy, :εzz, :εyz, :εxz, :εxy, :ep, :epa, :j1, :srj2d]
+# the keys the same codes carry in an axisymmetric analysis (src/tools/tensors.jl:182-193)
+const AXI_FIELD_SYMBOLS = [:σrr, :σyy, :σtt, :σyz, :σxz, :σry, :σvm, :σ1, :σ2, :σ3,
+                           :εrr, :εyy, :εtt, :εyz, :εxz, :εry, :ep, :epa, :j1, :srj2d]
 
 """
     nodal_patch_recovery_gpu(model::FEModel)
@@ -560,14 +643,16 @@ The `(V_rec, fields)` pair of nodal_patch_recovery(model), from the IP states th
 model's GPU handle holds (the last gpu_stage_solver! stage).
 """
 function nodal_patch_recovery_gpu(model::FEModel)
-    g = GPU_MODELS[objectid(model)]
-    n = Ref{Int32}(0)
-    codes = zeros(Int32, length(FIELD_SYMBOLS))
-    check(g, ccall((:amr_recovery_fields, LIB), Cint, (Ptr{Cvoid}, Ptr{Int32}, Int32, Ref{Int32}),
-                   g.h, codes, Int32(length(codes)), n))
-    V = zeros(length(model.nodes), n[])
-    n[] > 0 && check(g, ccall((:amr_recover_nodal, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, V))
-    return V, FIELD_SYMBOLS[codes[1:n[]] .+ 1]
+    with_all_elements(model) do g
+        n = Ref{Int32}(0)
+        codes = zeros(Int32, length(FIELD_SYMBOLS))
+        check(g, ccall((:amr_recovery_fields, LIB), Cint, (Ptr{Cvoid}, Ptr{Int32}, Int32, Ref{Int32}),
+                       g.h, codes, Int32(length(codes)), n))
+        V = zeros(length(model.nodes), n[])  # a handle over every element holds every used node
+        n[] > 0 && check(g, ccall((:amr_recover_nodal, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, V))
+        syms = model.ctx.stressmodel == :axisymmetric ? AXI_FIELD_SYMBOLS : FIELD_SYMBOLS
+        return V, syms[codes[1:n[]] .+ 1]
+    end
 end
 
 # GPU-backed model?  update_output_data! picks the recovery with it (the one-line hook at
@@ -584,6 +669,7 @@ function model_arrays(model::FEModel)
     elems = model.elems
     all(e -> e isa MechSolid || e isa HMSolid || e isa TMSolid, elems) ||
         error("AmaruGPU: only MechSolid, HMSolid and TMSolid elements are on the GPU path")
+    all(e -> e.active, elems) || error("AmaruGPU: batched and served models must have every element active")
     coords = zeros(3, length(model.nodes))
     for (i, n) in enumerate(model.nodes)
         coords[:, i] .= (n.coord.x, n.coord.y, n.coord.z)
@@ -666,6 +752,7 @@ function solve_batch!(b::GPUBatch, stages::Vector{Stage}; args...)
     eqs, Us, Fs, nus, nds, dofss = [], [], [], Int[], Int[], []
     for (m, st) in zip(b.models, stages)
         activate!(m, st)
+        all(e -> e.active, m.elems) || error("AmaruGPU: batched models must have every element active")
         dofs, nu = Amaru.configure_dofs!(m, st.bcs)
         m.ndofs = length(dofs)
         Uex, Fex = Amaru.get_bc_vals(m, st.bcs)
@@ -934,11 +1021,12 @@ struct CoupledDesc
 end
 
 function coupled_mount(model::FEModel, ndofs::Int, Δt::Float64, kind::Int32, key::Symbol)
-    g = get!(() -> GPUModel(model), GPU_MODELS, objectid(model))
-    nn = length(model.nodes)
-    eq4 = fill(Int64(-1), 4, nn)     # ux, uy, uz, the scalar; 0-based
+    g = gpu_model!(model)            # the active elements (the mounts loop over active_elems)
+    nn = length(g.nodes)
+    eq4 = fill(Int64(-1), 4, nn)     # ux, uy, uz, the scalar; 0-based, device node order
     phi = zeros(ndofs)               # dof.vals of the scalar DOFs, as the reference reads them
-    for (i, node) in enumerate(model.nodes)
+    for (i, id) in enumerate(g.nodes)
+        node = model.nodes[id]
         for (c, k) in enumerate((:ux, :uy, :uz))
             haskey(node.dofdict, k) && (eq4[c, i] = node.dofdict[k].eq_id - 1)
         end
@@ -948,8 +1036,8 @@ function coupled_mount(model::FEModel, ndofs::Int, Δt::Float64, kind::Int32, ke
             phi[dof.eq_id] = dof.vals[key]
         end
     end
-    prm = zeros(3, length(model.elems))
-    for (k, e) in enumerate(model.elems)
+    prm = zeros(3, length(g.elems))
+    for (k, e) in enumerate(g.elems)
         if kind == 0  # HMSolid: Biot's alpha, permeability, storativity (LinearElasticSeep)
             prm[:, k] .= (e.props.α, e.mat.k, e.mat.S)
         else          # TMSolid: thermal expansion, conductivity (LinearElasticThermo), rho cv

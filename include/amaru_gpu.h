@@ -193,6 +193,10 @@ int amr_get_state(amr_model *m, double *state);
 /* IP states in, same layout (copyto! of the IpState arrays, src/ip.jl:22-57): a
  * checkpoint restored, or states set by the caller. */
 int amr_set_state(amr_model *m, const double *state);
+/* The number of IPs of each element, in the caller's element order: its rows in the state layout
+ * above.  A host that moves states between handles over different element sets (a stage's
+ * toactivate, src/mech/mech-solver.jl:216-220) locates an element's rows with it. */
+int amr_get_elem_nips(const amr_model *m, int32_t *nips);
 int amr_get_sizes(const amr_model *m, int64_t *nnodes, int64_t *nelems, int64_t *nip_total, int64_t *nblocks);
 
 /* Distributed loads (compute_bc_vals!, src/bc.jl:116-136,175-194):
@@ -431,7 +435,7 @@ void amr_default_dyn_params(amr_dyn_params *p);
  * diag(L) phi = (1/lambda) K11 phi by LOBPCG with the multigrid V-cycle as preconditioner.
  * Needs amr_set_dofs and amr_set_density (every element rho > 0). */
 typedef struct {
-    int32_t nmodes;          /* default 5, at most 10 */
+    int32_t nmodes;          /* default 5, at most 42 (a LOBPCG block of at most 64 vectors) */
     int32_t max_iters;       /* LOBPCG iterations (default 1000) */
     double tol;              /* relative residual of every wanted pair (default 1e-7) */
 } amr_modal_params;
@@ -460,13 +464,19 @@ typedef struct {
 /* nthreads host threads format the arrays (0: all cores). */
 int amr_write_vtu(amr_model *m, const char *path, const amr_vtu_array *point_data, int32_t npoint,
                   const amr_vtu_array *cell_data, int32_t ncell, int32_t nthreads);
+/* save_vtu(...; compress=true) (src/mesh/io.jl:119-135,167-274): the same document with every array
+ * appended as a zlib block (level 4) in <AppendedData encoding="raw">, blocks compressed by nthreads
+ * host threads.  Needs the system zlib (libz.so.1); AMR_EUNSUPPORTED without it. */
+int amr_write_vtu_compressed(amr_model *m, const char *path, const amr_vtu_array *point_data, int32_t npoint,
+                             const amr_vtu_array *cell_data, int32_t ncell, int32_t nthreads);
 
 /* ---- output recovery ----
  * Nodal values of the IP fields: replaces nodal_patch_recovery (src/fe-model.jl:504-702)
  * as called by update_output_data! (:341-427) and get_node_and_elem_vals (:430-485).
  * Field codes name the keys of ip_state_vals (src/tools/tensors.jl:162-215,
  * src/mech/mat/von-mises.jl:159-168,330-341, src/mech/mat/drucker-prager.jl:152-163):
- * σxx σyy σzz σyz σxz σxy σvm σ1 σ2 σ3 εxx εyy εzz εyz εxz εxy ep epa j1 srj2d. */
+ * σxx σyy σzz σyz σxz σxy σvm σ1 σ2 σ3 εxx εyy εzz εyz εxz εxy ep epa j1 srj2d.  In an axisymmetric
+ * analysis the codes SXX SZZ SXY EXX EZZ EXY carry the keys σrr σtt σry εrr εtt εry. */
 enum {
     AMR_FIELD_SXX = 0, AMR_FIELD_SYY = 1, AMR_FIELD_SZZ = 2, AMR_FIELD_SYZ = 3, AMR_FIELD_SXZ = 4,
     AMR_FIELD_SXY = 5, AMR_FIELD_SVM = 6, AMR_FIELD_S1 = 7, AMR_FIELD_S2 = 8, AMR_FIELD_S3 = 9,

@@ -65,7 +65,8 @@ class OrcModel(C.Structure):
     _fields_ = [("ndim", C.c_int32), ("stressmodel", C.c_int32), ("thickness", C.c_double),
                 ("nnodes", C.c_int64), ("coords", C.c_void_p), ("nelem", C.c_int64), ("shape", C.c_void_p),
                 ("conn_ptr", C.c_void_p), ("conn", C.c_void_p), ("nips", C.c_void_p), ("mat_type", C.c_void_p),
-                ("mat_par", C.c_void_p), ("eq_id", C.c_void_p), ("ip_ptr", C.c_void_p), ("state", C.c_void_p)]
+                ("mat_par", C.c_void_p), ("eq_id", C.c_void_p), ("ip_ptr", C.c_void_p), ("state", C.c_void_p),
+                ("active", C.c_void_p), ("nactive", C.c_int64)]
 
 
 def lib():
@@ -494,6 +495,7 @@ class FEModel:
         self.conn_ptr[1:] = np.cumsum([len(c.nodes) for c in mesh.elems])
         self.conn = np.array([n for c in mesh.elems for n in c.nodes], dtype=np.int64)
         self.nips = np.full(ne, nips, dtype=np.int32)
+        self.active = np.ones(ne, dtype=bool)  # elem.active (src/element.jl:40, fe-model.jl:156)
         self.coords = np.ascontiguousarray(mesh.coords)
         self.nnodes = len(self.coords)
         self._setup_ips()
@@ -516,16 +518,29 @@ class FEModel:
         self.nips[:] = n
         self._setup_ips()
 
+    def active_elems(self):
+        """filter(elem -> elem.active, model.elems) (src/mech/mech-solver.jl:220): element ids."""
+        return np.nonzero(self.active)[0].astype(np.int64)
+
+    def active_nodes(self):
+        """The nodes of the active elements, by id (configure_dofs!, src/bc.jl:200-203)."""
+        act = self.active_elems()
+        if len(act) == len(self.shape):
+            return np.unique(self.conn)
+        return np.unique(np.concatenate([self.conn[self.conn_ptr[e]:self.conn_ptr[e + 1]] for e in act]))
+
     def cstruct(self):
         m = OrcModel()
+        act = None if self.active.all() else self.active_elems()
         self._keep = [self.coords, self.shape, self.conn_ptr, self.conn, self.nips, self.mat_type, self.mat_par,
-                      self.eq_id, self.ip_ptr, self.state]
+                      self.eq_id, self.ip_ptr, self.state, act]
         m.ndim, m.stressmodel, m.thickness = self.ndim, self.stressmodel, self.thickness
         m.nnodes, m.coords = self.nnodes, _p(self.coords)
         m.nelem, m.shape = len(self.shape), _p(self.shape)
         m.conn_ptr, m.conn, m.nips = _p(self.conn_ptr), _p(self.conn), _p(self.nips)
         m.mat_type, m.mat_par = _p(self.mat_type), _p(self.mat_par)
         m.eq_id, m.ip_ptr, m.state = _p(self.eq_id), _p(self.ip_ptr), _p(self.state)
+        m.active, m.nactive = (None, 0) if act is None else (_p(act), len(act))
         return m
 
     def elem_stiffness(self, e):
@@ -649,8 +664,8 @@ def _setup_bcs(model, bcs):
                 src = mesh.edges
             objs = _select_tagged(mesh, src, filt)
             nodes = sorted({n for f in objs for n in f.nodes})
-        else:
-            objs = _select_tagged(mesh, mesh.elems, filt)
+        else:  # over the active elements only (bc.jl:159)
+            objs = [c for c in _select_tagged(mesh, mesh.elems, filt) if model.active[c.id]]
             nodes = sorted({n for c in objs for n in c.nodes})
         for key in bc.conds:
             if key in model.dof_names:
@@ -669,7 +684,7 @@ def _select_tagged(mesh, cells, filt):
 
 def configure_dofs(model, bcs):
     """configure_dofs!(model, bcs): src/bc.jl:198-233.  Returns (dof list, nu, bc setup)."""
-    active = sorted(set(model.conn.tolist()))
+    active = model.active_nodes().tolist()
     presc, setup = _setup_bcs(model, bcs)
     dofs = [(n, k) for n in active for k in range(model.ndim)]
     udofs = [d for d in dofs if not presc[d]]
@@ -685,6 +700,8 @@ def _facet_forces(model, facet, key, val, t=0.0):
     """mech_boundary_forces: src/mech/elem/distributed.jl:76-152"""
     ndim = model.ndim
     isedge = key in ("qx", "qy", "qz", "qn")
+    if isedge and model.stressmodel == AXISYM:  # distributed.jl:89
+        raise ValueError("mech_boundary_forces: boundary condition %s is not applicable in a axisymmetric analysis" % key)
     th = 1.0 if isedge else model.thickness
     Cc = model.coords[facet.nodes, :ndim]
     R, W = quadrature(facet.shape, 0)
@@ -757,8 +774,22 @@ def _body_forces(model, cell, key, val):
     return F.reshape(-1)
 
 
+def _no_dof(model, nodes):
+    """A node of no active element keeps eq_id 0 (Dof(), src/dof.jl:15-17), so the reference's U[dof.eq_id] and
+    F[map] raise a BoundsError there: the oracle raises too."""
+    bad = [n for n in np.atleast_1d(nodes) if model.eq_id[n, 0] < 0]
+    if bad:
+        raise ValueError("boundary condition on node %d, which belongs to no active element" % (bad[0] + 1))
+
+
 def get_bc_vals(model, setup, ndofs, t=0.0):
     """get_bc_vals(model, bcs): src/bc.jl:237-249 (compute_bc_vals! :43-58,116-136,175-194)."""
+    for bc, objs in setup:
+        if isinstance(bc, NodeBC):
+            _no_dof(model, objs)
+        else:
+            for f in objs:
+                _no_dof(model, f.nodes)
     U = np.zeros(ndofs)
     F = np.zeros(ndofs)
     names = model.dof_names
@@ -800,8 +831,9 @@ def get_bc_vals(model, setup, ndofs, t=0.0):
 # Staged Newton driver: src/mech/mech-solver.jl:155-492, src/solver.jl:82-198
 # --------------------------------------------------------------------------
 class Stage:
-    def __init__(self, bcs, nincs=1, nouts=0):
+    def __init__(self, bcs, nincs=1, nouts=0, toactivate=()):
         self.bcs, self.nincs, self.nouts, self.status = bcs, nincs, nouts, "pending"
+        self.toactivate = list(toactivate)  # element ids (src/stage.jl:8,16)
 
 
 class MechAnalysis:
@@ -810,9 +842,9 @@ class MechAnalysis:
         self.stages = []
         self.log = []
 
-    def addstage(self, bcs, nincs=1, nouts=0):
+    def addstage(self, bcs, nincs=1, nouts=0, toactivate=()):
         """addstage!: src/analysis.jl:27-32"""
-        self.stages.append(Stage(list(bcs), nincs, nouts))
+        self.stages.append(Stage(list(bcs), nincs, nouts, toactivate))
 
     def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
               autoinc=False, quiet=True, nthreads=1, record=None):
@@ -836,6 +868,7 @@ class MechAnalysis:
 
     def _stage(self, stage, tol, rtol, rspan, dT0, dTmin, dTmax, scheme, maxits, autoinc, nthreads, record):
         model = self.model
+        model.active[np.asarray(stage.toactivate, dtype=np.int64)] = True  # mech-solver.jl:216-219
         dofs, nu, setup = configure_dofs(model, stage.bcs)
         ndofs = len(dofs)
         dof_n = np.array([d[0] for d in dofs], dtype=np.int64)

@@ -11,7 +11,7 @@ import math
 
 import numpy as np
 
-from .core import configure_dofs, get_bc_vals, mount_K, quadrature, shape_deriv, shape_func, solve_system, \
+from .core import AXISYM, configure_dofs, get_bc_vals, mount_K, quadrature, shape_deriv, shape_func, solve_system, \
     update_state
 
 EPS = 2.220446049250313e-16
@@ -38,7 +38,10 @@ def elem_mass(model, e):
         detJ = np.linalg.det(J)
         if not detJ > 0.0:
             raise RuntimeError("Negative Jacobian determinant in cell %d" % (e + 1))
-        coef = rho * detJ * w[q] * model.thickness
+        th = model.thickness
+        if model.stressmodel == AXISYM:  # th = 2 pi r at the IP (mech-solid.jl:180)
+            th = 2 * math.pi * float(C[:, 0] @ N)
+        coef = rho * detJ * w[q] * th
         M += coef * (Nm.T @ Nm)
     mp = model.eq_id[nodes, :ndim].reshape(-1)
     return M, mp

@@ -59,7 +59,13 @@ typedef struct {
     const int64_t *eq_id;    /* nnodes x 3, 0-based, -1 when absent */
     const int64_t *ip_ptr;   /* nelem+1 offsets into state */
     double *state;           /* nip_total x ORC_ST_LEN */
+    const int64_t *active;   /* the active elements in id order (mech-solver.jl:216-220), or null: all */
+    int64_t nactive;
 } orc_model;
+
+/* the element loops of mount_K and update_state! run over active_elems */
+static int64_t n_active(const orc_model *m) { return m->active ? m->nactive : m->nelem; }
+static int64_t active_elem(const orc_model *m, int64_t i) { return m->active ? m->active[i] : i; }
 
 /* ------------------------------------------------------------------------ */
 /* Shapes: src/shape/lines.jl, solids2d.jl, solids3d.jl                      */
@@ -837,14 +843,15 @@ int orc_elem_stiffness(const orc_model *m, int64_t e, double *Ke, int64_t *map) 
  * negative status (-3 negative Jacobian, -1 bad element).
  */
 int64_t orc_mount_K_coo(const orc_model *m, int nthreads, int64_t *R, int64_t *C, double *V, int64_t *bad_elem) {
-    int64_t ne = m->nelem;
+    int64_t ne = n_active(m);
     int64_t *off = (int64_t *)malloc((ne + 1) * sizeof(int64_t));
     int64_t *cnt = (int64_t *)calloc(ne, sizeof(int64_t));
     int status = 0;
     off[0] = 0;
-    for (int64_t e = 0; e < ne; e++) {
+    for (int64_t i = 0; i < ne; i++) {
+        int64_t e = active_elem(m, i);
         int64_t nn = m->conn_ptr[e + 1] - m->conn_ptr[e];
-        off[e + 1] = off[e] + nn * m->ndim * nn * m->ndim;
+        off[i + 1] = off[i] + nn * m->ndim * nn * m->ndim;
     }
     *bad_elem = -1;
 #ifdef _OPENMP
@@ -857,7 +864,8 @@ int64_t orc_mount_K_coo(const orc_model *m, int nthreads, int64_t *R, int64_t *C
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
-        for (int64_t e = 0; e < ne; e++) {
+        for (int64_t i = 0; i < ne; i++) {
+            int64_t e = active_elem(m, i);
             int nd = orc_elem_stiffness(m, e, Ke, map);
             if (nd < 0) {
 #ifdef _OPENMP
@@ -868,28 +876,28 @@ int64_t orc_mount_K_coo(const orc_model *m, int nthreads, int64_t *R, int64_t *C
                 }
                 continue;
             }
-            int64_t k = off[e];
+            int64_t k = off[i];
             for (int i = 0; i < nd; i++)
                 for (int j = 0; j < nd; j++) {
                     double val = Ke[i * nd + j];
                     if (fabs(val) < 2.220446049250313e-16) continue; /* eps() */
                     R[k] = map[i]; C[k] = map[j]; V[k] = val; k++;
                 }
-            cnt[e] = k - off[e];
+            cnt[i] = k - off[i];
         }
         free(Ke);
     }
     if (status) { free(off); free(cnt); return status; }
     /* compact in element order */
     int64_t w = 0;
-    for (int64_t e = 0; e < ne; e++) {
-        int64_t s = off[e];
+    for (int64_t i = 0; i < ne; i++) {
+        int64_t s = off[i];
         if (w != s) {
-            memmove(R + w, R + s, cnt[e] * sizeof(int64_t));
-            memmove(C + w, C + s, cnt[e] * sizeof(int64_t));
-            memmove(V + w, V + s, cnt[e] * sizeof(double));
+            memmove(R + w, R + s, cnt[i] * sizeof(int64_t));
+            memmove(C + w, C + s, cnt[i] * sizeof(int64_t));
+            memmove(V + w, V + s, cnt[i] * sizeof(double));
         }
-        w += cnt[e];
+        w += cnt[i];
     }
     free(off); free(cnt);
     return w;
@@ -974,7 +982,7 @@ static int update_elem(orc_model *m, int64_t e, const double *U, double *dF, int
  * in thread order (its message in msg).
  */
 int orc_update_state(orc_model *m, int nthreads, int64_t ndofs, const double *U, double *dFin, char *msg, int msglen) {
-    int64_t ne = m->nelem;
+    int64_t ne = n_active(m);
     int nt = nthreads > 0 ? nthreads : 1;
     if (ne < nt) nt = (int)(ne > 0 ? ne : 1);
     double *part = (double *)calloc((size_t)nt * ndofs, sizeof(double));
@@ -988,8 +996,8 @@ int orc_update_state(orc_model *m, int nthreads, int64_t ndofs, const double *U,
         int64_t nmax = (tid == nt - 1) ? ne : (int64_t)(tid + 1) * (ne / nt);
         double dF[MAXND];
         int64_t map[MAXND];
-        for (int64_t e = nmin; e < nmax; e++) {
-            int nd = update_elem(m, e, U, dF, map, msgs + 256 * tid, 256);
+        for (int64_t i = nmin; i < nmax; i++) {
+            int nd = update_elem(m, active_elem(m, i), U, dF, map, msgs + 256 * tid, 256);
             if (nd < 0) { st[tid] = nd; break; }
             for (int i = 0; i < nd; i++) part[(size_t)tid * ndofs + map[i]] += dF[i];
         }

@@ -14,7 +14,7 @@ Plain Python loops: meant for meshes of a few thousand nodes.
 """
 import numpy as np
 
-from .core import D3, PLANESTRESS, DRUCKER_PRAGER, VON_MISES, HEX8, HEX20, QUAD4, QUAD8, QUAD9, TET4, TET10, TRI3, \
+from .core import AXISYM, D3, PLANESTRESS, DRUCKER_PRAGER, VON_MISES, HEX8, HEX20, QUAD4, QUAD8, QUAD9, TET4, TET10, TRI3, \
     TRI6, quadrature, shape_func
 
 SR2 = 1.4142135623730951  # src/tools/constants.jl:3
@@ -25,6 +25,7 @@ CORNERS = {HEX8: 8, HEX20: 8, TET4: 4, TET10: 4, QUAD4: 4, QUAD8: 4, QUAD9: 4, T
 BASE_3D = ["σxx", "σyy", "σzz", "σyz", "σxz", "σxy", "σvm", "σ1", "σ2", "σ3",
            "εxx", "εyy", "εzz", "εyz", "εxz", "εxy"]
 BASE_2D = ["σxx", "σyy", "σzz", "σyz", "σxz", "σxy", "σvm", "σ1", "σ3", "εxx", "εyy", "εzz", "εxy"]
+BASE_AXI = ["σrr", "σyy", "σtt", "σry", "σvm", "εrr", "εyy", "εtt", "εry"]  # tensors.jl:182-193
 
 
 def J2(s):
@@ -42,7 +43,7 @@ def eigvals(s):
 
 def field_names(stressmodel, mat):
     """Keys of ip_state_vals for one material under one stress model, in the reference's order."""
-    base = BASE_3D if stressmodel == D3 else BASE_2D
+    base = BASE_3D if stressmodel == D3 else (BASE_AXI if stressmodel == AXISYM else BASE_2D)
     if mat == VON_MISES:
         return base + (["ep", "j1", "srj2d"] if stressmodel == PLANESTRESS else ["ep"])
     if mat == DRUCKER_PRAGER:
@@ -57,7 +58,10 @@ def ip_state_vals(stressmodel, mat, st):
     L = eigvals(s)
     d = {"σxx": s[0], "σyy": s[1], "σzz": s[2], "σyz": s[3] / SR2, "σxz": s[4] / SR2, "σxy": s[5] / SR2,
          "σvm": svm}
-    if stressmodel == D3:
+    if stressmodel == AXISYM:
+        d.update({"σrr": s[0], "σtt": s[2], "σry": s[5] / SR2, "εrr": e[0], "εyy": e[1], "εtt": e[2],
+                  "εry": e[5] / SR2})
+    elif stressmodel == D3:
         d.update({"σ1": L[0], "σ2": L[1], "σ3": L[2], "εxx": e[0], "εyy": e[1], "εzz": e[2],
                   "εyz": e[3] / SR2, "εxz": e[4] / SR2, "εxy": e[5] / SR2})
     else:

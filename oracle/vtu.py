@@ -1,10 +1,15 @@
 """Oracle restatement of Amaru.jl's VTU writer (test infrastructure only).
 
-save_vtu (src/mesh/io.jl:167-274) in ascii format, get_array_node! (:117-158) and the XML writer
-(src/tools/xml.jl:250-318), and the node_data / elem_data that update_output_data!
+save_vtu (src/mesh/io.jl:167-274) in ascii format and with compress=true, get_array_node! (:117-158) and
+the XML writer (src/tools/xml.jl:250-318), and the node_data / elem_data that update_output_data!
 (src/fe-model.jl:341-427) gives a model on this path.  Plain Python string building: meant for small
-models.
+models.  The compressed form deflates with Python's zlib at level 4 and the zlib stream defaults
+(window 15, memory level 8, default strategy), the settings of the reference's ZlibCompressorStream
+(CodecZlib).
 """
+import struct
+import zlib
+
 import numpy as np
 
 TAB = "   "
@@ -51,9 +56,29 @@ def data_array(name, a, level):
     return out
 
 
-def save_vtu(coords, conn_ptr, conn, shapes, node_data, elem_data):
-    """-> the file's text.  node_data / elem_data: lists of (name, array) in order."""
+def appended_array(name, a, level, buf):
+    """get_array_node! with compressed=true: a self-closing DataArray with format "appended" and the offset
+    of its block in buf, to which it appends the UInt64 header (1, size, size, compressed size) and the
+    zlib stream of the array's row-major bytes."""
+    a = np.asarray(a)
+    ncomp = 1 if a.ndim == 1 else a.shape[1]
+    node = TAB * level + '<DataArray type="%s" Name="%s" NumberOfComponents="%d" format="appended" offset="%d"/>\n' % (
+        TYPES[a.dtype], name, ncomp, len(buf))
+    raw = np.ascontiguousarray(a).tobytes()
+    z = zlib.compress(raw, 4)
+    buf += struct.pack("<4Q", 1, len(raw), len(raw), len(z)) + z
+    return node
+
+
+def save_vtu(coords, conn_ptr, conn, shapes, node_data, elem_data, compress=False):
+    """-> the file's text (bytes when compress).  node_data / elem_data: lists of (name, array) in order."""
     nn, ne = len(coords), len(shapes)
+    buf = bytearray()
+    if compress:
+        def data_array(name, a, level):  # noqa: F811  (the appended form)
+            return appended_array(name, a, level, buf)
+    else:
+        data_array = globals()["data_array"]
     s = '<?xml version="1.0" encoding="UTF-8"?>\n'
     s += "<!-- File generated by Amaru Finite Element Code -->\n"
     s += ('<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian" header_type="UInt64" '
@@ -78,8 +103,11 @@ def save_vtu(coords, conn_ptr, conn, shapes, node_data, elem_data):
         for k, v in arrs:
             s += data_array(k, v, 4)
         s += TAB * 3 + "</%s>\n" % tag
-    s += TAB * 2 + "</Piece>\n" + TAB + "</UnstructuredGrid>\n" + "</VTKFile>\n"
-    return s
+    s += TAB * 2 + "</Piece>\n" + TAB + "</UnstructuredGrid>\n"
+    if not compress:
+        return s + "</VTKFile>\n"
+    s += TAB + '<AppendedData encoding="raw">\n'
+    return s.encode("utf-8") + b"_" + bytes(buf) + b"\n" + (TAB + "</AppendedData>\n</VTKFile>\n").encode("utf-8")
 
 
 def output_data(ndim, nnodes, shapes, eq_id, U, F, V_rec, fields):

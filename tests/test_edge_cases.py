@@ -118,7 +118,6 @@ def _desc(**over):
     ("bad quadrature", -1, "integration points"),
     ("E not positive", -1, "E > 0"),
     ("nu at 0.5", -1, "nu < 0.5"),
-    ("axisymmetric", -10, "axisymmetric"),
     ("plane strain in 3-D", -1, "d3 stress model"),
     ("unknown material", -10, "material"),
     ("no elements", -1, "empty model"),
@@ -136,10 +135,6 @@ def test_bad_descriptions_are_refused(case, code, words):
         d["mat_params"][1, 0] = 0.0
     elif case == "nu at 0.5":
         d["mat_params"][0, 1] = 0.5
-    elif case == "axisymmetric":
-        mesh = A.Mesh(A.Block([[0, 0], [1.0, 0.2]], nx=2, ny=1, cellshape=A.QUAD4))
-        d = _desc(ndim=2, stressmodel=3, coords=mesh.coords, shape=mesh.shape.copy(), conn_ptr=mesh.conn_ptr.copy(),
-                  conn=mesh.conn.copy())
     elif case == "plane strain in 3-D":
         d["stressmodel"] = 1
     elif case == "unknown material":

@@ -227,7 +227,6 @@ def _desc(ndim=3, stressmodel=_lib.D3, thickness=1.0, **over):
 
 @pytest.mark.parametrize("kw,code,words", [
     (dict(ndim=4), -1, "ndim must be 2 or 3"),
-    (dict(ndim=2, stressmodel=_lib.AXISYMMETRIC), -10, "axisymmetric"),
     (dict(stressmodel=_lib.PLANESTRAIN), -1, "d3 stress model"),
     (dict(ndim=2, stressmodel=_lib.PLANESTRESS, thickness=0.0), -1, "thickness must be > 0"),
     (dict(ndim=2, stressmodel=_lib.PLANESTRAIN, thickness=float("nan")), -1, "thickness must be > 0"),

@@ -83,6 +83,35 @@ def test_gpu_modes_match_the_oracle(shape, n, nips):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape, n, nips, nmodes", [(A.HEX8, (3, 16, 3), 0, 24), (A.QUAD8, (4, 30), 0, 42)])
+def test_gpu_many_modes_match_the_oracle(shape, n, nips, nmodes):
+    """Blocks wider than one launch of the multi-vector kernels (24 modes: block 36; 42 modes, the
+    largest: block 63) against the oracle, frequencies to 1e-8 and the non-degenerate modes to 1e-5."""
+    sm = "planestrain" if len(n) == 2 else "d3"
+    mo, mg = _mesh(O, shape, n), _mesh(A, shape, n)
+    mg.coords = np.ascontiguousarray(mo.coords)
+    om = O.FEModel(mo, [("all", O.LinearElastic(**MAT))], stressmodel=sm, nips=nips)
+    gm = A.FEModel(mg, [("all", A.LinearElastic(**MAT))], A.MechContext(stressmodel=sm), nips=nips)
+    w, V, nu = O.modal(om, _bcs(O, len(n)), nmodes)
+    ana = A.ModalAnalysis(gm)
+    ana.addstage(_bcs(A, len(n)))
+    assert ana.solve(nmodes=nmodes, tol=1e-8, max_iters=3000)[0]
+    assert ana.modes.shape == (nu, nmodes)
+    assert np.abs(ana.freqs - w).max() <= 1e-8 * w.max(), (ana.freqs, w)
+    assert _same_modes(V, ana.modes, w, 1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_modal_block_limit_is_refused():
+    gm = A.FEModel(_mesh(A, A.QUAD4, (4, 40)), [("all", A.LinearElastic(**MAT))],
+                   A.MechContext(stressmodel="planestrain"))
+    ana = A.ModalAnalysis(gm)
+    ana.addstage(_bcs(A, 2))
+    with pytest.raises(Exception, match="nmodes must be in 1..42"):
+        ana.solve(nmodes=43)
+
+
+@pytest.mark.gpu
 def test_gpu_modal_residual_at_size():
     """HEX20 40x8x8 cantilever (about 73 k DOFs, 27 IPs): P v = lambda v for the returned pairs."""
     mesh = A.Mesh(A.Block([[0, 0, 0], [4.0, 0.8, 0.8]], nx=40, ny=8, nz=8, cellshape=A.HEX20))

@@ -145,7 +145,7 @@ def test_axisymmetric(shape):
     """test/mech/elem/axisymmetric.jl: the axisymmetric block [0,1]^2 (4x4 cells, E=100, nu=0.2, axis x=0 with
     ux=0, base uy=0, ty=-10 on top) equals its 3-D revolution at node (1, 1) to 1e-3.  Uniaxial compression is
     homogeneous, so both equal the exact u_r = nu*10/E = 0.02, u_y = -10/E = -0.1, which the restatement must
-    give.  (The GPU path refuses axisymmetric analyses.)"""
+    give."""
     mesh = O.Mesh(O.Block([[0, 0], [1, 1]], nx=4, ny=4, cellshape=shape))
     om = O.FEModel(mesh, [("all", O.LinearElastic(E=100.0, nu=0.2))], stressmodel="axisymmetric")
     ana = O.MechAnalysis(om)
