@@ -773,12 +773,15 @@ class BatchAnalysis:
         return self.joined.dev.autotune()
 
     def solve(self, tol=0.01, rtol=0.01, rspan=0.01, dT0=0.01, dTmin=1e-7, dTmax=0.1, scheme="FE", maxits=5,
-              autoinc=False, quiet=True, linear_rtol=1e-8, refine_every=32, max_iters=20000):
-        """solve!(ana; args...) for every part; returns a list of (success, message), one per part."""
+              autoinc=False, quiet=True, linear_rtol=1e-8, refine_every=32, max_iters=20000, solver="mixed"):
+        """solve!(ana; args...) for every part; returns a list of (success, message), one per part.  solver:
+        "mixed" (per-part block-Jacobi PCG, one persistent launch) or "amg" (per-part PCG preconditioned by
+        the joined model's multigrid V-cycle)."""
         checkargs("solve!", MECH_SOLVER_PARAMS, MECH_SOLVER_VALUES, tol=tol, rspan=rspan, rtol=rtol, dT0=dT0,
                   dTmin=dTmin, dTmax=dTmax, maxits=maxits, scheme=scheme)
         J = self.joined
-        lin = L.default_solve_opts(method=L.SOLVER_MIXED, rtol=linear_rtol, refine_every=refine_every,
+        method = {"mixed": L.SOLVER_MIXED, "amg": L.SOLVER_AMG}[solver]
+        lin = L.default_solve_opts(method=method, rtol=linear_rtol, refine_every=refine_every,
                                    max_iters=max_iters)
         result = [(True, "")] * len(self.models)
         failed = np.zeros(len(self.models), dtype=bool)

@@ -847,7 +847,12 @@ __global__ void k_dense_mv(int64_t nc, const V *Cinv, const V *b, V *x) {
     const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (r >= nc) return;
     V s = V(0);
-    for (int64_t c = lane; c < nc; c += 32) s = vfma(Cinv[r * nc + c], b[c], s);
+    // zero entries skipped: the inverse of a block-diagonal level (the parts of a batch) is block
+    // diagonal, and a part's non-finite values must not reach the others through 0 * inf
+    for (int64_t c = lane; c < nc; c += 32) {
+        const V a = Cinv[r * nc + c];
+        if (a != V(0)) s = vfma(a, b[c], s);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) x[r] = s;

@@ -17,6 +17,12 @@
 //   and replayed until every part has finished its stage.
 // * Autotuner: elements per CTA of the element kernels and resident CTAs per SM
 //   of the batched solve, timed on the model itself.
+// * Multigrid solve (AMR_SOLVER_AMG): no element joins two parts, so neither do the
+//   aggregates, prolongators and Galerkin products of the joined model's aggregation
+//   multigrid: one V-cycle of the joined model preconditions every part at once.  The
+//   PCG around it keeps its scalars per part (dot products per part, in a fixed order)
+//   and its state per part (iterating, refreshing the FP64 residual, done); one
+//   iteration of all parts is one CUDA graph, replayed until no part runs.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -697,6 +703,289 @@ __global__ void k_ip_commit(int64_t nip, const int32_t *ip_part, const PartCtl *
     }
 }
 
+// ---------------------------------------------------------------------------
+// Multigrid-preconditioned batched PCG: per-part state and kernels.  A part is BA_REFRESH for one
+// iteration whenever its FP64 true residual is due (at the start, after a 100x drop of the recursive
+// residual norm, when it looks converged, or every kBaSince iterations): its FP32 correction is folded
+// into the FP64 solution and r = b - K64 x recomputed, instead of a CG step.  Every other running part
+// takes a CG step; the V-cycle serves both.  Convergence is judged on the true residual, as in the
+// whole-model multigrid solver.
+// ---------------------------------------------------------------------------
+enum { BA_DONE = 0, BA_ITER = 1, BA_REFRESH = 2 };
+constexpr int kBaSince = 64;
+
+struct PartAmg {
+    double rz, pq, alpha, beta, rr, rr_true, bnorm2;
+    int32_t state, iters, refreshes, since, first, status, initial, pad;
+};
+
+__global__ void k_ba_init(int64_t np, const uint8_t *active, PartAmg *pa) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    PartAmg a{};
+    a.state = (!active || active[p]) ? BA_REFRESH : BA_DONE;
+    a.first = 1;
+    a.initial = 1;
+    pa[p] = a;
+}
+
+__global__ void k_ba_stamp(StepInfo *step, int end) {
+    if (end) atomicMax(&step->t1, global_ns());
+    else atomicMin(&step->t0, global_ns());
+}
+
+template <int B>
+__global__ void k_ba_pupdate(int64_t nn, const int32_t *__restrict__ node_part, const PartAmg *__restrict__ pa,
+                             const float *__restrict__ z, float *__restrict__ p) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn * B) return;
+    const PartAmg &a = pa[node_part[i / B]];
+    if (a.state != BA_ITER) return;
+    p[i] = a.first ? z[i] : fmaf((float)a.beta, p[i], z[i]);
+}
+
+// q = K32 p on the rows of the iterating parts: a half-warp per row
+template <int B>
+__global__ void __launch_bounds__(256) k_ba_spmv(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
+                                                 const int32_t *__restrict__ cj, const float *__restrict__ K,
+                                                 const int32_t *__restrict__ node_part, const PartAmg *__restrict__ pa,
+                                                 const float *__restrict__ p, float *__restrict__ q) {
+    constexpr int G = 16;
+    const int lane = threadIdx.x % G;
+    const unsigned hmask = 0xffffu << (16 * ((threadIdx.x >> 4) & 1));
+    const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t row = grp; row < nn; row += ng) {
+        if (pa[node_part[row]].state != BA_ITER) continue;  // uniform over the half-warp
+        float acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0f;
+        for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += G) {
+            const int64_t j = cj[k];
+            float xv[B];
+#pragma unroll
+            for (int d = 0; d < B; d++) xv[d] = __ldg(p + j * B + d);
+#pragma unroll
+            for (int c = 0; c < B; c++)
+#pragma unroll
+                for (int d = 0; d < B; d++) acc[c] = fmaf(__ldcs(K + (int64_t)(c * B + d) * nb + k), xv[d], acc[c]);
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < B; c++) acc[c] += __shfl_down_sync(hmask, acc[c], o, G);
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < B; c++) q[row * B + c] = acc[c];
+    }
+}
+
+// sums of two per-slot products over a part's slots [i0, i1): FP64 per thread in slot order, then a
+// fixed tree over the CTA; every thread receives the totals
+__device__ void ba_part_sums(int64_t i0, int64_t i1, const float *a, const float *b, const float *c,
+                             const float *d, double &s0, double &s1, double *sh) {
+    double v0 = 0.0, v1 = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        v0 += (double)a[i] * (double)b[i];
+        if (c) v1 += (double)c[i] * (double)d[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        v0 += __shfl_down_sync(0xffffffffu, v0, o);
+        v1 += __shfl_down_sync(0xffffffffu, v1, o);
+    }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[w] = v0; sh[32 + w] = v1; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int k = 0; k < nw; k++) { t0 += sh[k]; t1 += sh[32 + k]; }
+        sh[64] = t0;
+        sh[65] = t1;
+    }
+    __syncthreads();
+    s0 = sh[64];
+    s1 = sh[65];
+    __syncthreads();
+}
+
+// alpha = rz / p.q of every iterating part (CTA per part)
+__global__ void __launch_bounds__(256) k_ba_pq(int64_t np, int B, const int64_t *__restrict__ part_ptr,
+                                               const float *__restrict__ p, const float *__restrict__ q, PartAmg *pa) {
+    __shared__ double sh[66];
+    for (int64_t part = blockIdx.x; part < np; part += gridDim.x) {
+        if (pa[part].state != BA_ITER) continue;  // uniform over the CTA
+        double pq, unused;
+        ba_part_sums(part_ptr[part] * B, part_ptr[part + 1] * B, p, q, nullptr, nullptr, pq, unused, sh);
+        if (threadIdx.x == 0) {
+            PartAmg &a = pa[part];
+            if (!(pq > 0.0)) {  // breakdown (or NaN)
+                a.status = AMR_ENOCONV;
+                a.state = BA_DONE;
+            } else {
+                a.pq = pq;
+                a.alpha = a.rz / pq;
+                a.first = 0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int B>
+__global__ void k_ba_update(int64_t nn, const int32_t *__restrict__ node_part, const PartAmg *__restrict__ pa,
+                            const float *__restrict__ p, const float *__restrict__ q, float *__restrict__ x32,
+                            float *__restrict__ r32) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn * B) return;
+    const PartAmg &a = pa[node_part[i / B]];
+    if (a.state != BA_ITER) return;
+    const float al = (float)a.alpha;
+    x32[i] = fmaf(al, p[i], x32[i]);
+    r32[i] = fmaf(-al, q[i], r32[i]);
+}
+
+// refreshing parts: x += x32 at free slots, x32 = 0
+template <int B>
+__global__ void k_ba_fold(int64_t nn, const int32_t *__restrict__ node_part, const PartAmg *__restrict__ pa,
+                          const uint8_t *__restrict__ fm, float *__restrict__ x32, double *__restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn * B) return;
+    if (pa[node_part[i / B]].state != BA_REFRESH) return;
+    if (fm[i]) x[i] += (double)x32[i];
+    x32[i] = 0.0f;
+}
+
+// refreshing parts' rows: r = b - K64 x at free slots (0 at prescribed ones), reac = (K64 x) at prescribed
+// slots, r32 = r; four lanes per row
+template <int B>
+__global__ void __launch_bounds__(256) k_ba_refine(int64_t nn, int64_t nb, const int64_t *__restrict__ rp,
+                                                   const int32_t *__restrict__ cj, const double *__restrict__ A,
+                                                   const uint8_t *__restrict__ fm, const int32_t *__restrict__ node_part,
+                                                   const PartAmg *__restrict__ pa, const double *__restrict__ b,
+                                                   const double *__restrict__ x, double *__restrict__ reac,
+                                                   float *__restrict__ r32) {
+    constexpr int L = 4, RPW = 32 / L;
+    const int lane = threadIdx.x & 31, sub = lane & (L - 1);
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t n0 = warp * RPW; n0 < nn; n0 += nw * RPW) {  // whole warps: every lane reaches the shuffles
+        const int64_t n = n0 + lane / L;
+        const bool valid = n < nn && pa[node_part[n < nn ? n : 0]].state == BA_REFRESH;
+        double acc[B];
+#pragma unroll
+        for (int c = 0; c < B; c++) acc[c] = 0.0;
+        if (valid)
+            for (int64_t k = rp[n] + sub; k < rp[n + 1]; k += L) {
+                const int64_t j = __ldg(cj + k);
+                double xv[B];
+#pragma unroll
+                for (int d = 0; d < B; d++) xv[d] = __ldg(x + j * B + d);
+#pragma unroll
+                for (int c = 0; c < B; c++)
+#pragma unroll
+                    for (int d = 0; d < B; d++) acc[c] = fma(__ldg(A + (int64_t)(c * B + d) * nb + k), xv[d], acc[c]);
+            }
+#pragma unroll
+        for (int c = 0; c < B; c++)
+#pragma unroll
+            for (int o = L / 2; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+        if (valid && sub == 0)
+#pragma unroll
+            for (int c = 0; c < B; c++) {
+                const int64_t i = n * B + c;
+                double res = 0.0;
+                if (fm[i]) res = b[i] - acc[c];
+                else if (reac) reac[i] = acc[c];
+                r32[i] = (float)res;
+            }
+    }
+}
+
+// after the V-cycle: r.z and |r|^2 per running part (CTA per part), and its next state
+__global__ void __launch_bounds__(256) k_ba_rz(int64_t np, int B, const int64_t *__restrict__ part_ptr,
+                                               const float *__restrict__ r, const float *__restrict__ z, PartAmg *pa,
+                                               double stop_rel, double delta2, double tol2, int max_iters) {
+    __shared__ double sh[66];
+    for (int64_t part = blockIdx.x; part < np; part += gridDim.x) {
+        const int state = pa[part].state;
+        if (state == BA_DONE) continue;  // uniform over the CTA
+        double rz, rr;
+        ba_part_sums(part_ptr[part] * B, part_ptr[part + 1] * B, r, z, r, r, rz, rr, sh);
+        if (threadIdx.x == 0) {
+            PartAmg &a = pa[part];
+            if (state == BA_ITER) {
+                a.beta = rz / a.rz;
+                a.rz = rz;
+                a.rr = rr;
+                a.iters++;
+                a.since++;
+                if (isnan(rr)) { a.status = AMR_ENOCONV; a.state = BA_DONE; }
+                else if (!(rr > stop_rel * a.bnorm2) || rr <= delta2 * a.rr_true || a.since >= kBaSince) a.state = BA_REFRESH;
+                else if (a.iters >= max_iters) { a.status = AMR_ENOCONV; a.state = BA_DONE; }
+            } else {  // the true residual of a refresh
+                a.rz = rz;
+                a.rr = rr;
+                a.rr_true = rr;
+                if (a.initial) { a.bnorm2 = rr; a.initial = 0; }
+                else a.refreshes++;
+                a.since = 0;
+                if (isnan(rr)) { a.status = AMR_ENOCONV; a.state = BA_DONE; }
+                else if (!(a.bnorm2 > 0.0) || rr <= tol2 * a.bnorm2) a.state = BA_DONE;
+                else if (a.iters >= max_iters) { a.status = AMR_ENOCONV; a.state = BA_DONE; }
+                else a.state = BA_ITER;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// parts still running and the largest iteration count
+__global__ void k_ba_summary(int64_t np, const PartAmg *pa, int32_t *out) {
+    __shared__ int run, its;
+    if (threadIdx.x == 0) { run = 0; its = 0; }
+    __syncthreads();
+    int r = 0, m = 0;
+    for (int64_t p = threadIdx.x; p < np; p += blockDim.x) {
+        if (pa[p].state != BA_DONE) r++;
+        m = max(m, pa[p].iters);
+    }
+    atomicAdd(&run, r);
+    atomicMax(&its, m);
+    __syncthreads();
+    if (threadIdx.x == 0) { out[0] = run; out[1] = its; }
+}
+
+// the parts' results into the part statistics (CTA per part of the solve)
+__global__ void __launch_bounds__(256) k_ba_finish(int64_t np, int B, const int64_t *__restrict__ part_ptr,
+                                                   const uint8_t *__restrict__ active, const uint8_t *__restrict__ fm,
+                                                   const double *__restrict__ x, PartAmg *pa, PartStat *stat,
+                                                   int abort) {
+    __shared__ double sh[32];
+    for (int64_t part = blockIdx.x; part < np; part += gridDim.x) {
+        if (active && !active[part]) continue;
+        double um = 0.0;
+        for (int64_t i = part_ptr[part] * B + threadIdx.x; i < part_ptr[part + 1] * B; i += blockDim.x)
+            if (fm[i]) um = fmax(um, absnan(x[i]));
+        for (int o = 16; o > 0; o >>= 1) um = fmax(um, __shfl_down_sync(0xffffffffu, um, o));
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = um;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < (int)(blockDim.x >> 5); k++) um = fmax(um, sh[k]);
+            PartAmg &a = pa[part];
+            if (abort && a.state != BA_DONE) { a.status = AMR_ENOCONV; a.state = BA_DONE; }
+            PartStat s;
+            s.iters = a.iters;
+            s.refreshes = a.refreshes;
+            s.status = a.status;
+            s.pad = 0;
+            s.rel_residual = a.bnorm2 > 0.0 ? sqrt(a.rr_true / a.bnorm2) : 0.0;
+            s.umax = fmax(um, sh[0]);
+            stat[part] = s;
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 struct AmrBatch {
@@ -711,6 +1000,8 @@ struct AmrBatch {
     StepInfo *step = nullptr, *h_step = nullptr;
     unsigned long long *counter = nullptr;
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+    PartAmg *pamg = nullptr;         // per-part state of the multigrid solve
+    int32_t *bsum = nullptr, *h_bsum = nullptr;  // its summary: parts running, largest iteration count
     int ctas_per_sm = 2;  // until tuned: the residency the kernel is compiled for
     std::vector<PartCtl> h_ctl;
     std::vector<PartStat> h_stat;
@@ -725,7 +1016,9 @@ void amr_batch_free(amr_model *m) {
     amr_free(b->ip_part); amr_free(b->stat); amr_free(b->ctl); amr_free(b->active); amr_free(b->perr);
     amr_free(b->step); amr_free(b->counter);
     amr_free(b->x32); amr_free(b->r32); amr_free(b->z32); amr_free(b->p32); amr_free(b->q32);
+    amr_free(b->pamg); amr_free(b->bsum);
     amr_pinned_free(b->h_step);
+    amr_pinned_free(b->h_bsum);
     delete b;
     m->batch = nullptr;
 }
@@ -830,13 +1123,123 @@ void launch_pcg(amr_model *m, const PcgArgs &a, int ctas_per_sm) {
     AMR_CUDA(cudaGetLastError());
 }
 
+struct GraphScope {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    ~GraphScope() {
+        if (x) cudaGraphExecDestroy(x);
+        if (g) cudaGraphDestroy(g);
+    }
+};
+
+constexpr int kBaEvery = 4;  // iterations of the multigrid solve between host checks
+
+// The multigrid-preconditioned solve of every part (the active ones when active is given): x (free slots)
+// updated in place from b, reactions at the prescribed slots; the parts' results into the part statistics.
+// The iteration is captured as a CUDA graph once per call and replayed kBaEvery times between host checks.
+void batch_solve_amg(amr_model *m, double *x, const double *b_, double *reac, const amr_solve_opts &o,
+                     const uint8_t *active, StepInfo *step) {
+    AmrBatch *b = m->batch;
+    cudaStream_t s = m->stream;
+    const int64_t np = b->nparts, nn = m->nnodes, n = nn * m->B;
+    const int B = m->B;
+    amr_amg_prepare(m);
+    if (!b->pamg) {
+        amr_alloc(&b->pamg, np);
+        amr_alloc(&b->bsum, 2);
+        b->h_bsum = (int32_t *)amr_pinned_alloc(2 * sizeof(int32_t));
+    }
+    if (step) {
+        k_ba_stamp<<<1, 1, 0, s>>>(step, 0);
+        AMR_COUNT(1);
+    }
+    k_ba_init<<<nblk(np, 128), 128, 0, s>>>(np, active, b->pamg);
+    AMR_COUNT(1);
+    // every vector starts finite: the V-cycle runs over all parts, running or not
+    for (float *v : {b->x32, b->p32, b->r32, b->z32, b->q32}) AMR_CUDA(cudaMemsetAsync(v, 0, n * sizeof(float), s));
+    const double tol2 = o.rtol * o.rtol, stop_rel = 0.0625 * tol2, delta2 = 1e-4;
+    const int max_iters = o.max_iters > 0 ? o.max_iters : 20000;
+    const unsigned gs = nblk(n, 256), gsp = (unsigned)std::min<int64_t>(nblk(nn * 16, 256), (int64_t)device_sms() * 8);
+    const unsigned gr = (unsigned)std::min<int64_t>(nblk(nn * 8, 256), (int64_t)device_sms() * 8);
+    const unsigned gparts = (unsigned)std::min<int64_t>(np, (int64_t)device_sms() * 8);
+    auto one = [&]() {
+        if (B == 3) {
+            k_ba_pupdate<3><<<gs, 256, 0, s>>>(nn, b->node_part, b->pamg, b->z32, b->p32);
+            k_ba_spmv<3><<<gsp, 256, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K32, b->node_part, b->pamg, b->p32, b->q32);
+        } else {
+            k_ba_pupdate<2><<<gs, 256, 0, s>>>(nn, b->node_part, b->pamg, b->z32, b->p32);
+            k_ba_spmv<2><<<gsp, 256, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K32, b->node_part, b->pamg, b->p32, b->q32);
+        }
+        k_ba_pq<<<gparts, 256, 0, s>>>(np, B, b->part_ptr, b->p32, b->q32, b->pamg);
+        if (B == 3) {
+            k_ba_update<3><<<gs, 256, 0, s>>>(nn, b->node_part, b->pamg, b->p32, b->q32, b->x32, b->r32);
+            k_ba_fold<3><<<gs, 256, 0, s>>>(nn, b->node_part, b->pamg, m->free_mask, b->x32, x);
+            k_ba_refine<3><<<gr, 256, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b->node_part,
+                                               b->pamg, b_, x, reac, b->r32);
+        } else {
+            k_ba_update<2><<<gs, 256, 0, s>>>(nn, b->node_part, b->pamg, b->p32, b->q32, b->x32, b->r32);
+            k_ba_fold<2><<<gs, 256, 0, s>>>(nn, b->node_part, b->pamg, m->free_mask, b->x32, x);
+            k_ba_refine<2><<<gr, 256, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b->node_part,
+                                               b->pamg, b_, x, reac, b->r32);
+        }
+        AMR_COUNT(6);
+        amr_amg_vcycle(m, b->r32, b->z32);
+        k_ba_rz<<<gparts, 256, 0, s>>>(np, B, b->part_ptr, b->r32, b->z32, b->pamg, stop_rel, delta2, tol2, max_iters);
+        AMR_COUNT(1);
+        AMR_CUDA(cudaGetLastError());
+    };
+    GraphScope gr_;
+    const long long before = amr_g_launches.load();
+    AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    try {
+        one();
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        throw;
+    }
+    AMR_CUDA(cudaStreamEndCapture(s, &gr_.g));
+    const long long per_iter = amr_g_launches.load() - before;
+    AMR_COUNT(-per_iter);
+    AMR_CUDA(cudaGraphInstantiate(&gr_.x, gr_.g, 0));
+    // every part alternates CG steps and refreshes, so it is done within 2 max_iters + 2 iterations
+    const long long cap = 2LL * max_iters + 2;
+    long long done_iters = 0;
+    bool abort = false;
+    for (;;) {
+        for (int i = 0; i < kBaEvery; i++) {
+            AMR_CUDA(cudaGraphLaunch(gr_.x, s));
+            AMR_COUNT(per_iter);
+        }
+        done_iters += kBaEvery;
+        k_ba_summary<<<1, 256, 0, s>>>(np, b->pamg, b->bsum);
+        AMR_COUNT(1);
+        AMR_CUDA(cudaMemcpyAsync(b->h_bsum, b->bsum, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        if (b->h_bsum[0] == 0) break;
+        if (done_iters >= cap) { abort = true; break; }
+    }
+    k_ba_finish<<<gparts, 256, 0, s>>>(np, B, b->part_ptr, active, m->free_mask, x, b->pamg, b->stat, abort ? 1 : 0);
+    AMR_COUNT(1);
+    if (step) {
+        k_ba_stamp<<<1, 1, 0, s>>>(step, 1);
+        AMR_COUNT(1);
+    }
+    AMR_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 AmrSolveResult amr_batch_solve(amr_model *m, double *x, const double *b_, double *reac, const amr_solve_opts &o) {
     AmrBatch *b = m->batch;
     AmrSolveResult res{AMR_OK, 0, 0, 0.0, 0.0};
+    if (o.method != AMR_SOLVER_MIXED && o.method != AMR_SOLVER_AMG)
+        throw AmrError(AMR_EUNSUPPORTED, "batched solves use the mixed-precision solver, block-Jacobi or multigrid");
     AMR_CUDA(cudaEventRecord(m->ev0, m->stream));
-    launch_pcg(m, pcg_args(m, x, b_, reac, o, nullptr), b->ctas_per_sm);
+    if (o.method == AMR_SOLVER_AMG) batch_solve_amg(m, x, b_, reac, o, nullptr, nullptr);
+    else launch_pcg(m, pcg_args(m, x, b_, reac, o, nullptr), b->ctas_per_sm);
     AMR_CUDA(cudaEventRecord(m->ev1, m->stream));
     AMR_CUDA(cudaMemcpyAsync(b->h_stat.data(), b->stat, b->nparts * sizeof(PartStat), cudaMemcpyDeviceToHost,
                              m->stream));
@@ -875,15 +1278,6 @@ struct MaskScope {
     }
 };
 
-struct GraphScope {
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t x = nullptr;
-    ~GraphScope() {
-        if (x) cudaGraphExecDestroy(x);
-        if (g) cudaGraphDestroy(g);
-    }
-};
-
 }  // namespace
 
 int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const amr_stage_params &prm, double *U,
@@ -901,8 +1295,10 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
     }
     const bool corrector = prm.scheme != AMR_SCHEME_FE;
     if (prm.maxits < 1 || prm.nincs < 1) throw AmrError(AMR_EINVAL, "bad stage parameters");
-    if (prm.linear.method != AMR_SOLVER_MIXED)
-        throw AmrError(AMR_EUNSUPPORTED, "batched stages use the mixed-precision solver");
+    if (prm.linear.method != AMR_SOLVER_MIXED && prm.linear.method != AMR_SOLVER_AMG)
+        throw AmrError(AMR_EUNSUPPORTED, "batched stages use the mixed-precision solver, block-Jacobi or multigrid");
+    // the multigrid solve runs its own graph with host checks: its Newton iterations run uncaptured
+    const bool amg = prm.linear.method == AMR_SOLVER_AMG;
     const int64_t n = m->nnodes * m->B, np = b->nparts;
     std::vector<double *> v(10, nullptr);
     double *Ks = nullptr;  // the predictor's tangent, kept for the weighted corrector tangent
@@ -977,6 +1373,10 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
 
     MaskScope mask(m, b);
     GraphScope gr;
+    auto solve = [&](const PcgArgs &a) {
+        if (amg) batch_solve_amg(m, a.x, a.b, a.reac, prm.linear, b->active, b->step);
+        else launch_pcg(m, a, b->ctas_per_sm);
+    };
     // one Newton iteration of every running part
     auto iteration = [&]() {
         AMR_CUDA(cudaMemsetAsync(&b->step->t0, 0xff, sizeof(unsigned long long), s));
@@ -986,7 +1386,7 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
         AMR_COUNT(2);
         // the tangent at the current states (a corrector left the weighted one in K: mount it again)
         if (m->any_plastic || corrector) amr_stiffness(m);
-        launch_pcg(m, pa, b->ctas_per_sm);
+        solve(pa);
         k_ctl_mid<<<gp, 128, 0, s>>>(np, b->ctl, b->stat, b->active);
         k_slot_mid<<<gs, 256, 0, s>>>(sa);
         AMR_COUNT(2);
@@ -1000,7 +1400,8 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
             amr_combine_K(m, a1, Ks, a2);
             k_slot_corr<<<gs, 256, 0, s>>>(sa);
             AMR_COUNT(1);
-            launch_pcg(m, pc, b->ctas_per_sm);
+            if (amg) amr_amg_invalidate(m);  // K is the weighted tangent now
+            solve(pc);
             k_ctl_mid<<<gp, 128, 0, s>>>(np, b->ctl, b->stat, b->active);
             k_slot_mid2<<<gs, 256, 0, s>>>(sa);
             AMR_COUNT(2);
@@ -1015,28 +1416,35 @@ int amr_batch_stage(amr_model *m, const double *Uex, const double *Fex, const am
         AMR_CUDA(cudaGetLastError());
     };
     // capture it once; count its kernels per replay instead of at capture
-    const long long before = amr_g_launches.load();
-    AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-    try {
-        iteration();
-    } catch (...) {
-        cudaGraph_t g = nullptr;
-        cudaStreamEndCapture(s, &g);
-        if (g) cudaGraphDestroy(g);
-        cudaGetLastError();
-        throw;
+    long long per_iter = 0;
+    if (!amg) {
+        const long long before = amr_g_launches.load();
+        AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        try {
+            iteration();
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            throw;
+        }
+        AMR_CUDA(cudaStreamEndCapture(s, &gr.g));
+        per_iter = amr_g_launches.load() - before;
+        AMR_COUNT(-per_iter);
+        AMR_CUDA(cudaGraphInstantiate(&gr.x, gr.g, 0));
     }
-    AMR_CUDA(cudaStreamEndCapture(s, &gr.g));
-    const long long per_iter = amr_g_launches.load() - before;
-    AMR_COUNT(-per_iter);
-    AMR_CUDA(cudaGraphInstantiate(&gr.x, gr.g, 0));
 
     double solve_s = 0.0;
     int steps = 0;
     const int max_steps = 1000000;
     for (;;) {
-        AMR_CUDA(cudaGraphLaunch(gr.x, s));
-        AMR_COUNT(per_iter);
+        if (amg) {
+            iteration();
+        } else {
+            AMR_CUDA(cudaGraphLaunch(gr.x, s));
+            AMR_COUNT(per_iter);
+        }
         AMR_CUDA(cudaMemcpyAsync(b->h_step, b->step, sizeof(StepInfo), cudaMemcpyDeviceToHost, s));
         AMR_CUDA(cudaStreamSynchronize(s));
         if (b->h_step->t1 > b->h_step->t0) solve_s += (double)(b->h_step->t1 - b->h_step->t0) * 1e-9;

@@ -1117,7 +1117,8 @@ void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq) {
 }
 
 AmrSolveResult amr_solve_device(amr_model *m, double *x, const double *b, double *reac, const amr_solve_opts &o) {
-    if (m->batch && o.method == AMR_SOLVER_MIXED) return amr_batch_solve(m, x, b, reac, o);  // one CTA per part
+    if (m->batch && (o.method == AMR_SOLVER_MIXED || o.method == AMR_SOLVER_AMG))
+        return amr_batch_solve(m, x, b, reac, o);  // per part: one CTA each, or the joined multigrid
     if (o.method == AMR_SOLVER_AMG) return m->B == 3 ? solve_amg<3>(m, x, b, reac, o) : solve_amg<2>(m, x, b, reac, o);
     if (o.method == AMR_SOLVER_FP64) return m->B == 3 ? solve_fp64<3>(m, x, b, reac, o) : solve_fp64<2>(m, x, b, reac, o);
     if (o.method == AMR_SOLVER_AMG_FP64)

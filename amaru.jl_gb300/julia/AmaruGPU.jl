@@ -740,14 +740,16 @@ function GPUBatch(models::Vector{<:FEModel})
 end
 
 """
-    solve_batch!(b, stages; args...)
+    solve_batch!(b, stages; linear=:amg, args...)
 
 One stage per model (stages[i] for models[i]), run together: each model's DOFs are
 numbered by Amaru's configure_dofs! and its loads taken from get_bc_vals; the
-joined numbering puts every model's unknowns first.  Updates each model's dof
-values as mech_stage_solver! does and returns one status per model.
+joined numbering puts every model's unknowns first.  `linear` picks the per-part
+PCG's preconditioner: the joined model's multigrid V-cycle (:amg) or block-Jacobi
+in one persistent launch (:jacobi).  Updates each model's dof values as
+mech_stage_solver! does and returns one status per model.
 """
-function solve_batch!(b::GPUBatch, stages::Vector{Stage}; args...)
+function solve_batch!(b::GPUBatch, stages::Vector{Stage}; linear::Symbol=:amg, args...)
     args = Amaru.checkargs(args, Amaru.mech_solver_params)
     eqs, Us, Fs, nus, nds, dofss = [], [], [], Int[], Int[], []
     for (m, st) in zip(b.models, stages)
@@ -769,8 +771,9 @@ function solve_batch!(b::GPUBatch, stages::Vector{Stage}; args...)
     end
     ccall((:amr_set_dofs, LIB), Cint, (Ptr{Cvoid}, Ptr{Int64}, Int64, Int64), b.h, eq, ND, NU)
     scheme = Dict(:FE => 0, :ME => 1, :BE => 2, :Ralston => 3)[Symbol(args.scheme)]
+    method = linear === :jacobi ? Int32(0) : Int32(2)  # per-part block-Jacobi, or the joined multigrid
     p = StageParams(args.tol, args.rtol, args.rspan, args.dT0, args.dTmin, args.dTmax, scheme, args.maxits,
-                    args.autoinc, stages[1].nincs, stages[1].nouts, SolveOpts(0, 1e-8, 20000, 32))
+                    args.autoinc, stages[1].nincs, stages[1].nouts, SolveOpts(method, 1e-8, 20000, 32))
     U = zeros(ND); F = zeros(ND); stats = StageStats()
     ccall((:amr_stage_run, LIB), Cint,
           (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ref{StageParams}, Ptr{Float64}, Ptr{Float64}, Ref{StageStats}),

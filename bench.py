@@ -520,6 +520,11 @@ def dyn_leg(model, with_cpu):
                    "h2d_bytes": 4 * nd * 8, "d2h_bytes": 4 * nd * 8},
            "rhs_kernel": {"kernel": "k_dyn_rhs<3> (base + M x + (alpha M + beta K) y)", "avg_launch_s": rhs_t,
                           "bytes_per_launch": rhs_b, "achieved_gbs": rhs_b / rhs_t / 1e9}}
+    # FP64 work per launch: per block 2 B FMA on M (x and y) and B^2 on K; the FP64 pipe bounds it on GB300
+    fl = 2.0 * model.dev.sizes()["nblocks"] * (2 * 3 + 9)
+    pk = fp64_peak_tflops()
+    out["rhs_kernel"].update({"fp64_tflops": fl / rhs_t / 1e12, "fp64_peak_tflops": pk,
+                              "fp64_frac": fl / rhs_t / 1e12 / pk})
     if with_cpu:
         out["cpu_baseline"] = dyn_cpu_sample()
     return out
@@ -604,6 +609,8 @@ def _quad8_models(inst, cache, device):
 
 
 def batch_leg(count=512, steps=3):
+    """The batched stage of config 4 with the per-part multigrid-preconditioned PCG (the joined model's V-cycle)
+    and, beside it, with the per-part block-Jacobi PCG of one persistent launch."""
     import torch
     import amaru_gpu as A
     from amaru_gpu import _lib as L
@@ -621,47 +628,58 @@ def batch_leg(count=512, steps=3):
     tu = ba.autotune()
     J = ba.joined
     Uex, Fex = ba.configure(ba.stages[0].bcs)
-    p = L.default_stage_params(linear=L.default_solve_opts(method=L.SOLVER_MIXED, rtol=1e-8))
     dU, dF = torch.from_numpy(Uex).cuda(), torch.from_numpy(Fex).cuda()
     oU, oF = torch.zeros_like(dU), torch.zeros_like(dF)
-    secs, solve, launches = [], [], []
-    for r in range(steps + 1):
-        c0 = J.dev.launch_count()
-        rc, st = J.dev.stage_run_dev(dU.data_ptr(), dF.data_ptr(), p, oU.data_ptr(), oF.data_ptr())
-        if rc != 0:
-            raise RuntimeError(J.dev.last_error())
-        if r > 0:  # the first run is the warm-up
-            secs.append(st.seconds)
-            solve.append(st.solve_seconds)
-            launches.append(J.dev.launch_count() - c0)
-    ps = J.dev.part_stats()
-    kr = np.array([s.krylov_iterations for s in ps])
-    t = float(np.mean(secs))
-    # the same 32 models (every 16th) one at a time on their own handles, against the same 32 batched
-    samp = inst[::max(1, count // 32)][:32]
-    seq = 0.0
-    for m in _quad8_models(samp, cache, True):
-        setup = m.configure_dofs(bcs)
-        U0, F0 = m.get_bc_vals(setup)
-        m.dev.stage_run(U0, F0, p)
-        rc, _, _, s1 = m.dev.stage_run(U0, F0, p)
-        seq += s1.seconds
-        m.dev.close()
-    bs = A.BatchAnalysis(_quad8_models(samp, cache, False))
-    bs.addstage(bcs)
-    Us, Fs = bs.configure(bs.stages[0].bcs)
-    bs.joined.dev.stage_run(Us, Fs, p)
-    rc, _, _, s2 = bs.joined.dev.stage_run(Us, Fs, p)
-    return {"workload": "%d plane-strain QUAD8 models 2x1, n x n with n~U{10..60} (seed 0xC4), E lognormal(ln 200e3, "
-                        "0.2), nu~U[0.2,0.35], 9 IP, left edge fixed, unit tx on the right edge; one linear stage of "
-                        "every model in one batched stage (per-part PCG to 1e-8)" % count,
-            "models": count, "ndofs": int(J.ndofs), "ms_per_batch": t * 1e3, "solve_ms": float(np.mean(solve)) * 1e3,
-            "models_per_s": count / t, "dof_per_s": J.ndofs / t, "launches_per_batch": int(np.mean(launches)),
-            "krylov_iters_max": int(kr.max()), "krylov_iters_mean": float(kr.mean()),
-            "parts_converged": int(sum(s.status == 0 for s in ps)), "setup_s": setup_s,
-            "tuning": {"stiffness_epb": tu.stiffness_epb[0], "internal_epb": tu.internal_epb[0],
-                       "pcg_threads": tu.batch_threads, "pcg_ctas_per_sm": tu.batch_ctas_per_sm},
-            "sample_32": {"one_at_a_time_s": seq, "batched_s": s2.seconds, "speedup": seq / s2.seconds}}
+
+    def run(method):
+        p = L.default_stage_params(linear=L.default_solve_opts(method=method, rtol=1e-8))
+        secs, solve, launches = [], [], []
+        for r in range(steps + 1):
+            c0 = J.dev.launch_count()
+            rc, st = J.dev.stage_run_dev(dU.data_ptr(), dF.data_ptr(), p, oU.data_ptr(), oF.data_ptr())
+            if rc != 0:
+                raise RuntimeError(J.dev.last_error())
+            if r > 0:  # the first run is the warm-up
+                secs.append(st.seconds)
+                solve.append(st.solve_seconds)
+                launches.append(J.dev.launch_count() - c0)
+        ps = J.dev.part_stats()
+        kr = np.array([s.krylov_iterations for s in ps])
+        t = float(np.mean(secs))
+        out = {"ms_per_batch": t * 1e3, "solve_ms": float(np.mean(solve)) * 1e3, "models_per_s": count / t,
+               "dof_per_s": J.ndofs / t, "launches_per_batch": int(np.mean(launches)),
+               "krylov_iters_max": int(kr.max()), "krylov_iters_mean": float(kr.mean()),
+               "parts_converged": int(sum(s.status == 0 for s in ps))}
+        # the same 32 models (every 16th) one at a time on their own handles, against the same 32 batched
+        samp = inst[::max(1, count // 32)][:32]
+        seq = 0.0
+        for m in _quad8_models(samp, cache, True):
+            setup = m.configure_dofs(bcs)
+            U0, F0 = m.get_bc_vals(setup)
+            m.dev.stage_run(U0, F0, p)
+            rc, _, _, s1 = m.dev.stage_run(U0, F0, p)
+            seq += s1.seconds
+            m.dev.close()
+        bs = A.BatchAnalysis(_quad8_models(samp, cache, False))
+        bs.addstage(bcs)
+        Us, Fs = bs.configure(bs.stages[0].bcs)
+        bs.joined.dev.stage_run(Us, Fs, p)
+        rc, _, _, s2 = bs.joined.dev.stage_run(Us, Fs, p)
+        out["sample_32"] = {"one_at_a_time_s": seq, "batched_s": s2.seconds, "speedup": seq / s2.seconds}
+        return out
+
+    mg = run(L.SOLVER_AMG)
+    bj = run(L.SOLVER_MIXED)
+    out = {"workload": "%d plane-strain QUAD8 models 2x1, n x n with n~U{10..60} (seed 0xC4), E lognormal(ln 200e3, "
+                       "0.2), nu~U[0.2,0.35], 9 IP, left edge fixed, unit tx on the right edge; one linear stage of "
+                       "every model in one batched stage (per-part PCG to 1e-8 preconditioned by the joined model's "
+                       "multigrid V-cycle; block_jacobi: per-part block-Jacobi PCG in one persistent launch)" % count,
+           "models": count, "ndofs": int(J.ndofs), "solver": "multigrid", "setup_s": setup_s}
+    out.update(mg)
+    out["block_jacobi"] = bj
+    out["tuning"] = {"stiffness_epb": tu.stiffness_epb[0], "internal_epb": tu.internal_epb[0],
+                     "pcg_threads": tu.batch_threads, "pcg_ctas_per_sm": tu.batch_ctas_per_sm}
+    return out
 
 
 # ---------------------------------------------------------------------------
