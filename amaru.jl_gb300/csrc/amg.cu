@@ -166,6 +166,8 @@ struct AmrAmg {
     std::vector<AmgLevel> L;
     int64_t nc = 0;             // DOFs of the dense coarsest level
     double *Cd = nullptr;       // nc x 2nc FP64 work (Gauss-Jordan)
+    double *gjf = nullptr;      // nc: the row factors of one Gauss-Jordan step
+    cudaGraphExec_t gj_exec = nullptr;  // the Gauss-Jordan steps, captured once
     float *Cinv = nullptr;      // nc x nc inverse, FP32 cycle
     double *Cinv64 = nullptr;   // nc x nc inverse, FP64 cycle
     double *scratch = nullptr;  // norms: [0] result, [8..] per-CTA partials
@@ -214,7 +216,8 @@ void amr_amg_free(amr_model *m) {
         amr_free(v.diag); amr_free(v.agg); amr_free(v.aptr); amr_free(v.anodes);
         amr_free(v.cptr); amr_free(v.ck); amr_free(v.ci); amr_free(v.null_dof);
     }
-    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
+    if (g->gj_exec) cudaGraphExecDestroy(g->gj_exec);
+    amr_free(g->Cd); amr_free(g->gjf); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
     amr_free(g->A16); amr_free(g->rs); amr_free(g->xt);
     delete g;
     m->amg = nullptr;
@@ -407,7 +410,9 @@ static void amg_build_structure(amr_model *m) {
         g->L.push_back(lv);
         H.push_back(std::move(hc));
     }
+    if (g->nc > 32768) throw AmrError(AMR_EUNSUPPORTED, "the multigrid's coarsest level is too large to invert densely");
     amr_alloc(&g->Cd, (size_t)g->nc * 2 * g->nc);  // [A | I] for Gauss-Jordan
+    amr_alloc(&g->gjf, g->nc);
     amr_alloc(&g->Cinv, (size_t)g->nc * g->nc);
     amr_alloc(&g->scratch, 8 + kNormCtas);
     amr_alloc(&g->ticket, 1);
@@ -818,15 +823,24 @@ __global__ void k_dense_init(int64_t nc, double *C) {  // C is nc x 2nc: [A | I]
     const int64_t r = t / (2 * nc), c = t % (2 * nc);
     C[t] = (c >= nc && c - nc == r) ? 1.0 : 0.0;
 }
-// one Gauss-Jordan step on pivot p of an SPD matrix (no pivoting needed): rows r != p
-__global__ void k_gj_eliminate(int64_t nc, int64_t p, double *C) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// one Gauss-Jordan step on pivot p of an SPD matrix (no pivoting needed): the row factors
+// f_r = C[r][p] / C[p][p] (0 for the pivot row), one division per row
+__global__ void k_gj_factor(int64_t nc, int64_t p, const double *C, double *f) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nc) return;
     const int64_t w = 2 * nc;
-    if (t >= nc * w) return;
-    const int64_t r = t / w, c = t % w;
-    if (r == p || c == p) return;
-    const double f = C[r * w + p] / C[p * w + p];
-    C[r * w + c] -= f * C[p * w + c];
+    f[r] = (r == p) ? 0.0 : C[r * w + p] / C[p * w + p];
+}
+// then C[r][c] -= f_r C[p][c] for c != p; a grid row per matrix row, and rows with f_r = 0 (every row outside
+// the pivot's block when the level is block diagonal, as for the parts of a batch) are left as they are
+__global__ void k_gj_eliminate(int64_t nc, int64_t p, const double *f, double *C) {
+    const int64_t r = blockIdx.y;
+    const double fr = f[r];
+    if (fr == 0.0) return;
+    const int64_t w = 2 * nc;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w || c == p) return;
+    C[r * w + c] -= fr * C[p * w + c];
 }
 __global__ void k_gj_column(int64_t nc, int64_t p, double *C) {  // clear column p below/above the pivot
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -919,11 +933,13 @@ int sm_count() {
     return sms;
 }
 
-// the FP32 cycle's fine residual r = b - K x from the FP16 copy
+// the FP32 cycle's fine residual r = b - K x from the FP16 copy.  One wave of resident CTAs (the grid-stride
+// loop covers the rows): its registers allow 3 CTAs per SM, and a grid of 8 per SM left a partial last wave.
 template <int NB>
 void launch_res16(amr_model *m, const AmrAmg *g, const AmgLevel &L, const typename FineX<NB>::T *xt, const float *b,
                   float *r) {
-    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
+    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256),
+                                                      amr_resident_grid((const void *)k_bsr_res16<NB>, 256, 8));
     k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r);
     AMR_COUNT(1);
 }
@@ -933,10 +949,12 @@ template <int NB, class V>
 void bsr_res(cudaStream_t s, const AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask, const V *x, const V *b,
              V *out) {
     if constexpr (std::is_same<V, float>::value) {
-        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256), (int64_t)sm_count() * 8);
+        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256),
+                                                          amr_resident_grid((const void *)k_bsr_res<NB>, 256, 8));
         k_bsr_res<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, x, b, out);
     } else {
-        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
+        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256),
+                                                          amr_resident_grid((const void *)k_bsr_res64<NB>, 256, 8));
         k_bsr_res64<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, mask, x, b, out);
     }
     AMR_COUNT(1);
@@ -1093,11 +1111,27 @@ struct Cycle {
         k_dense_init<<<nblk(nc * w, 256), 256, 0, s>>>(nc, g->Cd);
         k_dense_expand<NM, V><<<nblk(D.n, 128), 128, 0, s>>>(D.n, D.rp, D.cj, vals<V>(D).A, D.nbs, g->Cd, nc);
         AMR_COUNT(2);
-        for (int64_t p = 0; p < nc; p++) {
-            k_gj_eliminate<<<nblk(nc * w, 256), 256, 0, s>>>(nc, p, g->Cd);
-            k_gj_column<<<nblk(nc, 256), 256, 0, s>>>(nc, p, g->Cd);
+        // the nc pivot steps as one CUDA graph, captured once per hierarchy (its buffers are fixed)
+        if (!g->gj_exec) {
+            cudaGraph_t gr = nullptr;
+            AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+            for (int64_t p = 0; p < nc; p++) {
+                k_gj_factor<<<nblk(nc, 256), 256, 0, s>>>(nc, p, g->Cd, g->gjf);
+                k_gj_eliminate<<<dim3(nblk(w, 256), (unsigned)nc), 256, 0, s>>>(nc, p, g->gjf, g->Cd);
+                k_gj_column<<<nblk(nc, 256), 256, 0, s>>>(nc, p, g->Cd);
+            }
+            const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+            if (ce == cudaSuccess) {
+                const cudaError_t ie = cudaGraphInstantiate(&g->gj_exec, gr, 0);
+                cudaGraphDestroy(gr);
+                AMR_CUDA(ie);
+            } else {
+                if (gr) cudaGraphDestroy(gr);
+                AMR_CUDA(ce);
+            }
         }
-        AMR_COUNT(2 * nc);
+        AMR_CUDA(cudaGraphLaunch(g->gj_exec, s));
+        AMR_COUNT(3 * nc);
         k_dense_extract<V><<<nblk(nc * nc, 256), 256, 0, s>>>(nc, g->Cd, coarse_inverse(g));
         AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());

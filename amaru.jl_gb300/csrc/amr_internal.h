@@ -241,6 +241,10 @@ double amr_norm_inf(amr_model *m, const double *v, const uint8_t *mask_or_null);
 void amr_eq_to_nm(amr_model *m, const double *d_eq, double *d_nm);  // scatter eq_id-ordered -> node-major (0 elsewhere)
 void amr_nm_to_eq(amr_model *m, const double *d_nm, double *d_eq);
 // amg.cu: multigrid preconditioner (structure per DOF numbering, values per assembly)
+// CTAs of `threads` threads that `kernel` keeps resident on the current device at once, at most cap_per_sm per
+// SM: the grid of a grid-stride kernel, so that its rows are spread over one wave (a partial last wave leaves
+// SMs idle).  Cached per kernel and device.
+unsigned amr_resident_grid(const void *kernel, int threads, int cap_per_sm);
 void amr_amg_prepare(amr_model *m);
 void amr_amg_vcycle(amr_model *m, const float *r, float *z);
 void amr_amg_prepare64(amr_model *m);                           // the same hierarchy in FP64

@@ -241,6 +241,23 @@ double round_sig3(double x) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+unsigned amr_resident_grid(const void *kernel, int threads, int cap_per_sm) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int64_t>, unsigned> cache;
+    int dev = 0;
+    AMR_CUDA(cudaGetDevice(&dev));
+    const int64_t key = ((int64_t)dev << 32) | ((int64_t)threads << 8) | (int64_t)(cap_per_sm & 0xff);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find({kernel, key});
+    if (it != cache.end()) return it->second;
+    int sms = 0, per = 0;
+    AMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    AMR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0));
+    const unsigned g = (unsigned)sms * (unsigned)std::max(1, std::min(per, cap_per_sm));
+    cache[{kernel, key}] = g;
+    return g;
+}
+
 extern "C" {
 
 const char *amr_create_error(void) { return g_create_error.c_str(); }

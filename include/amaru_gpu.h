@@ -443,14 +443,16 @@ typedef struct {
     int32_t iterations, block;
     double max_residual, seconds;
 } amr_modal_stats;
-/* omega: nmodes values; modes: nu x nmodes, column-major, in eq_id order (may be null). */
+/* omega: nmodes values; modes: nu x nmodes, column-major, in eq_id order (may be null).  stats are
+ * written also when LOBPCG stops without converging (AMR_ENOCONV): its iterations and residual. */
 int amr_modal_run(amr_model *m, const amr_modal_params *p, double *omega, double *modes, amr_modal_stats *stats);
 void amr_default_modal_params(amr_modal_params *p);
 
 /* ---- VTU output ----
  * save(model, "file.vtu") -> save_vtu (src/mesh/io.jl:167-274, ascii) with the XML writer of
  * src/tools/xml.jl:250-318, byte for byte: the model's points and cells, then the point and cell
- * arrays in the caller's order (update_output_data!'s node_data / elem_data). */
+ * arrays in the caller's order (update_output_data!'s node_data / elem_data).  The tag columns
+ * save_vtu adds for tagged elements (tag-s1, tag-s2, tag) are cell arrays the caller passes. */
 enum { AMR_VTU_FLOAT64 = 0, AMR_VTU_INT32 = 1, AMR_VTU_INT64 = 2, AMR_VTU_UINT64 = 3 };
 typedef struct {
     const char *name;        /* DataArray Name */
