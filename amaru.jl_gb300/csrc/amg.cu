@@ -933,13 +933,12 @@ int sm_count() {
     return sms;
 }
 
-// the FP32 cycle's fine residual r = b - K x from the FP16 copy.  One wave of resident CTAs (the grid-stride
-// loop covers the rows): its registers allow 3 CTAs per SM, and a grid of 8 per SM left a partial last wave.
+// the FP32 cycle's fine residual r = b - K x from the FP16 copy.  Its registers allow 3 CTAs per SM; a grid of
+// 8 per SM (2.67 waves) measured faster than one resident wave.
 template <int NB>
 void launch_res16(amr_model *m, const AmrAmg *g, const AmgLevel &L, const typename FineX<NB>::T *xt, const float *b,
                   float *r) {
-    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256),
-                                                      amr_resident_grid((const void *)k_bsr_res16<NB>, 256, 8));
+    const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
     k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r);
     AMR_COUNT(1);
 }
@@ -949,12 +948,10 @@ template <int NB, class V>
 void bsr_res(cudaStream_t s, const AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask, const V *x, const V *b,
              V *out) {
     if constexpr (std::is_same<V, float>::value) {
-        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256),
-                                                          amr_resident_grid((const void *)k_bsr_res<NB>, 256, 8));
+        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256), (int64_t)sm_count() * 8);
         k_bsr_res<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, x, b, out);
     } else {
-        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256),
-                                                          amr_resident_grid((const void *)k_bsr_res64<NB>, 256, 8));
+        const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
         k_bsr_res64<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, mask, x, b, out);
     }
     AMR_COUNT(1);

@@ -712,7 +712,9 @@ void amr_solver_free(amr_model *m) {
     m->sw = nullptr;
 }
 
-// the grid of a grid-stride kernel of kThreads threads: the CTAs it keeps resident (at most 8 per SM)
+// the grid of a grid-stride kernel of kThreads threads: the CTAs it keeps resident (at most 8 per SM).  The FP64
+// SpMV (FP64-pipe bound, 3 CTAs per SM) measured faster in one resident wave than in 8 CTAs per SM; the
+// HBM-bound FP32 and FP16 kernels measured slower, and keep 8 CTAs per SM.
 template <class K>
 static unsigned grid_of(K kernel) {
     return amr_resident_grid((const void *)kernel, kThreads, 8);
@@ -721,7 +723,7 @@ static unsigned grid_of(K kernel) {
 template <int B>
 static void launch_spmv32(amr_model *m, AmrSolveWork *w, const float *p, float *q) {
     using PT = typename DirVec<B>::T;
-    k_spmv32v<B><<<grid_of(k_spmv32v<B>), kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol,
+    k_spmv32v<B><<<(unsigned)w->grid_spmv, kThreads, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol,
                                                                       m->K32, reinterpret_cast<const PT *>(p), q,
                                                                       w->ctl, w->partials);
     AMR_COUNT(1);
@@ -752,7 +754,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     // free slots of x start at zero (the reduced system's initial guess)
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     unsigned g = (unsigned)w->grid;
-    k_refine<B><<<grid_of(k_refine<B>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac, w->r32,
+    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac, w->r32,
                                        w->z32, m->Minv32, w->ctl, w->partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
@@ -773,7 +775,7 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
             k_fold<B><<<nblk(w->n, 256), 256, 0, s>>>(nn, m->free_mask, w->x32, x);
             AMR_COUNT(1);
             AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
-            k_refine<B><<<grid_of(k_refine<B>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
                                                reac, w->r32, w->z32, m->Minv32, w->ctl, w->partials, 0, tol2);
             AMR_COUNT(1);
             res.refinements++;
@@ -825,7 +827,7 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     const unsigned g = (unsigned)w->grid;
     auto refresh = [&](int first) {
-        k_refine<B><<<grid_of(k_refine<B>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac,
+        k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x, reac,
                                            w->r32, w->z32, m->Minv32, w->ctl, w->partials, first, tol2);
         amr_amg_vcycle(m, w->r32, w->z32);
         k_rz32<B><<<g, kThreads, 0, s>>>(nn, w->r32, w->z32, w->ctl, w->partials, 0.0, 0.0, 1);
@@ -923,7 +925,7 @@ static AmrSolveResult solve_fp64(amr_model *m, double *x, const double *b, doubl
     }
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     const unsigned g = (unsigned)w->grid;
-    k_refine<B, double><<<grid_of(k_refine<B, double>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+    k_refine<B, double><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
                                                reac, w->r64, w->z64, m->Minv64, w->ctl, w->partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
@@ -938,7 +940,7 @@ static AmrSolveResult solve_fp64(amr_model *m, double *x, const double *b, doubl
         if (c.iters >= o.max_iters) { res.status = AMR_ENOCONV; break; }
         if (c.stop) {  // the recursive residual looks converged: check the true one
             AMR_CUDA(cudaMemsetAsync(&w->ctl->stop, 0, sizeof(int32_t), s));
-            k_refine<B, double><<<grid_of(k_refine<B, double>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b,
+            k_refine<B, double><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b,
                                                        x, reac, w->r64, w->z64, m->Minv64, w->ctl, w->partials, 0,
                                                        tol2);
             AMR_COUNT(1);
@@ -991,7 +993,7 @@ static AmrSolveResult solve_amg_fp64(amr_model *m, double *x, const double *b, d
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     const unsigned g = (unsigned)w->grid;
     auto refresh = [&](int first) {
-        k_refine<B, double><<<grid_of(k_refine<B, double>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
+        k_refine<B, double><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, x,
                                                    reac, w->r64, w->z64, m->Minv64, w->ctl, w->partials, first, tol2);
         amr_amg_vcycle64(m, w->r64, w->z64);
         k_rz64<B><<<g, kThreads, 0, s>>>(nn, w->r64, w->z64, w->ctl, w->partials, 0.0, 1);
@@ -1185,7 +1187,7 @@ static double time_residual64(amr_model *m, int reps) {
     AMR_CUDA(cudaMemsetAsync(b, 0, w->n * sizeof(double), s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     for (int i = 0; i < reps; i++) {
-        k_refine<B><<<grid_of(k_refine<B>), kThreads, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, u,
+        k_refine<B><<<g, kThreads, 0, s>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b, u,
                                            nullptr, w->r32, w->z32, m->Minv32, w->ctl, w->partials, 1, 1e-16);
         AMR_COUNT(1);
     }
@@ -1310,7 +1312,7 @@ AmrSolveResult solve_mixed_noalloc(amr_model *m, const NoAllocView &w, int grid,
     AMR_CUDA(cudaMemcpyAsync(w.ctl, &hc, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     AMR_CUDA(cudaEventRecord(m->ev0, s));
     const unsigned g = (unsigned)grid;
-    k_refine<B><<<grid_of(k_refine<B>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x, w.reac,
+    k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x, w.reac,
                                        w.r32, w.z32, m->Minv32, w.ctl, w.partials, 1, tol2);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
@@ -1329,7 +1331,7 @@ AmrSolveResult solve_mixed_noalloc(amr_model *m, const NoAllocView &w, int grid,
             k_fold<B><<<nblk(n, 256), 256, 0, s>>>(nn, m->free_mask, w.x32, w.x);
             AMR_COUNT(1);
             AMR_CUDA(cudaMemsetAsync(&w.ctl->stop, 0, sizeof(int32_t), s));
-            k_refine<B><<<grid_of(k_refine<B>), kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x,
+            k_refine<B><<<g, kThreads, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, w.b, w.x,
                                                w.reac, w.r32, w.z32, m->Minv32, w.ctl, w.partials, 0, tol2);
             AMR_COUNT(1);
             res.refinements++;
