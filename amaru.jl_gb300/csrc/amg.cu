@@ -179,6 +179,10 @@ struct AmrAmg {
     // largest diagonal entry, so |A16| <= 1 for an SPD K and the copy is exactly symmetric.  The residual
     // r = b - K x is then rs_i sum_j A16_ij xt_j with xt = x rs kept, one 16-byte gather per block, by the
     // smoother and the prolongation of that level.
+    // fine-level row gate of the FP32 cycle (nnodes bytes, null: every row): rows with 0 are skipped by the
+    // fine level's smoothing, residual, restriction and prolongation (their values go stale); set by the
+    // batched solve to the rows of its running parts, whose V-cycle is block diagonal over the parts
+    const uint8_t *gate = nullptr;
     __half *A16 = nullptr;      // SoA [B*B][bstride]
     float *rs = nullptr;        // nnodes: 1 / s_n
     float *xt = nullptr;        // nnodes x 4 (3-D) or x 2 (2-D): x rs
@@ -671,13 +675,15 @@ __global__ void __launch_bounds__(256) k_bsr_res16(int64_t n, const int64_t *__r
                                                    const int32_t *__restrict__ cj, const __half *__restrict__ A,
                                                    int64_t nbs, const float *__restrict__ rs,
                                                    const typename FineX<NB>::T *__restrict__ xt,
-                                                   const float *__restrict__ b, float *__restrict__ out) {
+                                                   const float *__restrict__ b, float *__restrict__ out,
+                                                   const uint8_t *__restrict__ gate) {
     constexpr int G = 4;
     const int lane = threadIdx.x % G;
     const unsigned gmask = 0xfu << (G * ((threadIdx.x & 31) / G));
     const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
     const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
     for (int64_t row = grp; row < n; row += ng) {
+        if (gate && !gate[row]) continue;  // uniform over the row's lanes
         float acc[NB];
 #pragma unroll
         for (int c = 0; c < NB; c++) acc[c] = 0.0f;
@@ -731,9 +737,9 @@ __global__ void __launch_bounds__(256) k_bsr_res16(int64_t n, const int64_t *__r
 template <int NB, class V>
 __global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Dinv, const V *__restrict__ r,
                        V *__restrict__ d, V *__restrict__ x, const float *__restrict__ rs = nullptr,
-                       typename FineX<NB>::T *__restrict__ xt = nullptr) {
+                       typename FineX<NB>::T *__restrict__ xt = nullptr, const uint8_t *__restrict__ gate = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (gate && !gate[i])) return;
     V rv[NB], xn[NB];
 #pragma unroll
     for (int c = 0; c < NB; c++) rv[c] = r[i * NB + c];
@@ -757,10 +763,12 @@ __global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Di
 
 // bc[a] = sum over the aggregate's nodes (in order) of T_i' r_i; warp per aggregate
 template <int NB, int NM, class V>
-__global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anodes, const V *T, const V *r, V *bc) {
+__global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anodes, const V *T, const V *r, V *bc,
+                           const uint8_t *gate = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (a >= na) return;
+    if (gate && !gate[anodes[aptr[a]]]) return;  // an aggregate lies in one part (uniform over the warp)
     V acc[NM];
 #pragma unroll
     for (int m = 0; m < NM; m++) acc[m] = V(0);
@@ -786,9 +794,9 @@ __global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anode
 // x_i += T_i xc[agg(i)]  (and xt_i = rs_i x_i on the fine level of the FP32 cycle)
 template <int NB, int NM, class V>
 __global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc, V *x, const float *rs = nullptr,
-                          typename FineX<NB>::T *xt = nullptr) {
+                          typename FineX<NB>::T *xt = nullptr, const uint8_t *gate = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (gate && !gate[i])) return;
     const int64_t a = agg[i];
     float v[NB];
 #pragma unroll
@@ -939,7 +947,7 @@ template <int NB>
 void launch_res16(amr_model *m, const AmrAmg *g, const AmgLevel &L, const typename FineX<NB>::T *xt, const float *b,
                   float *r) {
     const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
-    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r);
+    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r, g->gate);
     AMR_COUNT(1);
 }
 
@@ -1013,6 +1021,7 @@ struct Cycle {
         const bool half = kHalf && l == 0;
         XT *xt = half ? reinterpret_cast<XT *>(g->xt) : nullptr;
         const float *rs = half ? g->rs : nullptr;
+        const uint8_t *gate = half ? g->gate : nullptr;
         auto residual = [&]() {
             if constexpr (kHalf) {
                 if (half) {
@@ -1023,21 +1032,22 @@ struct Cycle {
             bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
         };
         // pre-smoothing from x = 0
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x, rs, xt);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x, rs, xt, gate);
         residual();
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, rs, xt);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, rs, xt, gate);
         // coarse correction
         residual();
         AmgLevel &C = g->L[l + 1];
         AmgVals<V> &cv = vals<V>(C);
-        k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r, cv.bv);
+        k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r, cv.bv,
+                                                                      gate);
         level(m, g, l + 1, cv.bv, cv.x);
-        k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt);
+        k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt, gate);
         // post-smoothing
         residual();
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x, rs, xt);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x, rs, xt, gate);
         residual();
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, nullptr, nullptr, gate);
         AMR_COUNT(7);
         AMR_CUDA(cudaGetLastError());
     }
@@ -1186,6 +1196,10 @@ void amr_amg_prepare64(amr_model *m) {
 }
 
 // z = V-cycle(r), fine-level node-major FP32 vectors, on the handle's stream
+void amr_amg_set_gate(amr_model *m, const uint8_t *gate) {
+    if (m->amg) m->amg->gate = gate;
+}
+
 void amr_amg_vcycle(amr_model *m, const float *r, float *z) {
     if (m->B == 3) Cycle<3, 6, float>::level(m, m->amg, 0, r, z);
     else Cycle<2, 3, float>::level(m, m->amg, 0, r, z);

@@ -729,6 +729,13 @@ __global__ void k_ba_init(int64_t np, const uint8_t *active, PartAmg *pa) {
     pa[p] = a;
 }
 
+// the fine-level rows the V-cycle works on: the nodes of running parts
+__global__ void k_ba_gate(int64_t nn, const int32_t *__restrict__ node_part, const PartAmg *__restrict__ pa,
+                          uint8_t *__restrict__ gate) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < nn) gate[n] = pa[node_part[n]].state != BA_DONE;
+}
+
 __global__ void k_ba_stamp(StepInfo *step, int end) {
     if (end) atomicMax(&step->t1, global_ns());
     else atomicMin(&step->t0, global_ns());
@@ -1001,6 +1008,7 @@ struct AmrBatch {
     unsigned long long *counter = nullptr;
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
     PartAmg *pamg = nullptr;         // per-part state of the multigrid solve
+    uint8_t *gate = nullptr;         // its fine-level row gate (nodes of running parts)
     int32_t *bsum = nullptr, *h_bsum = nullptr;  // its summary: parts running, largest iteration count
     int ctas_per_sm = 2;  // until tuned: the residency the kernel is compiled for
     std::vector<PartCtl> h_ctl;
@@ -1016,7 +1024,7 @@ void amr_batch_free(amr_model *m) {
     amr_free(b->ip_part); amr_free(b->stat); amr_free(b->ctl); amr_free(b->active); amr_free(b->perr);
     amr_free(b->step); amr_free(b->counter);
     amr_free(b->x32); amr_free(b->r32); amr_free(b->z32); amr_free(b->p32); amr_free(b->q32);
-    amr_free(b->pamg); amr_free(b->bsum);
+    amr_free(b->pamg); amr_free(b->bsum); amr_free(b->gate);
     amr_pinned_free(b->h_step);
     amr_pinned_free(b->h_bsum);
     delete b;
@@ -1146,6 +1154,7 @@ void batch_solve_amg(amr_model *m, double *x, const double *b_, double *reac, co
     amr_amg_prepare(m);
     if (!b->pamg) {
         amr_alloc(&b->pamg, np);
+        amr_alloc(&b->gate, nn);
         amr_alloc(&b->bsum, 2);
         b->h_bsum = (int32_t *)amr_pinned_alloc(2 * sizeof(int32_t));
     }
@@ -1182,13 +1191,19 @@ void batch_solve_amg(amr_model *m, double *x, const double *b_, double *reac, co
             k_ba_refine<2><<<gr, 256, 0, s>>>(nn, m->bstride, m->brow_ptr, m->bcol, m->K64, m->free_mask, b->node_part,
                                                b->pamg, b_, x, reac, b->r32);
         }
-        AMR_COUNT(6);
+        k_ba_gate<<<nblk(nn, 256), 256, 0, s>>>(nn, b->node_part, b->pamg, b->gate);
+        AMR_COUNT(7);
         amr_amg_vcycle(m, b->r32, b->z32);
         k_ba_rz<<<gparts, 256, 0, s>>>(np, B, b->part_ptr, b->r32, b->z32, b->pamg, stop_rel, delta2, tol2, max_iters);
         AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
     };
     GraphScope gr_;
+    struct GateScope {  // the cycle skips the rows of finished parts while this solve runs
+        amr_model *m;
+        GateScope(amr_model *m_, const uint8_t *g) : m(m_) { amr_amg_set_gate(m, g); }
+        ~GateScope() { amr_amg_set_gate(m, nullptr); }
+    } gate_scope(m, b->gate);
     const long long before = amr_g_launches.load();
     AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
     try {
