@@ -22,7 +22,7 @@ LINEAR_ELASTIC, VON_MISES, DRUCKER_PRAGER = 0, 1, 2
 LOAD_FACET, LOAD_BODY = 0, 1
 SOLVER_MIXED, SOLVER_FP64, SOLVER_AMG, SOLVER_AMG_FP64 = 0, 1, 2, 3
 ASSEMBLY_FAST, ASSEMBLY_REFERENCE = 0, 1
-KERNEL_SPMV32, KERNEL_RESIDUAL64, KERNEL_AMG_RESIDUAL, KERNEL_DYN_RHS = 0, 1, 5, 6
+KERNEL_SPMV32, KERNEL_RESIDUAL64, KERNEL_STIFFNESS, KERNEL_AMG_RESIDUAL, KERNEL_DYN_RHS = 0, 1, 2, 5, 6
 KERNEL_SPMV64, KERNEL_AMG_RESIDUAL64 = 7, 8
 PEAK_FP64_FMA, PEAK_FP32_FMA = 0, 1
 COUPLED_HYDRO, COUPLED_THERMO = 0, 1

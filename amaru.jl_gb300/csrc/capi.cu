@@ -1043,6 +1043,27 @@ int amr_time_kernel(amr_model *m, int32_t kernel, int32_t reps, double *avg_seco
         case AMR_KERNEL_DYN_RHS:
             t = amr_dyn_time_rhs(m, reps, &bytes);
             break;
+        case AMR_KERNEL_STIFFNESS: {  // the fast element kernels alone; the second output is their FP64 operations
+            if (m->assembly_mode != AMR_ASSEMBLY_FAST) throw AmrError(AMR_EINVAL, "time the fast assembly");
+            const int D = m->ndim;
+            for (const AmrGroup &g : m->groups) {
+                const double nen = g.nen, nip = g.nip, np = nen * (nen + 1) / 2;
+                // per IP: J and dN/dX (2 nen D^2 each), det and inverse (about 30), w g (nen D); per node pair:
+                // T_ab (an FMA per component per IP) and the lambda / mu combination (about 4 D^2)
+                const double per_elem = nip * (4.0 * nen * D * D + nen * D + 30.0) + np * (2.0 * D * D * nip + 4.0 * D * D);
+                bytes += per_elem * (double)g.count;
+            }
+            amr_stiffness_elements(m);  // warm-up
+            AMR_CUDA(cudaEventRecord(m->ev0, m->stream));
+            for (int i = 0; i < reps; i++) amr_stiffness_elements(m);
+            AMR_CUDA(cudaEventRecord(m->ev1, m->stream));
+            AMR_CUDA(cudaEventSynchronize(m->ev1));
+            float ms = 0.f;
+            AMR_CUDA(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+            t = ms * 1e-3 / reps;
+            if (int rc = amr_check_status(m)) throw AmrError(rc, "assembly failed");
+            break;
+        }
         default:
             throw AmrError(AMR_EINVAL, "kernel not timed by this entry point");
         }

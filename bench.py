@@ -300,6 +300,13 @@ def run_ours(a):
         dev.set_assembly(L.ASSEMBLY_FAST)
     assembly["fast_dof_per_s"] = ndofs / assembly["fast_s"]
     assembly["reference_order_dof_per_s"] = ndofs / assembly["reference_order_s"]
+    dev.assemble_K()  # K current again (the timing below reads it, and leaves it as it is)
+    st_t, st_fl = dev.time_kernel(L.KERNEL_STIFFNESS, 5)
+    pk64 = fp64_peak_tflops()
+    assembly["stiffness_kernel"] = {"kernel": "stiffness_kernel<3, 20> (pair-tensor element stiffness, FP64)",
+                                    "avg_launch_s": st_t, "fp64_flops_per_launch": st_fl,
+                                    "fp64_tflops": st_fl / st_t / 1e12, "fp64_peak_tflops": pk64,
+                                    "fp64_frac": st_fl / st_t / 1e12 / pk64}
 
     # e2e: the same step through the C ABI with host buffers (H2D inputs, D2H results inside)
     Uh = np.ascontiguousarray(Uex)

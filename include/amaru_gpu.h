@@ -368,7 +368,10 @@ int amr_autotune(amr_model *m, amr_tuning *out);
 /* Average device time of one launch of a hot kernel over `reps` launches,
  * timed with CUDA events on the handle's stream, and its algorithmic bytes
  * per launch.  Needs a preceding amr_assemble_K (and a solve for the SpMV). */
-enum { AMR_KERNEL_SPMV32 = 0, AMR_KERNEL_RESIDUAL64 = 1, AMR_KERNEL_STIFFNESS = 2, AMR_KERNEL_GATHER = 3,
+enum { AMR_KERNEL_SPMV32 = 0, AMR_KERNEL_RESIDUAL64 = 1,
+       AMR_KERNEL_STIFFNESS = 2 /* the fast element-stiffness kernels (no gather); bytes_per_launch returns their
+                                   FP64 operations per assembly instead of bytes */,
+       AMR_KERNEL_GATHER = 3,
        AMR_KERNEL_INTERNAL = 4, AMR_KERNEL_AMG_RESIDUAL = 5 /* the multigrid cycle's fine residual; after an AMG solve */,
        AMR_KERNEL_DYN_RHS = 6 /* base + M x + C y of the dynamic Newton loop; after amr_assemble_M */,
        AMR_KERNEL_SPMV64 = 7 /* the all-FP64 PCG's q = K64 p; after an AMR_SOLVER_FP64 solve */,
