@@ -175,6 +175,7 @@ SIGNATURES = {
     "amr_set_dofs": (C.c_int, [P, P, C.c_int64, C.c_int64]),
     "amr_set_youngs": (C.c_int, [P, P]),
     "amr_set_assembly": (C.c_int, [P, C.c_int32]),
+    "amr_set_amg_smoothing": (C.c_int, [P, C.c_int32]),
     "amr_assemble_K": (C.c_int, [P]),
     "amr_get_K_nnz": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "amr_get_K_csc": (C.c_int, [P, P, P, P]),
@@ -373,6 +374,11 @@ class DeviceModel:
     def set_assembly(self, mode):
         check(self.h, lib().amr_set_assembly(self.h, mode))
 
+    def set_amg_smoothing(self, on):
+        """Smoothed-aggregation prolongators (True, the default) or the tentative ones (False) for the
+        multigrid solvers (amr_set_amg_smoothing)."""
+        check(self.h, lib().amr_set_amg_smoothing(self.h, 1 if on else 0))
+
     def K_csc(self):
         """K as a scipy CSC matrix in eq_id order with the reference's stored-entry pattern."""
         import scipy.sparse as sp
@@ -428,11 +434,18 @@ class DeviceModel:
         check(self.h, lib().amr_solve(self.h, ptr(U), ptr(F), C.byref(o), C.byref(st)))
         return U, F, st
 
-    def stage_run(self, Uex, Fex, params):
+    def stage_run(self, Uex, Fex, params, out=None):
+        """out: (U, F) host arrays (ndofs float64, C-contiguous, e.g. views of pinned memory) to write into."""
         Uex = np.ascontiguousarray(Uex, dtype=np.float64)
         Fex = np.ascontiguousarray(Fex, dtype=np.float64)
-        U = np.zeros(self.ndofs)
-        F = np.zeros(self.ndofs)
+        if out is None:
+            U = np.zeros(self.ndofs)
+            F = np.zeros(self.ndofs)
+        else:
+            U, F = out
+            for a in (U, F):
+                if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.ndofs:
+                    raise ValueError("out arrays must be C-contiguous float64 of ndofs entries")
         st = StageStats()
         rc = lib().amr_stage_run(self.h, ptr(Uex), ptr(Fex), C.byref(params), ptr(U), ptr(F), C.byref(st))
         return rc, U, F, st

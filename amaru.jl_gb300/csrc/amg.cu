@@ -11,6 +11,13 @@
 // contribution list fixed at set-up, in a fixed order (no atomics).  The last
 // level (at most kDenseMax DOFs) is inverted densely.
 //
+// Smoothed aggregation (the default).  Each prolongator but the coarsest is
+// P = (I - w D^-1 A) T, w = 4 / (3 lambda), and the coarse operator P' A P is
+// formed on the device as P' (A P): A P per block of its pattern as a sum over
+// the row's blocks in order, then each coarse block as a sum over the fine rows
+// P reaches it from, in order.  The patterns of P, A P and P' A P and their
+// position maps are built on the host with the aggregation.
+//
 // Cycle.  V-cycle with a degree-2 Chebyshev smoother on the block-Jacobi
 // preconditioned operator (interval [lambda/30, 1.1 lambda], lambda estimated
 // by power iteration after each assembly) before and after the coarse
@@ -115,6 +122,16 @@ void sym_eig(int n, double *A, double *V, double *w) {
     for (int i = 0; i < n; i++) w[i] = A[i * n + i];
 }
 
+// f(a, e) on contiguous ranges of [0, n), one per thread (per-thread work arrays live in f)
+template <class F>
+void parallel_ranges(int64_t n, F f) {
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (n < 4096) nt = 1;
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++) th.emplace_back([&, t] { f(n * t / nt, n * (t + 1) / nt); });
+    for (auto &x : th) x.join();
+}
+
 template <class F>
 void parallel_for(int64_t n, F f) {
     unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -128,6 +145,105 @@ void parallel_for(int64_t n, F f) {
     for (auto &x : th) x.join();
 }
 
+// Patterns of the smoothed prolongator P = (I - w D^-1 A) T of one level (T: node i -> aggregate agg[i]),
+// of A P and of the coarse operator P' A P, with the maps their device builds read.
+struct SaPattern {
+    std::vector<int64_t> prp, pkp, qrp, ptp, crp;
+    std::vector<int32_t> pcj, pkk, qcj, qrow, pti, pts, ccj, crow;
+};
+
+// rows [0, n): out[r] = sorted distinct values that cand(r, push) pushes; two passes (count, fill)
+template <class C>
+void distinct_rows(int64_t n, int64_t nvals, C cand, std::vector<int64_t> &ptr, std::vector<int32_t> &col) {
+    ptr.assign(n + 1, 0);
+    parallel_ranges(n, [&](int64_t a, int64_t e) {
+        std::vector<int64_t> mark(nvals, -1);
+        for (int64_t r = a; r < e; r++) {
+            int64_t cnt = 0;
+            cand(r, [&](int32_t v) {
+                if (mark[v] != r) { mark[v] = r; cnt++; }
+            });
+            ptr[r + 1] = cnt;
+        }
+    });
+    for (int64_t r = 0; r < n; r++) ptr[r + 1] += ptr[r];
+    col.resize(ptr[n]);
+    parallel_ranges(n, [&](int64_t a, int64_t e) {
+        std::vector<int64_t> mark(nvals, -1);
+        for (int64_t r = a; r < e; r++) {
+            int32_t *o = col.data() + ptr[r];
+            int64_t cnt = 0;
+            cand(r, [&](int32_t v) {
+                if (mark[v] != r) { mark[v] = r; o[cnt++] = v; }
+            });
+            std::sort(o, o + cnt);
+        }
+    });
+}
+
+void sa_pattern(const HostLevel &h, const std::vector<int32_t> &agg, int64_t na, SaPattern &S) {
+    const int64_t n = h.n;
+    // P: row i reaches the aggregates of its neighbours
+    distinct_rows(n, na, [&](int64_t i, auto push) {
+        for (int64_t k = h.rp[i]; k < h.rp[i + 1]; k++) push(agg[h.cj[k]]);
+    }, S.prp, S.pcj);
+    const int64_t np = S.prp[n];
+    // each P block's blocks of A: the row's blocks whose column lies in that aggregate, in order
+    S.pkp.assign(np + 1, 0);
+    S.pkk.resize(h.rp[n]);
+    parallel_ranges(n, [&](int64_t a, int64_t e) {
+        for (int64_t i = a; i < e; i++) {
+            int64_t o = h.rp[i];
+            for (int64_t s = S.prp[i]; s < S.prp[i + 1]; s++) {
+                S.pkp[s] = o;
+                for (int64_t k = h.rp[i]; k < h.rp[i + 1]; k++)
+                    if (agg[h.cj[k]] == S.pcj[s]) S.pkk[o++] = (int32_t)k;
+            }
+        }
+    });
+    S.pkp[np] = h.rp[n];
+    // A P: row i reaches the aggregates of its neighbours' P rows
+    distinct_rows(n, na, [&](int64_t i, auto push) {
+        for (int64_t k = h.rp[i]; k < h.rp[i + 1]; k++) {
+            const int32_t j = h.cj[k];
+            for (int64_t t = S.prp[j]; t < S.prp[j + 1]; t++) push(S.pcj[t]);
+        }
+    }, S.qrp, S.qcj);
+    S.qrow.resize(S.qrp[n]);
+    parallel_for(n, [&](int64_t i) {
+        for (int64_t q = S.qrp[i]; q < S.qrp[i + 1]; q++) S.qrow[q] = (int32_t)i;
+    });
+    // P by columns, rows ascending
+    S.ptp.assign(na + 1, 0);
+    for (int64_t s = 0; s < np; s++) S.ptp[S.pcj[s] + 1]++;
+    for (int64_t c = 0; c < na; c++) S.ptp[c + 1] += S.ptp[c];
+    S.pti.resize(np);
+    S.pts.resize(np);
+    {
+        std::vector<int64_t> fill(S.ptp.begin(), S.ptp.end() - 1);
+        for (int64_t i = 0; i < n; i++)
+            for (int64_t s = S.prp[i]; s < S.prp[i + 1]; s++) {
+                const int64_t o = fill[S.pcj[s]]++;
+                S.pti[o] = (int32_t)i;
+                S.pts[o] = (int32_t)s;
+            }
+    }
+    // P' A P: coarse row I reaches the columns of the A P rows of the fine rows P reaches I from
+    distinct_rows(na, na, [&](int64_t I, auto push) {
+        push((int32_t)I);  // every coarse row has its diagonal block, even an aggregate of nodes without blocks
+        for (int64_t e = S.ptp[I]; e < S.ptp[I + 1]; e++) {
+            const int32_t i = S.pti[e];
+            for (int64_t q = S.qrp[i]; q < S.qrp[i + 1]; q++) push(S.qcj[q]);
+        }
+    }, S.crp, S.ccj);
+    S.crow.resize(S.crp[na]);
+    for (int64_t I = 0; I < na; I++)
+        for (int64_t c = S.crp[I]; c < S.crp[I + 1]; c++) S.crow[c] = (int32_t)I;
+    if (S.crp[na] >= ((int64_t)1 << 31) || S.qrp[n] >= ((int64_t)1 << 31) || np >= ((int64_t)1 << 31) ||
+        h.rp[n] >= ((int64_t)1 << 31))
+        throw AmrError(AMR_EUNSUPPORTED, "the smoothed multigrid's patterns exceed 32-bit indices");
+}
+
 }  // namespace
 
 // Values of one level in one precision: the FP32 cycle preconditions the mixed solver; the FP64 cycle,
@@ -137,6 +253,8 @@ struct AmgVals {
     V *A = nullptr;     // this level's matrix (levels >= 1): BSR, b x b blocks, SoA values [b*b][nbs]
     V *Dinv = nullptr;  // n x b*b block-Jacobi inverses (level 0: the solver's own)
     V *T = nullptr;     // n x b x NM prolongator blocks to the next level
+    V *P = nullptr;     // smoothed prolongator: np blocks of b x NM (row-major), AoS
+    V *Q = nullptr;     // A P: nq blocks of b x NM, AoS (work of the coarse operator's build)
     V *x = nullptr, *bv = nullptr, *r = nullptr, *d = nullptr;  // vectors of this level (n*b)
     double lam = 1.0;
 };
@@ -157,6 +275,15 @@ struct AmgLevel {
     int32_t *ck = nullptr, *ci = nullptr;
     uint8_t *null_dof = nullptr;  // coarse DOFs with no mode (aggregate of prescribed DOFs): identity
     std::vector<double> hT;       // the prolongator blocks on the host (uploaded in FP64 on first use)
+    // smoothed prolongator P (block rows = this level's nodes, block columns = aggregates): its pattern,
+    // each P block's contributing blocks of A (pkk[pkp[s]..pkp[s+1]], ascending, a permutation of the
+    // row's blocks), P by columns (aggregate -> (row, P block), rows ascending), the pattern of A P (with
+    // each block's row) and the row of each coarse block
+    bool smooth = false;
+    int64_t np = 0, nq = 0;
+    int64_t *prp = nullptr, *pkp = nullptr, *qrp = nullptr, *ptp = nullptr;
+    int32_t *pcj = nullptr, *pkk = nullptr, *qcj = nullptr, *qrow = nullptr, *pti = nullptr, *pts = nullptr,
+            *crow = nullptr;
     AmgVals<float> f32;
     AmgVals<double> f64;
 };
@@ -202,7 +329,7 @@ void free_vals(AmgVals<V> &v, bool owns_matrix) {
         amr_free(v.A);
         amr_free(v.Dinv);
     }
-    amr_free(v.T);
+    amr_free(v.T); amr_free(v.P); amr_free(v.Q);
     amr_free(v.x); amr_free(v.bv); amr_free(v.r); amr_free(v.d);
 }
 }  // namespace
@@ -219,6 +346,8 @@ void amr_amg_free(amr_model *m) {
         free_vals(v.f64, l > 0);
         amr_free(v.diag); amr_free(v.agg); amr_free(v.aptr); amr_free(v.anodes);
         amr_free(v.cptr); amr_free(v.ck); amr_free(v.ci); amr_free(v.null_dof);
+        amr_free(v.prp); amr_free(v.pkp); amr_free(v.qrp); amr_free(v.ptp); amr_free(v.pcj); amr_free(v.pkk);
+        amr_free(v.qcj); amr_free(v.qrow); amr_free(v.pti); amr_free(v.pts); amr_free(v.crow);
     }
     if (g->gj_exec) cudaGraphExecDestroy(g->gj_exec);
     amr_free(g->Cd); amr_free(g->gjf); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
@@ -349,55 +478,81 @@ static void amg_build_structure(amr_model *m) {
                 for (int p = 0; p < NM; p++)
                     hc.nns[((size_t)a * NM + k) * NM + p] = sc[k] > 0.0 ? std::sqrt(w[k]) * V[p * NM + k] : 0.0;
         });
-        // coarse pattern and contribution lists, coarse row by coarse row
-        std::vector<std::vector<int32_t>> ccols(na);
-        std::vector<std::vector<int64_t>> ccnt(na);
-        std::vector<std::vector<int32_t>> ck(na), ci(na);
-        parallel_for(na, [&](int64_t a) {
-            std::vector<std::tuple<int32_t, int32_t, int32_t>> e;  // (coarse column, fine block, fine row)
-            // every coarse row has its diagonal block, even an aggregate of nodes without blocks
-            e.emplace_back((int32_t)a, -1, -1);
-            for (int64_t q = aptr[a]; q < aptr[a + 1]; q++) {
-                const int32_t i = anodes[q];
-                for (int64_t k = h.rp[i]; k < h.rp[i + 1]; k++) e.emplace_back(agg[h.cj[k]], (int32_t)k, i);
-            }
-            std::stable_sort(e.begin(), e.end(),
-                             [](const auto &u, const auto &v) { return std::get<0>(u) < std::get<0>(v); });
-            for (size_t s = 0; s < e.size(); s++) {
-                if (s == 0 || std::get<0>(e[s]) != std::get<0>(e[s - 1])) {
-                    ccols[a].push_back(std::get<0>(e[s]));
-                    ccnt[a].push_back(0);
+        if (m->amg_smooth) {
+            SaPattern S;
+            sa_pattern(h, agg, na, S);
+            lv.smooth = true;
+            lv.np = S.prp[h.n];
+            lv.nq = S.qrp[h.n];
+            auto up64 = [&](int64_t *&d, const std::vector<int64_t> &v) {
+                amr_alloc(&d, std::max<size_t>(v.size(), 1));
+                amr_h2d(m, d, v.data(), v.size() * sizeof(int64_t));
+            };
+            auto up32 = [&](int32_t *&d, const std::vector<int32_t> &v) {
+                amr_alloc(&d, std::max<size_t>(v.size(), 1));
+                amr_h2d(m, d, v.data(), v.size() * sizeof(int32_t));
+            };
+            up64(lv.prp, S.prp); up64(lv.pkp, S.pkp); up64(lv.qrp, S.qrp); up64(lv.ptp, S.ptp);
+            up32(lv.pcj, S.pcj); up32(lv.pkk, S.pkk); up32(lv.qcj, S.qcj); up32(lv.qrow, S.qrow);
+            up32(lv.pti, S.pti); up32(lv.pts, S.pts); up32(lv.crow, S.crow);
+            amr_alloc(&lv.f32.P, (size_t)std::max<int64_t>(lv.np, 1) * h.b * NM);
+            amr_alloc(&lv.f32.Q, (size_t)std::max<int64_t>(lv.nq, 1) * h.b * NM);
+            hc.rp = std::move(S.crp);
+            hc.cj = std::move(S.ccj);
+        } else {
+            // coarse pattern and contribution lists, coarse row by coarse row
+            std::vector<std::vector<int32_t>> ccols(na);
+            std::vector<std::vector<int64_t>> ccnt(na);
+            std::vector<std::vector<int32_t>> ck(na), ci(na);
+            parallel_for(na, [&](int64_t a) {
+                std::vector<std::tuple<int32_t, int32_t, int32_t>> e;  // (coarse column, fine block, fine row)
+                // every coarse row has its diagonal block, even an aggregate of nodes without blocks
+                e.emplace_back((int32_t)a, -1, -1);
+                for (int64_t q = aptr[a]; q < aptr[a + 1]; q++) {
+                    const int32_t i = anodes[q];
+                    for (int64_t k = h.rp[i]; k < h.rp[i + 1]; k++) e.emplace_back(agg[h.cj[k]], (int32_t)k, i);
                 }
-                if (std::get<1>(e[s]) < 0) continue;  // the diagonal sentinel contributes nothing
-                ccnt[a].back()++;
-                ck[a].push_back(std::get<1>(e[s]));
-                ci[a].push_back(std::get<2>(e[s]));
+                std::stable_sort(e.begin(), e.end(),
+                                 [](const auto &u, const auto &v) { return std::get<0>(u) < std::get<0>(v); });
+                for (size_t s = 0; s < e.size(); s++) {
+                    if (s == 0 || std::get<0>(e[s]) != std::get<0>(e[s - 1])) {
+                        ccols[a].push_back(std::get<0>(e[s]));
+                        ccnt[a].push_back(0);
+                    }
+                    if (std::get<1>(e[s]) < 0) continue;  // the diagonal sentinel contributes nothing
+                    ccnt[a].back()++;
+                    ck[a].push_back(std::get<1>(e[s]));
+                    ci[a].push_back(std::get<2>(e[s]));
+                }
+            });
+            hc.rp.assign(na + 1, 0);
+            for (int64_t a = 0; a < na; a++) hc.rp[a + 1] = hc.rp[a] + (int64_t)ccols[a].size();
+            hc.cj.resize(hc.rp[na]);
+            std::vector<int64_t> cptr(hc.rp[na] + 1, 0);
+            std::vector<int32_t> cks, cis;
+            cks.reserve(lv.nblocks);
+            cis.reserve(lv.nblocks);
+            for (int64_t a = 0; a < na; a++) {
+                for (size_t s = 0; s < ccols[a].size(); s++) {
+                    const int64_t cb = hc.rp[a] + (int64_t)s;
+                    hc.cj[cb] = ccols[a][s];
+                    cptr[cb + 1] = cptr[cb] + ccnt[a][s];
+                }
+                cks.insert(cks.end(), ck[a].begin(), ck[a].end());
+                cis.insert(cis.end(), ci[a].begin(), ci[a].end());
             }
-        });
-        hc.rp.assign(na + 1, 0);
-        for (int64_t a = 0; a < na; a++) hc.rp[a + 1] = hc.rp[a] + (int64_t)ccols[a].size();
-        hc.cj.resize(hc.rp[na]);
-        std::vector<int64_t> cptr(hc.rp[na] + 1, 0);
-        std::vector<int32_t> cks, cis;
-        cks.reserve(lv.nblocks);
-        cis.reserve(lv.nblocks);
-        for (int64_t a = 0; a < na; a++) {
-            for (size_t s = 0; s < ccols[a].size(); s++) {
-                const int64_t cb = hc.rp[a] + (int64_t)s;
-                hc.cj[cb] = ccols[a][s];
-                cptr[cb + 1] = cptr[cb] + ccnt[a][s];
-            }
-            cks.insert(cks.end(), ck[a].begin(), ck[a].end());
-            cis.insert(cis.end(), ci[a].begin(), ci[a].end());
+            amr_alloc(&lv.cptr, cptr.size());
+            amr_alloc(&lv.ck, std::max<size_t>(cks.size(), 1));
+            amr_alloc(&lv.ci, std::max<size_t>(cis.size(), 1));
+            amr_h2d(m, lv.cptr, cptr.data(), cptr.size() * sizeof(int64_t));
+            amr_h2d(m, lv.ck, cks.data(), cks.size() * sizeof(int32_t));
+            amr_h2d(m, lv.ci, cis.data(), cis.size() * sizeof(int32_t));
         }
         lv.naggs = na;
         amr_alloc(&lv.agg, h.n);
         amr_alloc(&lv.f32.T, T.size());
         amr_alloc(&lv.aptr, na + 1);
         amr_alloc(&lv.anodes, h.n);
-        amr_alloc(&lv.cptr, cptr.size());
-        amr_alloc(&lv.ck, cks.size());
-        amr_alloc(&lv.ci, cis.size());
         amr_alloc(&lv.null_dof, nulld.size());
         amr_h2d(m, lv.agg, agg.data(), h.n * sizeof(int32_t));
         {
@@ -407,9 +562,6 @@ static void amg_build_structure(amr_model *m) {
         lv.hT = std::move(T);
         amr_h2d(m, lv.aptr, aptr.data(), aptr.size() * sizeof(int64_t));
         amr_h2d(m, lv.anodes, anodes.data(), h.n * sizeof(int32_t));
-        amr_h2d(m, lv.cptr, cptr.data(), cptr.size() * sizeof(int64_t));
-        amr_h2d(m, lv.ck, cks.data(), cks.size() * sizeof(int32_t));
-        amr_h2d(m, lv.ci, cis.data(), cis.size() * sizeof(int32_t));
         amr_h2d(m, lv.null_dof, nulld.data(), nulld.size());
         g->L.push_back(lv);
         H.push_back(std::move(hc));
@@ -480,6 +632,133 @@ __global__ void k_galerkin(int64_t ncb, const int64_t *cptr, const int32_t *ck, 
 }
 
 // coarse DOFs without a mode get an identity equation
+// smoothed prolongator, thread per row i: P_s = [pcj[s] == agg(i)] T_i - w Dinv_i sum_k A_k T_cj[k] over the
+// P block's blocks k of A in order; rows of prescribed DOFs (mask 0) are zero
+template <int BF, int NM, class V>
+__global__ void k_sa_prolongator(int64_t n, const int64_t *prp, const int32_t *pcj, const int64_t *pkp,
+                                 const int32_t *pkk, const int32_t *cjf, const V *Af, int64_t nbsf, const V *T,
+                                 const V *Dinv, const int32_t *agg, V w, const uint8_t *mask, V *P) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t ai = agg[i];
+    V Di[BF * BF];
+#pragma unroll
+    for (int q = 0; q < BF * BF; q++) Di[q] = Dinv[i * BF * BF + q];
+    bool fr[BF];
+#pragma unroll
+    for (int c = 0; c < BF; c++) fr[c] = mask ? mask[i * BF + c] != 0 : true;
+    for (int64_t s = prp[i]; s < prp[i + 1]; s++) {
+        V M[BF * NM];  // sum of A_k T_j
+#pragma unroll
+        for (int q = 0; q < BF * NM; q++) M[q] = V(0);
+        for (int64_t e = pkp[s]; e < pkp[s + 1]; e++) {
+            const int64_t k = pkk[e];
+            const int64_t j = cjf[k];
+            V a[BF * BF];
+#pragma unroll
+            for (int q = 0; q < BF * BF; q++) a[q] = Af[(int64_t)q * nbsf + k];
+#pragma unroll
+            for (int d = 0; d < BF; d++)
+#pragma unroll
+                for (int mm = 0; mm < NM; mm++) {
+                    const V t = T[(j * BF + d) * NM + mm];
+#pragma unroll
+                    for (int c = 0; c < BF; c++) M[c * NM + mm] = vfma(a[c * BF + d], t, M[c * NM + mm]);
+                }
+        }
+        const bool own = pcj[s] == ai;
+#pragma unroll
+        for (int c = 0; c < BF; c++)
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) {
+                V v = V(0);
+#pragma unroll
+                for (int d = 0; d < BF; d++) v = vfma(Di[c * BF + d], M[d * NM + mm], v);
+                const V p = (own ? T[(i * BF + c) * NM + mm] : V(0)) - w * v;
+                P[s * BF * NM + c * NM + mm] = fr[c] ? p : V(0);
+            }
+    }
+}
+
+// A P, thread per block q of its pattern (row i, aggregate J): sum over the row's blocks k of A in order of
+// A_k P_t, t the block of P row cj[k] in column J (if any)
+template <int BF, int NM, class V>
+__global__ void k_sa_ap(int64_t nq, const int32_t *qrow, const int32_t *qcj, const int64_t *rpf, const int32_t *cjf,
+                        const V *Af, int64_t nbsf, const int64_t *prp, const int32_t *pcj, const V *P, V *Q) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int64_t i = qrow[q];
+    const int32_t J = qcj[q];
+    V acc[BF * NM];
+#pragma unroll
+    for (int u = 0; u < BF * NM; u++) acc[u] = V(0);
+    for (int64_t k = rpf[i]; k < rpf[i + 1]; k++) {
+        const int64_t j = cjf[k];
+        int64_t t = -1;
+        for (int64_t u = prp[j]; u < prp[j + 1]; u++) {
+            const int32_t c = pcj[u];
+            if (c >= J) {
+                if (c == J) t = u;
+                break;
+            }
+        }
+        if (t < 0) continue;
+        const V *pt = P + t * BF * NM;
+#pragma unroll
+        for (int d = 0; d < BF; d++) {
+            V a[BF];
+#pragma unroll
+            for (int c = 0; c < BF; c++) a[c] = Af[(int64_t)(c * BF + d) * nbsf + k];
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) {
+                const V pv = pt[d * NM + mm];
+#pragma unroll
+                for (int c = 0; c < BF; c++) acc[c * NM + mm] = vfma(a[c], pv, acc[c * NM + mm]);
+            }
+        }
+    }
+    V *o = Q + q * BF * NM;
+#pragma unroll
+    for (int u = 0; u < BF * NM; u++) o[u] = acc[u];
+}
+
+// coarse operator P' (A P), thread per coarse block (I, J): sum over the fine rows i that P reaches I from
+// (block s), in order, of P_s' Q_iJ (if row i of A P has column J)
+template <int BF, int NM, class V>
+__global__ void k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *ccj, const int64_t *ptp,
+                              const int32_t *pti, const int32_t *pts, const V *P, const int64_t *qrp,
+                              const int32_t *qcj, const V *Q, V *Ac, int64_t nbsc) {
+    const int64_t cb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cb >= ncb) return;
+    const int32_t I = crow[cb], J = ccj[cb];
+    V acc[NM * NM];
+#pragma unroll
+    for (int u = 0; u < NM * NM; u++) acc[u] = V(0);
+    for (int64_t e = ptp[I]; e < ptp[I + 1]; e++) {
+        const int64_t i = pti[e];
+        int64_t lo = qrp[i], hi = qrp[i + 1];  // J in the sorted columns of row i of A P
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (qcj[mid] < J) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo >= qrp[i + 1] || qcj[lo] != J) continue;
+        const V *ps = P + (int64_t)pts[e] * BF * NM, *qv = Q + lo * BF * NM;
+#pragma unroll
+        for (int c = 0; c < BF; c++) {
+            V pr[NM], qr[NM];
+#pragma unroll
+            for (int u = 0; u < NM; u++) { pr[u] = ps[c * NM + u]; qr[u] = qv[c * NM + u]; }
+#pragma unroll
+            for (int a = 0; a < NM; a++)
+#pragma unroll
+                for (int b = 0; b < NM; b++) acc[a * NM + b] = vfma(pr[a], qr[b], acc[a * NM + b]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < NM * NM; u++) Ac[(int64_t)u * nbsc + cb] = acc[u];
+}
+
 template <int NM, class V>
 __global__ void k_null_identity(int64_t n, const uint8_t *nulld, const int64_t *diag, V *A, int64_t nbs) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -814,6 +1093,72 @@ __global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc
     }
 }
 
+// bc[I] = sum over the fine rows i that P reaches I from (block s), in order, of P_s' r_i; warp per aggregate
+template <int NB, int NM, class V>
+__global__ void k_restrict_sa(int64_t na, const int64_t *ptp, const int32_t *pti, const int32_t *pts, const V *P,
+                              const V *r, V *bc, const uint8_t *gate = nullptr) {
+    const int lane = threadIdx.x & 31;
+    const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (a >= na) return;
+    // the rows P reaches an aggregate from lie in the aggregate's part (uniform over the warp)
+    if (gate && ptp[a] < ptp[a + 1] && !gate[pti[ptp[a]]]) return;
+    V acc[NM];
+#pragma unroll
+    for (int mm = 0; mm < NM; mm++) acc[mm] = V(0);
+    for (int64_t e = ptp[a] + lane; e < ptp[a + 1]; e += 32) {
+        const int64_t i = pti[e];
+        const V *ps = P + (int64_t)pts[e] * NB * NM;
+#pragma unroll
+        for (int c = 0; c < NB; c++) {
+            const V rv = r[i * NB + c];
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) acc[mm] = vfma(ps[c * NM + mm], rv, acc[mm]);
+        }
+    }
+#pragma unroll
+    for (int mm = 0; mm < NM; mm++) {
+        V v = acc[mm];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) bc[a * NM + mm] = v;
+    }
+}
+
+// x_i += sum over row i's P blocks s of P_s xc[pcj[s]]  (and xt_i = rs_i x_i on the fine level of the FP32
+// cycle)
+template <int NB, int NM, class V>
+__global__ void k_prolong_sa(int64_t n, const int64_t *prp, const int32_t *pcj, const V *P, const V *xc, V *x,
+                             const float *rs = nullptr, typename FineX<NB>::T *xt = nullptr,
+                             const uint8_t *gate = nullptr) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (gate && !gate[i])) return;
+    V s[NB];
+#pragma unroll
+    for (int c = 0; c < NB; c++) s[c] = x[i * NB + c];
+    for (int64_t t = prp[i]; t < prp[i + 1]; t++) {
+        const V *pt = P + t * NB * NM;
+        const V *xa = xc + (int64_t)pcj[t] * NM;
+        V xv[NM];
+#pragma unroll
+        for (int mm = 0; mm < NM; mm++) xv[mm] = xa[mm];
+#pragma unroll
+        for (int c = 0; c < NB; c++)
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) s[c] = vfma(pt[c * NM + mm], xv[mm], s[c]);
+    }
+    float v[NB];
+#pragma unroll
+    for (int c = 0; c < NB; c++) {
+        x[i * NB + c] = s[c];
+        v[c] = (float)s[c];
+    }
+    if (xt) {
+#pragma unroll
+        for (int c = 0; c < NB; c++) v[c] *= rs[i];
+        xt[i] = FineX<NB>::make(v);
+    }
+}
+
 // dense coarsest level: expand the BSR matrix, invert it (Gauss-Jordan, FP64), multiply
 template <int NM, class V>
 __global__ void k_dense_expand(int64_t n, const int64_t *rp, const int32_t *cj, const V *A, int64_t nbs, double *C,
@@ -1039,10 +1384,17 @@ struct Cycle {
         residual();
         AmgLevel &C = g->L[l + 1];
         AmgVals<V> &cv = vals<V>(C);
-        k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r, cv.bv,
-                                                                      gate);
+        if (L.smooth)
+            k_restrict_sa<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.ptp, L.pti, L.pts, v.P, v.r,
+                                                                             cv.bv, gate);
+        else
+            k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r,
+                                                                          cv.bv, gate);
         level(m, g, l + 1, cv.bv, cv.x);
-        k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt, gate);
+        if (L.smooth)
+            k_prolong_sa<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.prp, L.pcj, v.P, cv.x, x, rs, xt, gate);
+        else
+            k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt, gate);
         // post-smoothing
         residual();
         k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x, rs, xt, gate);
@@ -1078,6 +1430,29 @@ struct Cycle {
         }
         return lam;
     }
+    // the coarse operator of level l + 1 from level l: T' A T, or P' (A P) with P smoothed from T
+    template <int BF>
+    static void coarse(amr_model *m, AmrAmg *g, size_t l, const V *A, int64_t nbs, const uint8_t *mask) {
+        cudaStream_t s = m->stream;
+        AmgLevel &F = g->L[l], &C = g->L[l + 1];
+        AmgVals<V> &fv = vals<V>(F), &cv = vals<V>(C);
+        if (!F.smooth) {
+            k_galerkin<BF, NM, V><<<nblk(C.nblocks * 32, 256), 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, A,
+                                                                             nbs, fv.T, cv.A, C.nbs);
+            AMR_COUNT(1);
+            return;
+        }
+        fv.lam = lambda<BF>(m, g, F, A, nbs, mask);
+        const V w = (V)(4.0 / (3.0 * fv.lam));
+        auto grid = [](int64_t n) { return std::max(1u, nblk(n, 128)); };
+        k_sa_prolongator<BF, NM, V><<<grid(F.n), 128, 0, s>>>(F.n, F.prp, F.pcj, F.pkp, F.pkk, F.cj, A, nbs,
+                                                                    fv.T, fv.Dinv, F.agg, w, mask, fv.P);
+        k_sa_ap<BF, NM, V><<<grid(F.nq), 128, 0, s>>>(F.nq, F.qrow, F.qcj, F.rp, F.cj, A, nbs, F.prp, F.pcj,
+                                                            fv.P, fv.Q);
+        k_sa_galerkin<BF, NM, V><<<grid(C.nblocks), 128, 0, s>>>(C.nblocks, F.crow, C.cj, F.ptp, F.pti, F.pts,
+                                                                       fv.P, F.qrp, F.qcj, fv.Q, cv.A, C.nbs);
+        AMR_COUNT(3);
+    }
     static void numeric(amr_model *m, AmrAmg *g) {
         cudaStream_t s = m->stream;
         const size_t nl = g->L.size();
@@ -1085,15 +1460,10 @@ struct Cycle {
         for (size_t l = 0; l + 1 < nl; l++) {
             AmgLevel &F = g->L[l], &C = g->L[l + 1];
             AmgVals<V> &fv = vals<V>(F), &cv = vals<V>(C);
-            const unsigned gc = nblk(C.nblocks * 32, 256);
-            if (l == 0)
-                k_galerkin<B, NM, V><<<gc, 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, fine_A(m), m->bstride,
-                                                        fv.T, cv.A, C.nbs);
-            else
-                k_galerkin<NM, NM, V><<<gc, 256, 0, s>>>(C.nblocks, F.cptr, F.ck, F.ci, F.cj, fv.A, F.nbs, fv.T, cv.A,
-                                                         C.nbs);
+            if (l == 0) coarse<B>(m, g, l, fine_A(m), m->bstride, fine_mask(m));
+            else coarse<NM>(m, g, l, fv.A, F.nbs, nullptr);
             k_null_identity<NM, V><<<nblk(C.n * NM, 256), 256, 0, s>>>(C.n, F.null_dof, C.diag, cv.A, C.nbs);
-            AMR_COUNT(2);
+            AMR_COUNT(1);
             if (l + 2 < nl) {
                 k_block_inverse<NM, V><<<nblk(C.n, 128), 128, 0, s>>>(C.n, C.diag, cv.A, C.nbs, cv.Dinv);
                 AMR_COUNT(1);
@@ -1107,8 +1477,9 @@ struct Cycle {
             AMR_COUNT(2);
             AMR_CUDA(cudaGetLastError());
         }
-        for (size_t l = 0; l + 1 < nl; l++) {
+        for (size_t l = 0; l + 1 < nl; l++) {  // (a smoothed level's lambda came with its prolongator)
             AmgLevel &L = g->L[l];
+            if (L.smooth) continue;
             vals<V>(L).lam = l == 0 ? lambda<B>(m, g, L, fine_A(m), m->bstride, fine_mask(m))
                                     : lambda<NM>(m, g, L, vals<V>(L).A, L.nbs, nullptr);
         }
@@ -1160,6 +1531,10 @@ void ensure_fp64(amr_model *m, AmrAmg *g) {
         if (!L.hT.empty()) {
             amr_alloc(&v.T, L.hT.size());
             amr_h2d(m, v.T, L.hT.data(), L.hT.size() * sizeof(double));
+        }
+        if (L.smooth) {
+            amr_alloc(&v.P, (size_t)std::max<int64_t>(L.np, 1) * L.b * g->NM);
+            amr_alloc(&v.Q, (size_t)std::max<int64_t>(L.nq, 1) * L.b * g->NM);
         }
     }
     amr_alloc(&g->Cinv64, (size_t)g->nc * g->nc);

@@ -122,6 +122,7 @@ struct amr_model {
     std::string err;
     bool any_plastic = false;
     int assembly_mode = AMR_ASSEMBLY_FAST;
+    int amg_smooth = 1;  // multigrid prolongators: smoothed (1) or the tentative ones (0)
     // the last whole-model static stage's Newton iterations, and the hook after each converged increment
     std::vector<amr_iteration_record> stage_log;
     amr_increment_fn inc_fn = nullptr;

@@ -530,6 +530,17 @@ int amr_set_assembly(amr_model *m, int32_t mode) {
     });
 }
 
+int amr_set_amg_smoothing(amr_model *m, int32_t on) {
+    return guarded(m, [&] {
+        if (on != 0 && on != 1) throw AmrError(AMR_EINVAL, "smoothing is 0 or 1");
+        if (m->amg_smooth != on) {
+            m->amg_smooth = on;
+            amr_amg_free(m);  // the hierarchy is rebuilt at the next multigrid solve
+        }
+        return AMR_OK;
+    });
+}
+
 int amr_assemble_K(amr_model *m) {
     return guarded(m, [&] {
         assemble(m);

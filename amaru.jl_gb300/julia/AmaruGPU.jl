@@ -255,6 +255,18 @@ function mount_K(g::GPUModel; reference_order::Bool=true)
 end
 
 """
+    set_amg_smoothing!(g, on::Bool)
+
+Smoothed-aggregation prolongators (true, the default) or the tentative ones
+(false) for the multigrid solves of `g` (amr_set_amg_smoothing).
+"""
+function set_amg_smoothing!(g::GPUModel, on::Bool)
+    st = check(g, ccall((:amr_set_amg_smoothing, LIB), Cint, (Ptr{Cvoid}, Int32), g.h, on ? 1 : 0))
+    st === nothing || error(st.message)
+    return g
+end
+
+"""
     update_state!(g, dU) -> (dFin, status)
 
 update_state!(elems, dU, t) on the device (trial states from the committed ones).
@@ -1081,6 +1093,6 @@ gpu_tm_mount_global_matrices(model::FEModel, ndofs::Int, Δt::Float64) = coupled
 export GPUModel, solve_gpu!, gpu_stage_solver!, GPUBatch, solve_batch!, GPUServer, submit!, wait!,
        nodal_patch_recovery_gpu, has_gpu, gpu_dyn_stage_solver!, gpu_modal_solver!, save_gpu,
        sizes, get_state, set_state!, commit_state!, restore_state!, set_youngs!, estimate_bytes, stats, autotune!,
-       rayleigh_coefficients, gpu_hm_mount_global_matrices, gpu_tm_mount_global_matrices
+       rayleigh_coefficients, gpu_hm_mount_global_matrices, gpu_tm_mount_global_matrices, set_amg_smoothing!
 
 end # module

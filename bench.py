@@ -250,6 +250,13 @@ def run_ours(a):
                 kern["amg_residual64"] = dev.time_kernel(L.KERNEL_AMG_RESIDUAL64, 20)
             if name == "fp64":
                 kern["spmv64"] = dev.time_kernel(L.KERNEL_SPMV64, 20)
+        # the multigrid solve with the tentative (unsmoothed) prolongators, for the smoothing's share
+        dev.set_amg_smoothing(False)
+        try:
+            runs["amg_unsmoothed"] = dev.solve(U0, F0, L.default_solve_opts(method=L.SOLVER_AMG, rtol=1e-8,
+                                                                            max_iters=200000))
+        finally:
+            dev.set_amg_smoothing(True)
         nu = model.nu
         ref = np.abs(runs["fp64"][0][:nu]).max()
         flops64 = 2.0 * 9 * sizes["nblocks"]  # one FP64 FMA per scalar nonzero
@@ -271,7 +278,7 @@ def run_ours(a):
             "speedup_vs_fp64_block_jacobi": runs["fp64"][2].seconds / runs["amg" if a.solver == "amg"
                                                                             else "mixed"][2].seconds,
             "max_rel_dU_vs_fp64": {n: float(np.abs(runs[n][0][:nu] - runs["fp64"][0][:nu]).max() / ref)
-                                   for n in ("amg", "amg_fp64", "mixed")},
+                                   for n in ("amg", "amg_fp64", "mixed", "amg_unsmoothed")},
             "fp64_kernels": fp64_kernels, "fp64_peak_tflops": fp64_peak,
             "fp64_peak_source": "measured: amr_measure_peak (FP64 FMA chains on every SM, CUDA events)"})
 
@@ -308,14 +315,20 @@ def run_ours(a):
                                     "fp64_tflops": st_fl / st_t / 1e12, "fp64_peak_tflops": pk64,
                                     "fp64_frac": st_fl / st_t / 1e12 / pk64}
 
-    # e2e: the same step through the C ABI with host buffers (H2D inputs, D2H results inside)
-    Uh = np.ascontiguousarray(Uex)
-    Fh = np.ascontiguousarray(Fex)
+    # e2e: the same step through the C ABI with host buffers (H2D inputs, D2H results inside), the buffers in
+    # pinned host memory
+    def pinned(v):
+        return torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).pin_memory().numpy()
+    Uh, Fh = pinned(Uex), pinned(Fex)
+    outs = (pinned(np.zeros(ndofs)), pinned(np.zeros(ndofs)))
+    rc, _, _, _ = dev.stage_run(Uh, Fh, prm, out=outs)  # untimed: rebuilds what the comparisons above replaced
+    if rc != 0:
+        raise RuntimeError(dev.last_error())
     e2e_t = []
     for _ in range(a.steps):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        rc, U, F, st = dev.stage_run(Uh, Fh, prm)
+        rc, U, F, st = dev.stage_run(Uh, Fh, prm, out=outs)
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t1)
         if rc != 0:
@@ -931,13 +944,25 @@ def run_reference(a):
 def amg_solve_only(a):
     """Profile driver: the bench workload at --mesh, assembled once, then --steps multigrid solves of it."""
     from amaru_gpu import _lib as L
+    import torch
     model, Uex, Fex = workload_gpu(*dims(a.mesh))
-    model.dev.assemble_K()
-    out = []
-    for _ in range(max(a.steps, 1)):
-        _, _, st = model.dev.solve(Uex, Fex, L.default_solve_opts(method=L.SOLVER_AMG, rtol=1e-8))
-        out.append({"s": st.seconds, "iterations": st.iterations, "rel_residual": st.rel_residual})
-    return {"amg_solve_only": a.mesh, "solves": out}
+    res = {"amg_solve_only": a.mesh}
+    for smooth in (True, False):
+        model.dev.set_amg_smoothing(smooth)
+        out = []
+        for rep in range(max(a.steps, 1) + 1):
+            model.dev.assemble_K()  # a new K: the hierarchy's values are rebuilt by the solve
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            _, _, st = model.dev.solve(Uex, Fex, L.default_solve_opts(method=L.SOLVER_AMG, rtol=1e-8))
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t1
+            if rep > 0:  # the first solve also builds the hierarchy's structure on the host
+                out.append({"s": st.seconds, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                            "wall_s": wall})
+        res["smoothed" if smooth else "unsmoothed"] = out
+    model.dev.set_amg_smoothing(True)
+    return res
 
 
 def main():

@@ -170,6 +170,14 @@ int amr_set_youngs(amr_model *m, const double *E);
 enum { AMR_ASSEMBLY_FAST = 0, AMR_ASSEMBLY_REFERENCE = 1 };
 int amr_set_assembly(amr_model *m, int32_t mode);
 
+/* Prolongators of the multigrid preconditioner (AMR_SOLVER_AMG, AMR_SOLVER_AMG_FP64).
+ * 1 (default): smoothed aggregation, P = (I - 4/(3 lambda) D^-1 A) T on every level but the
+ *   coarsest, T the rigid-body tentative prolongator, D the node-block diagonal and lambda the
+ *   power-iteration estimate of the largest eigenvalue of D^-1 A; coarse operator P' A P.
+ * 0: the tentative prolongators themselves (unsmoothed aggregation); coarse operator T' A T.
+ * A change rebuilds the hierarchy at the next multigrid solve. */
+int amr_set_amg_smoothing(amr_model *m, int32_t on);
+
 /* mount_K (src/mech/mech-solver.jl:78-110): element stiffness
  * (src/mech/elem/mech-solid.jl:124-166) with the tangent of each IP's current
  * state, deterministic assembly into the device pattern. */
