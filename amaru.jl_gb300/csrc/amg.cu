@@ -255,6 +255,10 @@ struct AmgVals {
     V *T = nullptr;     // n x b x NM prolongator blocks to the next level
     V *P = nullptr;     // smoothed prolongator: np blocks of b x NM (row-major), AoS
     V *Q = nullptr;     // A P: nq blocks of b x NM, AoS (work of the coarse operator's build)
+    // the FP32 cycle's smoothed prolongator in FP16 (P holds the same rounded values, so the coarse operator
+    // is the Galerkin product of the prolongator the cycle applies): by rows (prolongation) and by columns
+    // in the order of ptp/pti (restriction), np blocks of b x NM each
+    __half *P16 = nullptr, *P16T = nullptr;
     V *x = nullptr, *bv = nullptr, *r = nullptr, *d = nullptr;  // vectors of this level (n*b)
     double lam = 1.0;
 };
@@ -293,7 +297,6 @@ struct AmrAmg {
     std::vector<AmgLevel> L;
     int64_t nc = 0;             // DOFs of the dense coarsest level
     double *Cd = nullptr;       // nc x 2nc FP64 work (Gauss-Jordan)
-    double *gjf = nullptr;      // nc: the row factors of one Gauss-Jordan step
     cudaGraphExec_t gj_exec = nullptr;  // the Gauss-Jordan steps, captured once
     float *Cinv = nullptr;      // nc x nc inverse, FP32 cycle
     double *Cinv64 = nullptr;   // nc x nc inverse, FP64 cycle
@@ -310,6 +313,9 @@ struct AmrAmg {
     // fine level's smoothing, residual, restriction and prolongation (their values go stale); set by the
     // batched solve to the rows of its running parts, whose V-cycle is block diagonal over the parts
     const uint8_t *gate = nullptr;
+    // the solve's stop flag (null: none): set while a PCG iteration graph is replayed, so the V-cycles of the
+    // iterations left in a chunk after the recursive residual has triggered a refresh return at once
+    const int32_t *halt = nullptr;
     __half *A16 = nullptr;      // SoA [B*B][bstride]
     float *rs = nullptr;        // nnodes: 1 / s_n
     float *xt = nullptr;        // nnodes x 4 (3-D) or x 2 (2-D): x rs
@@ -329,7 +335,7 @@ void free_vals(AmgVals<V> &v, bool owns_matrix) {
         amr_free(v.A);
         amr_free(v.Dinv);
     }
-    amr_free(v.T); amr_free(v.P); amr_free(v.Q);
+    amr_free(v.T); amr_free(v.P); amr_free(v.Q); amr_free(v.P16); amr_free(v.P16T);
     amr_free(v.x); amr_free(v.bv); amr_free(v.r); amr_free(v.d);
 }
 }  // namespace
@@ -350,7 +356,7 @@ void amr_amg_free(amr_model *m) {
         amr_free(v.qcj); amr_free(v.qrow); amr_free(v.pti); amr_free(v.pts); amr_free(v.crow);
     }
     if (g->gj_exec) cudaGraphExecDestroy(g->gj_exec);
-    amr_free(g->Cd); amr_free(g->gjf); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
+    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
     amr_free(g->A16); amr_free(g->rs); amr_free(g->xt);
     delete g;
     m->amg = nullptr;
@@ -496,6 +502,8 @@ static void amg_build_structure(amr_model *m) {
             up32(lv.pcj, S.pcj); up32(lv.pkk, S.pkk); up32(lv.qcj, S.qcj); up32(lv.qrow, S.qrow);
             up32(lv.pti, S.pti); up32(lv.pts, S.pts); up32(lv.crow, S.crow);
             amr_alloc(&lv.f32.P, (size_t)std::max<int64_t>(lv.np, 1) * h.b * NM);
+            amr_alloc(&lv.f32.P16, (size_t)std::max<int64_t>(lv.np, 1) * h.b * NM);
+            amr_alloc(&lv.f32.P16T, (size_t)std::max<int64_t>(lv.np, 1) * h.b * NM);
             amr_alloc(&lv.f32.Q, (size_t)std::max<int64_t>(lv.nq, 1) * h.b * NM);
             hc.rp = std::move(S.crp);
             hc.cj = std::move(S.ccj);
@@ -568,7 +576,6 @@ static void amg_build_structure(amr_model *m) {
     }
     if (g->nc > 32768) throw AmrError(AMR_EUNSUPPORTED, "the multigrid's coarsest level is too large to invert densely");
     amr_alloc(&g->Cd, (size_t)g->nc * 2 * g->nc);  // [A | I] for Gauss-Jordan
-    amr_alloc(&g->gjf, g->nc);
     amr_alloc(&g->Cinv, (size_t)g->nc * g->nc);
     amr_alloc(&g->scratch, 8 + kNormCtas);
     amr_alloc(&g->ticket, 1);
@@ -759,6 +766,28 @@ __global__ void k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *c
     for (int u = 0; u < NM * NM; u++) Ac[(int64_t)u * nbsc + cb] = acc[u];
 }
 
+// The FP32 cycle's prolongator rounded to FP16 (saturated at the FP16 range): P16 by rows, P16T by columns
+// (block e = block pts[e]), and P replaced by the rounded values.  Thread per block.
+template <int S>
+__global__ void k_sa_half(int64_t np, float *P, __half *P16) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np) return;
+#pragma unroll
+    for (int u = 0; u < S; u++) {
+        const __half h = __float2half_rn(fminf(fmaxf(P[t * S + u], -65504.0f), 65504.0f));
+        P16[t * S + u] = h;
+        P[t * S + u] = __half2float(h);
+    }
+}
+template <int S>
+__global__ void k_sa_half_t(int64_t np, const int32_t *pts, const __half *P16, __half *P16T) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    const __half *src = P16 + (int64_t)pts[e] * S;
+#pragma unroll
+    for (int u = 0; u < S; u++) P16T[e * S + u] = src[u];
+}
+
 template <int NM, class V>
 __global__ void k_null_identity(int64_t n, const uint8_t *nulld, const int64_t *diag, V *A, int64_t nbs) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -802,7 +831,9 @@ template <int NB>
 __global__ void __launch_bounds__(256) k_bsr_res(int64_t n, const int64_t *__restrict__ rp,
                                                  const int32_t *__restrict__ cj, const float *__restrict__ A,
                                                  int64_t nbs, const float *__restrict__ x,
-                                                 const float *__restrict__ b, float *__restrict__ out) {
+                                                 const float *__restrict__ b, float *__restrict__ out,
+                                                 const int32_t *__restrict__ halt = nullptr) {
+    if (halt && *halt) return;
     constexpr int G = 16, U = 2;
     const int lane = threadIdx.x % G;
     const unsigned hmask = 0xffffu << (16 * ((threadIdx.x >> 4) & 1));
@@ -853,7 +884,8 @@ __global__ void __launch_bounds__(256) k_bsr_res64(int64_t n, const int64_t *__r
                                                    const int32_t *__restrict__ cj, const double *__restrict__ A,
                                                    int64_t nbs, const uint8_t *__restrict__ mask,
                                                    const double *__restrict__ x, const double *__restrict__ b,
-                                                   double *__restrict__ out) {
+                                                   double *__restrict__ out, const int32_t *__restrict__ halt = nullptr) {
+    if (halt && *halt) return;
     constexpr int RL = 4, RPW = 32 / RL;
     const int lane = threadIdx.x & 31, sub = lane & (RL - 1);
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -955,7 +987,8 @@ __global__ void __launch_bounds__(256) k_bsr_res16(int64_t n, const int64_t *__r
                                                    int64_t nbs, const float *__restrict__ rs,
                                                    const typename FineX<NB>::T *__restrict__ xt,
                                                    const float *__restrict__ b, float *__restrict__ out,
-                                                   const uint8_t *__restrict__ gate) {
+                                                   const uint8_t *__restrict__ gate, const int32_t *__restrict__ halt) {
+    if (halt && *halt) return;
     constexpr int G = 4;
     const int lane = threadIdx.x % G;
     const unsigned gmask = 0xfu << (G * ((threadIdx.x & 31) / G));
@@ -1016,9 +1049,10 @@ __global__ void __launch_bounds__(256) k_bsr_res16(int64_t n, const int64_t *__r
 template <int NB, class V>
 __global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Dinv, const V *__restrict__ r,
                        V *__restrict__ d, V *__restrict__ x, const float *__restrict__ rs = nullptr,
-                       typename FineX<NB>::T *__restrict__ xt = nullptr, const uint8_t *__restrict__ gate = nullptr) {
+                       typename FineX<NB>::T *__restrict__ xt = nullptr, const uint8_t *__restrict__ gate = nullptr,
+                       const int32_t *__restrict__ halt = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (gate && !gate[i])) return;
+    if (i >= n || (gate && !gate[i]) || (halt && *halt)) return;
     V rv[NB], xn[NB];
 #pragma unroll
     for (int c = 0; c < NB; c++) rv[c] = r[i * NB + c];
@@ -1043,10 +1077,10 @@ __global__ void k_cheb(int64_t n, int mode, V s1, V s2, const V *__restrict__ Di
 // bc[a] = sum over the aggregate's nodes (in order) of T_i' r_i; warp per aggregate
 template <int NB, int NM, class V>
 __global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anodes, const V *T, const V *r, V *bc,
-                           const uint8_t *gate = nullptr) {
+                           const uint8_t *gate = nullptr, const int32_t *halt = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (a >= na) return;
+    if (a >= na || (halt && *halt)) return;
     if (gate && !gate[anodes[aptr[a]]]) return;  // an aggregate lies in one part (uniform over the warp)
     V acc[NM];
 #pragma unroll
@@ -1073,9 +1107,10 @@ __global__ void k_restrict(int64_t na, const int64_t *aptr, const int32_t *anode
 // x_i += T_i xc[agg(i)]  (and xt_i = rs_i x_i on the fine level of the FP32 cycle)
 template <int NB, int NM, class V>
 __global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc, V *x, const float *rs = nullptr,
-                          typename FineX<NB>::T *xt = nullptr, const uint8_t *gate = nullptr) {
+                          typename FineX<NB>::T *xt = nullptr, const uint8_t *gate = nullptr,
+                          const int32_t *halt = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (gate && !gate[i])) return;
+    if (i >= n || (gate && !gate[i]) || (halt && *halt)) return;
     const int64_t a = agg[i];
     float v[NB];
 #pragma unroll
@@ -1096,10 +1131,10 @@ __global__ void k_prolong(int64_t n, const int32_t *agg, const V *T, const V *xc
 // bc[I] = sum over the fine rows i that P reaches I from (block s), in order, of P_s' r_i; warp per aggregate
 template <int NB, int NM, class V>
 __global__ void k_restrict_sa(int64_t na, const int64_t *ptp, const int32_t *pti, const int32_t *pts, const V *P,
-                              const V *r, V *bc, const uint8_t *gate = nullptr) {
+                              const V *r, V *bc, const uint8_t *gate = nullptr, const int32_t *halt = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (a >= na) return;
+    if (a >= na || (halt && *halt)) return;
     // the rows P reaches an aggregate from lie in the aggregate's part (uniform over the warp)
     if (gate && ptp[a] < ptp[a + 1] && !gate[pti[ptp[a]]]) return;
     V acc[NM];
@@ -1129,9 +1164,9 @@ __global__ void k_restrict_sa(int64_t na, const int64_t *ptp, const int32_t *pti
 template <int NB, int NM, class V>
 __global__ void k_prolong_sa(int64_t n, const int64_t *prp, const int32_t *pcj, const V *P, const V *xc, V *x,
                              const float *rs = nullptr, typename FineX<NB>::T *xt = nullptr,
-                             const uint8_t *gate = nullptr) {
+                             const uint8_t *gate = nullptr, const int32_t *halt = nullptr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (gate && !gate[i])) return;
+    if (i >= n || (gate && !gate[i]) || (halt && *halt)) return;
     V s[NB];
 #pragma unroll
     for (int c = 0; c < NB; c++) s[c] = x[i * NB + c];
@@ -1159,6 +1194,111 @@ __global__ void k_prolong_sa(int64_t n, const int64_t *prp, const int32_t *pcj, 
     }
 }
 
+// row c of an FP16 prolongator block (NM entries) as floats: paired loads when NM is even (the block then
+// starts on a 4-byte boundary)
+template <int NM>
+__device__ __forceinline__ void half_row(const __half *blk, int c, float *v) {
+    if constexpr (NM % 2 == 0) {
+        const __half2 *p2 = reinterpret_cast<const __half2 *>(blk + c * NM);
+#pragma unroll
+        for (int h = 0; h < NM / 2; h++) {
+            const float2 f = __half22float2(p2[h]);
+            v[2 * h] = f.x;
+            v[2 * h + 1] = f.y;
+        }
+    } else {
+#pragma unroll
+        for (int mm = 0; mm < NM; mm++) v[mm] = __half2float(blk[c * NM + mm]);
+    }
+}
+
+// the FP32 cycle's restriction with the FP16 prolongator by columns: bc[I] = sum over e of P16T_e' r_pti[e];
+// TPA threads per aggregate (a warp, or a whole CTA of TPA threads where the aggregates are few and long),
+// threads over consecutive blocks, the partial sums reduced in a fixed order
+template <int NB, int NM, int TPA>
+__global__ void k_restrict_sa16(int64_t na, const int64_t *ptp, const int32_t *pti, const __half *PT,
+                                const float *r, float *bc, const uint8_t *gate = nullptr,
+                                const int32_t *halt = nullptr) {
+    static_assert(TPA == 32 || TPA == 256, "a warp or a CTA of 256 per aggregate");
+    const int lane = threadIdx.x & 31, tid = threadIdx.x % TPA;
+    const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    if (a >= na || (halt && *halt)) return;  // (uniform over a CTA when TPA is the CTA)
+    if (gate && ptp[a] < ptp[a + 1] && !gate[pti[ptp[a]]]) return;
+    float acc[NM];
+#pragma unroll
+    for (int mm = 0; mm < NM; mm++) acc[mm] = 0.0f;
+    for (int64_t e = ptp[a] + tid; e < ptp[a + 1]; e += TPA) {
+        const int64_t i = pti[e];
+        const __half *ps = PT + e * NB * NM;
+#pragma unroll
+        for (int c = 0; c < NB; c++) {
+            const float rv = r[i * NB + c];
+            float pv[NM];
+            half_row<NM>(ps, c, pv);
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) acc[mm] = fmaf(pv[mm], rv, acc[mm]);
+        }
+    }
+#pragma unroll
+    for (int mm = 0; mm < NM; mm++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[mm] += __shfl_down_sync(0xffffffffu, acc[mm], o);
+    if constexpr (TPA == 32) {
+        if (lane == 0)
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) bc[a * NM + mm] = acc[mm];
+    } else {
+        __shared__ float part[TPA / 32][NM];
+        if (lane == 0)
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) part[tid >> 5][mm] = acc[mm];
+        __syncthreads();
+        if (tid < NM) {
+            float v = 0.0f;
+            for (int w = 0; w < TPA / 32; w++) v += part[w][tid];
+            bc[a * NM + tid] = v;
+        }
+    }
+}
+
+// the FP32 cycle's prolongation with the FP16 prolongator by rows: x_i += sum over row i's blocks t of
+// P16_t xc[pcj[t]] (and xt_i = rs_i x_i on the fine level)
+template <int NB, int NM>
+__global__ void k_prolong_sa16(int64_t n, const int64_t *prp, const int32_t *pcj, const __half *P, const float *xc,
+                               float *x, const float *rs = nullptr, typename FineX<NB>::T *xt = nullptr,
+                               const uint8_t *gate = nullptr, const int32_t *halt = nullptr) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (gate && !gate[i]) || (halt && *halt)) return;
+    float s[NB];
+#pragma unroll
+    for (int c = 0; c < NB; c++) s[c] = x[i * NB + c];
+    for (int64_t t = prp[i]; t < prp[i + 1]; t++) {
+        const __half *pt = P + t * NB * NM;
+        const float *xa = xc + (int64_t)pcj[t] * NM;
+        float xv[NM];
+#pragma unroll
+        for (int mm = 0; mm < NM; mm++) xv[mm] = xa[mm];
+#pragma unroll
+        for (int c = 0; c < NB; c++) {
+            float pv[NM];
+            half_row<NM>(pt, c, pv);
+#pragma unroll
+            for (int mm = 0; mm < NM; mm++) s[c] = fmaf(pv[mm], xv[mm], s[c]);
+        }
+    }
+    float v[NB];
+#pragma unroll
+    for (int c = 0; c < NB; c++) {
+        x[i * NB + c] = s[c];
+        v[c] = s[c];
+    }
+    if (xt) {
+#pragma unroll
+        for (int c = 0; c < NB; c++) v[c] *= rs[i];
+        xt[i] = FineX<NB>::make(v);
+    }
+}
+
 // dense coarsest level: expand the BSR matrix, invert it (Gauss-Jordan, FP64), multiply
 template <int NM, class V>
 __global__ void k_dense_expand(int64_t n, const int64_t *rp, const int32_t *cj, const V *A, int64_t nbs, double *C,
@@ -1176,29 +1316,24 @@ __global__ void k_dense_init(int64_t nc, double *C) {  // C is nc x 2nc: [A | I]
     const int64_t r = t / (2 * nc), c = t % (2 * nc);
     C[t] = (c >= nc && c - nc == r) ? 1.0 : 0.0;
 }
-// one Gauss-Jordan step on pivot p of an SPD matrix (no pivoting needed): the row factors
-// f_r = C[r][p] / C[p][p] (0 for the pivot row), one division per row
-__global__ void k_gj_factor(int64_t nc, int64_t p, const double *C, double *f) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nc) return;
-    const int64_t w = 2 * nc;
-    f[r] = (r == p) ? 0.0 : C[r * w + p] / C[p * w + p];
-}
-// then C[r][c] -= f_r C[p][c] for c != p; a grid row per matrix row, and rows with f_r = 0 (every row outside
-// the pivot's block when the level is block diagonal, as for the parts of a batch) are left as they are
-__global__ void k_gj_eliminate(int64_t nc, int64_t p, const double *f, double *C) {
+// One Gauss-Jordan step on pivot p of an SPD matrix (no pivoting needed), one launch: a grid row per matrix
+// row r != p, with the factor f_r = C[r][p] / C[p][p] (rows with f_r = 0, every row outside the pivot's block
+// when the level is block diagonal as for the parts of a batch, are left as they are), then
+// C[r][c] -= f_r C[p][c] for the columns c > p.  Columns c <= p of the left half are not updated: the pivot
+// row is zero there once eliminated, and of them only the diagonal, which no later step changes, is read
+// afterwards.  Nothing a step writes (rows r != p, columns > p) is read by another CTA of the same step.
+__global__ void k_gj_step(int64_t nc, int64_t p, double *C) {
     const int64_t r = blockIdx.y;
-    const double fr = f[r];
-    if (fr == 0.0) return;
+    if (r == p) return;
     const int64_t w = 2 * nc;
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= w || c == p) return;
+    __shared__ double sf;  // the FP64 division once per CTA, not per thread: the FP64 pipe is narrow
+    if (threadIdx.x == 0) sf = C[r * w + p] / C[p * w + p];
+    __syncthreads();
+    const double fr = sf;
+    if (fr == 0.0) return;
+    const int64_t c = p + 1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= w) return;
     C[r * w + c] -= fr * C[p * w + c];
-}
-__global__ void k_gj_column(int64_t nc, int64_t p, double *C) {  // clear column p below/above the pivot
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nc || r == p) return;
-    C[r * 2 * nc + p] = 0.0;
 }
 template <class V>
 __global__ void k_dense_extract(int64_t nc, const double *C, V *Cinv) {
@@ -1209,10 +1344,10 @@ __global__ void k_dense_extract(int64_t nc, const double *C, V *Cinv) {
 }
 // x = Cinv b, warp per row
 template <class V>
-__global__ void k_dense_mv(int64_t nc, const V *Cinv, const V *b, V *x) {
+__global__ void k_dense_mv(int64_t nc, const V *Cinv, const V *b, V *x, const int32_t *halt = nullptr) {
     const int lane = threadIdx.x & 31;
     const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r >= nc) return;
+    if (r >= nc || (halt && *halt)) return;
     V s = V(0);
     // zero entries skipped: the inverse of a block-diagonal level (the parts of a batch) is block
     // diagonal, and a part's non-finite values must not reach the others through 0 * inf
@@ -1292,20 +1427,21 @@ template <int NB>
 void launch_res16(amr_model *m, const AmrAmg *g, const AmgLevel &L, const typename FineX<NB>::T *xt, const float *b,
                   float *r) {
     const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
-    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r, g->gate);
+    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r, g->gate,
+                                                 g->halt);
     AMR_COUNT(1);
 }
 
 // r = b - A x on a level (mask: rows of the identity, FP64 fine level only)
 template <int NB, class V>
 void bsr_res(cudaStream_t s, const AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask, const V *x, const V *b,
-             V *out) {
+             V *out, const int32_t *halt = nullptr) {
     if constexpr (std::is_same<V, float>::value) {
         const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 16, 256), (int64_t)sm_count() * 8);
-        k_bsr_res<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, x, b, out);
+        k_bsr_res<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, x, b, out, halt);
     } else {
         const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
-        k_bsr_res64<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, mask, x, b, out);
+        k_bsr_res64<NB><<<grid, 256, 0, s>>>(L.n, L.rp, L.cj, A, nbs, mask, x, b, out, halt);
     }
     AMR_COUNT(1);
 }
@@ -1345,7 +1481,7 @@ struct Cycle {
         cudaStream_t s = m->stream;
         AmgLevel &L = g->L[l];
         if (l + 1 == g->L.size()) {
-            k_dense_mv<V><<<nblk(g->nc * 32, 256), 256, 0, s>>>(g->nc, coarse_inverse(g), b, x);
+            k_dense_mv<V><<<nblk(g->nc * 32, 256), 256, 0, s>>>(g->nc, coarse_inverse(g), b, x, g->halt);
             AMR_COUNT(1);
             return;
         }
@@ -1367,6 +1503,7 @@ struct Cycle {
         XT *xt = half ? reinterpret_cast<XT *>(g->xt) : nullptr;
         const float *rs = half ? g->rs : nullptr;
         const uint8_t *gate = half ? g->gate : nullptr;
+        const int32_t *halt = g->halt;
         auto residual = [&]() {
             if constexpr (kHalf) {
                 if (half) {
@@ -1374,32 +1511,46 @@ struct Cycle {
                     return;
                 }
             }
-            bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r);
+            bsr_res<NB, V>(s, L, A, nbs, mask, x, b, v.r, halt);
         };
         // pre-smoothing from x = 0
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x, rs, xt, gate);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 0, V(0), s2a, v.Dinv, b, v.d, x, rs, xt, gate, halt);
         residual();
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, rs, xt, gate);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, rs, xt, gate, halt);
         // coarse correction
         residual();
         AmgLevel &C = g->L[l + 1];
         AmgVals<V> &cv = vals<V>(C);
-        if (L.smooth)
-            k_restrict_sa<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.ptp, L.pti, L.pts, v.P, v.r,
-                                                                             cv.bv, gate);
-        else
+        if (L.smooth) {
+            if constexpr (std::is_same<V, float>::value)
+            {
+                // a warp per aggregate, or a CTA per aggregate where there are too few for a wave of warps
+                if (L.naggs >= 8 * (int64_t)sm_count())
+                    k_restrict_sa16<NB, NM, 32><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.ptp, L.pti,
+                                                                                       v.P16T, v.r, cv.bv, gate, halt);
+                else
+                    k_restrict_sa16<NB, NM, 256><<<(unsigned)L.naggs, 256, 0, s>>>(L.naggs, L.ptp, L.pti, v.P16T, v.r,
+                                                                                   cv.bv, gate, halt);
+            }
+            else
+                k_restrict_sa<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.ptp, L.pti, L.pts, v.P,
+                                                                                 v.r, cv.bv, gate, halt);
+        } else
             k_restrict<NB, NM, V><<<nblk(L.naggs * 32, 256), 256, 0, s>>>(L.naggs, L.aptr, L.anodes, v.T, v.r,
-                                                                          cv.bv, gate);
+                                                                          cv.bv, gate, halt);
         level(m, g, l + 1, cv.bv, cv.x);
-        if (L.smooth)
-            k_prolong_sa<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.prp, L.pcj, v.P, cv.x, x, rs, xt, gate);
-        else
-            k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt, gate);
+        if (L.smooth) {
+            if constexpr (std::is_same<V, float>::value)
+                k_prolong_sa16<NB, NM><<<gn, 256, 0, s>>>(L.n, L.prp, L.pcj, v.P16, cv.x, x, rs, xt, gate, halt);
+            else
+                k_prolong_sa<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.prp, L.pcj, v.P, cv.x, x, rs, xt, gate, halt);
+        } else
+            k_prolong<NB, NM, V><<<gn, 256, 0, s>>>(L.n, L.agg, v.T, cv.x, x, rs, xt, gate, halt);
         // post-smoothing
         residual();
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x, rs, xt, gate);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 1, V(0), s2a, v.Dinv, v.r, v.d, x, rs, xt, gate, halt);
         residual();
-        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, nullptr, nullptr, gate);
+        k_cheb<NB, V><<<gn, 256, 0, s>>>(L.n, 2, s1, s2b, v.Dinv, v.r, v.d, x, nullptr, nullptr, gate, halt);
         AMR_COUNT(7);
         AMR_CUDA(cudaGetLastError());
     }
@@ -1447,6 +1598,11 @@ struct Cycle {
         auto grid = [](int64_t n) { return std::max(1u, nblk(n, 128)); };
         k_sa_prolongator<BF, NM, V><<<grid(F.n), 128, 0, s>>>(F.n, F.prp, F.pcj, F.pkp, F.pkk, F.cj, A, nbs,
                                                                     fv.T, fv.Dinv, F.agg, w, mask, fv.P);
+        if constexpr (std::is_same<V, float>::value) {  // the FP32 cycle applies P in FP16
+            k_sa_half<BF * NM><<<grid(F.np), 128, 0, s>>>(F.np, fv.P, fv.P16);
+            k_sa_half_t<BF * NM><<<grid(F.np), 128, 0, s>>>(F.np, F.pts, fv.P16, fv.P16T);
+            AMR_COUNT(2);
+        }
         k_sa_ap<BF, NM, V><<<grid(F.nq), 128, 0, s>>>(F.nq, F.qrow, F.qcj, F.rp, F.cj, A, nbs, F.prp, F.pcj,
                                                             fv.P, fv.Q);
         k_sa_galerkin<BF, NM, V><<<grid(C.nblocks), 128, 0, s>>>(C.nblocks, F.crow, C.cj, F.ptp, F.pti, F.pts,
@@ -1493,11 +1649,8 @@ struct Cycle {
         if (!g->gj_exec) {
             cudaGraph_t gr = nullptr;
             AMR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-            for (int64_t p = 0; p < nc; p++) {
-                k_gj_factor<<<nblk(nc, 256), 256, 0, s>>>(nc, p, g->Cd, g->gjf);
-                k_gj_eliminate<<<dim3(nblk(w, 256), (unsigned)nc), 256, 0, s>>>(nc, p, g->gjf, g->Cd);
-                k_gj_column<<<nblk(nc, 256), 256, 0, s>>>(nc, p, g->Cd);
-            }
+            for (int64_t p = 0; p < nc; p++)
+                k_gj_step<<<dim3(nblk(w - p - 1, 256), (unsigned)nc), 256, 0, s>>>(nc, p, g->Cd);
             const cudaError_t ce = cudaStreamEndCapture(s, &gr);
             if (ce == cudaSuccess) {
                 const cudaError_t ie = cudaGraphInstantiate(&g->gj_exec, gr, 0);
@@ -1509,7 +1662,7 @@ struct Cycle {
             }
         }
         AMR_CUDA(cudaGraphLaunch(g->gj_exec, s));
-        AMR_COUNT(3 * nc);
+        AMR_COUNT(nc);
         k_dense_extract<V><<<nblk(nc * nc, 256), 256, 0, s>>>(nc, g->Cd, coarse_inverse(g));
         AMR_COUNT(1);
         AMR_CUDA(cudaGetLastError());
@@ -1573,6 +1726,11 @@ void amr_amg_prepare64(amr_model *m) {
 // z = V-cycle(r), fine-level node-major FP32 vectors, on the handle's stream
 void amr_amg_set_gate(amr_model *m, const uint8_t *gate) {
     if (m->amg) m->amg->gate = gate;
+}
+
+// a device flag read by every kernel of the cycle: while it is nonzero they return at once
+void amr_amg_set_halt(amr_model *m, const int32_t *halt) {
+    if (m->amg) m->amg->halt = halt;
 }
 
 void amr_amg_vcycle(amr_model *m, const float *r, float *z) {

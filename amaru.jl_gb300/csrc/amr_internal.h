@@ -250,6 +250,7 @@ void amr_amg_prepare(amr_model *m);
 void amr_amg_vcycle(amr_model *m, const float *r, float *z);
 // rows of the fine level the FP32 cycle skips (bytes per node, 0 = skip; null: none): a batch's finished parts
 void amr_amg_set_gate(amr_model *m, const uint8_t *gate);
+void amr_amg_set_halt(amr_model *m, const int32_t *halt);
 void amr_amg_prepare64(amr_model *m);                           // the same hierarchy in FP64
 void amr_amg_vcycle64(amr_model *m, const double *r, double *z);
 void amr_amg_invalidate(amr_model *m);

@@ -806,6 +806,14 @@ static AmrSolveResult solve_mixed(amr_model *m, double *x, const double *b, doub
     return res;
 }
 
+// The V-cycle's kernels read the solve's stop flag while this scope lives: the iterations a replayed chunk
+// holds after the flag is raised (a refresh or convergence is due) then cost launches only.
+struct HaltScope {
+    amr_model *m;
+    HaltScope(amr_model *m_, const int32_t *flag) : m(m_) { amr_amg_set_halt(m, flag); }
+    ~HaltScope() { amr_amg_set_halt(m, nullptr); }
+};
+
 // solve_system! with the multigrid preconditioner: the mixed solver's PCG (FP32 Krylov vectors,
 // FP64 true-residual refreshes decide convergence) with z = V-cycle(r) in place of block-Jacobi.
 template <int B>
@@ -835,6 +843,7 @@ static AmrSolveResult solve_amg(amr_model *m, double *x, const double *b, double
         AMR_CUDA(cudaGetLastError());
     };
     refresh(1);
+    HaltScope halt_scope(m, &w->ctl->stop);
     // one iteration as a CUDA graph, captured once its arguments are fixed (after the first
     // refresh: stop_rr depends on |b|), then replayed; its kernels are counted per replay
     cudaGraph_t graph = nullptr;
@@ -1001,6 +1010,7 @@ static AmrSolveResult solve_amg_fp64(amr_model *m, double *x, const double *b, d
         AMR_CUDA(cudaGetLastError());
     };
     refresh(1);
+    HaltScope halt_scope(m, &w->ctl->stop);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     long long per_iter = 0;
