@@ -285,6 +285,7 @@ struct AmgLevel {
     // each block's row) and the row of each coarse block
     bool smooth = false;
     int64_t np = 0, nq = 0;
+    int p_steps = 0, q_steps = 0;  // halvings of a lower-bound search in the longest row of P / of A P
     int64_t *prp = nullptr, *pkp = nullptr, *qrp = nullptr, *ptp = nullptr;
     int32_t *pcj = nullptr, *pkk = nullptr, *qcj = nullptr, *qrow = nullptr, *pti = nullptr, *pts = nullptr,
             *crow = nullptr;
@@ -300,8 +301,9 @@ struct AmrAmg {
     cudaGraphExec_t gj_exec = nullptr;  // the Gauss-Jordan steps, captured once
     float *Cinv = nullptr;      // nc x nc inverse, FP32 cycle
     double *Cinv64 = nullptr;   // nc x nc inverse, FP64 cycle
-    double *scratch = nullptr;  // norms: [0] result, [8..] per-CTA partials
+    double *scratch = nullptr;  // norms: [0] result, [1] the power iteration's estimate, [8..] per-CTA partials
     unsigned int *ticket = nullptr;
+    int32_t *pstop = nullptr;   // the power iteration met a zero or non-finite norm: its remaining steps return
     int64_t dofs_version = -1;
     bool numeric_valid = false, numeric64_valid = false;
     // The FP32 cycle's fine-level residual reads an FP16 copy of the symmetrically scaled matrix
@@ -356,7 +358,7 @@ void amr_amg_free(amr_model *m) {
         amr_free(v.qcj); amr_free(v.qrow); amr_free(v.pti); amr_free(v.pts); amr_free(v.crow);
     }
     if (g->gj_exec) cudaGraphExecDestroy(g->gj_exec);
-    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket);
+    amr_free(g->Cd); amr_free(g->Cinv); amr_free(g->Cinv64); amr_free(g->scratch); amr_free(g->ticket); amr_free(g->pstop);
     amr_free(g->A16); amr_free(g->rs); amr_free(g->xt);
     delete g;
     m->amg = nullptr;
@@ -490,6 +492,16 @@ static void amg_build_structure(amr_model *m) {
             lv.smooth = true;
             lv.np = S.prp[h.n];
             lv.nq = S.qrp[h.n];
+            {
+                int64_t mp = 0, mq = 0;
+                for (int64_t i = 0; i < h.n; i++) {
+                    mp = std::max(mp, S.prp[i + 1] - S.prp[i]);
+                    mq = std::max(mq, S.qrp[i + 1] - S.qrp[i]);
+                }
+                auto bits = [](int64_t v) { int b = 0; while (v > 0) { b++; v >>= 1; } return b; };
+                lv.p_steps = bits(mp);
+                lv.q_steps = bits(mq);
+            }
             auto up64 = [&](int64_t *&d, const std::vector<int64_t> &v) {
                 amr_alloc(&d, std::max<size_t>(v.size(), 1));
                 amr_h2d(m, d, v.data(), v.size() * sizeof(int64_t));
@@ -579,6 +591,7 @@ static void amg_build_structure(amr_model *m) {
     amr_alloc(&g->Cinv, (size_t)g->nc * g->nc);
     amr_alloc(&g->scratch, 8 + kNormCtas);
     amr_alloc(&g->ticket, 1);
+    amr_alloc(&g->pstop, 1);
     amr_alloc(&g->A16, (size_t)m->bstride * B * B);
     amr_alloc(&g->rs, m->nnodes);
     amr_alloc(&g->xt, (size_t)m->nnodes * (B == 3 ? 4 : 2));
@@ -687,40 +700,74 @@ __global__ void k_sa_prolongator(int64_t n, const int64_t *prp, const int32_t *p
     }
 }
 
+// Lower bound of J in the sorted columns c[base, base + len) in `steps` halvings (steps >= the bit length of
+// the longest row), for U independent rows at once so that their dependent loads overlap: on return
+// base[u] is the first position whose column is >= J[u].
+template <int U>
+__device__ __forceinline__ void lower_bounds(const int32_t *c, int64_t *base, int64_t *len, const int32_t *J,
+                                             int steps) {
+    for (int st = 0; st < steps; st++)
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (len[u] > 0) {
+                const int64_t half = len[u] >> 1;
+                if (c[base[u] + half] < J[u]) {
+                    base[u] += half + 1;
+                    len[u] -= half + 1;
+                } else {
+                    len[u] = half;
+                }
+            }
+}
+
 // A P, thread per block q of its pattern (row i, aggregate J): sum over the row's blocks k of A in order of
-// A_k P_t, t the block of P row cj[k] in column J (if any)
+// A_k P_t, t the block of P row cj[k] in column J (if any).  Four blocks k at a time: their P rows are searched
+// together, then the products are added in order of k.
 template <int BF, int NM, class V>
-__global__ void k_sa_ap(int64_t nq, const int32_t *qrow, const int32_t *qcj, const int64_t *rpf, const int32_t *cjf,
-                        const V *Af, int64_t nbsf, const int64_t *prp, const int32_t *pcj, const V *P, V *Q) {
+__global__ void __launch_bounds__(128) k_sa_ap(int64_t nq, const int32_t *qrow, const int32_t *qcj,
+                                                const int64_t *rpf, const int32_t *cjf, const V *Af, int64_t nbsf,
+                                                const int64_t *prp, const int32_t *pcj, const V *P, V *Q,
+                                                int steps) {
+    constexpr int U = 4;
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int64_t i = qrow[q];
     const int32_t J = qcj[q];
+    const int32_t Ju[U] = {J, J, J, J};
     V acc[BF * NM];
 #pragma unroll
     for (int u = 0; u < BF * NM; u++) acc[u] = V(0);
-    for (int64_t k = rpf[i]; k < rpf[i + 1]; k++) {
-        const int64_t j = cjf[k];
-        int64_t t = -1;
-        for (int64_t u = prp[j]; u < prp[j + 1]; u++) {
-            const int32_t c = pcj[u];
-            if (c >= J) {
-                if (c == J) t = u;
-                break;
+    const int64_t k1 = rpf[i + 1];
+    for (int64_t kb = rpf[i]; kb < k1; kb += U) {
+        int64_t base[U], len[U], end[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (kb + u < k1) {
+                const int64_t j = cjf[kb + u];
+                base[u] = prp[j];
+                end[u] = prp[j + 1];
+            } else {
+                base[u] = end[u] = 0;
             }
+            len[u] = end[u] - base[u];
         }
-        if (t < 0) continue;
-        const V *pt = P + t * BF * NM;
+        lower_bounds<U>(pcj, base, len, Ju, steps);
 #pragma unroll
-        for (int d = 0; d < BF; d++) {
-            V a[BF];
+        for (int u = 0; u < U; u++) {
+            if (base[u] >= end[u] || pcj[base[u]] != J) continue;
+            const int64_t k = kb + u;
+            const V *pt = P + base[u] * BF * NM;
 #pragma unroll
-            for (int c = 0; c < BF; c++) a[c] = Af[(int64_t)(c * BF + d) * nbsf + k];
+            for (int d = 0; d < BF; d++) {
+                V a[BF];
 #pragma unroll
-            for (int mm = 0; mm < NM; mm++) {
-                const V pv = pt[d * NM + mm];
+                for (int c = 0; c < BF; c++) a[c] = Af[(int64_t)(c * BF + d) * nbsf + k];
 #pragma unroll
-                for (int c = 0; c < BF; c++) acc[c * NM + mm] = vfma(a[c], pv, acc[c * NM + mm]);
+                for (int mm = 0; mm < NM; mm++) {
+                    const V pv = pt[d * NM + mm];
+#pragma unroll
+                    for (int c = 0; c < BF; c++) acc[c * NM + mm] = vfma(a[c], pv, acc[c * NM + mm]);
+                }
             }
         }
     }
@@ -730,36 +777,50 @@ __global__ void k_sa_ap(int64_t nq, const int32_t *qrow, const int32_t *qcj, con
 }
 
 // coarse operator P' (A P), thread per coarse block (I, J): sum over the fine rows i that P reaches I from
-// (block s), in order, of P_s' Q_iJ (if row i of A P has column J)
+// (block s), in order, of P_s' Q_iJ (if row i of A P has column J).  Four rows i at a time: their A P rows are
+// searched together, then the products are added in order.
 template <int BF, int NM, class V>
-__global__ void k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *ccj, const int64_t *ptp,
-                              const int32_t *pti, const int32_t *pts, const V *P, const int64_t *qrp,
-                              const int32_t *qcj, const V *Q, V *Ac, int64_t nbsc) {
+__global__ void __launch_bounds__(128) k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *ccj,
+                                                      const int64_t *ptp, const int32_t *pti, const int32_t *pts,
+                                                      const V *P, const int64_t *qrp, const int32_t *qcj,
+                                                      const V *Q, V *Ac, int64_t nbsc, int steps) {
+    constexpr int U = 4;
     const int64_t cb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (cb >= ncb) return;
     const int32_t I = crow[cb], J = ccj[cb];
+    const int32_t Ju[U] = {J, J, J, J};
     V acc[NM * NM];
 #pragma unroll
     for (int u = 0; u < NM * NM; u++) acc[u] = V(0);
-    for (int64_t e = ptp[I]; e < ptp[I + 1]; e++) {
-        const int64_t i = pti[e];
-        int64_t lo = qrp[i], hi = qrp[i + 1];  // J in the sorted columns of row i of A P
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (qcj[mid] < J) lo = mid + 1;
-            else hi = mid;
+    const int64_t e1 = ptp[I + 1];
+    for (int64_t eb = ptp[I]; eb < e1; eb += U) {
+        int64_t base[U], len[U], end[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (eb + u < e1) {
+                const int64_t i = pti[eb + u];
+                base[u] = qrp[i];
+                end[u] = qrp[i + 1];
+            } else {
+                base[u] = end[u] = 0;
+            }
+            len[u] = end[u] - base[u];
         }
-        if (lo >= qrp[i + 1] || qcj[lo] != J) continue;
-        const V *ps = P + (int64_t)pts[e] * BF * NM, *qv = Q + lo * BF * NM;
+        lower_bounds<U>(qcj, base, len, Ju, steps);
 #pragma unroll
-        for (int c = 0; c < BF; c++) {
-            V pr[NM], qr[NM];
+        for (int u = 0; u < U; u++) {
+            if (base[u] >= end[u] || qcj[base[u]] != J) continue;
+            const V *ps = P + (int64_t)pts[eb + u] * BF * NM, *qv = Q + base[u] * BF * NM;
 #pragma unroll
-            for (int u = 0; u < NM; u++) { pr[u] = ps[c * NM + u]; qr[u] = qv[c * NM + u]; }
+            for (int c = 0; c < BF; c++) {
+                V pr[NM], qr[NM];
 #pragma unroll
-            for (int a = 0; a < NM; a++)
+                for (int w = 0; w < NM; w++) { pr[w] = ps[c * NM + w]; qr[w] = qv[c * NM + w]; }
 #pragma unroll
-                for (int b = 0; b < NM; b++) acc[a * NM + b] = vfma(pr[a], qr[b], acc[a * NM + b]);
+                for (int a = 0; a < NM; a++)
+#pragma unroll
+                    for (int b = 0; b < NM; b++) acc[a * NM + b] = vfma(pr[a], qr[b], acc[a * NM + b]);
+            }
         }
     }
 #pragma unroll
@@ -767,25 +828,20 @@ __global__ void k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *c
 }
 
 // The FP32 cycle's prolongator rounded to FP16 (saturated at the FP16 range): P16 by rows, P16T by columns
-// (block e = block pts[e]), and P replaced by the rounded values.  Thread per block.
-template <int S>
-__global__ void k_sa_half(int64_t np, float *P, __half *P16) {
+// (block e = block pts[e]), and P replaced by the rounded values.  Thread per entry (np blocks of S).
+__global__ void k_sa_half(int64_t n, float *P, __half *P16) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= np) return;
-#pragma unroll
-    for (int u = 0; u < S; u++) {
-        const __half h = __float2half_rn(fminf(fmaxf(P[t * S + u], -65504.0f), 65504.0f));
-        P16[t * S + u] = h;
-        P[t * S + u] = __half2float(h);
-    }
+    if (t >= n) return;
+    const __half h = __float2half_rn(fminf(fmaxf(P[t], -65504.0f), 65504.0f));
+    P16[t] = h;
+    P[t] = __half2float(h);
 }
 template <int S>
 __global__ void k_sa_half_t(int64_t np, const int32_t *pts, const __half *P16, __half *P16T) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= np) return;
-    const __half *src = P16 + (int64_t)pts[e] * S;
-#pragma unroll
-    for (int u = 0; u < S; u++) P16T[e * S + u] = src[u];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np * S) return;
+    const int64_t e = t / S;
+    P16T[t] = P16[(int64_t)pts[e] * S + (t - e * S)];
 }
 
 template <int NM, class V>
@@ -1363,7 +1419,9 @@ __global__ void k_dense_mv(int64_t nc, const V *Cinv, const V *b, V *x, const in
 // sum of squares for the power iteration: per-CTA partials (fixed element assignment), the last CTA
 // adds them in CTA order
 template <class V>
-__global__ void k_norm2(int64_t n, const V *v, double *partials, unsigned int *ticket, double *out) {
+__global__ void k_norm2(int64_t n, const V *v, double *partials, unsigned int *ticket, double *out,
+                        const int32_t *halt = nullptr) {
+    if (halt && *halt) return;  // (uniform: no CTA takes a ticket)
     __shared__ double sh[256];
     __shared__ bool last;
     double s = 0.0;
@@ -1407,6 +1465,52 @@ __global__ void k_scale(int64_t n, V s, V *x) {
     if (i < n) x[i] *= s;
 }
 
+// xt_i = rs_i x_i (the fine level's scaled iterate), thread per node
+template <int NB>
+__global__ void k_make_xt(int64_t n, const float *x, const float *rs, typename FineX<NB>::T *xt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float v[NB];
+#pragma unroll
+    for (int c = 0; c < NB; c++) v[c] = x[i * NB + c] * rs[i];
+    xt[i] = FineX<NB>::make(v);
+}
+
+// Power iteration on the device, with one host read at the end.  Start: the estimate 1 and no stop.
+__global__ void k_power_init(double *scratch, int32_t *stop) {
+    scratch[1] = 1.0;
+    *stop = 0;
+}
+// Next iterate from bv = Dinv A x and n2 = |bv|^2 (scratch[0]): x = bv / sqrt(n2), the estimate sqrt(n2) kept
+// in scratch[1]; a zero or non-finite n2 raises the stop flag and keeps the previous estimate and iterate.
+// Thread per node; xt_i = rs_i x_i as well where the fine level of the FP32 cycle reads it.
+template <int NB, class V>
+__global__ void k_power_next(int64_t n, const V *bv, V *x, double *scratch, int32_t *stop, const float *rs,
+                             typename FineX<NB>::T *xt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || *stop) return;
+    const double n2 = scratch[0];
+    if (!(n2 > 0.0)) {
+        if (i == 0) *stop = 1;  // (every thread sees the same n2 and leaves x as it is)
+        return;
+    }
+    const double lam = sqrt(n2);
+    if (i == 0) scratch[1] = lam;
+    const V sc = (V)(1.0 / lam);
+    float v[NB];
+#pragma unroll
+    for (int c = 0; c < NB; c++) {
+        const V xv = bv[i * NB + c] * sc;
+        x[i * NB + c] = xv;
+        v[c] = (float)xv;
+    }
+    if (xt) {
+#pragma unroll
+        for (int c = 0; c < NB; c++) v[c] *= rs[i];
+        xt[i] = FineX<NB>::make(v);
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1425,10 +1529,9 @@ int sm_count() {
 // 8 per SM (2.67 waves) measured faster than one resident wave.
 template <int NB>
 void launch_res16(amr_model *m, const AmrAmg *g, const AmgLevel &L, const typename FineX<NB>::T *xt, const float *b,
-                  float *r) {
+                  float *r, const uint8_t *gate, const int32_t *halt) {
     const unsigned grid = (unsigned)std::min<int64_t>(nblk(L.n * 4, 256), (int64_t)sm_count() * 8);
-    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r, g->gate,
-                                                 g->halt);
+    k_bsr_res16<NB><<<grid, 256, 0, m->stream>>>(L.n, L.rp, L.cj, g->A16, m->bstride, g->rs, xt, b, r, gate, halt);
     AMR_COUNT(1);
 }
 
@@ -1507,7 +1610,7 @@ struct Cycle {
         auto residual = [&]() {
             if constexpr (kHalf) {
                 if (half) {
-                    launch_res16<NB>(m, g, L, xt, b, v.r);
+                    launch_res16<NB>(m, g, L, xt, b, v.r, g->gate, g->halt);
                     return;
                 }
             }
@@ -1557,28 +1660,42 @@ struct Cycle {
     // largest eigenvalue of Dinv A by power iteration (15 steps from a pseudo-random start, which excites
     // the localized high-frequency modes of distorted elements; |x| = 1 after each step)
     template <int NB>
+    // (the fine level of the FP32 cycle iterates on the FP16 copy the cycle's residuals read; the steps run
+    // without host reads, a device flag ending them early at a zero or non-finite norm)
     static double lambda(amr_model *m, AmrAmg *g, AmgLevel &L, const V *A, int64_t nbs, const uint8_t *mask) {
         cudaStream_t s = m->stream;
         AmgVals<V> &v = vals<V>(L);
         const int64_t nv = L.n * NB;
         const unsigned gnorm = (unsigned)std::min<int64_t>(kNormCtas, std::max<int64_t>(1, nblk(nv, 256)));
+        using XT = typename FineX<NB>::T;
+        constexpr bool kHalf = std::is_same<V, float>::value && NB == B && (NB == 2 || NB == 3);
+        const bool half = kHalf && &L == &g->L[0];
+        XT *xt = half ? reinterpret_cast<XT *>(g->xt) : nullptr;
+        const float *rs = half ? g->rs : nullptr;
+        const int32_t *stop = g->pstop;
+        k_power_init<<<1, 1, 0, s>>>(g->scratch, g->pstop);
         k_fill_random<V><<<nblk(nv, 256), 256, 0, s>>>(nv, std::sqrt(3.0 / (double)nv), mask, v.x);
-        AMR_COUNT(1);
-        double lam = 1.0;
-        for (int it = 0; it < 15; it++) {
-            bsr_res<NB, V>(s, L, A, nbs, mask, v.x, nullptr, v.r);
-            k_cheb<NB, V><<<nblk(L.n, 256), 256, 0, s>>>(L.n, 0, V(0), V(1), v.Dinv, v.r, v.d, v.bv);  // bv = Dinv A x
-            k_norm2<V><<<gnorm, 256, 0, s>>>(nv, v.bv, g->scratch + 8, g->ticket, g->scratch);
-            AMR_COUNT(2);
-            double n2 = 0.0;
-            AMR_CUDA(cudaMemcpyAsync(&n2, g->scratch, sizeof(double), cudaMemcpyDeviceToHost, s));
-            AMR_CUDA(cudaStreamSynchronize(s));
-            if (!(n2 > 0.0)) break;
-            lam = std::sqrt(n2);
-            AMR_CUDA(cudaMemcpyAsync(v.x, v.bv, nv * sizeof(V), cudaMemcpyDeviceToDevice, s));
-            k_scale<V><<<nblk(nv, 256), 256, 0, s>>>(nv, (V)(1.0 / lam), v.x);
+        AMR_COUNT(2);
+        if (half) {  // xt of the start vector
+            k_make_xt<NB><<<nblk(L.n, 256), 256, 0, s>>>(L.n, reinterpret_cast<const float *>(v.x), rs, xt);
             AMR_COUNT(1);
         }
+        for (int it = 0; it < 15; it++) {
+            if constexpr (kHalf) {
+                if (half) launch_res16<NB>(m, g, L, xt, nullptr, v.r, nullptr, stop);
+                else bsr_res<NB, V>(s, L, A, nbs, mask, v.x, nullptr, v.r, stop);
+            } else {
+                bsr_res<NB, V>(s, L, A, nbs, mask, v.x, nullptr, v.r, stop);
+            }
+            k_cheb<NB, V><<<nblk(L.n, 256), 256, 0, s>>>(L.n, 0, V(0), V(1), v.Dinv, v.r, v.d, v.bv, nullptr,
+                                                         nullptr, nullptr, stop);  // bv = Dinv A x
+            k_norm2<V><<<gnorm, 256, 0, s>>>(nv, v.bv, g->scratch + 8, g->ticket, g->scratch, stop);
+            k_power_next<NB, V><<<nblk(L.n, 256), 256, 0, s>>>(L.n, v.bv, v.x, g->scratch, g->pstop, rs, xt);
+            AMR_COUNT(3);
+        }
+        double lam = 1.0;
+        AMR_CUDA(cudaMemcpyAsync(&lam, g->scratch + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
         return lam;
     }
     // the coarse operator of level l + 1 from level l: T' A T, or P' (A P) with P smoothed from T
@@ -1599,20 +1716,29 @@ struct Cycle {
         k_sa_prolongator<BF, NM, V><<<grid(F.n), 128, 0, s>>>(F.n, F.prp, F.pcj, F.pkp, F.pkk, F.cj, A, nbs,
                                                                     fv.T, fv.Dinv, F.agg, w, mask, fv.P);
         if constexpr (std::is_same<V, float>::value) {  // the FP32 cycle applies P in FP16
-            k_sa_half<BF * NM><<<grid(F.np), 128, 0, s>>>(F.np, fv.P, fv.P16);
-            k_sa_half_t<BF * NM><<<grid(F.np), 128, 0, s>>>(F.np, F.pts, fv.P16, fv.P16T);
+            k_sa_half<<<grid(F.np * BF * NM), 128, 0, s>>>(F.np * BF * NM, fv.P, fv.P16);
+            k_sa_half_t<BF * NM><<<grid(F.np * BF * NM), 128, 0, s>>>(F.np, F.pts, fv.P16, fv.P16T);
             AMR_COUNT(2);
         }
         k_sa_ap<BF, NM, V><<<grid(F.nq), 128, 0, s>>>(F.nq, F.qrow, F.qcj, F.rp, F.cj, A, nbs, F.prp, F.pcj,
-                                                            fv.P, fv.Q);
+                                                            fv.P, fv.Q, F.p_steps);
         k_sa_galerkin<BF, NM, V><<<grid(C.nblocks), 128, 0, s>>>(C.nblocks, F.crow, C.cj, F.ptp, F.pti, F.pts,
-                                                                       fv.P, F.qrp, F.qcj, fv.Q, cv.A, C.nbs);
+                                                                       fv.P, F.qrp, F.qcj, fv.Q, cv.A, C.nbs,
+                                                                       F.q_steps);
         AMR_COUNT(3);
     }
     static void numeric(amr_model *m, AmrAmg *g) {
         cudaStream_t s = m->stream;
         const size_t nl = g->L.size();
         vals<V>(g->L[0]).Dinv = fine_Dinv(m);
+        // (first: the fine level's power iteration reads it)
+        if constexpr (std::is_same<V, float>::value) {  // the fine level's FP16 copy
+            AmgLevel &F = g->L[0];
+            k_fine_scale<B><<<nblk(F.n, 256), 256, 0, s>>>(F.n, F.diag, m->K32, m->bstride, g->rs);
+            k_fine_half<B><<<nblk(F.n * 32, 256), 256, 0, s>>>(F.n, F.rp, F.cj, m->K32, m->bstride, g->rs, g->A16);
+            AMR_COUNT(2);
+            AMR_CUDA(cudaGetLastError());
+        }
         for (size_t l = 0; l + 1 < nl; l++) {
             AmgLevel &F = g->L[l], &C = g->L[l + 1];
             AmgVals<V> &fv = vals<V>(F), &cv = vals<V>(C);
@@ -1624,13 +1750,6 @@ struct Cycle {
                 k_block_inverse<NM, V><<<nblk(C.n, 128), 128, 0, s>>>(C.n, C.diag, cv.A, C.nbs, cv.Dinv);
                 AMR_COUNT(1);
             }
-            AMR_CUDA(cudaGetLastError());
-        }
-        if constexpr (std::is_same<V, float>::value) {  // the fine level's FP16 copy
-            AmgLevel &F = g->L[0];
-            k_fine_scale<B><<<nblk(F.n, 256), 256, 0, s>>>(F.n, F.diag, m->K32, m->bstride, g->rs);
-            k_fine_half<B><<<nblk(F.n * 32, 256), 256, 0, s>>>(F.n, F.rp, F.cj, m->K32, m->bstride, g->rs, g->A16);
-            AMR_COUNT(2);
             AMR_CUDA(cudaGetLastError());
         }
         for (size_t l = 0; l + 1 < nl; l++) {  // (a smoothed level's lambda came with its prolongator)
@@ -1761,9 +1880,9 @@ double amr_amg_time_residual(amr_model *m, int reps, bool fp64, double *bytes) {
             if (B == 3) bsr_res<3, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
             else bsr_res<2, double>(s, L, m->K64, m->bstride, m->free_mask, L.f64.x, L.f64.bv, L.f64.r);
         } else if (B == 3) {
-            launch_res16<3>(m, g, L, reinterpret_cast<const float4 *>(g->xt), L.f32.bv, L.f32.r);
+            launch_res16<3>(m, g, L, reinterpret_cast<const float4 *>(g->xt), L.f32.bv, L.f32.r, nullptr, nullptr);
         } else {
-            launch_res16<2>(m, g, L, reinterpret_cast<const float2 *>(g->xt), L.f32.bv, L.f32.r);
+            launch_res16<2>(m, g, L, reinterpret_cast<const float2 *>(g->xt), L.f32.bv, L.f32.r, nullptr, nullptr);
         }
     }
     AMR_CUDA(cudaEventRecord(m->ev1, s));
