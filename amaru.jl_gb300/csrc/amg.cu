@@ -285,7 +285,7 @@ struct AmgLevel {
     // each block's row) and the row of each coarse block
     bool smooth = false;
     int64_t np = 0, nq = 0;
-    int p_steps = 0, q_steps = 0;  // halvings of a lower-bound search in the longest row of P / of A P
+    int p_steps = 0;  // halvings of a lower-bound search in the longest row of P
     int64_t *prp = nullptr, *pkp = nullptr, *qrp = nullptr, *ptp = nullptr;
     int32_t *pcj = nullptr, *pkk = nullptr, *qcj = nullptr, *qrow = nullptr, *pti = nullptr, *pts = nullptr,
             *crow = nullptr;
@@ -493,14 +493,11 @@ static void amg_build_structure(amr_model *m) {
             lv.np = S.prp[h.n];
             lv.nq = S.qrp[h.n];
             {
-                int64_t mp = 0, mq = 0;
-                for (int64_t i = 0; i < h.n; i++) {
-                    mp = std::max(mp, S.prp[i + 1] - S.prp[i]);
-                    mq = std::max(mq, S.qrp[i + 1] - S.qrp[i]);
-                }
-                auto bits = [](int64_t v) { int b = 0; while (v > 0) { b++; v >>= 1; } return b; };
-                lv.p_steps = bits(mp);
-                lv.q_steps = bits(mq);
+                int64_t mp = 0;
+                for (int64_t i = 0; i < h.n; i++) mp = std::max(mp, S.prp[i + 1] - S.prp[i]);
+                int b = 0;
+                for (int64_t v = mp; v > 0; v >>= 1) b++;
+                lv.p_steps = b;
             }
             auto up64 = [&](int64_t *&d, const std::vector<int64_t> &v) {
                 amr_alloc(&d, std::max<size_t>(v.size(), 1));
@@ -777,50 +774,36 @@ __global__ void __launch_bounds__(128) k_sa_ap(int64_t nq, const int32_t *qrow, 
 }
 
 // coarse operator P' (A P), thread per coarse block (I, J): sum over the fine rows i that P reaches I from
-// (block s), in order, of P_s' Q_iJ (if row i of A P has column J).  Four rows i at a time: their A P rows are
-// searched together, then the products are added in order.
+// (block s), in order, of P_s' Q_iJ (if row i of A P has column J)
 template <int BF, int NM, class V>
-__global__ void __launch_bounds__(128) k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *ccj,
-                                                      const int64_t *ptp, const int32_t *pti, const int32_t *pts,
-                                                      const V *P, const int64_t *qrp, const int32_t *qcj,
-                                                      const V *Q, V *Ac, int64_t nbsc, int steps) {
-    constexpr int U = 4;
+__global__ void k_sa_galerkin(int64_t ncb, const int32_t *crow, const int32_t *ccj, const int64_t *ptp,
+                              const int32_t *pti, const int32_t *pts, const V *P, const int64_t *qrp,
+                              const int32_t *qcj, const V *Q, V *Ac, int64_t nbsc) {
     const int64_t cb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (cb >= ncb) return;
     const int32_t I = crow[cb], J = ccj[cb];
-    const int32_t Ju[U] = {J, J, J, J};
     V acc[NM * NM];
 #pragma unroll
     for (int u = 0; u < NM * NM; u++) acc[u] = V(0);
-    const int64_t e1 = ptp[I + 1];
-    for (int64_t eb = ptp[I]; eb < e1; eb += U) {
-        int64_t base[U], len[U], end[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            if (eb + u < e1) {
-                const int64_t i = pti[eb + u];
-                base[u] = qrp[i];
-                end[u] = qrp[i + 1];
-            } else {
-                base[u] = end[u] = 0;
-            }
-            len[u] = end[u] - base[u];
+    for (int64_t e = ptp[I]; e < ptp[I + 1]; e++) {
+        const int64_t i = pti[e];
+        int64_t lo = qrp[i], hi = qrp[i + 1];  // J in the sorted columns of row i of A P
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (qcj[mid] < J) lo = mid + 1;
+            else hi = mid;
         }
-        lower_bounds<U>(qcj, base, len, Ju, steps);
+        if (lo >= qrp[i + 1] || qcj[lo] != J) continue;
+        const V *ps = P + (int64_t)pts[e] * BF * NM, *qv = Q + lo * BF * NM;
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            if (base[u] >= end[u] || qcj[base[u]] != J) continue;
-            const V *ps = P + (int64_t)pts[eb + u] * BF * NM, *qv = Q + base[u] * BF * NM;
+        for (int c = 0; c < BF; c++) {
+            V pr[NM], qr[NM];
 #pragma unroll
-            for (int c = 0; c < BF; c++) {
-                V pr[NM], qr[NM];
+            for (int u = 0; u < NM; u++) { pr[u] = ps[c * NM + u]; qr[u] = qv[c * NM + u]; }
 #pragma unroll
-                for (int w = 0; w < NM; w++) { pr[w] = ps[c * NM + w]; qr[w] = qv[c * NM + w]; }
+            for (int a = 0; a < NM; a++)
 #pragma unroll
-                for (int a = 0; a < NM; a++)
-#pragma unroll
-                    for (int b = 0; b < NM; b++) acc[a * NM + b] = vfma(pr[a], qr[b], acc[a * NM + b]);
-            }
+                for (int b = 0; b < NM; b++) acc[a * NM + b] = vfma(pr[a], qr[b], acc[a * NM + b]);
         }
     }
 #pragma unroll
@@ -1723,8 +1706,7 @@ struct Cycle {
         k_sa_ap<BF, NM, V><<<grid(F.nq), 128, 0, s>>>(F.nq, F.qrow, F.qcj, F.rp, F.cj, A, nbs, F.prp, F.pcj,
                                                             fv.P, fv.Q, F.p_steps);
         k_sa_galerkin<BF, NM, V><<<grid(C.nblocks), 128, 0, s>>>(C.nblocks, F.crow, C.cj, F.ptp, F.pti, F.pts,
-                                                                       fv.P, F.qrp, F.qcj, fv.Q, cv.A, C.nbs,
-                                                                       F.q_steps);
+                                                                       fv.P, F.qrp, F.qcj, fv.Q, cv.A, C.nbs);
         AMR_COUNT(3);
     }
     static void numeric(amr_model *m, AmrAmg *g) {

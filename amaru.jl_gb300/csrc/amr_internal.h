@@ -76,6 +76,10 @@ struct amr_model {
     int64_t *contrib_ptr = nullptr; // nblocks+1
     int64_t *contrib = nullptr;     // element block slots, element order
     int64_t ncontrib = 0;
+    // the gather's block order: blocks grouped by their number of contributions (ascending, stable), so
+    // a warp's lanes loop over equal counts; and the row of each block
+    int32_t *gorder = nullptr;      // nblocks
+    int32_t *grow = nullptr;        // nblocks
     std::vector<int64_t> h_brow_ptr;
     std::vector<int32_t> h_bcol;
     // values

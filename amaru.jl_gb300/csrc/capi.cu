@@ -439,7 +439,8 @@ int amr_model_destroy(amr_model *m) {
     for (AmrGroup &g : m->groups) amr_free(g.tab);
     amr_free(m->coords); amr_free(m->conn); amr_free(m->conn_ptr); amr_free(m->mat_type); amr_free(m->mat_par);
     amr_free(m->ip_ptr); amr_free(m->kel_ptr); amr_free(m->inc_ptr); amr_free(m->inc); amr_free(m->brow_ptr);
-    amr_free(m->bcol); amr_free(m->contrib_ptr); amr_free(m->contrib); amr_free(m->Kel); amr_free(m->K64);
+    amr_free(m->bcol); amr_free(m->contrib_ptr); amr_free(m->contrib); amr_free(m->gorder); amr_free(m->grow);
+    amr_free(m->Kel); amr_free(m->K64);
     amr_free(m->K32); amr_free(m->keep); amr_free(m->Minv32); amr_free(m->Minv64); amr_free(m->eq_id);
     amr_free(m->free_mask); amr_free(m->dof_node); amr_free(m->st); amr_free(m->stbk); amr_free(m->Fel);
     amr_free(m->fel_ptr); amr_free(m->d_status); amr_free(m->rho); amr_free(m->M64); amr_free(m->Mkeep);

@@ -318,6 +318,73 @@ __device__ __forceinline__ double ip_geometry(int nen, const double *dNdR, const
     return det;
 }
 
+// Pair sums of the 3-D stiffness in float-float arithmetic (a value is hi + lo, two FP32 numbers, about 48
+// significant bits).  On this GPU the FP32 pipe issues some 70 times as many FMAs per clock as the FP64 pipe,
+// which bounds the FP64 element kernels; a float-float FMA takes about 12 FP32 operations.  Terms are
+// products of two FP64 inputs split as hi = fl32(x), lo = fl32(x - hi); the product's hi*hi part is
+// exact (Dekker's two-product with an FMA), the cross terms are added in FP32, lo*lo (2^-48 relative) is
+// dropped, and the sum keeps its rounding errors (Knuth's two-sum).  Relative error per pair sum about
+// 1e-13 of its largest term (27 terms), for terms within the FP32 exponent range.
+// Every operation is an explicit round-to-nearest intrinsic, so the compiler fuses none of them.
+struct FF {
+    float hi, lo;
+};
+// x split into hi + lo, the pair kept in the 8 bytes of a double (hi in the low word): the shared arrays of
+// g and w g are rewritten in place and stay double arrays.  The split is done on the integer pipe from the
+// bit pattern (conversions from FP64 take the FP64 pipe): hi = x with its 52-bit fraction cut to 23 bits,
+// lo = the remaining 29 bits cut to a float's 24 significant bits, both with the sign of x, so that
+// |x - hi - lo| < 2^-46 |x|.  Zeros give two zeros; subnormal, infinite or NaN x, |x| below 2^-78 (where lo
+// could leave the normal float range) or above the float range fall back to conversions.
+__device__ __forceinline__ double ff_split(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0 && (b << 1) == 0) return __hiloint2double((int)sign, (int)sign);  // +-0
+    const int e = ex - 1023;
+    if (ex == 0 || ex == 0x7ff || e < -78 || e > 127) {  // (lo could leave the normal float range)
+        const float h = __double2float_rn(x);
+        const float l = __double2float_rn(x - (double)h);
+        return __hiloint2double(__float_as_int(l), __float_as_int(h));
+    }
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    const unsigned hb = sign | ((unsigned)(e + 127) << 23) | (unsigned)(mant >> 29);
+    const unsigned m29 = (unsigned)(mant & 0x1FFFFFFFull);
+    unsigned lb = 0;
+    if (m29 != 0) {
+        const int p = 31 - __clz((int)m29);  // the leading one of the tail, bit 0..28
+        const int le = e - 52 + p;
+        if (le >= -126) {
+            const unsigned frac = (p >= 23 ? (m29 >> (p - 23)) : (m29 << (23 - p))) & 0x7FFFFFu;
+            lb = sign | ((unsigned)(le + 127) << 23) | frac;
+        }
+    }
+    return __hiloint2double((int)lb, (int)hb);
+}
+__device__ __forceinline__ float2 ff_get(double packed) {
+    return make_float2(__int_as_float(__double2loint(packed)), __int_as_float(__double2hiint(packed)));
+}
+// a b as a float-float pair (packed): the exact hi*hi product plus the cross terms, renormalised
+__device__ __forceinline__ double ff_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float h = __fadd_rn(p, e);
+    const float l = __fsub_rn(e, __fsub_rn(h, p));
+    return __hiloint2double(__float_as_int(l), __float_as_int(h));
+}
+__device__ __forceinline__ void ff_fma(float2 a, float2 b, FF &s) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float t = __fadd_rn(s.hi, p);
+    const float bp = __fsub_rn(t, s.hi);
+    const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s.lo = __fadd_rn(s.lo, __fadd_rn(err, e));
+    s.hi = t;
+}
+
 // S(m) g : the symmetric tensor of Mandel vector m applied to g (= B_a^T m)
 template <int DIM>
 __device__ __forceinline__ void sym_apply(const double *m, const double *g, double *v) {
@@ -337,11 +404,10 @@ __device__ __forceinline__ void sym_apply(const double *m, const double *g, doub
 // (element, node pair a<=b) accumulates T_ab / P_ab over the IPs and writes
 // the two element blocks (a,b), (b,a) to the staging array.
 // ---------------------------------------------------------------------------
-// CTAs per SM the stiffness kernel's registers allow: two, so one CTA's geometry phase (a thread per IP)
-// overlaps another's pair phase; three for HEX20, measured faster on the 100x40x40 block despite a
-// few spilled registers
+// CTAs per SM the stiffness kernel's registers allow: two, so one CTA's geometry phase (FP64 pipe)
+// overlaps another's pair phase (FP32 pipe in 3-D)
 template <int DIM, int NEN>
-constexpr int stiff_min_blocks() { return (DIM == 3 && NEN == 20) ? 3 : 2; }
+constexpr int stiff_min_blocks() { return 2; }
 
 template <int DIM, int NEN>
 __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_kernel(ModelArgs M, GroupArgs G, int epb, double *Kel,
@@ -376,6 +442,76 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
     if (threadIdx.x < epb) sPl[threadIdx.x] = 0;
     __syncthreads();
 
+    if constexpr (DIM == 3) {
+        // 3-D: the geometry spread over the CTA (the FP64 pipe is the bound, and a thread per IP left it to one
+        // warp while the others waited at the barrier).  (a) thread per (element, IP, Jacobian entry)
+        double *sJ = sH;                     // epb x nip x 9: J, then its inverse
+        double *sMv = sJ + epb * nip * 9;    // epb x nip x 6: the plastic tangent's vector m
+        for (int t = threadIdx.x; t < ne * nip * 9; t += blockDim.x) {
+            const int el = t / (nip * 9), r = t % (nip * 9), ip = r / 9, a = (r % 9) / 3, bb = r % 3;
+            const double *C = sC + el * NEN * DIM, *dN = dNdR + ip * NEN * DIM;
+            double J = 0.0;
+            for (int i = 0; i < NEN; i++) J = fma(C[i * DIM + a], dN[i * DIM + bb], J);
+            sJ[(el * nip + ip) * 9 + r % 9] = J;
+        }
+        __syncthreads();
+        // (b) thread per (element, IP): determinant, inverse, weight and the material's tangent
+        for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
+            const int el = t / nip, ip = t % nip;
+            const int64_t e = e0 + el;
+            double *J = sJ + (el * nip + ip) * 9;
+            const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[5] * J[6] - J[3] * J[8], c2 = J[3] * J[7] - J[4] * J[6];
+            const double det = J[0] * c0 + J[1] * c1 + J[2] * c2;
+            const double rd = 1.0 / det;
+            double iJ[9];
+            iJ[0] = c0 * rd; iJ[1] = (J[2] * J[7] - J[1] * J[8]) * rd; iJ[2] = (J[1] * J[5] - J[2] * J[4]) * rd;
+            iJ[3] = c1 * rd; iJ[4] = (J[0] * J[8] - J[2] * J[6]) * rd; iJ[5] = (J[2] * J[3] - J[0] * J[5]) * rd;
+            iJ[6] = c2 * rd; iJ[7] = (J[1] * J[6] - J[0] * J[7]) * rd; iJ[8] = (J[0] * J[4] - J[1] * J[3]) * rd;
+#pragma unroll
+            for (int q = 0; q < 9; q++) J[q] = iJ[q];
+            if (!(det > 0.0)) set_status(status, AMR_ENEGJAC, e);
+            const double w = det * wq[ip] * M.thickness;
+            sW[el * nip + ip] = w;
+            const double *par = M.mat_par + 8 * e;
+            const int64_t gi = M.ip_ptr[e] + ip;
+            double sig[6];
+            for (int i = 0; i < 6; i++) sig[i] = st[i * M.nip_total + gi];
+            double lam, mu, m[6];
+            lame(par[0], par[1], ps, lam, mu);
+            if (ip == 0) { sLam[el] = lam; sMu[el] = mu; }
+            const double gam = plastic_tangent(M.mat_type[e], par, ps, sig, st[AMR_ST_EPA * M.nip_total + gi],
+                                               st[AMR_ST_DL * M.nip_total + gi], lam, mu, m);
+            sGam[el * nip + ip] = gam * w;
+            if (gam != 0.0) {
+                sPl[el] = 1;
+                for (int i = 0; i < 6; i++) sMv[(el * nip + ip) * 6 + i] = m[i];
+            }
+        }
+        __syncthreads();
+        // (c) thread per (element, IP, node): g = dN/dX, the plastic vector S(m) g, and g and w g as float-float
+        // pairs for the pair sums
+        for (int t = threadIdx.x; t < ne * nip * NEN; t += blockDim.x) {
+            const int el = t / (nip * NEN), r = t % (nip * NEN), ip = r / NEN, i = r % NEN;
+            const double *iJ = sJ + (el * nip + ip) * 9, *dN = dNdR + ip * NEN * DIM + i * DIM;
+            double g[DIM];
+#pragma unroll
+            for (int bb = 0; bb < DIM; bb++) {
+                double sum = 0.0;
+#pragma unroll
+                for (int a = 0; a < DIM; a++) sum = fma(dN[a], iJ[a * DIM + bb], sum);
+                g[bb] = sum;
+            }
+            const int ipo = (el * nip + ip) * NEN * DIM + i * DIM;
+            if (sGam[el * nip + ip] != 0.0) sym_apply<DIM>(sMv + (el * nip + ip) * 6, g, sV + ipo);
+            const float2 wf = ff_get(ff_split(sW[el * nip + ip]));
+#pragma unroll
+            for (int bb = 0; bb < DIM; bb++) {
+                const double gs = ff_split(g[bb]);
+                sG[ipo + bb] = gs;
+                sWG[ipo + bb] = ff_mul(wf, ff_get(gs));
+            }
+        }
+    } else
     for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
         int el = t / nip, ip = t % nip;
         int64_t e = e0 + el;
@@ -428,13 +564,32 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
         for (int q = 0; q < BB; q++) { T[q] = 0.0; P[q] = 0.0; }
         const double *gbase = sG + el * nip * NEN * DIM;
         const double *wgbase = sWG + el * nip * NEN * DIM;
-        for (int ip = 0; ip < nip; ip++) {
-            const double *wa = wgbase + ip * NEN * DIM + a * DIM;
-            const double *gb = gbase + ip * NEN * DIM + b * DIM;
+        if (DIM == 3) {
+            FF t[BB];
 #pragma unroll
-            for (int i = 0; i < DIM; i++)
+            for (int q = 0; q < BB; q++) t[q] = FF{0.0f, 0.0f};
+            for (int ip = 0; ip < nip; ip++) {
+                const double *wa = wgbase + ip * NEN * DIM + a * DIM;
+                const double *gb = gbase + ip * NEN * DIM + b * DIM;
+                float2 wv[DIM], gv[DIM];
 #pragma unroll
-                for (int j = 0; j < DIM; j++) T[i * DIM + j] = fma(wa[i], gb[j], T[i * DIM + j]);
+                for (int i = 0; i < DIM; i++) { wv[i] = ff_get(wa[i]); gv[i] = ff_get(gb[i]); }
+#pragma unroll
+                for (int i = 0; i < DIM; i++)
+#pragma unroll
+                    for (int j = 0; j < DIM; j++) ff_fma(wv[i], gv[j], t[i * DIM + j]);
+            }
+#pragma unroll
+            for (int q = 0; q < BB; q++) T[q] = (double)t[q].hi + (double)t[q].lo;
+        } else {
+            for (int ip = 0; ip < nip; ip++) {
+                const double *wa = wgbase + ip * NEN * DIM + a * DIM;
+                const double *gb = gbase + ip * NEN * DIM + b * DIM;
+#pragma unroll
+                for (int i = 0; i < DIM; i++)
+#pragma unroll
+                    for (int j = 0; j < DIM; j++) T[i * DIM + j] = fma(wa[i], gb[j], T[i * DIM + j]);
+            }
         }
         if (sPl[el]) {
             const double *vbase = sV + el * nip * NEN * DIM;
@@ -718,42 +873,45 @@ __device__ __forceinline__ bool is_nan_bits(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 
+// A thread per block, the blocks taken in the order gorder, which groups them by their number of
+// contributions: a warp's lanes then run equal contribution loops.  (A warp per node row with a lane per
+// block left most lanes idle on the FP64 pipe, which bounds this kernel: the blocks of a HEX20 node row have
+// 1 to 8 contributions each.)
 template <int B>
-__global__ void gather_kernel(int64_t nnodes, int64_t nblocks, const int64_t *brow_ptr, const int32_t *bcol,
-                              const int64_t *contrib_ptr, const int64_t *contrib, const double *Kel,
-                              const uint8_t *free_mask, double *K64, float *K32, uint16_t *keep, float *Minv32,
-                              double *Minv64, int32_t *status) {
+__global__ void gather_kernel(int64_t nblocks, const int32_t *gorder, const int32_t *grow, const int32_t *bcol,
+                                     const int64_t *contrib_ptr, const int64_t *contrib, const double *Kel,
+                                     const uint8_t *free_mask, double *K64, int64_t stride, float *K32,
+                                     uint16_t *keep, float *Minv32, double *Minv64, int32_t *status) {
     constexpr int BB = B * B;
-    int lane = threadIdx.x & 31;
-    int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (n >= nnodes) return;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nblocks) return;
+    const int64_t k = gorder[t];
+    const int64_t n = grow[k];
     uint8_t fr[B];
 #pragma unroll
     for (int c = 0; c < B; c++) fr[c] = free_mask ? free_mask[n * B + c] : 1;
-    for (int64_t k = brow_ptr[n] + lane; k < brow_ptr[n + 1]; k += 32) {
-        double v[BB];
+    double v[BB];
 #pragma unroll
-        for (int q = 0; q < BB; q++) v[q] = 0.0;
-        unsigned kb = 0;
-        for (int64_t c = contrib_ptr[k]; c < contrib_ptr[k + 1]; c++) {
-            const double *src = Kel + contrib[c] * BB;
-#pragma unroll
-            for (int q = 0; q < BB; q++) {
-                double x = src[q];
-                if (!below_eps(x)) { v[q] += x; kb |= 1u << q; }  // NaN is pushed, as in mount_K
-            }
-        }
-        int32_t j = bcol[k];
-        bool nan = false;
+    for (int q = 0; q < BB; q++) v[q] = 0.0;
+    unsigned kb = 0;
+    for (int64_t c = contrib_ptr[k]; c < contrib_ptr[k + 1]; c++) {
+        const double *src = Kel + contrib[c] * BB;
 #pragma unroll
         for (int q = 0; q < BB; q++) {
-            K64[(int64_t)q * nblocks + k] = v[q];
-            nan |= is_nan_bits(v[q]);
+            double x = src[q];
+            if (!below_eps(x)) { v[q] += x; kb |= 1u << q; }  // NaN is pushed, as in mount_K
         }
-        if (nan) set_status(status, AMR_ENAN, -1);
-        if (keep) keep[k] = (uint16_t)kb;
-        finish_block<B>(n, k, j, nblocks, v, fr, free_mask, K32, Minv32, Minv64);
     }
+    const int32_t j = bcol[k];
+    bool nan = false;
+#pragma unroll
+    for (int q = 0; q < BB; q++) {
+        K64[(int64_t)q * stride + k] = v[q];
+        nan |= is_nan_bits(v[q]);
+    }
+    if (nan) set_status(status, AMR_ENAN, -1);
+    if (keep) keep[k] = (uint16_t)kb;
+    finish_block<B>(n, k, j, stride, v, fr, free_mask, K32, Minv32, Minv64);
 }
 
 // K = a1 Ks + a2 K (the weighted tangent of the ME / BE / Ralston schemes, mech-solver.jl:280-288,
@@ -1100,8 +1258,11 @@ template <int DIM, int NEN>
 void launch_stiff(amr_model *m, const AmrGroup &g) {
     GroupArgs ga{g.tab, g.nip, g.first, g.count};
     int epb = g.epb;
+    // coordinates, g, plastic vectors, w, gamma w, w g; then the axisymmetric N / r (2-D) or the Jacobians and
+    // plastic tangent vectors (3-D)
     size_t smem = sizeof(double) * (size_t)epb * (NEN * DIM + 3 * g.nip * NEN * DIM + 2 * g.nip +
-                                                 (m->stressmodel == AMR_AXISYMMETRIC ? g.nip * NEN : 0));
+                                                 (m->stressmodel == AMR_AXISYMMETRIC ? g.nip * NEN : 0) +
+                                                 (DIM == 3 ? 15 * g.nip : 0));
     constexpr int NP = NEN * (NEN + 1) / 2;
     int threads = epb * NP;
     threads = ((threads + 31) / 32) * 32;
@@ -1183,15 +1344,15 @@ void amr_stiffness_elements(amr_model *m) {
 
 void amr_stiffness(amr_model *m) {
     amr_stiffness_elements(m);
-    unsigned grid = nblk(m->nnodes * 32, 256);
+    unsigned grid = nblk(m->nblocks, 256);
     if (m->B == 3) {
-        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
-                                                      m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
-                                                      m->Minv32, m->Minv64, m->d_status);
+        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nblocks, m->gorder, m->grow, m->bcol, m->contrib_ptr,
+                                                             m->contrib, m->Kel, m->free_mask, m->K64, m->bstride,
+                                                             m->K32, m->keep, m->Minv32, m->Minv64, m->d_status);
     } else {
-        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
-                                                      m->contrib, m->Kel, m->free_mask, m->K64, m->K32, m->keep,
-                                                      m->Minv32, m->Minv64, m->d_status);
+        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nblocks, m->gorder, m->grow, m->bcol, m->contrib_ptr,
+                                                             m->contrib, m->Kel, m->free_mask, m->K64, m->bstride,
+                                                             m->K32, m->keep, m->Minv32, m->Minv64, m->d_status);
     }
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
@@ -1234,15 +1395,15 @@ void amr_mass(amr_model *m) {
             m, g, [&](auto n) { launch(std::integral_constant<int, 3>(), n); },
             [&](auto n) { launch(std::integral_constant<int, 2>(), n); });
     }
-    unsigned grid = nblk(m->nnodes * 32, 256);
+    unsigned grid = nblk(m->nblocks, 256);
     if (m->B == 3)
-        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
-                                                      m->contrib, m->Kel, m->free_mask, m->M64, nullptr, m->Mkeep,
-                                                      nullptr, nullptr, m->d_status);
+        gather_kernel<3><<<grid, 256, 0, m->stream>>>(m->nblocks, m->gorder, m->grow, m->bcol, m->contrib_ptr,
+                                                             m->contrib, m->Kel, m->free_mask, m->M64, m->bstride,
+                                                             nullptr, m->Mkeep, nullptr, nullptr, m->d_status);
     else
-        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nnodes, m->bstride, m->brow_ptr, m->bcol, m->contrib_ptr,
-                                                      m->contrib, m->Kel, m->free_mask, m->M64, nullptr, m->Mkeep,
-                                                      nullptr, nullptr, m->d_status);
+        gather_kernel<2><<<grid, 256, 0, m->stream>>>(m->nblocks, m->gorder, m->grow, m->bcol, m->contrib_ptr,
+                                                             m->contrib, m->Kel, m->free_mask, m->M64, m->bstride,
+                                                             nullptr, m->Mkeep, nullptr, nullptr, m->d_status);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
 }

@@ -193,6 +193,32 @@ __global__ void contrib_rows(const int32_t *conn, const int64_t *conn_ptr, const
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// ---- the gather's block order ----
+constexpr int kCountCap = 32;  // contribution counts above it share the last group
+__device__ __forceinline__ int count_group(const int64_t *cptr, int64_t k) {
+    const int64_t c = cptr[k + 1] - cptr[k];
+    return c < kCountCap ? (int)c : kCountCap;
+}
+__global__ void block_rows(int64_t nnodes, const int64_t *brow_ptr, int32_t *grow) {  // warp per row
+    const int lane = threadIdx.x & 31;
+    const int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= nnodes) return;
+    for (int64_t k = brow_ptr[n] + lane; k < brow_ptr[n + 1]; k += 32) grow[k] = (int32_t)n;
+}
+__global__ void group_hist(int64_t nb, const int64_t *cptr, unsigned long long *hist) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nb) atomicAdd(hist + count_group(cptr, k), 1ull);  // integer counts: the totals are exact
+}
+__global__ void group_flags(int64_t nb, const int64_t *cptr, int v, int64_t *flags) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nb) flags[k] = count_group(cptr, k) == v;
+}
+__global__ void group_scatter(int64_t nb, const int64_t *cptr, int v, const int64_t *pos, int64_t off,
+                              int32_t *order) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nb && count_group(cptr, k) == v) order[off + pos[k]] = (int32_t)k;
+}
+
 }  // namespace
 
 void amr_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s) {
@@ -283,6 +309,40 @@ void amr_build_pattern(amr_model *m) {
                                     m->bcol, bcnt, m->contrib_ptr, m->contrib);
     AMR_COUNT(1);
     AMR_CUDA(cudaGetLastError());
+    // 4. the gather's order: blocks grouped by contribution count, block order kept within a group (a
+    // deterministic scan per non-empty group), and each block's row
+    amr_alloc(&m->grow, std::max<int64_t>(m->nblocks, 1));
+    amr_alloc(&m->gorder, std::max<int64_t>(m->nblocks, 1));
+    block_rows<<<gc, 256, 0, s>>>(m->nnodes, m->brow_ptr, m->grow);
+    AMR_COUNT(1);
+    {
+        unsigned long long *hist = nullptr;
+        amr_alloc(&hist, kCountCap + 1);
+        AMR_CUDA(cudaMemsetAsync(hist, 0, (kCountCap + 1) * sizeof(unsigned long long), s));
+        group_hist<<<nblk(m->nblocks, 256), 256, 0, s>>>(m->nblocks, m->contrib_ptr, hist);
+        AMR_COUNT(1);
+        unsigned long long hh[kCountCap + 1];
+        AMR_CUDA(cudaMemcpyAsync(hh, hist, sizeof hh, cudaMemcpyDeviceToHost, s));
+        AMR_CUDA(cudaStreamSynchronize(s));
+        amr_free(hist);
+        int64_t *flags = nullptr, *pos = nullptr;
+        amr_alloc(&flags, std::max<int64_t>(m->nblocks, 1));
+        amr_alloc(&pos, m->nblocks + 1);
+        int64_t off = 0;
+        for (int v = 0; v <= kCountCap; v++) {
+            if (hh[v] == 0) continue;
+            group_flags<<<nblk(m->nblocks, 256), 256, 0, s>>>(m->nblocks, m->contrib_ptr, v, flags);
+            AMR_COUNT(1);
+            amr_scan_i64(flags, pos, m->nblocks, s);
+            group_scatter<<<nblk(m->nblocks, 256), 256, 0, s>>>(m->nblocks, m->contrib_ptr, v, pos, off, m->gorder);
+            AMR_COUNT(1);
+            off += (int64_t)hh[v];
+        }
+        AMR_CUDA(cudaGetLastError());
+        AMR_CUDA(cudaStreamSynchronize(s));
+        amr_free(flags);
+        amr_free(pos);
+    }
     // host copy of the pattern (export in the reference layout)
     m->h_brow_ptr.resize(m->nnodes + 1);
     m->h_bcol.resize(m->nblocks);
