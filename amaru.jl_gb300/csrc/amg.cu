@@ -149,7 +149,7 @@ void parallel_for(int64_t n, F f) {
 // of A P and of the coarse operator P' A P, with the maps their device builds read.
 struct SaPattern {
     std::vector<int64_t> prp, pkp, qrp, ptp, crp;
-    std::vector<int32_t> pcj, pkk, qcj, qrow, pti, pts, ccj, crow;
+    std::vector<int32_t> pcj, prow, pkk, qcj, qrow, pti, pts, ccj, crow;
 };
 
 // rows [0, n): out[r] = sorted distinct values that cand(r, push) pushes; two passes (count, fill)
@@ -188,6 +188,10 @@ void sa_pattern(const HostLevel &h, const std::vector<int32_t> &agg, int64_t na,
         for (int64_t k = h.rp[i]; k < h.rp[i + 1]; k++) push(agg[h.cj[k]]);
     }, S.prp, S.pcj);
     const int64_t np = S.prp[n];
+    S.prow.resize(np);
+    parallel_for(n, [&](int64_t i) {
+        for (int64_t t = S.prp[i]; t < S.prp[i + 1]; t++) S.prow[t] = (int32_t)i;
+    });
     // each P block's blocks of A: the row's blocks whose column lies in that aggregate, in order
     S.pkp.assign(np + 1, 0);
     S.pkk.resize(h.rp[n]);
@@ -287,8 +291,8 @@ struct AmgLevel {
     int64_t np = 0, nq = 0;
     int p_steps = 0;  // halvings of a lower-bound search in the longest row of P
     int64_t *prp = nullptr, *pkp = nullptr, *qrp = nullptr, *ptp = nullptr;
-    int32_t *pcj = nullptr, *pkk = nullptr, *qcj = nullptr, *qrow = nullptr, *pti = nullptr, *pts = nullptr,
-            *crow = nullptr;
+    int32_t *pcj = nullptr, *prow = nullptr, *pkk = nullptr, *qcj = nullptr, *qrow = nullptr, *pti = nullptr,
+            *pts = nullptr, *crow = nullptr;
     AmgVals<float> f32;
     AmgVals<double> f64;
 };
@@ -354,7 +358,8 @@ void amr_amg_free(amr_model *m) {
         free_vals(v.f64, l > 0);
         amr_free(v.diag); amr_free(v.agg); amr_free(v.aptr); amr_free(v.anodes);
         amr_free(v.cptr); amr_free(v.ck); amr_free(v.ci); amr_free(v.null_dof);
-        amr_free(v.prp); amr_free(v.pkp); amr_free(v.qrp); amr_free(v.ptp); amr_free(v.pcj); amr_free(v.pkk);
+        amr_free(v.prp); amr_free(v.pkp); amr_free(v.qrp); amr_free(v.ptp); amr_free(v.pcj); amr_free(v.prow);
+        amr_free(v.pkk);
         amr_free(v.qcj); amr_free(v.qrow); amr_free(v.pti); amr_free(v.pts); amr_free(v.crow);
     }
     if (g->gj_exec) cudaGraphExecDestroy(g->gj_exec);
@@ -508,7 +513,7 @@ static void amg_build_structure(amr_model *m) {
                 amr_h2d(m, d, v.data(), v.size() * sizeof(int32_t));
             };
             up64(lv.prp, S.prp); up64(lv.pkp, S.pkp); up64(lv.qrp, S.qrp); up64(lv.ptp, S.ptp);
-            up32(lv.pcj, S.pcj); up32(lv.pkk, S.pkk); up32(lv.qcj, S.qcj); up32(lv.qrow, S.qrow);
+            up32(lv.pcj, S.pcj); up32(lv.prow, S.prow); up32(lv.pkk, S.pkk); up32(lv.qcj, S.qcj); up32(lv.qrow, S.qrow);
             up32(lv.pti, S.pti); up32(lv.pts, S.pts); up32(lv.crow, S.crow);
             amr_alloc(&lv.f32.P, (size_t)std::max<int64_t>(lv.np, 1) * h.b * NM);
             amr_alloc(&lv.f32.P16, (size_t)std::max<int64_t>(lv.np, 1) * h.b * NM);
@@ -649,14 +654,15 @@ __global__ void k_galerkin(int64_t ncb, const int64_t *cptr, const int32_t *ck, 
 }
 
 // coarse DOFs without a mode get an identity equation
-// smoothed prolongator, thread per row i: P_s = [pcj[s] == agg(i)] T_i - w Dinv_i sum_k A_k T_cj[k] over the
-// P block's blocks k of A in order; rows of prescribed DOFs (mask 0) are zero
+// smoothed prolongator, thread per block s of P (row i = prow[s]): P_s = [pcj[s] == agg(i)] T_i - w Dinv_i
+// sum_k A_k T_cj[k] over the P block's blocks k of A in order; rows of prescribed DOFs (mask 0) are zero
 template <int BF, int NM, class V>
-__global__ void k_sa_prolongator(int64_t n, const int64_t *prp, const int32_t *pcj, const int64_t *pkp,
+__global__ void k_sa_prolongator(int64_t np, const int32_t *prow, const int32_t *pcj, const int64_t *pkp,
                                  const int32_t *pkk, const int32_t *cjf, const V *Af, int64_t nbsf, const V *T,
                                  const V *Dinv, const int32_t *agg, V w, const uint8_t *mask, V *P) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= np) return;
+    const int64_t i = prow[s];
     const int32_t ai = agg[i];
     V Di[BF * BF];
 #pragma unroll
@@ -664,7 +670,7 @@ __global__ void k_sa_prolongator(int64_t n, const int64_t *prp, const int32_t *p
     bool fr[BF];
 #pragma unroll
     for (int c = 0; c < BF; c++) fr[c] = mask ? mask[i * BF + c] != 0 : true;
-    for (int64_t s = prp[i]; s < prp[i + 1]; s++) {
+    {
         V M[BF * NM];  // sum of A_k T_j
 #pragma unroll
         for (int q = 0; q < BF * NM; q++) M[q] = V(0);
@@ -1696,7 +1702,7 @@ struct Cycle {
         fv.lam = lambda<BF>(m, g, F, A, nbs, mask);
         const V w = (V)(4.0 / (3.0 * fv.lam));
         auto grid = [](int64_t n) { return std::max(1u, nblk(n, 128)); };
-        k_sa_prolongator<BF, NM, V><<<grid(F.n), 128, 0, s>>>(F.n, F.prp, F.pcj, F.pkp, F.pkk, F.cj, A, nbs,
+        k_sa_prolongator<BF, NM, V><<<grid(F.np), 128, 0, s>>>(F.np, F.prow, F.pcj, F.pkp, F.pkk, F.cj, A, nbs,
                                                                     fv.T, fv.Dinv, F.agg, w, mask, fv.P);
         if constexpr (std::is_same<V, float>::value) {  // the FP32 cycle applies P in FP16
             k_sa_half<<<grid(F.np * BF * NM), 128, 0, s>>>(F.np * BF * NM, fv.P, fv.P16);

@@ -830,6 +830,23 @@ __device__ void invert_block(const double *A, double *X) {
     }
 }
 
+// x rounded to the nearest float (ties to even), on the integer pipe from the bit pattern: bitwise the same
+// as the conversion instruction, which takes the FP64 pipe on this GPU.  Zeros, subnormals, infinities, NaN and
+// results outside the normal float range take the conversion instruction.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7ff);
+    const int e = ex - 1023;
+    if (ex == 0 || ex == 0x7ff || e < -126 || e > 127) return __double2float_rn(x);
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    const unsigned keep = (unsigned)(mant >> 29), rem = (unsigned)(mant & 0x1FFFFFFFull);
+    const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (keep & 1u))) ? 1u : 0u;
+    const unsigned r = ((unsigned)(e + 127) << 23) + keep + up;  // a carry into the exponent is the right result
+    if ((r >> 23) >= 255u) return __double2float_rn(x);          // rounds to infinity
+    return __uint_as_float(sign | r);
+}
+
 // Block k (row n, column j) of K with values v: the Dirichlet-masked FP32 copy (unit diagonal at
 // prescribed DOFs) and, on the diagonal, the block-Jacobi inverses.
 template <int B>
@@ -852,13 +869,13 @@ __device__ __forceinline__ void finish_block(int64_t n, int64_t k, int32_t j, in
         }
     if (K32)
 #pragma unroll
-        for (int q = 0; q < BB; q++) K32[(int64_t)q * nblocks + k] = (float)mk[q];
+        for (int q = 0; q < BB; q++) K32[(int64_t)q * nblocks + k] = d2f_rn(mk[q]);
     if (j == n) {
         double X[BB];
         invert_block<B>(mk, X);
 #pragma unroll
         for (int q = 0; q < BB; q++) {
-            if (Minv32) Minv32[n * BB + q] = (float)X[q];
+            if (Minv32) Minv32[n * BB + q] = d2f_rn(X[q]);
             if (Minv64) Minv64[n * BB + q] = X[q];
         }
     }
@@ -894,7 +911,16 @@ __global__ void gather_kernel(int64_t nblocks, const int32_t *gorder, const int3
 #pragma unroll
     for (int q = 0; q < BB; q++) v[q] = 0.0;
     unsigned kb = 0;
-    for (int64_t c = contrib_ptr[k]; c < contrib_ptr[k + 1]; c++) {
+    const int64_t c0 = contrib_ptr[k], c1 = contrib_ptr[k + 1];
+    if (c0 < c1) {  // the first contribution is taken as it is: 0 + x = x, one FP64 add per entry saved
+        const double *src = Kel + contrib[c0] * BB;
+#pragma unroll
+        for (int q = 0; q < BB; q++) {
+            const double x = src[q];
+            if (!below_eps(x)) { v[q] = x; kb |= 1u << q; }  // (-0 is below eps: v stays +0, as 0 + x leaves it)
+        }
+    }
+    for (int64_t c = c0 + 1; c < c1; c++) {
         const double *src = Kel + contrib[c] * BB;
 #pragma unroll
         for (int q = 0; q < BB; q++) {
