@@ -871,7 +871,9 @@ __global__ void k_block_inverse(int64_t n, const int64_t *diag, const V *A, int6
 }
 
 // r = b - A x  (or y = A x with b == nullptr): a half-warp per node row, two blocks per lane in
-// flight, the matrix streamed (evict-first), x through the read-only path (it is constant here)
+// flight, x through the read-only path (it is constant here).  A fine-level matrix (3x3 or 2x2 blocks) is
+// streamed (evict-first); a coarse level's (NB x NB, the modes' count) is read with the default policy, so
+// that it stays in L2 between the cycle's passes while the fine level streams past it.
 template <int NB>
 __global__ void __launch_bounds__(256) k_bsr_res(int64_t n, const int64_t *__restrict__ rp,
                                                  const int32_t *__restrict__ cj, const float *__restrict__ A,
@@ -896,9 +898,15 @@ __global__ void __launch_bounds__(256) k_bsr_res(int64_t n, const int64_t *__res
             for (int u = 0; u < U; u++) {
                 const int64_t k = kb + u * G;
                 const bool ok = k < k1;
-                j[u] = ok ? __ldcs(cj + k) : 0;
+                if constexpr (NB <= 3) {
+                    j[u] = ok ? __ldcs(cj + k) : 0;
 #pragma unroll
-                for (int q = 0; q < NB * NB; q++) a[u][q] = ok ? __ldcs(A + (int64_t)q * nbs + k) : 0.0f;
+                    for (int q = 0; q < NB * NB; q++) a[u][q] = ok ? __ldcs(A + (int64_t)q * nbs + k) : 0.0f;
+                } else {
+                    j[u] = ok ? __ldg(cj + k) : 0;
+#pragma unroll
+                    for (int q = 0; q < NB * NB; q++) a[u][q] = ok ? __ldg(A + (int64_t)q * nbs + k) : 0.0f;
+                }
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
