@@ -373,6 +373,27 @@ __device__ __forceinline__ double ff_mul(float2 a, float2 b) {
     const float l = __fsub_rn(e, __fsub_rn(h, p));
     return __hiloint2double(__float_as_int(l), __float_as_int(h));
 }
+// s += b (a float-float pair), by two-sum
+__device__ __forceinline__ void ff_acc(float2 b, FF &s) {
+    const float t = __fadd_rn(s.hi, b.x);
+    const float bp = __fsub_rn(t, s.hi);
+    const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, bp)), __fsub_rn(b.x, bp));
+    s.lo = __fadd_rn(s.lo, __fadd_rn(err, b.y));
+    s.hi = t;
+}
+// the pair renormalised (|lo| at most half an ulp of hi), as the next operation's input
+__device__ __forceinline__ float2 ff_norm(FF s) {
+    const float h = __fadd_rn(s.hi, s.lo);
+    return make_float2(h, __fsub_rn(s.lo, __fsub_rn(h, s.hi)));
+}
+// a float widened to double on the integer pipe (exact); zeros, subnormals, infinities and NaN take the
+// conversion instruction
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f), ex = (u >> 23) & 0xffu;
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    return __hiloint2double((int)((u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)),
+                            (int)((u & 0x7u) << 29));
+}
 __device__ __forceinline__ void ff_fma(float2 a, float2 b, FF &s) {
     const float p = __fmul_rn(a.x, b.x);
     float e = __fmaf_rn(a.x, b.x, -p);
@@ -564,10 +585,10 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
         for (int q = 0; q < BB; q++) { T[q] = 0.0; P[q] = 0.0; }
         const double *gbase = sG + el * nip * NEN * DIM;
         const double *wgbase = sWG + el * nip * NEN * DIM;
+        FF tf[BB];  // 3-D: T_ab in float-float
         if (DIM == 3) {
-            FF t[BB];
 #pragma unroll
-            for (int q = 0; q < BB; q++) t[q] = FF{0.0f, 0.0f};
+            for (int q = 0; q < BB; q++) tf[q] = FF{0.0f, 0.0f};
             for (int ip = 0; ip < nip; ip++) {
                 const double *wa = wgbase + ip * NEN * DIM + a * DIM;
                 const double *gb = gbase + ip * NEN * DIM + b * DIM;
@@ -577,10 +598,8 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
 #pragma unroll
                 for (int i = 0; i < DIM; i++)
 #pragma unroll
-                    for (int j = 0; j < DIM; j++) ff_fma(wv[i], gv[j], t[i * DIM + j]);
+                    for (int j = 0; j < DIM; j++) ff_fma(wv[i], gv[j], tf[i * DIM + j]);
             }
-#pragma unroll
-            for (int q = 0; q < BB; q++) T[q] = (double)t[q].hi + (double)t[q].lo;
         } else {
             for (int ip = 0; ip < nip; ip++) {
                 const double *wa = wgbase + ip * NEN * DIM + a * DIM;
@@ -607,15 +626,38 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
             }
         }
         const double lam = sLam[el], mu = sMu[el];
-        double tr = 0.0;
-#pragma unroll
-        for (int i = 0; i < DIM; i++) tr += T[i * DIM + i];
         double K[BB];
+        if (DIM == 3) {
+            // lambda T + mu T' + mu tr(T) I in float-float too, each entry widened to FP64 once (one FP64 add), then
+            // the plastic part in FP64
+            float2 tn[BB];
 #pragma unroll
-        for (int i = 0; i < DIM; i++)
+            for (int q = 0; q < BB; q++) tn[q] = ff_norm(tf[q]);
+            FF trs{tn[0].x, tn[0].y};
+            ff_acc(tn[4], trs);
+            ff_acc(tn[8], trs);
+            const float2 trn = ff_norm(trs);
+            const float2 lamf = ff_get(ff_split(lam)), muf = ff_get(ff_split(mu));
 #pragma unroll
-            for (int j = 0; j < DIM; j++)
-                K[i * DIM + j] = lam * T[i * DIM + j] + mu * T[j * DIM + i] + (i == j ? mu * tr : 0.0) - P[i * DIM + j];
+            for (int i = 0; i < DIM; i++)
+#pragma unroll
+                for (int j = 0; j < DIM; j++) {
+                    FF kk{0.0f, 0.0f};
+                    ff_fma(lamf, tn[i * DIM + j], kk);
+                    ff_fma(muf, tn[j * DIM + i], kk);
+                    if (i == j) ff_fma(muf, trn, kk);
+                    K[i * DIM + j] = (f2d(kk.hi) + f2d(kk.lo)) - P[i * DIM + j];
+                }
+        } else {
+            double tr = 0.0;
+#pragma unroll
+            for (int i = 0; i < DIM; i++) tr += T[i * DIM + i];
+#pragma unroll
+            for (int i = 0; i < DIM; i++)
+#pragma unroll
+                for (int j = 0; j < DIM; j++)
+                    K[i * DIM + j] = lam * T[i * DIM + j] + mu * T[j * DIM + i] + (i == j ? mu * tr : 0.0) - P[i * DIM + j];
+        }
         if (axi) {  // hoop terms: X1 = sum w h_a g_b, X2 = sum w g_a h_b, X3 = sum w h_a h_b
             double X1[2] = {0.0, 0.0}, X2[2] = {0.0, 0.0}, X3 = 0.0;
             for (int ip = 0; ip < nip; ip++) {

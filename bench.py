@@ -310,10 +310,10 @@ def run_ours(a):
     dev.assemble_K()  # K current again (the timing below reads it, and leaves it as it is)
     st_t, st_fl = dev.time_kernel(L.KERNEL_STIFFNESS, 5)
     pk64 = fp64_peak_tflops()
-    # the operation count is that of the pair form in FP64; in 3-D the pair sums (3/4 of it) run in float-float
-    # on the FP32 pipe, so the rate is an FP64-equivalent rate and may exceed the FP64 FMA peak
+    # the operation count is that of the pair form in FP64; in 3-D the pair sums (3/4 of it) and the blocks run in
+    # float-float on the FP32 pipe, so the rate is an FP64-equivalent rate and may exceed the FP64 FMA peak
     assembly["stiffness_kernel"] = {"kernel": "stiffness_kernel<3, 20> (pair-tensor element stiffness: FP64 geometry, "
-                                              "float-float pair sums)",
+                                              "float-float pair sums and blocks)",
                                     "avg_launch_s": st_t, "elements_per_s": sizes["nelems"] / st_t,
                                     "fp64_equivalent_flops_per_launch": st_fl,
                                     "fp64_equivalent_tflops": st_fl / st_t / 1e12, "fp64_peak_tflops": pk64}
