@@ -34,6 +34,9 @@ struct AmrGroup {             // elements sharing (shape, quadrature)
     double *tab = nullptr;    // device: [nip][nen*ndim] dN/dR, then [nip] w, then [nip][nen] N
     int epb = 1;              // elements per CTA for the stiffness kernel (autotuned)
     int epb_int = 0;          // elements per CTA for the internal-force kernel (0: by quadrature size)
+    // 3-D geometry cache, the same at every assembly (coordinates are fixed): dN/dX as
+    // [element][node * 3 + component][IP] and w = detJ * weight * thickness as [element][IP] (FP64)
+    double *geo_g = nullptr, *geo_w = nullptr;
 };
 
 struct AmrSolveWork;          // solver workspace (solver.cu)
@@ -90,6 +93,8 @@ struct amr_model {
     float *Minv32 = nullptr;        // nnodes x BB block-Jacobi inverse (masked)
     double *Minv64 = nullptr;       // nnodes x BB (FP64 block-Jacobi, comparator path)
     bool K_valid = false;
+    bool geo_valid = false;         // the groups' geometry caches are built (and no element is inverted)
+    bool geo_tried = false;         // a build was attempted (not again after an inverted element)
     // dofs
     int64_t ndofs = 0, nu = 0;
     std::vector<int64_t> h_eq_id;   // nnodes x 3

@@ -436,7 +436,9 @@ int amr_model_destroy(amr_model *m) {
     amr_batch_free(m);
     amr_amg_free(m);
     amr_recovery_free(m);
-    for (AmrGroup &g : m->groups) amr_free(g.tab);
+    for (AmrGroup &g : m->groups) {
+        amr_free(g.tab); amr_free(g.geo_g); amr_free(g.geo_w);
+    }
     amr_free(m->coords); amr_free(m->conn); amr_free(m->conn_ptr); amr_free(m->mat_type); amr_free(m->mat_par);
     amr_free(m->ip_ptr); amr_free(m->kel_ptr); amr_free(m->inc_ptr); amr_free(m->inc); amr_free(m->brow_ptr);
     amr_free(m->bcol); amr_free(m->contrib_ptr); amr_free(m->contrib); amr_free(m->gorder); amr_free(m->grow);

@@ -37,6 +37,7 @@ struct GroupArgs {
     const double *tab;  // [nip][nen*dim] dNdR, [nip] w, [nip][nen] N
     int nip;
     int64_t first, count;
+    const double *geo_g = nullptr, *geo_w = nullptr;  // 3-D geometry cache of the group (null: compute it)
 };
 
 struct ModelArgs {
@@ -419,6 +420,25 @@ __device__ __forceinline__ void sym_apply(const double *m, const double *g, doub
     }
 }
 
+// The 3-D geometry cache of a group: thread per (element, IP), dN/dX and w = detJ * weight * thickness by
+// ip_geometry, the same operations as the element kernels' own; *bad set where detJ <= 0 (the cache is then
+// not used, and the element kernels report the element as before).
+template <int NEN>
+__global__ void geometry_kernel(ModelArgs M, GroupArgs G, double *geo_g, double *geo_w, int32_t *bad) {
+    const int nip = G.nip;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G.count * nip) return;
+    const int64_t el = t / nip;
+    const int ip = (int)(t % nip);
+    const int64_t e = G.first + el;
+    double C[NEN * 3], g[NEN * 3];
+    for (int q = 0; q < NEN * 3; q++) C[q] = M.coords[3 * (int64_t)M.conn[M.conn_ptr[e] + q / 3] + q % 3];
+    const double det = ip_geometry<3>(NEN, G.tab + ip * NEN * 3, C, g);
+    if (!(det > 0.0)) atomicExch(bad, 1);
+    for (int q = 0; q < NEN * 3; q++) geo_g[(el * NEN * 3 + q) * nip + ip] = g[q];
+    geo_w[el * nip + ip] = det * G.tab[nip * NEN * 3 + ip] * M.thickness;
+}
+
 // ---------------------------------------------------------------------------
 // Stiffness: EPB elements per CTA.  Phase 1: thread per (element, IP) builds
 // g, w and the plastic vectors in shared memory.  Phase 2: thread per
@@ -464,6 +484,48 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
     __syncthreads();
 
     if constexpr (DIM == 3) {
+      if (G.geo_g) {
+        // 3-D with the geometry cache: (b) thread per (element, IP): w and the material's tangent; (c) thread per
+        // (element, node, IP): dN/dX from the cache, the plastic vector and the float-float splits
+        double *sMv = sH;                    // epb x nip x 6: the plastic tangent's vector m
+        const int64_t el0 = e0 - G.first;
+        for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
+            const int el = t / nip, ip = t % nip;
+            const int64_t e = e0 + el;
+            const double w = G.geo_w[(el0 + el) * nip + ip];
+            sW[el * nip + ip] = w;
+            const double *par = M.mat_par + 8 * e;
+            const int64_t gi = M.ip_ptr[e] + ip;
+            double sig[6];
+            for (int i = 0; i < 6; i++) sig[i] = st[i * M.nip_total + gi];
+            double lam, mu, m[6];
+            lame(par[0], par[1], ps, lam, mu);
+            if (ip == 0) { sLam[el] = lam; sMu[el] = mu; }
+            const double gam = plastic_tangent(M.mat_type[e], par, ps, sig, st[AMR_ST_EPA * M.nip_total + gi],
+                                               st[AMR_ST_DL * M.nip_total + gi], lam, mu, m);
+            sGam[el * nip + ip] = gam * w;
+            if (gam != 0.0) {
+                sPl[el] = 1;
+                for (int i = 0; i < 6; i++) sMv[(el * nip + ip) * 6 + i] = m[i];
+            }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < ne * nip * NEN; t += blockDim.x) {
+            const int el = t / (nip * NEN), r = t % (nip * NEN), i = r / nip, ip = r % nip;
+            double g[DIM];
+#pragma unroll
+            for (int bb = 0; bb < DIM; bb++) g[bb] = G.geo_g[((el0 + el) * NEN * DIM + i * DIM + bb) * nip + ip];
+            const int ipo = (el * nip + ip) * NEN * DIM + i * DIM;
+            if (sGam[el * nip + ip] != 0.0) sym_apply<DIM>(sMv + (el * nip + ip) * 6, g, sV + ipo);
+            const float2 wf = ff_get(ff_split(sW[el * nip + ip]));
+#pragma unroll
+            for (int bb = 0; bb < DIM; bb++) {
+                const double gs = ff_split(g[bb]);
+                sG[ipo + bb] = gs;
+                sWG[ipo + bb] = ff_mul(wf, ff_get(gs));
+            }
+        }
+      } else {
         // 3-D: the geometry spread over the CTA (the FP64 pipe is the bound, and a thread per IP left it to one
         // warp while the others waited at the barrier).  (a) thread per (element, IP, Jacobian entry)
         double *sJ = sH;                     // epb x nip x 9: J, then its inverse
@@ -532,6 +594,7 @@ __global__ void __launch_bounds__(256, stiff_min_blocks<DIM, NEN>()) stiffness_k
                 sWG[ipo + bb] = ff_mul(wf, ff_get(gs));
             }
         }
+      }
     } else
     for (int t = threadIdx.x; t < ne * nip; t += blockDim.x) {
         int el = t / nip, ip = t % nip;
@@ -1147,7 +1210,14 @@ __global__ void __launch_bounds__(256, 2) internal_kernel(ModelArgs M, GroupArgs
         int64_t e = e0 + el;
         if (elem_skipped(M, e)) continue;
         double g[NEN * DIM];
-        double det = ip_geometry<DIM>(NEN, dNdR + ip * NEN * DIM, sC + el * NEN * DIM, g);
+        double det = 0.0, wc = 0.0;  // (with the cache: wc = detJ * weight * thickness from it)
+        if (DIM == 3 && G.geo_g) {
+            const int64_t el0 = e - G.first;
+            for (int q = 0; q < NEN * DIM; q++) g[q] = G.geo_g[(el0 * NEN * DIM + q) * nip + ip];
+            wc = G.geo_w[el0 * nip + ip];
+        } else {
+            det = ip_geometry<DIM>(NEN, dNdR + ip * NEN * DIM, sC + el * NEN * DIM, g);
+        }
         const double *u = sU + el * NEN * DIM;
         double de[6] = {0, 0, 0, 0, 0, 0};
         for (int a = 0; a < NEN; a++) {
@@ -1186,7 +1256,7 @@ __global__ void __launch_bounds__(256, 2) internal_kernel(ModelArgs M, GroupArgs
             for (int i = 0; i < 6; i++) ds[i] = 0.0;
         }
         for (int f = 0; f < AMR_NST; f++) st[f * M.nip_total + gi] = s1[f];
-        double coef = det * wq[ip] * th;
+        const double coef = (DIM == 3 && G.geo_g) ? wc : det * wq[ip] * th;
         double *fo = sF + (el * nip + ip) * NEN * DIM;
         for (int a = 0; a < NEN; a++) {
             double v[DIM];
@@ -1324,7 +1394,7 @@ ModelArgs margs(amr_model *m) {
 
 template <int DIM, int NEN>
 void launch_stiff(amr_model *m, const AmrGroup &g) {
-    GroupArgs ga{g.tab, g.nip, g.first, g.count};
+    GroupArgs ga{g.tab, g.nip, g.first, g.count, m->geo_valid ? g.geo_g : nullptr, m->geo_valid ? g.geo_w : nullptr};
     int epb = g.epb;
     // coordinates, g, plastic vectors, w, gamma w, w g; then the axisymmetric N / r (2-D) or the Jacobians and
     // plastic tangent vectors (3-D)
@@ -1353,7 +1423,7 @@ void launch_stiff_ref(amr_model *m, const AmrGroup &g) {
 
 template <int DIM, int NEN>
 void launch_internal(amr_model *m, const AmrGroup &g, const double *dU) {
-    GroupArgs ga{g.tab, g.nip, g.first, g.count};
+    GroupArgs ga{g.tab, g.nip, g.first, g.count, m->geo_valid ? g.geo_g : nullptr, m->geo_valid ? g.geo_w : nullptr};
     int epb = g.epb_int > 0 ? g.epb_int : ((g.nip >= 16) ? 4 : 16);
     size_t smem = sizeof(double) * (size_t)epb * (2 * NEN * DIM + g.nip * NEN * DIM);
     int threads = std::max(epb * g.nip, epb * NEN * DIM);
@@ -1397,7 +1467,46 @@ int amr_check_status(amr_model *m) {
     return code;
 }
 
+// Builds the 3-D groups' geometry caches once per model (the coordinates never change).  If an element is
+// inverted the caches are dropped and the element kernels compute the geometry themselves, reporting the
+// element at each call as they did without a cache.
+void amr_ensure_geometry(amr_model *m) {
+    if (m->geo_valid || m->ndim != 3) return;
+    if (m->geo_tried) return;
+    m->geo_tried = true;
+    int32_t *bad = nullptr;
+    amr_alloc(&bad, 1);
+    AMR_CUDA(cudaMemsetAsync(bad, 0, sizeof(int32_t), m->stream));
+    for (AmrGroup &g : m->groups) {
+        amr_alloc(&g.geo_g, (size_t)std::max<int64_t>(g.count, 1) * g.nip * g.nen * 3);
+        amr_alloc(&g.geo_w, (size_t)std::max<int64_t>(g.count, 1) * g.nip);
+        GroupArgs ga{g.tab, g.nip, g.first, g.count};
+        const unsigned grid = nblk(std::max<int64_t>(g.count * g.nip, 1), 128);
+        dispatch(
+            m, g,
+            [&](auto n) {
+                geometry_kernel<decltype(n)::value><<<grid, 128, 0, m->stream>>>(margs(m), ga, g.geo_g, g.geo_w, bad);
+            },
+            [&](auto) {});
+        AMR_COUNT(1);
+    }
+    AMR_CUDA(cudaGetLastError());
+    int32_t hb = 0;
+    AMR_CUDA(cudaMemcpyAsync(&hb, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, m->stream));
+    AMR_CUDA(cudaStreamSynchronize(m->stream));
+    amr_free(bad);
+    if (hb) {
+        for (AmrGroup &g : m->groups) {
+            amr_free(g.geo_g); amr_free(g.geo_w);
+            g.geo_g = g.geo_w = nullptr;
+        }
+        return;
+    }
+    m->geo_valid = true;
+}
+
 void amr_stiffness_elements(amr_model *m) {
+    if (m->assembly_mode != AMR_ASSEMBLY_REFERENCE) amr_ensure_geometry(m);
     for (const AmrGroup &g : m->groups) {
         if (m->assembly_mode == AMR_ASSEMBLY_REFERENCE)
             dispatch(
@@ -1493,6 +1602,7 @@ void amr_dyn_combine(amr_model *m, const double *Ks, double s1, double s2, doubl
 }
 
 void amr_update_elements(amr_model *m, const double *dU_nm, double *dFin_nm) {
+    amr_ensure_geometry(m);
     for (const AmrGroup &g : m->groups) {
         dispatch(
             m, g, [&](auto n) { launch_internal<3, decltype(n)::value>(m, g, dU_nm); },

@@ -30,7 +30,7 @@ using Clock = std::chrono::steady_clock;
 int64_t model_bytes(const amr_model_desc *d, int method) {
     if (!d || d->nnodes <= 0 || d->nelems <= 0 || !d->shape || !d->nips) return -1;
     const int64_t N = d->nnodes, E = d->nelems, B = d->ndim, BB = B * B;
-    int64_t S = 0, C = 0, Q = 0;
+    int64_t S = 0, C = 0, Q = 0, G = 0;
     double R[64 * 3], w[64];
     for (int64_t e = 0; e < E; e++) {
         const int np = amr::shape_npoints(d->shape[e]);
@@ -39,6 +39,7 @@ int64_t model_bytes(const amr_model_desc *d, int method) {
         S += (int64_t)np * np;
         C += np;
         Q += nq;
+        if (B == 3) G += (int64_t)nq * (3 * np + 1);  // the 3-D geometry cache: dN/dX and w per IP
     }
     const int64_t NB = std::min<int64_t>(S, N * N);  // node blocks of the pattern
     int64_t b = 0;
@@ -51,6 +52,7 @@ int64_t model_bytes(const amr_model_desc *d, int method) {
     if (method == AMR_SOLVER_FP64 || method == AMR_SOLVER_AMG_FP64) b += 4 * 8 * N * B;  // FP64 Krylov vectors
     if (method == AMR_SOLVER_AMG_FP64) b += 80 * N * B;          // FP64 cycle vectors and prolongator
     b += 14 * 8 * N * B;                                         // stage vectors (host-buffer stage)
+    b += 8 * G;                                                  // 3-D geometry cache (FP64)
     b += (int64_t)64 << 20;                                      // allocation granularity and tables
     return b;
 }
